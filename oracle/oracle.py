@@ -1,0 +1,250 @@
+"""ctypes front end of the CPU oracle (liboracle.so) -- TEST INFRASTRUCTURE.
+
+Only the test suite, the smoke check and the CPU-baseline leg of the bench
+import this module, and only as the checker or as the timed CPU baseline.
+The product library never imports, links or falls back to anything here.
+
+Also reads the record files written by the reference driver
+(oracle/ref/ref_driver.cpp) and runs that driver when it has been built
+(oracle/_ref/pisces_ref, present only where the reference tree was).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "pisces_ref")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+def build(quiet: bool = True) -> str:
+    """Compile liboracle.so from pisces_oracle.c (gcc + OpenMP)."""
+    src = os.path.join(HERE, "pisces_oracle.c")
+    cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm"]
+    subprocess.run(cmd, check=True, capture_output=quiet)
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.or_sine_dvr.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp]
+        L.or_matvec.argtypes = [_ip, C.POINTER(_dp), _dp, _dp, _dp]
+        L.or_diagonal.argtypes = [_ip, C.POINTER(_dp), _dp, _dp]
+        L.or_piab_start.argtypes = [_ip, C.POINTER(_dp), _dp]
+        L.or_dpp_sites.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _dp, _ip]
+        L.or_dpp_sites.restype = C.c_int
+        L.or_potential_ions_add.argtypes = [_ip, C.POINTER(_dp), C.c_int, _dp, _dp, C.c_double, C.c_double, _dp]
+        L.or_potential_spherical.argtypes = [_ip, C.POINTER(_dp), C.c_double, _dp]
+        L.or_solve.argtypes = [_ip, C.POINTER(_dp), C.POINTER(_dp), _dp, C.c_int, C.c_int, C.c_int, C.c_int,
+                               C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_long), C.c_long]
+        L.or_solve.restype = C.c_int
+        L.or_syev.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+class _Tables(C.Structure):
+    _fields_ = [("nsites", C.c_int), ("sites", _dp),
+                ("ncharges", C.c_int), ("charges", _dp), ("charge_site", _ip),
+                ("ndipoles", C.c_int), ("dipoles", _dp), ("dipole_site", _ip),
+                ("nsto", C.c_int), ("sto", _dp), ("sto_site", _ip),
+                ("npol", C.c_int), ("pol_alpha", _dp), ("pol_site", _ip),
+                ("charge_damp", C.c_double), ("dipole_damp", C.c_double), ("pol_damp", C.c_double)]
+
+
+def sine_dvr(n: int, L: float):
+    x = np.empty(n)
+    t = np.empty(n * (n + 1) // 2)
+    lib().or_sine_dvr(n, 1.0, -0.5 * L, 0.5 * L, _d(x), _d(t))
+    return x, t
+
+
+def unpack(tp: np.ndarray, n: int) -> np.ndarray:
+    T = np.zeros((n, n))
+    a, b = np.tril_indices(n)
+    T[a, b] = tp
+    T[b, a] = tp
+    return T
+
+
+class Grid:
+    """Sine-DVR grid in the reference convention (walls at -L/2, +L/2)."""
+
+    def __init__(self, n, L):
+        self.n = np.ascontiguousarray(n, dtype=np.int32)
+        self.L = np.asarray(L, dtype=np.float64)
+        self.x, self.tp = [], []
+        for a in range(3):
+            xa, ta = sine_dvr(int(self.n[a]), float(self.L[a]))
+            self.x.append(xa)
+            self.tp.append(ta)
+        self._tp_ptrs = (_dp * 3)(*[_d(t) for t in self.tp])
+        self._x_ptrs = (_dp * 3)(*[_d(t) for t in self.x])
+
+    @property
+    def N(self):
+        return int(np.prod(self.n))
+
+    def matvec(self, v, x):
+        y = np.empty(self.N)
+        lib().or_matvec(_i(self.n), self._tp_ptrs, _d(v), _d(np.ascontiguousarray(x)), _d(y))
+        return y
+
+    def diagonal(self, v):
+        d = np.empty(self.N)
+        lib().or_diagonal(_i(self.n), self._tp_ptrs, _d(v), _d(d))
+        return d
+
+    def piab(self):
+        w = np.empty(self.N)
+        lib().or_piab_start(_i(self.n), self._x_ptrs, _d(w))
+        return w
+
+    def potential_dpp(self, sites, charges, charge_site, dipoles, dipole_site, parts=False):
+        """Default DPPGTOP model V on the grid from the water-site tables."""
+        nw = len(sites) // 12
+        sites = np.ascontiguousarray(sites, dtype=np.float64)
+        charges = np.ascontiguousarray(charges, dtype=np.float64)
+        charge_site = np.ascontiguousarray(charge_site, dtype=np.int32)
+        dipoles = np.ascontiguousarray(dipoles, dtype=np.float64)
+        dipole_site = np.ascontiguousarray(dipole_site, dtype=np.int32)
+        sto = np.empty(8 * nw)
+        sto_site = np.empty(4 * nw, dtype=np.int32)
+        pa = np.empty(nw)
+        ps = np.empty(nw, dtype=np.int32)
+        t = _Tables()
+        L = lib()
+        L.or_dpp_default_tables.argtypes = [C.c_int, _dp, _dp, _ip, _dp, _ip, _dp, _ip, _dp, _ip, C.POINTER(_Tables)]
+        L.or_dpp_default_tables(nw, _d(sites), _d(charges), _i(charge_site), _d(dipoles), _i(dipole_site),
+                                _d(sto), _i(sto_site), _d(pa), _i(ps), C.byref(t))
+        v = np.empty(self.N)
+        out = [np.empty(self.N) for _ in range(4)]
+        L.or_potential_dpp.argtypes = [_ip, C.POINTER(_dp), C.POINTER(_Tables), _dp, _dp, _dp, _dp, _dp]
+        L.or_potential_dpp(_i(self.n), self._x_ptrs, C.byref(t), _d(v), *[_d(o) for o in out])
+        return (v, *out) if parts else v
+
+    def add_ions(self, v, pos_bohr, q, r_cation=2.9, r_anion=1.0):
+        pos = np.ascontiguousarray(pos_bohr, dtype=np.float64)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        lib().or_potential_ions_add(_i(self.n), self._x_ptrs, len(q), _d(pos), _d(q), r_cation, r_anion, _d(v))
+        return v
+
+    def spherical(self, k):
+        v = np.empty(self.N)
+        lib().or_potential_spherical(_i(self.n), self._x_ptrs, float(k), _d(v))
+        return v
+
+    def solve(self, v, nstates=1, maxsub=20, maxiter=100, ptol=5, corrflag=1, startvec=1, max_matvec=0):
+        """Reference-algorithm Davidson; returns (status, evals, vectors, n_matvec)."""
+        ev = np.zeros(nstates)
+        B = np.zeros(self.N * maxsub)
+        nmv = C.c_long(0)
+        st = lib().or_solve(_i(self.n), self._tp_ptrs, self._x_ptrs, _d(np.ascontiguousarray(v)), nstates, maxsub,
+                            maxiter, ptol, corrflag, startvec, _d(ev), _d(B), C.byref(nmv), int(max_matvec))
+        return st, ev, B[: self.N * nstates].reshape(nstates, self.N), nmv.value
+
+
+def dpp_sites(waters_angstrom):
+    """Rigid-water DPP site tables (sites, charges, charge_site, dipoles, dipole_site, iters)."""
+    w = np.ascontiguousarray(waters_angstrom, dtype=np.float64).reshape(-1)
+    nw = len(w) // 9
+    sites = np.empty(12 * nw)
+    q = np.empty(3 * nw)
+    qs = np.empty(3 * nw, dtype=np.int32)
+    d = np.empty(9 * nw)
+    ds = np.empty(3 * nw, dtype=np.int32)
+    it = lib().or_dpp_sites(nw, _d(w), _d(sites), _d(q), _i(qs), _d(d), _i(ds))
+    return sites, q, qs, d, ds, it
+
+
+def syev(a):
+    n = a.shape[0]
+    A = np.asfortranarray(a, dtype=np.float64).copy()
+    w = np.empty(n)
+    V = np.empty((n, n), order="F")
+    lib().or_syev(n, A.ctypes.data_as(_dp), n, _d(w), V.ctypes.data_as(_dp), n)
+    return w, V
+
+
+# ---------------------------------------------------------------- reference driver
+
+def read_records(path):
+    """Parse a record file written by the reference driver."""
+    out = {}
+    with open(path, "rb") as f:
+        if f.read(8) != b"PGREC1\0\0":
+            raise ValueError("not a record file")
+        while True:
+            head = f.read(64)
+            if len(head) < 64:
+                break
+            name = head.split(b"\0", 1)[0].decode()
+            kind = f.read(8)[:1]
+            (n,) = struct.unpack("<Q", f.read(8))
+            if kind == b"d":
+                out[name] = np.frombuffer(f.read(8 * n), dtype="<f8").copy()
+            else:
+                out[name] = np.frombuffer(f.read(4 * n), dtype="<i4").copy()
+    return out
+
+
+def have_reference() -> bool:
+    return os.path.exists(REF_BIN)
+
+
+def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, maxiter=100, ptol=5, startvec=1,
+                  spherical_k=None, matvec_seed=None, fulldiag=False, diagonalize=True, dump_wavefn=True,
+                  threads=None):
+    """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration."""
+    if not have_reference():
+        raise FileNotFoundError(REF_BIN)
+    with tempfile.TemporaryDirectory() as td:
+        inp = os.path.join(td, "in.txt")
+        out = os.path.join(td, "out.rec")
+        lines = [f"grid {n[0]} {n[1]} {n[2]} {L[0]!r} {L[1]!r} {L[2]!r}",
+                 f"diag {nstates} {method} {maxsub} {maxiter} {ptol} {startvec}"]
+        if waters is not None and len(waters):
+            w = np.asarray(waters, dtype=np.float64).reshape(-1, 9)
+            lines.append(f"waters {len(w)}")
+            lines += [" ".join(repr(float(c)) for c in row) for row in w]
+        if ions is not None and len(ions):
+            io = np.asarray(ions, dtype=np.float64).reshape(-1, 4)
+            lines.append(f"ions {len(io)}")
+            lines += [" ".join(repr(float(c)) for c in row) for row in io]
+        if spherical_k is not None:
+            lines.append(f"spherical {spherical_k!r}")
+        if matvec_seed is not None:
+            lines.append(f"matvec_seed {int(matvec_seed)}")
+        lines += [f"fulldiag {int(fulldiag)}", f"diagonalize {int(diagonalize)}",
+                  f"dump_wavefn {int(dump_wavefn)}", f"out {out}"]
+        with open(inp, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        env = dict(os.environ)
+        if threads:
+            env["OMP_NUM_THREADS"] = str(threads)
+        subprocess.run([REF_BIN, inp], check=True, stdout=subprocess.DEVNULL, stderr=subprocess.PIPE, env=env)
+        return read_records(out)

@@ -1,0 +1,281 @@
+// Oracle driver for the reference PISCES CPU code (test infrastructure only).
+//
+// Links the reference's own objects (compiled unmodified from their source
+// tree) and replays the single-point sequence of
+// ClusterAnion::SetUpClusterAnion / SinglePoint / EnergyFromConfiguration
+// (src/ClusterAnion.cpp:92-112, 114-125, 192-290) through public APIs:
+//   WaterCluster::SetStructure -> GetConfiguration -> SetConfiguration ->
+//   CalcEnergy -> GetLists / ReportInducedDipoles / ReportPolSitesAndField,
+//   Potential::Setup, DVR::SetupDVR / ComputePotential / DiagonalizeSetup /
+//   Diagonalize.
+// It writes every intermediate the GPU path must reproduce (grid points,
+// kinetic matrices, site tables, V on the grid with its four parts, diag(H),
+// one H*x product, eigenvalues and eigenvectors) to a binary record file at
+// full double precision, which the fixture generator turns into golden files.
+//
+// The water + ion configuration has no single reference model: the ions use
+// the reference Bloomfield potential (src/NaCl.cpp:260-318) in a second
+// Potential object, evaluated on the same grid and added to V before the
+// reference Davidson runs.
+//
+// DVR keeps its grid, V and kinetic matrices private; this driver is test
+// code, so it opens the class up to read them.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <vector>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+#include <chrono>
+#include <mpi.h>
+#include "vecdefs.h"
+#include "constants.h"
+#include "GTO.h"
+#include "MO.h"
+#include "AtomCenter.h"
+#include "Water.h"
+#include "DPP.h"
+#define private public
+#include "Potential.h"
+#include "DVR.h"
+#undef private
+#include "lapackblas.h"
+
+namespace {
+
+struct Record {
+  std::string name;
+  char kind;  // 'd' double, 'i' int32
+  std::vector<double> d;
+  std::vector<int> i;
+};
+
+std::vector<Record> g_records;
+
+void put(const std::string& name, const double* p, size_t n) {
+  Record r; r.name = name; r.kind = 'd'; r.d.assign(p, p + n); g_records.push_back(r);
+}
+void put(const std::string& name, const int* p, size_t n) {
+  Record r; r.name = name; r.kind = 'i'; r.i.assign(p, p + n); g_records.push_back(r);
+}
+void put1(const std::string& name, double v) { put(name, &v, 1); }
+void put1i(const std::string& name, int v) { put(name, &v, 1); }
+
+// File layout: magic "PGREC1\0\0", then per record: 64-byte zero-padded name,
+// 8-byte kind ('d' or 'i' then zeros), uint64 count, raw little-endian data.
+void write_records(const std::string& path) {
+  FILE* f = fopen(path.c_str(), "wb");
+  if (!f) { perror(path.c_str()); exit(2); }
+  fwrite("PGREC1\0\0", 1, 8, f);
+  for (const Record& r : g_records) {
+    char name[64] = {0}; strncpy(name, r.name.c_str(), 63);
+    char kind[8] = {0}; kind[0] = r.kind;
+    unsigned long long n = r.kind == 'd' ? r.d.size() : r.i.size();
+    fwrite(name, 1, 64, f); fwrite(kind, 1, 8, f); fwrite(&n, 8, 1, f);
+    if (r.kind == 'd') fwrite(r.d.data(), 8, n, f); else fwrite(r.i.data(), 4, n, f);
+  }
+  fclose(f);
+}
+
+// splitmix64 -> uniform [-1, 1); the vector is also written out, so nothing
+// else has to reproduce this generator.
+double next_uniform(unsigned long long& s) {
+  unsigned long long z = (s += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+struct Input {
+  int n[3] = {16, 16, 16};
+  double L[3] = {20, 20, 20};
+  int nstates = 1, method = 2, maxsub = 20, maxiter = 100, ptol = 5, startvec = 1;
+  std::vector<double> waters;  // 9 per water, Angstrom
+  std::vector<double> ions;    // x y z q per ion, Angstrom
+  double spherical_k = -1;     // >=0: harmonic model potential instead of waters
+  long long matvec_seed = -1;
+  int fulldiag = 0;
+  int diagonalize = 1;
+  int dump_wavefn = 1;
+  std::string out = "out.rec";
+};
+
+Input read_input(const char* path) {
+  Input in;
+  std::ifstream f(path);
+  if (!f) { fprintf(stderr, "cannot open %s\n", path); exit(2); }
+  std::string key;
+  while (f >> key) {
+    if (key == "grid") { f >> in.n[0] >> in.n[1] >> in.n[2] >> in.L[0] >> in.L[1] >> in.L[2]; }
+    else if (key == "diag") { f >> in.nstates >> in.method >> in.maxsub >> in.maxiter >> in.ptol >> in.startvec; }
+    else if (key == "waters") { int nw; f >> nw; in.waters.resize(9 * nw); for (double& v : in.waters) f >> v; }
+    else if (key == "ions") { int ni; f >> ni; in.ions.resize(4 * ni); for (double& v : in.ions) f >> v; }
+    else if (key == "spherical") { f >> in.spherical_k; }
+    else if (key == "matvec_seed") { f >> in.matvec_seed; }
+    else if (key == "fulldiag") { f >> in.fulldiag; }
+    else if (key == "diagonalize") { f >> in.diagonalize; }
+    else if (key == "dump_wavefn") { f >> in.dump_wavefn; }
+    else if (key == "out") { f >> in.out; }
+    else { fprintf(stderr, "unknown key %s\n", key.c_str()); exit(2); }
+  }
+  return in;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 2) { fprintf(stderr, "usage: %s input.txt\n", argv[0]); return 2; }
+  Input in = read_input(argv[1]);
+  int provided; MPI_Init_thread(&argc, &argv, MPI_THREAD_FUNNELED, &provided);
+
+  // Default electron-water model parameters (src/GetInput.cpp:43-63).
+  iVec potflag(6);
+  potflag[0] = 3; potflag[1] = 2; potflag[2] = 0; potflag[3] = 1; potflag[4] = 0; potflag[5] = 0;
+  double potpara[100] = {0};
+  potpara[0] = 9.745; potpara[1] = 2.536; potpara[2] = 4.4837; potpara[3] = 1.7724;
+  potpara[4] = 1.7724; potpara[5] = 4.4837; potpara[6] = 0.5 / sqrt(potpara[0]); potpara[10] = 20.0;
+
+  DVR Hel;
+  Hel.SetupDVR(in.n, 0, 1, in.L, 0);
+  Hel.SetVerbose(0);
+  Hel.DiagonalizeSetup(in.nstates, in.method, in.maxsub, in.maxiter, in.ptol);
+  const int ngp = Hel.ngp;
+
+  put("n", in.n, 3);
+  put("L", in.L, 3);
+  for (int a = 0; a < 3; ++a) {
+    int off = a == 0 ? 0 : (a == 1 ? Hel.max1db[0] : Hel.max1db[0] + Hel.max1db[1]);
+    put(std::string("x") + char('0' + a), Hel.x_dvr + off, in.n[a]);
+    put(std::string("tpacked") + char('0' + a), Hel.e_kin[a], (size_t)in.n[a] * (in.n[a] + 1) / 2);
+  }
+
+  Potential Vel;
+  Vel.SetVerbose(0);
+  WaterCluster WaterN;
+  const int nW = (int)in.waters.size() / 9;
+  double t_pot = 0;
+  if (in.spherical_k >= 0) {
+    double pp[3] = {0, 0, in.spherical_k};
+    Vel.SetupSphericalPotential(pp);
+    auto t0 = std::chrono::steady_clock::now();
+    Hel.ComputePotential(Vel);
+    t_pot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  } else if (nW > 0) {
+    // src/ClusterAnion.cpp:104-106, 84-88, 204-206: structure in Angstrom,
+    // no centre-of-mass shift (CoMOrigin default 0), standard DPP charges.
+    WaterN.SetStructure(nW, in.waters.data(), 1, 0, 0, 0);
+    dVec conf(6 * nW);
+    WaterN.GetConfiguration(nW, conf.data(), 1.0, 0);
+    WaterN.SetConfiguration(nW, conf.data(), 1, 0);
+    double E0 = WaterN.CalcEnergy(0);
+    put1("E0", E0);
+
+    int nSites = 0, nCharges = 0, nDipoles = 0;
+    WaterN.ReportNoOfSites(nSites, nCharges, nDipoles);
+    int nPntPol = WaterN.ReportNoOfPolSites();
+    dVec Sites(3 * nSites), Charges(nCharges), Dipoles(3 * nDipoles), DmuByDR(3 * nSites * 3 * nDipoles);
+    iVec iqs(nCharges), ids(nDipoles);
+    dVec Alphas(nPntPol), Epc(3 * nPntPol);
+    iVec ips(nPntPol);
+    WaterN.GetLists(nSites, Sites.data(), nCharges, Charges.data(), iqs.data(), nDipoles, Dipoles.data(),
+                    ids.data(), DmuByDR.data(), 0);
+    put("mol_dipoles", Dipoles.data(), 3 * nDipoles);
+    nDipoles *= 3;
+    Dipoles.resize(3 * nDipoles);
+    ids.resize(nDipoles);
+    WaterN.ReportInducedDipoles(nDipoles, Dipoles.data(), ids.data(), 0);
+    WaterN.ReportPolSitesAndField(nPntPol, Alphas.data(), ips.data(), Epc.data(), 0);
+    put("sites", Sites.data(), Sites.size());
+    put("charges", Charges.data(), Charges.size());
+    put("charge_site", iqs.data(), iqs.size());
+    put("dipoles", Dipoles.data(), Dipoles.size());
+    put("dipole_site", ids.data(), ids.size());
+    put("alphas", Alphas.data(), Alphas.size());
+    put("alpha_site", ips.data(), ips.size());
+    put("epc", Epc.data(), Epc.size());
+
+    Vel.Setup(potflag, nSites, Sites.data(), nCharges, Charges.data(), iqs.data(), nDipoles, Dipoles.data(),
+              ids.data(), nPntPol, Alphas.data(), ips.data(), Epc.data(), DmuByDR.data(), potpara);
+    auto t0 = std::chrono::steady_clock::now();
+    Hel.ComputePotential(Vel);
+    t_pot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    put("v_pc", Hel.v_diag_pc, ngp);
+    put("v_ind", Hel.v_diag_ind, ngp);
+    put("v_rep", Hel.v_diag_rep, ngp);
+    put("v_pol", Hel.v_diag_pol, ngp);
+  }
+  put1("t_potential", t_pot);
+
+  const int nI = (int)in.ions.size() / 4;
+  if (nI > 0) {
+    // Ions: Bloomfield erf-damped charges, rNa = 2.9, rCl = 1.0 bohr (src/NaCl.cpp:95-96).
+    dVec ipos(3 * nI), iq(nI);
+    iVec isite(nI);
+    for (int k = 0; k < nI; ++k) {
+      for (int c = 0; c < 3; ++c) ipos[3 * k + c] = in.ions[4 * k + c] * Angs2Bohr;
+      iq[k] = in.ions[4 * k + 3];
+      isite[k] = k;
+    }
+    double pp[2] = {2.9, 1.0};
+    Potential Vion;
+    Vion.SetVerbose(0);
+    Vion.SetupBloomfield(nI, ipos.data(), nI, iq.data(), isite.data(), pp);
+    put("ion_sites", ipos.data(), ipos.size());
+    put("ion_charges", iq.data(), iq.size());
+    dVec vion(ngp);
+    // Same grid-point order as DVR::ComputePotential (x fastest).
+    for (int k = 0; k < in.n[2]; ++k)
+      for (int j = 0; j < in.n[1]; ++j)
+        for (int i = 0; i < in.n[0]; ++i) {
+          double q[3] = {Hel.x_dvr[i], Hel.x_dvr[Hel.max1db[0] + j], Hel.x_dvr[Hel.max1db[0] + Hel.max1db[1] + k]};
+          vion[i + in.n[0] * (j + in.n[1] * k)] = Vion.Evaluate(q);
+        }
+    put("v_ion", vion.data(), ngp);
+    for (int g = 0; g < ngp; ++g) Hel.v_diag[g] += vion[g];
+  }
+  put("v", Hel.v_diag, ngp);
+
+  dVec diag(ngp);
+  Hel.ComputeDiagonal(diag.data());
+  put("diag", diag.data(), ngp);
+
+  if (in.matvec_seed >= 0) {
+    unsigned long long s = (unsigned long long)in.matvec_seed;
+    dVec x(ngp), y(ngp);
+    for (double& v : x) v = next_uniform(s);
+    DVR::counter kc; Hel.m_pkc = &kc;
+    Hel.MatrixTimesVector(x.data(), y.data());
+    put("mv_x", x.data(), ngp);
+    put("mv_y", y.data(), ngp);
+  }
+
+  if (in.fulldiag) {
+    if (ngp > 2000) { fprintf(stderr, "fulldiag needs ngp <= 2000\n"); return 2; }
+    dVec h((size_t)ngp * ngp), w(ngp);
+    Hel.build_h(h.data());
+    int info = 0, lwork = 5 * ngp;
+    dVec work(lwork);
+    dsyev("N", "U", (int*)&ngp, h.data(), (int*)&ngp, w.data(), work.data(), &lwork, &info);
+    if (info != 0) { fprintf(stderr, "dsyev info %d\n", info); return 3; }
+    put("full_evals", w.data(), ngp);
+  }
+
+  if (in.diagonalize) {
+    dVec ev(in.nstates);
+    auto t0 = std::chrono::steady_clock::now();
+    int nconv = Hel.Diagonalize(in.startvec, ev.data());
+    double t_diag = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    put1i("nconv", nconv);
+    put("evals", ev.data(), in.nstates);
+    put1("t_diagonalize", t_diag);
+    if (in.dump_wavefn) put("wavefn", Hel.wavefn.data(), (size_t)ngp * in.nstates);
+    fprintf(stderr, "nconv %d t_diag %.3f s\n", nconv, t_diag);
+    for (int k = 0; k < in.nstates; ++k) fprintf(stderr, "E[%d] = %.17g\n", k, ev[k]);
+  }
+  write_records(in.out);
+  return 0;
+}

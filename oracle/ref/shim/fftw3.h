@@ -1,0 +1,33 @@
+/* FFTW3 stand-in for the oracle build.  The sine-DVR path only constructs and
+ * destroys plans (the Davidson driver builds an FFT engine it never uses); any
+ * attempt to execute a plan aborts, so a silent wrong answer is impossible. */
+#ifndef ORACLE_SHIM_FFTW3_H
+#define ORACLE_SHIM_FFTW3_H
+#include <stdlib.h>
+#include <stdio.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+typedef double fftw_complex[2];
+typedef struct oracle_fftw_plan_s* fftw_plan;
+#define FFTW_FORWARD (-1)
+#define FFTW_BACKWARD (+1)
+#define FFTW_ESTIMATE (1U << 6)
+#define FFTW_MEASURE (0U)
+void* fftw_malloc(size_t n);
+void fftw_free(void* p);
+fftw_plan fftw_plan_dft_r2c_3d(int n0, int n1, int n2, double* in, fftw_complex* out, unsigned flags);
+fftw_plan fftw_plan_dft_c2r_3d(int n0, int n1, int n2, fftw_complex* in, double* out, unsigned flags);
+fftw_plan fftw_plan_dft_3d(int n0, int n1, int n2, fftw_complex* in, fftw_complex* out, int sign, unsigned flags);
+fftw_plan fftw_plan_dft_r2c(int rank, const int* n, double* in, fftw_complex* out, unsigned flags);
+fftw_plan fftw_plan_dft_c2r(int rank, const int* n, fftw_complex* in, double* out, unsigned flags);
+fftw_plan fftw_plan_dft(int rank, const int* n, fftw_complex* in, fftw_complex* out, int sign, unsigned flags);
+void fftw_execute(const fftw_plan p);
+void fftw_destroy_plan(fftw_plan p);
+int fftw_init_threads(void);
+void fftw_plan_with_nthreads(int n);
+void fftw_cleanup_threads(void);
+#ifdef __cplusplus
+}
+#endif
+#endif
