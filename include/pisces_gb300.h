@@ -1,0 +1,216 @@
+/*
+ * pisces_gb300 -- C ABI of the GB300 (sm_103a) excess-electron eigensolve path.
+ *
+ * One shared library, libpisces_gb300.so, replaces the reference PISCES hot
+ * path: the sine-DVR kinetic builder, the grid evaluation of the
+ * electron-water model potential, the H*X product and the reverse-
+ * communication Davidson eigensolver.  Reference citations are paths inside
+ * the reference source tree.
+ *
+ * Conventions (identical to the reference):
+ *   - grid index g = i + nx*(j + ny*k), x fastest (src/mtx.cpp:15-19);
+ *   - box walls at -L/2 and +L/2 per axis, n interior points (src/DVR.cpp:603);
+ *   - blocks of vectors are contiguous columns, X[v*N + g]
+ *     (src/davdriver.cpp:67-70);
+ *   - all reals are IEEE double, lengths in bohr, energies in hartree;
+ *     water input coordinates in Angstrom (src/GetInput.cpp:256).
+ *
+ * Pointers named *_dev are device pointers on the handle's GPU; pointers
+ * named *_host are host pointers.  A `stream` argument is a cudaStream_t
+ * passed as void* (NULL = the legacy default stream).  No call keeps a
+ * caller pointer past its return.  Every call returns a pg_status; the text
+ * of the last error on the calling thread is pg_last_error().  Nothing
+ * exits the process (the reference calls exit(1)/exit(42) instead).
+ */
+#ifndef PISCES_GB300_H
+#define PISCES_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  PG_OK = 0,
+  PG_BAD_ARG = 1,        /* invalid size, pointer or flag */
+  PG_OOM = 2,            /* device or host allocation failed, or admission refused */
+  PG_NOT_CONVERGED = 3,  /* Davidson reached its macro-iteration limit (reference: warning, src/Davidson.cpp:332-340) */
+  PG_DEVICE_TIMEOUT = 4, /* a bounded device-side wait ran out */
+  PG_NUMERIC = 5,        /* NaN/Inf or a failed small eigensolve (reference: src/Davidson.cpp:225-226) */
+  PG_CUDA = 6,           /* a CUDA runtime call failed */
+  PG_UNSUPPORTED = 7     /* valid but not implemented on this path */
+} pg_status;
+
+typedef enum { PG_FP64 = 0, PG_MIXED = 1 } pg_precision;
+
+const char* pg_last_error(void);
+int pg_version(void);
+/* Number of CUDA kernels this library has launched since it was loaded. */
+long pg_kernel_launches(void);
+
+/* ------------------------------------------------------------------ kinetic */
+
+/* 1-D sine DVR: grid points x[n] and the kinetic matrix of a particle of
+ * mass mu in the box (x0, xNp1).  ldt == 0: packed lower triangle, element
+ * (a,b) b<=a at a*(a+1)/2+b; ldt >= n: full symmetric matrix with leading
+ * dimension ldt.  Replaces sine_dvr() (src/sine_dvr.h:1, src/sine_dvr.cpp:45-131),
+ * same arguments and meaning (the verbose flag is dropped).  Host-only. */
+pg_status pg_sine_dvr(int n, double mu, double x0, double xNp1, double* x_host, double* ekin_host, int ldt);
+
+/* --------------------------------------------------------------------- grid */
+
+typedef struct pg_grid pg_grid;
+
+/* A 3-D sine-DVR grid on the current device: n[3] points per axis, box
+ * lengths L[3].  Builds the three kinetic matrices (full, FP64, plus the
+ * split-TF32 copies of the mixed form) in device memory.  Replaces
+ * DVR::SetupDVR with DVRType 0 (src/DVR.cpp:64-161, 524-651). */
+pg_status pg_grid_create(const int n[3], const double L[3], pg_grid** out);
+pg_status pg_grid_destroy(pg_grid* g);
+/* Number of grid points (n0*n1*n2). */
+long pg_grid_npoints(const pg_grid* g);
+/* Grid points per axis (host copies, n[a] doubles each; any may be NULL). */
+pg_status pg_grid_points(const pg_grid* g, double* x_host, double* y_host, double* z_host);
+/* Kinetic matrix of one axis as a full n x n host matrix. */
+pg_status pg_grid_kinetic(const pg_grid* g, int axis, double* t_host);
+
+/* diag(H) = V + Tx_ii + Ty_jj + Tz_kk (DVR::ComputeDiagonal, src/DVR.cpp:1808-1881). */
+pg_status pg_diagonal(const pg_grid* g, const double* v_dev, double* diag_dev, void* stream);
+
+/* Half-box particle-in-a-box start vector (DVR::ParticleInAnDBoxWf, src/DVR.cpp:1725-1805). */
+pg_status pg_piab_start(const pg_grid* g, double* wf_dev, void* stream);
+
+/* ----------------------------------------------------------------- potential */
+
+/* Electron-site potential tables in the reference's list form
+ * (Potential::Setup arguments, src/Potential.h:38-42; per-term lists set by
+ * SetSites/SetCharges/SetDipoles and the repulsive-core and polarisable-site
+ * setup, src/Potential.cpp:234-593, 699-728, 1817-1861).  Host pointers.
+ * Site indices refer to `sites`.  Damping follows DampType 2 (effective
+ * radius r0; src/Potential.cpp:1188-1366); the polarisation term is the
+ * first-order -alpha/(2 R^4) form (PolType 1, AdiabaticPolPot 0). */
+typedef struct {
+  int nsites;   const double* sites;                            /* 3*nsites, bohr */
+  int ncharges; const double* charges;   const int* charge_site;
+  int ndipoles; const double* dipoles;   const int* dipole_site; /* 3*ndipoles */
+  int nsto;     const double* sto;       const int* sto_site;    /* (exponent, coefficient) pairs: c*exp(-z*R) */
+  int npol;     const double* pol_alpha; const int* pol_site;
+  double charge_damp, dipole_damp, pol_damp;                      /* r0 per term */
+} pg_sites;
+
+/* V(r) on every grid point, and optionally its four parts
+ * (charges, induced dipoles, repulsive core, polarisation) as parts_dev[4*N]
+ * in that order.  Replaces DVR::ComputePotential + Potential::Evaluate /
+ * EvaluateDPPGTOP (src/DVR.cpp:661-859, src/Potential.cpp:128-182, 844-956).
+ * At most one charge, one dipole, one polarisable site and two repulsive
+ * Slater functions may sit on one site (PG_UNSUPPORTED otherwise). */
+pg_status pg_potential_eval(const pg_grid* g, const pg_sites* tables, double* v_dev, double* parts_dev, void* stream);
+
+/* Adds Bloomfield erf-damped ion charges, -q erf(R/r_ion)/R, with r_ion =
+ * r_cation for q > 0 and r_anion otherwise (Potential::EvaluateBloomfield,
+ * src/NaCl.cpp:260-318).  pos_host: 3*nions bohr. */
+pg_status pg_potential_ions_add(const pg_grid* g, int nions, const double* pos_host, const double* q_host,
+                                double r_cation, double r_anion, double* v_dev, void* stream);
+
+/* Harmonic model potential 0.5*k*r^2 (Potential::EvaluateSphericalPotential,
+ * src/Model_pot.cpp:144-156). */
+pg_status pg_potential_spherical(const pg_grid* g, double k, double* v_dev, void* stream);
+
+/* Rigid-water DPP site producer (host): projects each O,H,H triple onto the
+ * rigid model (Water::Reposition, src/Water.cpp:695-824), solves the damped
+ * self-consistent induced dipoles (WaterCluster::CalcInducedDipoles,
+ * src/DPP.cpp:760-1060) and returns the electron's lists
+ * (WaterCluster::GetLists / ReportInducedDipoles, src/DPP.cpp:402-529):
+ *   sites[12*nw] (O,H1,H2,M), charges[3*nw]/charge_site[3*nw] (H1,H2,M),
+ *   dipoles[9*nw]/dipole_site[3*nw] (O,H1,H2).
+ * *scf_iters receives the SCF iteration count (-1: not converged). */
+pg_status pg_water_sites(int nw, const double* waters_angstrom, double* sites, double* charges, int* charge_site,
+                         double* dipoles, int* dipole_site, int* scf_iters);
+
+/* Default electron-water model tables for those lists: 4-STO repulsive core
+ * scaled by 1/4.4837, one polarisable site (alpha 9.745) per water on M,
+ * damping radii 1.7724/1.7724/2.536 (src/GetInput.cpp:43-63,
+ * src/Potential.cpp:699-728, 326-338).  Caller storage: sto[8*nw],
+ * sto_site[4*nw], pol_alpha[nw], pol_site[nw]; `out` points into the inputs. */
+pg_status pg_water_default_tables(int nw, const double* sites, const double* charges, const int* charge_site,
+                                  const double* dipoles, const int* dipole_site, double* sto, int* sto_site,
+                                  double* pol_alpha, int* pol_site, pg_sites* out);
+
+/* ------------------------------------------------------------------- H * X */
+
+/* Y = H X for nvec vectors: H = V + Tx (+) Ty (+) Tz.  precision PG_FP64:
+ * FP64 arithmetic throughout; PG_MIXED: kinetic contractions as split-TF32
+ * tensor-core products accumulated in FP32, V*X in FP64.  Replaces
+ * DVR::MatrixTimesVector applied vector by vector (src/mtx.cpp:22-109,
+ * src/davdriver.cpp:67-78). */
+pg_status pg_hx(const pg_grid* g, const double* v_dev, const double* x_dev, double* y_dev, int nvec, int precision,
+                void* stream);
+
+/* ---------------------------------------------------------------- Davidson */
+
+typedef struct pg_davidson pg_davidson;
+
+/* Caller-owned state for the reverse-communication Davidson (the reference
+ * keeps it in function statics, src/Davidson.cpp:114-143, so only one solve
+ * per process can run; any number of handles can run here). */
+pg_status pg_davidson_create(pg_davidson** out);
+pg_status pg_davidson_destroy(pg_davidson* d);
+
+/* Work-array length in doubles (DavidsonWorkSize, src/Davidson.cpp:46-52). */
+long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag);
+
+/* One step of the reverse-communication Davidson: same arguments, meaning
+ * and return codes as Davidson() (src/Davidson.h:2-15, src/Davidson.cpp:61-376)
+ * plus the state handle and a stream.  B_dev, Z_dev (ndim*maxsub), diag_dev
+ * (ndim) and work_dev (pg_davidson_work_size) are device arrays; evals_host,
+ * nconv and inout are host.  *ret = 1: compute Z[inout[1]+v] = H B[inout[0]+v]
+ * for v < inout[2], then call again; *ret = 0: done (converged eigenpairs in
+ * evals_host and B_dev[0..nroots), *nconv converged; PG_NOT_CONVERGED if the
+ * macro-iteration limit was reached). */
+pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int nroots, int maxmacro, int tol, int corrflag,
+                          double* evals_host, int* nconv, double* B_dev, double* Z_dev, const double* diag_dev,
+                          double* work_dev, int* inout, int* ret, void* stream);
+
+typedef struct {
+  int nroots;     /* states wanted (nStates) */
+  int maxsub;     /* max subspace (maxSubspace, default 20) */
+  int maxiter;    /* max macro iterations (maxIter, default 100) */
+  int ptol;       /* residual threshold 10^-ptol (pTol) */
+  int corrflag;   /* 0 residual, 1 Davidson (default), 2 Jacobi-Davidson */
+  int precision;  /* pg_precision of the H*X products */
+  int startvec;   /* 0: start vectors given in evecs_dev; 1: PiaB + random; 2: random */
+  int refine;     /* PG_MIXED only: finish with FP64 H*X Rayleigh-Ritz on the converged vectors */
+} pg_solve_params;
+
+typedef struct {
+  int nconv;
+  int n_matvec;      /* single-vector H*x products */
+  int n_iter;        /* Davidson subspace iterations */
+  int n_restart;
+  double residual[64];   /* final |r| per root (first min(nroots,64)) */
+  double seconds;        /* wall time of the solve */
+} pg_solve_stats;
+
+/* Full eigensolve on the device: start vectors (DVR::Diagonalize,
+ * src/DVR.cpp:405-453), the Davidson driver loop (DVR::davdriver,
+ * src/davdriver.cpp:28-96) with block H*X products.  evecs_dev: nroots*N
+ * doubles (in: start vectors when startvec == 0; out: eigenvectors).
+ * evals_host: nroots. */
+pg_status pg_solve(const pg_grid* g, const double* v_dev, const pg_solve_params* p, double* evals_host,
+                   double* evecs_dev, pg_solve_stats* stats, void* stream);
+
+/* Whole single point from host data: water coordinates (Angstrom, 9 per
+ * water) and optional ions (x,y,z in Angstrom, q) -> site tables (host),
+ * V(r) (device), eigensolve (device) -> eigenvalues and, if evecs_host is
+ * not NULL, eigenvectors (nroots*N) copied back.  The reference's
+ * ClusterAnion::EnergyFromConfiguration (src/ClusterAnion.cpp:192-290)
+ * binding-energy part. */
+pg_status pg_cluster_solve(const int n[3], const double L[3], int nw, const double* waters_angstrom, int nions,
+                           const double* ions_angstrom_q, const pg_solve_params* p, double* evals_host,
+                           double* evecs_host, pg_solve_stats* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -222,7 +222,8 @@ def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, 
     """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration."""
     if not have_reference():
         raise FileNotFoundError(REF_BIN)
-    with tempfile.TemporaryDirectory() as td:
+    os.makedirs(os.path.join(HERE, "_ref", "tmp"), exist_ok=True)
+    with tempfile.TemporaryDirectory(dir=os.path.join(HERE, "_ref", "tmp")) as td:
         inp = os.path.join(td, "in.txt")
         out = os.path.join(td, "out.rec")
         lines = [f"grid {n[0]} {n[1]} {n[2]} {L[0]!r} {L[1]!r} {L[2]!r}",

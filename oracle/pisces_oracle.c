@@ -10,6 +10,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <stdio.h>
 
 /* The reference's own value of pi, truncated to 15 digits
  * (src/sine_dvr.cpp:24, src/constants.h:4); the kinetic matrix and the
@@ -647,6 +648,11 @@ int or_davidson(or_davidson_state* st, int ndim, int maxsub, int nroots, int max
       or_gemv(N, m, Z, V + (long)r * maxsub, rv);
       or_axpy(N, -sse[r], ritz + (long)r * N, rv);
       st->residuals[r] = or_nrm2(N, rv);
+    }
+    if (getenv("ORACLE_TRACE")) { /* iteration trace, as the reference prints at verbose > 1 (:262-267) */
+      fprintf(stderr, "%3d", m);
+      for (int r = 0; r < nroots; ++r) fprintf(stderr, "  %16.12f %10.3e", sse[r], st->residuals[r]);
+      fprintf(stderr, "  nconv=%d\n", *nconv);
     }
     /* convergence and locking (:272-297) */
     int newly = 0;

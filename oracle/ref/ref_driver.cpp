@@ -159,10 +159,20 @@ int main(int argc, char** argv) {
   const int nW = (int)in.waters.size() / 9;
   double t_pot = 0;
   if (in.spherical_k >= 0) {
+    // DVR::ComputePotential cannot take this model: it asks every Potential
+    // for five energy parts (src/DVR.cpp:767-768), SetupSphericalPotential
+    // never sets that count, and ReportEnergies exits
+    // (src/Potential.cpp:1897-1900).  Sample Potential::Evaluate directly,
+    // in the same point order (x fastest).
     double pp[3] = {0, 0, in.spherical_k};
     Vel.SetupSphericalPotential(pp);
     auto t0 = std::chrono::steady_clock::now();
-    Hel.ComputePotential(Vel);
+    for (int k = 0; k < in.n[2]; ++k)
+      for (int j = 0; j < in.n[1]; ++j)
+        for (int i = 0; i < in.n[0]; ++i) {
+          double q[3] = {Hel.x_dvr[i], Hel.x_dvr[Hel.max1db[0] + j], Hel.x_dvr[Hel.max1db[0] + Hel.max1db[1] + k]};
+          Hel.v_diag[i + in.n[0] * (j + in.n[1] * k)] = Vel.Evaluate(q);
+        }
     t_pot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   } else if (nW > 0) {
     // src/ClusterAnion.cpp:104-106, 84-88, 204-206: structure in Angstrom,
@@ -223,6 +233,9 @@ int main(int argc, char** argv) {
     double pp[2] = {2.9, 1.0};
     Potential Vion;
     Vion.SetVerbose(0);
+    // SetupBloomfield stores its model flag in PotFlags[0] (src/NaCl.cpp:264)
+    // without sizing the vector; give it its one element first.
+    Vion.PotFlags.resize(1);
     Vion.SetupBloomfield(nI, ipos.data(), nI, iq.data(), isite.data(), pp);
     put("ion_sites", ipos.data(), ipos.size());
     put("ion_charges", iq.data(), iq.size());

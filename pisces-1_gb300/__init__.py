@@ -1,0 +1,351 @@
+"""pisces_gb300 -- Python front end of libpisces_gb300.so (the GB300 eigensolve path).
+
+Thin ctypes layer over the C ABI declared in include/pisces_gb300.h.  Device
+arrays are torch CUDA tensors (float64, contiguous); host arrays are numpy.
+There is no CPU fallback: if the library is missing or no GPU is present the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpisces_gb300.so")
+
+PG_OK, PG_BAD_ARG, PG_OOM, PG_NOT_CONVERGED, PG_DEVICE_TIMEOUT, PG_NUMERIC, PG_CUDA, PG_UNSUPPORTED = range(8)
+PG_FP64, PG_MIXED = 0, 1
+_STATUS = {0: "ok", 1: "bad argument", 2: "out of memory", 3: "not converged", 4: "device timeout", 5: "numeric",
+           6: "cuda error", 7: "unsupported"}
+
+
+class PiscesError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class NotConverged(PiscesError):
+    pass
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+
+class Sites(C.Structure):
+    """pg_sites: the electron-site lists (host pointers)."""
+    _fields_ = [("nsites", C.c_int), ("sites", _dp),
+                ("ncharges", C.c_int), ("charges", _dp), ("charge_site", _ip),
+                ("ndipoles", C.c_int), ("dipoles", _dp), ("dipole_site", _ip),
+                ("nsto", C.c_int), ("sto", _dp), ("sto_site", _ip),
+                ("npol", C.c_int), ("pol_alpha", _dp), ("pol_site", _ip),
+                ("charge_damp", C.c_double), ("dipole_damp", C.c_double), ("pol_damp", C.c_double)]
+
+
+class SolveParams(C.Structure):
+    _fields_ = [("nroots", C.c_int), ("maxsub", C.c_int), ("maxiter", C.c_int), ("ptol", C.c_int),
+                ("corrflag", C.c_int), ("precision", C.c_int), ("startvec", C.c_int), ("refine", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("nconv", C.c_int), ("n_matvec", C.c_int), ("n_iter", C.c_int), ("n_restart", C.c_int),
+                ("residual", C.c_double * 64), ("seconds", C.c_double)]
+
+    def as_dict(self, nroots):
+        return {"nconv": self.nconv, "n_matvec": self.n_matvec, "n_iter": self.n_iter, "n_restart": self.n_restart,
+                "residual": list(self.residual[:nroots]), "seconds": self.seconds}
+
+
+_lib = None
+
+# exported C-ABI symbols (also checked by the CPU tests against the header)
+SYMBOLS = {
+    "pg_last_error": (C.c_char_p, []),
+    "pg_version": (C.c_int, []),
+    "pg_kernel_launches": (C.c_long, []),
+    "pg_sine_dvr": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
+    "pg_grid_create": (C.c_int, [_ip, _dp, C.POINTER(_vp)]),
+    "pg_grid_destroy": (C.c_int, [_vp]),
+    "pg_grid_npoints": (C.c_long, [_vp]),
+    "pg_grid_points": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "pg_grid_kinetic": (C.c_int, [_vp, C.c_int, _dp]),
+    "pg_diagonal": (C.c_int, [_vp, _vp, _vp, _vp]),
+    "pg_piab_start": (C.c_int, [_vp, _vp, _vp]),
+    "pg_potential_eval": (C.c_int, [_vp, C.POINTER(Sites), _vp, _vp, _vp]),
+    "pg_potential_ions_add": (C.c_int, [_vp, C.c_int, _dp, _dp, C.c_double, C.c_double, _vp, _vp]),
+    "pg_potential_spherical": (C.c_int, [_vp, C.c_double, _vp, _vp]),
+    "pg_water_sites": (C.c_int, [C.c_int, _dp, _dp, _dp, _ip, _dp, _ip, _ip]),
+    "pg_water_default_tables": (C.c_int, [C.c_int, _dp, _dp, _ip, _dp, _ip, _dp, _ip, _dp, _ip, C.POINTER(Sites)]),
+    "pg_hx": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "pg_davidson_create": (C.c_int, [C.POINTER(_vp)]),
+    "pg_davidson_destroy": (C.c_int, [_vp]),
+    "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    "pg_davidson_rci": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
+                                  _vp, _vp, _ip, _ip, _vp]),
+    "pg_solve": (C.c_int, [_vp, _vp, C.POINTER(SolveParams), _dp, _vp, C.POINTER(SolveStats), _vp]),
+    "pg_cluster_solve": (C.c_int, [_ip, _dp, C.c_int, _dp, C.c_int, _dp, C.POINTER(SolveParams), _dp, _dp,
+                                   C.POINTER(SolveStats), _vp]),
+    "pg_glibc_rand_check": (C.c_int, [C.c_int, _ip]),
+}
+
+
+def lib():
+    """Load libpisces_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise PiscesError(PG_UNSUPPORTED, f"{LIB_PATH} is missing: build it with pisces-1_gb300/build.py")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SYMBOLS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status):
+    if status != PG_OK:
+        msg = lib().pg_last_error().decode(errors="replace")
+        if status == PG_NOT_CONVERGED:
+            raise NotConverged(status, msg)
+        raise PiscesError(status, msg)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _dev(t):
+    """Device pointer of a contiguous float64 CUDA tensor."""
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise TypeError("expected a contiguous float64 CUDA tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return C.c_void_p(int(stream))
+
+
+def sine_dvr(n, L, mu=1.0, packed=True):
+    """1-D sine DVR on (-L/2, L/2): grid points and kinetic matrix (packed or full)."""
+    x = np.empty(n)
+    t = np.empty(n * (n + 1) // 2 if packed else n * n)
+    _check(lib().pg_sine_dvr(n, mu, -0.5 * L, 0.5 * L, _d(x), _d(t), 0 if packed else n))
+    return x, (t if packed else t.reshape(n, n))
+
+
+class WaterTables:
+    """Default electron-water model tables built from water coordinates (Angstrom)."""
+
+    def __init__(self, waters_angstrom):
+        w = np.ascontiguousarray(waters_angstrom, dtype=np.float64).reshape(-1)
+        nw = len(w) // 9
+        if nw * 9 != len(w) or nw == 0:
+            raise ValueError("waters must be n x 9 Angstrom coordinates")
+        self.nw = nw
+        self.waters = w
+        self.sites = np.empty(12 * nw)
+        self.charges = np.empty(3 * nw)
+        self.charge_site = np.empty(3 * nw, dtype=np.int32)
+        self.dipoles = np.empty(9 * nw)
+        self.dipole_site = np.empty(3 * nw, dtype=np.int32)
+        it = C.c_int(0)
+        _check(lib().pg_water_sites(nw, _d(w), _d(self.sites), _d(self.charges), _i(self.charge_site),
+                                    _d(self.dipoles), _i(self.dipole_site), C.byref(it)))
+        self.scf_iters = it.value
+        self.sto = np.empty(8 * nw)
+        self.sto_site = np.empty(4 * nw, dtype=np.int32)
+        self.pol_alpha = np.empty(nw)
+        self.pol_site = np.empty(nw, dtype=np.int32)
+        self.table = Sites()
+        _check(lib().pg_water_default_tables(nw, _d(self.sites), _d(self.charges), _i(self.charge_site),
+                                             _d(self.dipoles), _i(self.dipole_site), _d(self.sto), _i(self.sto_site),
+                                             _d(self.pol_alpha), _i(self.pol_site), C.byref(self.table)))
+
+    @classmethod
+    def from_lists(cls, sites, charges, charge_site, dipoles, dipole_site):
+        """Tables from site lists produced elsewhere (e.g. by the reference)."""
+        self = cls.__new__(cls)
+        self.sites = np.ascontiguousarray(sites, dtype=np.float64)
+        nw = len(self.sites) // 12
+        self.nw = nw
+        self.charges = np.ascontiguousarray(charges, dtype=np.float64)
+        self.charge_site = np.ascontiguousarray(charge_site, dtype=np.int32)
+        self.dipoles = np.ascontiguousarray(dipoles, dtype=np.float64)
+        self.dipole_site = np.ascontiguousarray(dipole_site, dtype=np.int32)
+        self.scf_iters = None
+        self.sto = np.empty(8 * nw)
+        self.sto_site = np.empty(4 * nw, dtype=np.int32)
+        self.pol_alpha = np.empty(nw)
+        self.pol_site = np.empty(nw, dtype=np.int32)
+        self.table = Sites()
+        _check(lib().pg_water_default_tables(nw, _d(self.sites), _d(self.charges), _i(self.charge_site),
+                                             _d(self.dipoles), _i(self.dipole_site), _d(self.sto), _i(self.sto_site),
+                                             _d(self.pol_alpha), _i(self.pol_site), C.byref(self.table)))
+        return self
+
+
+class Grid:
+    """3-D sine-DVR grid on the current CUDA device (pg_grid)."""
+
+    def __init__(self, n, L):
+        n = np.ascontiguousarray(n, dtype=np.int32)
+        L = np.ascontiguousarray(L, dtype=np.float64)
+        h = _vp()
+        _check(lib().pg_grid_create(_i(n), _d(L), C.byref(h)))
+        self._h = h
+        self.n = tuple(int(v) for v in n)
+        self.L = tuple(float(v) for v in L)
+        self.N = int(lib().pg_grid_npoints(h))
+
+    def close(self):
+        if self._h:
+            lib().pg_grid_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def points(self):
+        xs = [np.empty(m) for m in self.n]
+        _check(lib().pg_grid_points(self._h, _d(xs[0]), _d(xs[1]), _d(xs[2])))
+        return xs
+
+    def kinetic(self, axis):
+        t = np.empty((self.n[axis], self.n[axis]))
+        _check(lib().pg_grid_kinetic(self._h, axis, _d(t)))
+        return t
+
+    def _new(self, count=1):
+        import torch
+        return torch.empty(count * self.N, dtype=torch.float64, device="cuda")
+
+    def potential(self, tables: WaterTables, parts=False, stream=None):
+        v = self._new()
+        p = self._new(4) if parts else None
+        _check(lib().pg_potential_eval(self._h, C.byref(tables.table), _dev(v), _dev(p) if parts else None,
+                                       _stream(stream)))
+        return (v, p.view(4, self.N)) if parts else v
+
+    def add_ions(self, v, pos_bohr, q, r_cation=2.9, r_anion=1.0, stream=None):
+        pos = np.ascontiguousarray(pos_bohr, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        _check(lib().pg_potential_ions_add(self._h, len(q), _d(pos), _d(q), r_cation, r_anion, _dev(v),
+                                           _stream(stream)))
+        return v
+
+    def spherical(self, k, stream=None):
+        v = self._new()
+        _check(lib().pg_potential_spherical(self._h, float(k), _dev(v), _stream(stream)))
+        return v
+
+    def diagonal(self, v, stream=None):
+        d = self._new()
+        _check(lib().pg_diagonal(self._h, _dev(v), _dev(d), _stream(stream)))
+        return d
+
+    def piab(self, stream=None):
+        w = self._new()
+        _check(lib().pg_piab_start(self._h, _dev(w), _stream(stream)))
+        return w
+
+    def hx(self, v, X, nvec=None, precision=PG_FP64, out=None, stream=None):
+        nvec = X.numel() // self.N if nvec is None else nvec
+        Y = self._new(nvec) if out is None else out
+        _check(lib().pg_hx(self._h, _dev(v), _dev(X), _dev(Y), nvec, precision, _stream(stream)))
+        return Y
+
+    def solve(self, v, nroots=1, maxsub=20, maxiter=100, ptol=5, corrflag=1, precision=PG_FP64, startvec=1,
+              refine=1, start=None, stream=None, raise_on_nonconv=True):
+        """Device Davidson eigensolve; returns (evals, evecs[nroots, N] on the device, stats dict)."""
+        import torch
+        p = SolveParams(nroots, maxsub, maxiter, ptol, corrflag, precision, 0 if start is not None else startvec,
+                        refine)
+        ev = np.zeros(nroots)
+        vec = torch.empty(nroots * self.N, dtype=torch.float64, device="cuda")
+        if start is not None:
+            vec.copy_(start.reshape(-1))
+        st = SolveStats()
+        s = lib().pg_solve(self._h, _dev(v), C.byref(p), _d(ev), _dev(vec), C.byref(st), _stream(stream))
+        if s != PG_OK and (s != PG_NOT_CONVERGED or raise_on_nonconv):
+            _check(s)
+        return ev, vec.view(nroots, self.N), st.as_dict(nroots)
+
+
+class Davidson:
+    """Reverse-communication Davidson (pg_davidson_rci), the drop-in for the
+    reference's Davidson() with a caller-owned state instead of statics."""
+
+    def __init__(self):
+        h = _vp()
+        _check(lib().pg_davidson_create(C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().pg_davidson_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def work_size(ndim, maxsub, nroots, corrflag):
+        return int(lib().pg_davidson_work_size(ndim, maxsub, nroots, corrflag))
+
+    def step(self, ndim, maxsub, nroots, maxmacro, tol, corrflag, evals, nconv, B, Z, diag, work, inout,
+             stream=None):
+        """One call: returns (status, ret) with ret as the reference's return code."""
+        ret = C.c_int(0)
+        s = lib().pg_davidson_rci(self._h, ndim, maxsub, nroots, maxmacro, tol, corrflag, _d(evals), C.byref(nconv),
+                                  _dev(B), _dev(Z), _dev(diag), _dev(work), _i(inout), C.byref(ret), _stream(stream))
+        return s, ret.value
+
+
+def cluster_solve(n, L, waters_angstrom, ions=None, nroots=1, maxsub=20, maxiter=100, ptol=5, corrflag=1,
+                  precision=PG_FP64, startvec=1, refine=1, want_vectors=True, stream=None):
+    """Whole single point from host data (pg_cluster_solve): eigenvalues (and vectors) on the host."""
+    n = np.ascontiguousarray(n, dtype=np.int32)
+    L = np.ascontiguousarray(L, dtype=np.float64)
+    w = np.ascontiguousarray(waters_angstrom, dtype=np.float64).reshape(-1)
+    io = np.ascontiguousarray(ions if ions is not None else np.zeros((0, 4)), dtype=np.float64).reshape(-1)
+    N = int(np.prod(n))
+    ev = np.zeros(nroots)
+    vec = np.empty(nroots * N) if want_vectors else None
+    p = SolveParams(nroots, maxsub, maxiter, ptol, corrflag, precision, startvec, refine)
+    st = SolveStats()
+    s = lib().pg_cluster_solve(_i(n), _d(L), len(w) // 9, _d(w), len(io) // 4, _d(io) if len(io) else None,
+                               C.byref(p), _d(ev), _d(vec) if want_vectors else None, C.byref(st),
+                               _stream(stream) if stream is not None else None)
+    _check(s)
+    return ev, (vec.reshape(nroots, N) if want_vectors else None), st.as_dict(nroots)
+
+
+def glibc_rand_stream(count):
+    """The library's restatement of the C library rand() sequence after srand(1)."""
+    out = np.empty(count, dtype=np.int32)
+    lib().pg_glibc_rand_check(count, _i(out))
+    return out

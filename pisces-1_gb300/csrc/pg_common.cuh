@@ -1,0 +1,98 @@
+// Shared helpers of libpisces_gb300: status/error text, CUDA checks, grid handle.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "pisces_gb300.h"
+
+namespace pg {
+
+// Last error text, per calling thread.
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define PG_CUDA_TRY(expr)                                                                  \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      ::pg::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
+      return PG_CUDA;                                                                      \
+    }                                                                                      \
+  } while (0)
+
+#define PG_TRY(expr)                  \
+  do {                                \
+    pg_status s_ = (expr);            \
+    if (s_ != PG_OK) return s_;       \
+  } while (0)
+
+#define PG_ARG(cond, ...)             \
+  do {                                \
+    if (!(cond)) {                    \
+      ::pg::set_error(__VA_ARGS__);   \
+      return PG_BAD_ARG;              \
+    }                                 \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Kernel launches issued by this library (every launch site calls check_launch).
+void count_launch();
+
+// Launch-status check after a kernel launch.
+inline pg_status check_launch(const char* what) {
+  count_launch();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("launch of %s failed: %s", what, cudaGetErrorString(e));
+    return PG_CUDA;
+  }
+  return PG_OK;
+}
+
+// Device buffer owned by RAII (cudaMalloc/cudaFree).
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  pg_status alloc(size_t count) {
+    release();
+    if (count == 0) return PG_OK;
+    if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      set_error("cudaMalloc of %zu bytes failed", count * sizeof(T));
+      return PG_OOM;
+    }
+    n = count;
+    return PG_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+}  // namespace pg
+
+// The grid handle: sizes, host copies of the 1-D data and device kinetic matrices.
+struct pg_grid {
+  int n[3];
+  double L[3];
+  long N;
+  int device;
+  std::vector<double> x[3];        // grid points per axis
+  std::vector<double> t[3];        // full symmetric kinetic matrices, n x n row-major (host)
+  pg::DevBuf<double> t_dev[3];     // same, FP64, on the device
+  pg::DevBuf<float> t_hi[3];       // TF32-rounded high part (stored as fp32)
+  pg::DevBuf<float> t_lo[3];       // TF32-rounded remainder T - hi
+  pg::DevBuf<double> x_dev[3];     // grid points on the device
+};

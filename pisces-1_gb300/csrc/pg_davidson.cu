@@ -1,0 +1,581 @@
+// Reverse-communication Davidson on the device, the driver loop, and the
+// whole single point from host data.
+//
+// pg_davidson_rci restates the reference algorithm of Davidson()
+// (src/Davidson.cpp:61-376) step for step -- same subspace growth, restart
+// rule, locking weight, correction vectors and return protocol -- with every
+// O(N) operation a device kernel (pg_linalg.cu) and only O(maxsub^2) data on
+// the host: the subspace matrix S, its eigenvectors and the convergence
+// bookkeeping.  Differences that do not change the subspace:
+//   - S = Z^T B is extended by its new columns only (the reference recomputes
+//     all of it each iteration, src/Davidson.cpp:220, 385-393; the values it
+//     reads -- the upper triangle -- are the same dot products);
+//   - a correction vector is orthogonalised against the basis by block
+//     classical Gram-Schmidt run twice (c = B^T v, v -= B c, twice, then
+//     normalise), where the reference projects and renormalises against one
+//     basis vector at a time, twice each (src/Davidson.cpp:447-474); both
+//     produce the normalised component of v orthogonal to span(B);
+//   - the subspace eigenproblem uses a cyclic Jacobi solver (LAPACK dsyev in
+//     the reference, src/Davidson.cpp:224) on the same upper triangle.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pg_linalg.cuh"
+
+struct pg_davidson {
+  int status = 0;
+  int jmacro = 0, nsub = 0, nnewB = 0, nnewZ = 0;
+  int s_valid = 0;  // columns of S that hold Z^T B of the current basis
+  int ndim = 0, maxsub = 0, nroots = 0;
+  double thresh = 0;
+  std::vector<double> S, V, sse, residuals, conv_w;
+  std::vector<int> ccode, bindex;
+  pg::RedScratch rs;
+  pg::DevBuf<double> dcoef;  // maxsub * maxsub coefficients / Gram blocks
+  pg::DevBuf<double> dsq;    // squared norms / scalars (4 * maxsub)
+  // counters for the solve statistics
+  long n_iter = 0, n_restart = 0;
+};
+
+namespace pg {
+
+namespace {
+
+constexpr int kT = 256;
+
+int blocks_for(long N) {
+  long b = (N + kT - 1) / kT;
+  return (int)(b < 152L * 8 ? (b > 0 ? b : 1) : 152L * 8);
+}
+
+// ritz_r = U_r / |U_r|;  res_r = W_r - lambda_r ritz_r   (src/Davidson.cpp:240-260)
+__global__ void k_ritz_residual(long N, int nr, double* __restrict__ U, double* __restrict__ W,
+                                const double* __restrict__ usq, const double* __restrict__ lam) {
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x)
+    for (int r = 0; r < nr; ++r) {
+      const double u = U[(long)r * N + g] * (1.0 / sqrt(usq[r]));
+      U[(long)r * N + g] = u;
+      W[(long)r * N + g] = W[(long)r * N + g] + (-lam[r]) * u;
+    }
+}
+
+// Davidson correction (lambda - diag H)^-1 r with the 1e-12 floor
+// (DavidsonCorrectionVector, src/Davidson.cpp:557-566).
+__global__ void k_precond(long N, double* __restrict__ r, const double* __restrict__ diag, double lambda) {
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
+    double d = lambda - diag[g];
+    if (fabs(d) < 1e-12) d = 1e-12;
+    r[g] /= d;
+  }
+}
+
+// First half of the zeroth-order Jacobi-Davidson correction
+// (src/Davidson.cpp:537-545): r <- -M r, jd <- M u, M = (diag H - lambda)^-1.
+__global__ void k_jd_prep(long N, double* __restrict__ r, double* __restrict__ jd, const double* __restrict__ u,
+                          const double* __restrict__ diag, double lambda) {
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
+    double m = diag[g] - lambda;
+    if (fabs(m) < 1e-12) m = 1e-12;
+    m = 1.0 / m;
+    r[g] *= -m;
+    jd[g] = m * u[g];
+  }
+}
+
+// r += f jd with f = dots[0] / dots[1]  (src/Davidson.cpp:547-548)
+__global__ void k_jd_finish(long N, double* __restrict__ r, const double* __restrict__ jd,
+                            const double* __restrict__ dots) {
+  const double f = dots[0] / dots[1];
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x)
+    r[g] += f * jd[g];
+}
+
+// Cyclic Jacobi on the upper triangle of the m x m matrix S (leading
+// dimension ld); eigenvalues ascending into w, eigenvectors into V (ld).
+bool small_syev(int m, const double* S, int ld, double* w, double* V) {
+  std::vector<double> a((size_t)m * m);
+  for (int j = 0; j < m; ++j)
+    for (int i = 0; i <= j; ++i) a[i + (size_t)j * m] = a[j + (size_t)i * m] = S[i + (size_t)j * ld];
+  std::vector<double> v((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) v[i + (size_t)i * m] = 1.0;
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0, tot = 0;
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) {
+        const double e = a[i + (size_t)j * m] * a[i + (size_t)j * m];
+        tot += e;
+        if (i != j) off += e;
+      }
+    if (off == 0 || off <= 1e-32 * tot) break;
+    for (int p = 0; p < m - 1; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = a[p + (size_t)q * m];
+        if (apq == 0) continue;
+        const double th = (a[q + (size_t)q * m] - a[p + (size_t)p * m]) / (2 * apq);
+        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
+        const double c = 1 / sqrt(t * t + 1), s = t * c;
+        for (int k = 0; k < m; ++k) {
+          const double akp = a[k + (size_t)p * m], akq = a[k + (size_t)q * m];
+          a[k + (size_t)p * m] = c * akp - s * akq;
+          a[k + (size_t)q * m] = s * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double apk = a[p + (size_t)k * m], aqk = a[q + (size_t)k * m];
+          a[p + (size_t)k * m] = c * apk - s * aqk;
+          a[q + (size_t)k * m] = s * apk + c * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double vkp = v[k + (size_t)p * m], vkq = v[k + (size_t)q * m];
+          v[k + (size_t)p * m] = c * vkp - s * vkq;
+          v[k + (size_t)q * m] = s * vkp + c * vkq;
+        }
+      }
+  }
+  std::vector<int> order(m);
+  for (int i = 0; i < m; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return a[x + (size_t)x * m] < a[y + (size_t)y * m]; });
+  for (int c = 0; c < m; ++c) {
+    const int o = order[c];
+    w[c] = a[o + (size_t)o * m];
+    if (!std::isfinite(w[c])) return false;
+    for (int k = 0; k < m; ++k) V[k + (size_t)c * ld] = v[k + (size_t)o * m];
+  }
+  return true;
+}
+
+}  // namespace
+}  // namespace pg
+
+extern "C" pg_status pg_davidson_create(pg_davidson** out) {
+  PG_ARG(out, "pg_davidson_create: null argument");
+  *out = new pg_davidson();
+  return PG_OK;
+}
+
+extern "C" pg_status pg_davidson_destroy(pg_davidson* d) {
+  delete d;
+  return PG_OK;
+}
+
+extern "C" long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag) {
+  // DavidsonWorkSize (src/Davidson.cpp:46-52); same layout of the work array.
+  if (corrflag == 2) return 2L * maxsub * maxsub + 11L * maxsub + (2L * nroots + 1) * ndim;
+  return 2L * maxsub * maxsub + 11L * maxsub + 2L * nroots * ndim;
+}
+
+namespace pg {
+namespace {
+
+pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
+  if (d->ndim == ndim && d->maxsub >= maxsub && d->nroots >= nroots && d->dcoef.p) return PG_OK;
+  PG_TRY(d->dcoef.alloc((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
+  PG_TRY(d->dsq.alloc((size_t)4 * std::max(maxsub, 16)));
+  d->ndim = ndim;
+  d->maxsub = maxsub;
+  d->nroots = nroots;
+  return PG_OK;
+}
+
+// The one combine that must keep X: v <- 1*v - B c.
+pg_status cgs_pass(pg_davidson* d, long N, const double* B, int nbas, double* vec, cudaStream_t st) {
+  double* c = d->dcoef.p;
+  double* one = d->dsq.p + 3 * std::max(d->maxsub, 16);
+  PG_TRY(gram(N, B, nbas, vec, 1, c, d->rs, st));
+  PG_TRY(combine(N, B, nbas, c, nbas, -1.0, vec, one, false, vec, 1, nullptr, d->rs, st));
+  return PG_OK;
+}
+
+pg_status orthonormalise(pg_davidson* d, long N, double* vec, const double* B, int nbas, double* out,
+                         cudaStream_t st) {
+  if (nbas > 0) {
+    PG_TRY(cgs_pass(d, N, B, nbas, vec, st));
+    PG_TRY(cgs_pass(d, N, B, nbas, vec, st));
+  }
+  double* sq = d->dsq.p;
+  PG_TRY(sqnorms(N, vec, 1, sq, d->rs, st));
+  PG_TRY(combine(N, nullptr, 0, nullptr, 1, 0.0, vec, sq, true, out, 1, nullptr, d->rs, st));
+  return PG_OK;
+}
+
+}  // namespace
+}  // namespace pg
+
+extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int nroots, int maxmacro, int tol,
+                                     int corrflag, double* evals, int* nconv, double* B, double* Z,
+                                     const double* diag, double* work, int* inout, int* ret, void* stream) {
+  using namespace pg;
+  PG_ARG(d && evals && nconv && B && Z && diag && work && inout && ret, "pg_davidson_rci: null argument");
+  PG_ARG(ndim > 0 && nroots > 0 && maxsub > nroots && maxsub <= 128 && nroots <= kMaxCombine,
+         "pg_davidson_rci: need 0 < nroots <= %d, nroots < maxsub <= 128 (ndim=%d maxsub=%d nroots=%d)",
+         kMaxCombine, ndim, maxsub, nroots);
+  cudaStream_t st = as_stream(stream);
+  const long N = ndim;
+  const int ms = maxsub;
+  // device work-array layout (src/Davidson.cpp:181-187); S and V live on the host
+  double* ritz = work + 2L * ms * ms + 11L * ms;
+  double* res = ritz + N * nroots;
+  double* jd = res + N * nroots;
+  if (corrflag < 0 || corrflag > 2) corrflag = 1;
+
+  if (d->status == 0) {  // first call (src/Davidson.cpp:145-193)
+    PG_TRY(ensure_scratch(d, ndim, maxsub, nroots));
+    d->jmacro = 1;
+    d->nsub = 0;
+    d->nnewB = nroots;
+    d->s_valid = 0;
+    d->thresh = pow(10.0, -tol);
+    d->S.assign((size_t)ms * ms, 0.0);
+    d->V.assign((size_t)ms * ms, 0.0);
+    d->sse.assign(ms, 0.0);
+    d->residuals.assign(nroots, 0.0);
+    d->conv_w.assign(nroots, 0.0);
+    d->ccode.assign(nroots, 0);
+    d->bindex.assign(nroots, 0);
+    d->n_iter = d->n_restart = 0;
+    const double one = 1.0;
+    PG_CUDA_TRY(cudaMemcpyAsync(d->dsq.p + 3 * std::max(d->maxsub, 16), &one, sizeof(double),
+                                cudaMemcpyHostToDevice, st));
+    // orthonormalise the start vectors (GramSchmidt, src/Davidson.cpp:482-514)
+    for (int i = 0; i < nroots; ++i) PG_TRY(orthonormalise(d, N, B + i * N, B, i, B + i * N, st));
+    d->status = 1;
+  }
+  PG_ARG(d->status == 1 && d->ndim == ndim, "pg_davidson_rci: state does not match this problem");
+
+  for (;;) {
+    if (d->nnewB > 0) {  // hand the new block to the caller (src/Davidson.cpp:209-217)
+      inout[0] = d->nsub;
+      inout[1] = d->nsub;
+      inout[2] = d->nnewB;
+      d->nnewZ = d->nnewB;
+      d->nnewB = 0;
+      *ret = 1;
+      return PG_OK;
+    }
+    d->n_iter++;
+    const int m = d->nsub + d->nnewZ;
+    // new columns of S = Z^T B (upper triangle is what the eigensolver reads)
+    {
+      const int c0 = d->s_valid;
+      const int nc = m - c0;
+      const int per = std::max(1, kMaxGramOut / m);
+      for (int cb = 0; cb < nc; cb += per) {
+        const int k = std::min(per, nc - cb);
+        PG_TRY(gram(N, Z, m, B + (long)(c0 + cb) * N, k, d->dcoef.p + (size_t)cb * m, d->rs, st));
+      }
+      std::vector<double> cols((size_t)m * nc);
+      PG_CUDA_TRY(cudaMemcpyAsync(cols.data(), d->dcoef.p, sizeof(double) * m * nc, cudaMemcpyDeviceToHost, st));
+      PG_CUDA_TRY(cudaStreamSynchronize(st));
+      // gram output is [a*nb + b] per chunk: a = Z column i, b = new B column
+      for (int cb = 0; cb < nc; cb += per) {
+        const int k = std::min(per, nc - cb);
+        const double* blk = cols.data() + (size_t)cb * m;
+        for (int i = 0; i < m; ++i)
+          for (int b = 0; b < k; ++b) d->S[i + (size_t)(c0 + cb + b) * ms] = blk[(size_t)i * k + b];
+      }
+      d->s_valid = m;
+    }
+    d->nsub = m;
+    if (!small_syev(m, d->S.data(), ms, d->sse.data(), d->V.data())) {
+      set_error("pg_davidson_rci: subspace eigensolve produced a non-finite value");
+      d->status = 0;
+      return PG_NUMERIC;
+    }
+    // overlap of each root with the converged space (src/Davidson.cpp:229-237)
+    for (int r = 0; r < nroots; ++r) {
+      double s = 0;
+      for (int c = 0; c < *nconv; ++c) s += d->V[c + (size_t)r * ms] * d->V[c + (size_t)r * ms];
+      d->conv_w[r] = *nconv > 0 ? sqrt(s) : 0.0;
+    }
+    // Ritz vectors u = B v (renormalised) and residuals Z v - lambda u
+    // (src/Davidson.cpp:240-269), all roots in one pass
+    double* dV = d->dcoef.p;
+    double* dlam = d->dsq.p + ms;
+    double* usq = d->dsq.p;
+    double* rsq = d->dsq.p + 2 * ms;
+    PG_CUDA_TRY(cudaMemcpyAsync(dV, d->V.data(), sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
+    PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->sse.data(), sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
+    PG_TRY(combine(N, B, m, dV, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st));
+    PG_TRY(combine(N, Z, m, dV, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st));
+    k_ritz_residual<<<blocks_for(N), kT, 0, st>>>(N, nroots, ritz, res, usq, dlam);
+    PG_TRY(check_launch("k_ritz_residual"));
+    PG_TRY(sqnorms(N, res, nroots, rsq, d->rs, st));
+    std::vector<double> hr(nroots);
+    PG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsq, sizeof(double) * nroots, cudaMemcpyDeviceToHost, st));
+    PG_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int r = 0; r < nroots; ++r) {
+      d->residuals[r] = sqrt(hr[r]);
+      if (!std::isfinite(d->residuals[r])) {
+        set_error("pg_davidson_rci: non-finite residual norm for root %d", r);
+        d->status = 0;
+        return PG_NUMERIC;
+      }
+    }
+    // convergence and locking (src/Davidson.cpp:272-289)
+    int newly = 0;
+    for (int r = 0; r < nroots; ++r) {
+      if (d->conv_w[r] > 0.95) {
+        d->ccode[r] = 0;
+      } else if (d->residuals[r] < d->thresh) {
+        d->ccode[r] = 1;
+        d->bindex[r] = *nconv;
+        PG_CUDA_TRY(cudaMemcpyAsync(B + (long)(*nconv) * N, ritz + (long)r * N, sizeof(double) * N,
+                                    cudaMemcpyDeviceToDevice, st));
+        *nconv += 1;
+        newly += 1;
+      } else {
+        d->ccode[r] = 2;
+      }
+    }
+    if (*nconv == nroots) {  // src/Davidson.cpp:290-297
+      memcpy(evals, d->sse.data(), sizeof(double) * nroots);
+      PG_CUDA_TRY(cudaMemcpyAsync(B, ritz, sizeof(double) * N * nroots, cudaMemcpyDeviceToDevice, st));
+      PG_CUDA_TRY(cudaStreamSynchronize(st));
+      d->status = 0;
+      *ret = 0;
+      return PG_OK;
+    }
+    // restart (src/Davidson.cpp:303-346)
+    if (d->nsub == ms || newly > 0) {
+      d->n_restart++;
+      d->nnewB = 0;
+      for (int r = 0; r < nroots; ++r)
+        if (d->ccode[r] == 2) {
+          PG_CUDA_TRY(cudaMemcpyAsync(B + (long)(d->nnewB + *nconv) * N, ritz + (long)r * N, sizeof(double) * N,
+                                      cudaMemcpyDeviceToDevice, st));
+          d->bindex[r] = *nconv + d->nnewB;
+          d->nnewB += 1;
+        }
+      // Z v of the kept vectors, built in the Ritz block (root order, as the
+      // reference does) and copied into Z as one block
+      for (int r = 0; r < nroots; ++r)
+        if (d->ccode[r] > 0) {
+          const int jz = d->bindex[r];
+          PG_TRY(combine(N, Z, d->nsub, dV + (size_t)r * ms, ms, 1.0, nullptr, nullptr, false, ritz + (long)jz * N, 1,
+                         nullptr, d->rs, st));
+        }
+      const long first = *nconv - newly;
+      const long cnt = (long)(d->nnewB + newly);
+      if (cnt > 0)
+        PG_CUDA_TRY(cudaMemcpyAsync(Z + first * N, ritz + first * N, sizeof(double) * N * cnt,
+                                    cudaMemcpyDeviceToDevice, st));
+      d->nsub = nroots;
+      d->s_valid = 0;
+      d->jmacro += 1;
+      if (d->jmacro >= maxmacro) {
+        // The reference returns 0 here with its state still set and only
+        // prints the unconverged list (src/Davidson.cpp:332-340).
+        PG_CUDA_TRY(cudaStreamSynchronize(st));
+        *ret = 0;
+        set_error("pg_davidson_rci: %d of %d roots converged after %d macro iterations", *nconv, nroots,
+                  d->jmacro);
+        d->status = 0;
+        return PG_NOT_CONVERGED;
+      }
+    }
+    // correction vectors (src/Davidson.cpp:353-371)
+    d->nnewB = 0;
+    for (int r = 0; r < nroots; ++r) {
+      if (d->nsub + d->nnewB == ms) break;
+      if (d->ccode[r] < 2) continue;
+      double* rv = res + (long)r * N;
+      if (corrflag == 1) {
+        k_precond<<<blocks_for(N), kT, 0, st>>>(N, rv, diag, d->sse[r]);
+        PG_TRY(check_launch("k_precond"));
+      } else if (corrflag == 2) {
+        k_jd_prep<<<blocks_for(N), kT, 0, st>>>(N, rv, jd, ritz + (long)r * N, diag, d->sse[r]);
+        PG_TRY(check_launch("k_jd_prep"));
+        double* dots = d->dsq.p + 2 * ms;  // (u . r, u . jd)
+        PG_TRY(gram(N, ritz + (long)r * N, 1, rv, 1, dots, d->rs, st));
+        PG_TRY(gram(N, ritz + (long)r * N, 1, jd, 1, dots + 1, d->rs, st));
+        k_jd_finish<<<blocks_for(N), kT, 0, st>>>(N, rv, jd, dots);
+        PG_TRY(check_launch("k_jd_finish"));
+      }
+      const int slot = d->nsub + d->nnewB;
+      PG_TRY(orthonormalise(d, N, rv, B, slot, B + (long)slot * N, st));
+      d->nnewB++;
+    }
+  }
+}
+
+// ----------------------------------------------------------------- driver
+
+namespace pg {
+namespace {
+
+// glibc's rand(): the additive feedback generator r[i] = r[i-3] + r[i-31]
+// seeded by a Lehmer sequence, outputs r[i] >> 1 after 310 discarded values.
+// The reference draws its random start vectors from rand() in an unseeded
+// process (seed 1, src/DVR.cpp:52-59, 440-445); this reproduces that stream.
+struct GlibcRand {
+  unsigned ring[34];
+  long pos = 34;
+  explicit GlibcRand(unsigned seed) {
+    long long v[34];
+    v[0] = seed;
+    for (int i = 1; i < 31; ++i) {
+      v[i] = (16807LL * v[i - 1]) % 2147483647LL;
+      if (v[i] < 0) v[i] += 2147483647LL;
+    }
+    for (int i = 31; i < 34; ++i) v[i] = v[i - 31];
+    for (int i = 0; i < 34; ++i) ring[i] = (unsigned)v[i];
+    for (int i = 34; i < 344; ++i) next_raw();
+  }
+  unsigned next_raw() {
+    const unsigned x = ring[(pos - 31) % 34] + ring[(pos - 3) % 34];
+    ring[pos % 34] = x;
+    ++pos;
+    return x;
+  }
+  int operator()() { return (int)(next_raw() >> 1); }
+};
+
+constexpr int kRandMax = 2147483647;
+
+pg_status start_vectors(const pg_grid* g, int nroots, int startvec, double* B, cudaStream_t st) {
+  const long N = g->N;
+  int istart = 0;
+  if (startvec == 1) {
+    PG_TRY(pg_piab_start(g, B, st));
+    istart = 1;
+  }
+  if (istart < nroots) {
+    // Randm11 (src/DVR.cpp:52-59): sign draw, then magnitude draw
+    GlibcRand rnd(1);
+    std::vector<double> h((size_t)(nroots - istart) * N);
+    for (auto& x : h) {
+      if (rnd() > kRandMax / 2) x = (double)rnd() / kRandMax;
+      else x = -(double)rnd() / kRandMax;
+    }
+    PG_CUDA_TRY(cudaMemcpyAsync(B + (long)istart * N, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice,
+                                st));
+    PG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return PG_OK;
+}
+
+}  // namespace
+}  // namespace pg
+
+extern "C" int pg_glibc_rand_check(int count, int* out) {
+  pg::GlibcRand r(1);
+  for (int i = 0; i < count; ++i) out[i] = r();
+  return 0;
+}
+
+extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_params* p, double* evals,
+                              double* evecs, pg_solve_stats* stats, void* stream) {
+  using namespace pg;
+  PG_ARG(g && v && p && evals && evecs, "pg_solve: null argument");
+  PG_ARG(p->nroots > 0 && p->maxsub > p->nroots && p->maxiter > 0 && p->ptol > 0, "pg_solve: bad parameters");
+  PG_ARG(p->precision == PG_FP64 || p->precision == PG_MIXED, "pg_solve: unknown precision");
+  PG_ARG(g->N < (1L << 31), "pg_solve: grid too large for the reverse-communication interface");
+  auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t st = as_stream(stream);
+  const long N = g->N;
+  const int ms = p->maxsub, nr = p->nroots;
+  DevBuf<double> B, Z, diag, work;
+  PG_TRY(B.alloc((size_t)ms * N));
+  PG_TRY(Z.alloc((size_t)ms * N));
+  PG_TRY(diag.alloc(N));
+  PG_TRY(work.alloc((size_t)pg_davidson_work_size((int)N, ms, nr, p->corrflag)));
+  if (p->startvec == 0)
+    PG_CUDA_TRY(cudaMemcpyAsync(B.p, evecs, sizeof(double) * N * nr, cudaMemcpyDeviceToDevice, st));
+  else
+    PG_TRY(start_vectors(g, nr, p->startvec, B.p, st));
+  PG_TRY(pg_diagonal(g, v, diag.p, st));
+  pg_davidson d;
+  int inout[3] = {0, 0, 0}, nconv = 0, ret = 1;
+  long nmv = 0;
+  pg_status s = PG_OK;
+  while (ret != 0) {  // DVR::davdriver loop (src/davdriver.cpp:58-86)
+    s = pg_davidson_rci(&d, (int)N, ms, nr, p->maxiter, p->ptol, p->corrflag, evals, &nconv, B.p, Z.p, diag.p,
+                        work.p, inout, &ret, st);
+    if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
+    if (ret == 1) {
+      // the whole block in one launch (the reference multiplies vector by vector)
+      PG_TRY(pg_hx(g, v, B.p + (long)inout[0] * N, Z.p + (long)inout[1] * N, inout[2], p->precision, st));
+      nmv += inout[2];
+    }
+  }
+  const pg_status conv_status = s;
+  if (p->precision == PG_MIXED && p->refine) {
+    // FP64 Rayleigh-Ritz on the converged vectors: Z = H B with the FP64
+    // operator, S = B^T Z, eigenpairs of S rotate the vectors.
+    PG_TRY(pg_hx(g, v, B.p, Z.p, nr, PG_FP64, st));
+    nmv += nr;
+    PG_TRY(gram(N, Z.p, nr, B.p, nr, d.dcoef.p, d.rs, st));
+    std::vector<double> S((size_t)nr * nr), w(nr), V((size_t)nr * nr);
+    PG_CUDA_TRY(cudaMemcpyAsync(S.data(), d.dcoef.p, sizeof(double) * nr * nr, cudaMemcpyDeviceToHost, st));
+    PG_CUDA_TRY(cudaStreamSynchronize(st));
+    std::vector<double> Sc((size_t)nr * nr);  // gram gives [i*nr + j] = Z_i . B_j = S(i,j)
+    for (int i = 0; i < nr; ++i)
+      for (int j = 0; j < nr; ++j) Sc[i + (size_t)j * nr] = S[(size_t)i * nr + j];
+    if (!small_syev(nr, Sc.data(), nr, w.data(), V.data())) return PG_NUMERIC;
+    PG_CUDA_TRY(cudaMemcpyAsync(d.dcoef.p, V.data(), sizeof(double) * nr * nr, cudaMemcpyHostToDevice, st));
+    PG_TRY(combine(N, B.p, nr, d.dcoef.p, nr, 1.0, nullptr, nullptr, false, evecs, nr, nullptr, d.rs, st));
+    for (int r = 0; r < nr; ++r) evals[r] = w[r];
+  } else {
+    PG_CUDA_TRY(cudaMemcpyAsync(evecs, B.p, sizeof(double) * N * nr, cudaMemcpyDeviceToDevice, st));
+  }
+  PG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (stats) {
+    memset(stats, 0, sizeof(*stats));
+    stats->nconv = nconv;
+    stats->n_matvec = (int)nmv;
+    stats->n_iter = (int)d.n_iter;
+    stats->n_restart = (int)d.n_restart;
+    for (int r = 0; r < nr && r < 64; ++r) stats->residual[r] = r < (int)d.residuals.size() ? d.residuals[r] : 0;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return conv_status;
+}
+
+extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw, const double* waters, int nions,
+                                      const double* ions, const pg_solve_params* p, double* evals, double* evecs_host,
+                                      pg_solve_stats* stats, void* stream) {
+  using namespace pg;
+  PG_ARG(n && L && p && evals && nw >= 0 && nions >= 0, "pg_cluster_solve: bad arguments");
+  PG_ARG(nw == 0 || waters, "pg_cluster_solve: null water coordinates");
+  PG_ARG(nions == 0 || ions, "pg_cluster_solve: null ion list");
+  PG_ARG(p->startvec != 0, "pg_cluster_solve: start vectors 0 need pg_solve");
+  cudaStream_t st = as_stream(stream);
+  pg_grid* g = nullptr;
+  PG_TRY(pg_grid_create(n, L, &g));
+  struct GridGuard { pg_grid* g; ~GridGuard() { pg_grid_destroy(g); } } guard{g};
+  const long N = g->N;
+  DevBuf<double> v, vec;
+  PG_TRY(v.alloc(N));
+  PG_TRY(vec.alloc((size_t)N * p->nroots));
+  if (nw > 0) {
+    std::vector<double> sites(12 * (size_t)nw), q(3 * (size_t)nw), dip(9 * (size_t)nw), sto(8 * (size_t)nw),
+        pa(nw);
+    std::vector<int> qs(3 * (size_t)nw), ds(3 * (size_t)nw), ss(4 * (size_t)nw), ps(nw);
+    int it = 0;
+    PG_TRY(pg_water_sites(nw, waters, sites.data(), q.data(), qs.data(), dip.data(), ds.data(), &it));
+    pg_sites t;
+    PG_TRY(pg_water_default_tables(nw, sites.data(), q.data(), qs.data(), dip.data(), ds.data(), sto.data(),
+                                   ss.data(), pa.data(), ps.data(), &t));
+    PG_TRY(pg_potential_eval(g, &t, v.p, nullptr, st));
+  } else {
+    PG_CUDA_TRY(cudaMemsetAsync(v.p, 0, sizeof(double) * N, st));
+  }
+  if (nions > 0) {
+    std::vector<double> pos(3 * (size_t)nions), qi(nions);
+    const double a2b = 1.0 / 0.52917720859;
+    for (int i = 0; i < nions; ++i) {
+      for (int c = 0; c < 3; ++c) pos[3 * i + c] = ions[4 * i + c] * a2b;
+      qi[i] = ions[4 * i + 3];
+    }
+    PG_TRY(pg_potential_ions_add(g, nions, pos.data(), qi.data(), 2.9, 1.0, v.p, st));
+  }
+  pg_status s = pg_solve(g, v.p, p, evals, vec.p, stats, stream);
+  if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
+  if (evecs_host)
+    PG_CUDA_TRY(cudaMemcpyAsync(evecs_host, vec.p, sizeof(double) * N * p->nroots, cudaMemcpyDeviceToHost, st));
+  PG_CUDA_TRY(cudaStreamSynchronize(st));
+  return s;
+}

@@ -1,0 +1,206 @@
+// Grid handle, sine-DVR kinetic builder, diag(H) and the particle-in-a-box
+// start vector.
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+
+#include "pg_common.cuh"
+
+namespace pg {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+const char* last_error() { return g_err; }
+
+static std::atomic<long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+// The reference defines the sine DVR with a 15-digit value of pi
+// (src/sine_dvr.cpp:24, src/constants.h:4); the kinetic matrix and the
+// particle-in-a-box start vector use it, so it is kept here.
+constexpr double kRefPi = 3.14159265358979;
+
+}  // namespace pg
+
+extern "C" const char* pg_last_error(void) { return pg::last_error(); }
+extern "C" int pg_version(void) { return 100; }
+extern "C" long pg_kernel_launches(void) { return pg::g_launches.load(); }
+
+extern "C" pg_status pg_sine_dvr(int n, double mu, double x0, double xNp1, double* x, double* ekin, int ldt) {
+  PG_ARG(n > 0 && x && ekin && mu > 0 && xNp1 > x0, "pg_sine_dvr: bad arguments");
+  PG_ARG(ldt == 0 || ldt >= n, "pg_sine_dvr: ldt must be 0 (packed) or >= n");
+  // Equidistant interior points and the analytic DVR kinetic matrix of the
+  // particle-in-a-box basis (Colbert-Miller / Light-Carrington, Phys. Rep.
+  // 324, 1 (2000) eq. B.62, B.65), term order as src/sine_dvr.cpp:47-111.
+  const double dx = (xNp1 - x0) / (double)(n + 1);
+  for (int j = 0; j < n; ++j) x[j] = x0 + dx * (double)(j + 1);
+  const double f1 = 0.5 * pg::kRefPi * pg::kRefPi / (mu * (dx * dx));
+  const double f2 = pg::kRefPi / (double)(n + 1);
+  const double f3 = (double)((n + 1) * (n + 1));
+  auto at = [&](int a, int b) -> double& {
+    return ldt > 0 ? ekin[a + (long)ldt * b] : ekin[(long)a * (a + 1) / 2 + b];
+  };
+  for (int a = 0; a < n; ++a) {
+    const double s = sin((a + 1) * f2);
+    at(a, a) = f1 * (1.0 / 3.0 + 1.0 / (6.0 * f3) - 0.5 / (f3 * (s * s)));
+  }
+  for (int a = 0; a < n; ++a)
+    for (int b = 0; b < a; ++b) {
+      const double d = cos(f2 * (a + 1)) - cos(f2 * (b + 1));
+      double v = f1 * 2.0 / f3 * sin(f2 * (a + 1)) * sin(f2 * (b + 1)) / (d * d);
+      if ((a - b) % 2 == 1) v *= -1.0;
+      at(a, b) = v;
+    }
+  if (ldt > 0)
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < a; ++b) ekin[b + (long)a * ldt] = ekin[a + (long)b * ldt];
+  return PG_OK;
+}
+
+namespace {
+
+// Round to the TF32 grid (10 explicit mantissa bits), nearest-even, as fp32.
+float to_tf32(float f) {
+  unsigned u;
+  memcpy(&u, &f, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return f;
+  const unsigned lsb = (u >> 13) & 1u;
+  u += 0xfffu + lsb;
+  u &= 0xffffe000u;
+  float r;
+  memcpy(&r, &u, 4);
+  return r;
+}
+
+__global__ void k_diagonal(int nx, int ny, int nz, const double* __restrict__ v, const double* __restrict__ tx,
+                           const double* __restrict__ ty, const double* __restrict__ tz, double* __restrict__ diag) {
+  const long N = (long)nx * ny * nz;
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(g % nx);
+    const long r = g / nx;
+    const int j = (int)(r % ny);
+    const int k = (int)(r / ny);
+    // V first, then the axis diagonals in x, y, z order (src/DVR.cpp:1811-1831).
+    double d = v[g];
+    d = __dadd_rn(d, tx[(long)i * nx + i]);
+    d = __dadd_rn(d, ty[(long)j * ny + j]);
+    d = __dadd_rn(d, tz[(long)k * nz + k]);
+    diag[g] = d;
+  }
+}
+
+__global__ void k_piab(int nx, int ny, int nz, const double* __restrict__ xs, const double* __restrict__ ys,
+                       const double* __restrict__ zs, double* __restrict__ wf) {
+  const long N = (long)nx * ny * nz;
+  const int n[3] = {nx, ny, nz};
+  const double* xa[3] = {xs, ys, zs};
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(g % nx);
+    const long r = g / nx;
+    const int idx[3] = {i, (int)(r % ny), (int)(r / ny)};
+    // Product of half-box sines, zero outside [x0/2, -x0/2] with x0 the first
+    // grid point and L the first-to-last span (src/DVR.cpp:1737-1789).
+    double w = 1;
+    for (int a = 0; a < 3; ++a) {
+      const double x0 = xa[a][0];
+      const double L = xa[a][n[a] - 1] - x0;
+      const double q = xa[a][idx[a]];
+      if (q < x0 / 2 || q > -x0 / 2) w = 0.0;
+      else w *= sin(pg::kRefPi / L * 2.0 * (q - x0 / 2.0));
+    }
+    wf[g] = w;
+  }
+}
+
+int grid_blocks(long N, int threads) {
+  long b = (N + threads - 1) / threads;
+  const long cap = 152L * 16;
+  return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+}  // namespace
+
+extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid** out) {
+  PG_ARG(n && L && out, "pg_grid_create: null argument");
+  for (int a = 0; a < 3; ++a) {
+    PG_ARG(n[a] >= 2 && n[a] <= 1024, "pg_grid_create: n[%d] = %d out of range [2, 1024]", a, n[a]);
+    PG_ARG(L[a] > 0 && std::isfinite(L[a]), "pg_grid_create: L[%d] must be positive", a);
+  }
+  PG_ARG((double)n[0] * n[1] * n[2] < 2.0e9, "pg_grid_create: too many grid points");
+  pg_grid* g = new pg_grid();
+  cudaGetDevice(&g->device);
+  g->N = 1;
+  for (int a = 0; a < 3; ++a) {
+    g->n[a] = n[a];
+    g->L[a] = L[a];
+    g->N *= n[a];
+    const int m = n[a];
+    g->x[a].resize(m);
+    g->t[a].resize((size_t)m * m);
+    pg_status s = pg_sine_dvr(m, 1.0, -0.5 * L[a], 0.5 * L[a], g->x[a].data(), g->t[a].data(), m);
+    if (s != PG_OK) { delete g; return s; }
+    std::vector<float> hi((size_t)m * m), lo((size_t)m * m);
+    for (size_t e = 0; e < hi.size(); ++e) {
+      hi[e] = to_tf32((float)g->t[a][e]);
+      lo[e] = to_tf32((float)(g->t[a][e] - (double)hi[e]));
+    }
+    if ((s = g->t_dev[a].alloc((size_t)m * m)) != PG_OK || (s = g->t_hi[a].alloc((size_t)m * m)) != PG_OK ||
+        (s = g->t_lo[a].alloc((size_t)m * m)) != PG_OK || (s = g->x_dev[a].alloc(m)) != PG_OK) {
+      delete g;
+      return s;
+    }
+    if (cudaMemcpy(g->t_dev[a].p, g->t[a].data(), sizeof(double) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->t_hi[a].p, hi.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->t_lo[a].p, lo.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->x_dev[a].p, g->x[a].data(), sizeof(double) * m, cudaMemcpyHostToDevice) != cudaSuccess) {
+      pg::set_error("pg_grid_create: upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+      delete g;
+      return PG_CUDA;
+    }
+  }
+  *out = g;
+  return PG_OK;
+}
+
+extern "C" pg_status pg_grid_destroy(pg_grid* g) {
+  delete g;
+  return PG_OK;
+}
+
+extern "C" long pg_grid_npoints(const pg_grid* g) { return g ? g->N : 0; }
+
+extern "C" pg_status pg_grid_points(const pg_grid* g, double* x, double* y, double* z) {
+  PG_ARG(g, "pg_grid_points: null grid");
+  double* o[3] = {x, y, z};
+  for (int a = 0; a < 3; ++a)
+    if (o[a]) memcpy(o[a], g->x[a].data(), sizeof(double) * g->n[a]);
+  return PG_OK;
+}
+
+extern "C" pg_status pg_grid_kinetic(const pg_grid* g, int axis, double* t) {
+  PG_ARG(g && t && axis >= 0 && axis < 3, "pg_grid_kinetic: bad arguments");
+  memcpy(t, g->t[axis].data(), sizeof(double) * g->t[axis].size());
+  return PG_OK;
+}
+
+extern "C" pg_status pg_diagonal(const pg_grid* g, const double* v, double* diag, void* stream) {
+  PG_ARG(g && v && diag, "pg_diagonal: null argument");
+  k_diagonal<<<grid_blocks(g->N, 256), 256, 0, pg::as_stream(stream)>>>(g->n[0], g->n[1], g->n[2], v, g->t_dev[0].p,
+                                                                        g->t_dev[1].p, g->t_dev[2].p, diag);
+  return pg::check_launch("k_diagonal");
+}
+
+extern "C" pg_status pg_piab_start(const pg_grid* g, double* wf, void* stream) {
+  PG_ARG(g && wf, "pg_piab_start: null argument");
+  k_piab<<<grid_blocks(g->N, 256), 256, 0, pg::as_stream(stream)>>>(g->n[0], g->n[1], g->n[2], g->x_dev[0].p,
+                                                                     g->x_dev[1].p, g->x_dev[2].p, wf);
+  return pg::check_launch("k_piab");
+}

@@ -1,0 +1,96 @@
+// Y = H X on the 3-D sine-DVR grid, FP64 form.
+//
+// H = diag(V) + Tx (+) Ty (+) Tz: for every grid point and vector,
+//   y = v x + sum_b Tx[i,b] x[b,j,k] + sum_b Ty[j,b] x[i,b,k] + sum_b Tz[k,b] x[i,j,b]
+// (src/mtx.cpp:35-104 applies the same operator line by line with dspmv).
+//
+// On GB300 the FP64 pipe retires about 1 TFLOP/s (a warp-wide DFMA every ~70
+// cycles per SM sub-partition), two orders of magnitude below the load and
+// FP32 throughput, so this form is bound by DFMA issue and the kernel is
+// organised around it: one thread owns one grid point for up to four vectors
+// (four independent accumulators), every operand load is either coalesced
+// (consecutive i across the warp: x along y and z, and Tx read as T[b][i],
+// T being symmetric) or a warp-wide broadcast (x along x, Ty, Tz), and X
+// stays in L2 between the three sweeps.  No tiling is needed to reach the
+// DFMA roofline; the mixed form (pg_hx_tc.cu) is the fast path.
+#include "pg_common.cuh"
+
+namespace {
+
+template <int NV>
+__global__ void __launch_bounds__(256) k_hx_fp64(int nx, int ny, int nz, const double* __restrict__ tx,
+                                                 const double* __restrict__ ty, const double* __restrict__ tz,
+                                                 const double* __restrict__ v, const double* __restrict__ X,
+                                                 double* __restrict__ Y, int nvec) {
+  const long N = (long)nx * ny * nz;
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int v0 = blockIdx.y * NV;
+  if (g >= N) return;
+  const int i = (int)(g % nx);
+  const long r = g / nx;
+  const int j = (int)(r % ny);
+  const int k = (int)(r / ny);
+  const int nv = nvec - v0 < NV ? nvec - v0 : NV;
+  const double* Xv = X + (long)v0 * N;
+  double acc[NV];
+  const double vg = v[g];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) acc[q] = q < nv ? vg * Xv[(long)q * N + g] : 0.0;
+  // x sweep: T[b][i] (coalesced over i), x[b,j,k] broadcast
+  {
+    const long base = (long)nx * (j + (long)ny * k);
+    for (int b = 0; b < nx; ++b) {
+      const double t = tx[(long)b * nx + i];
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+        if (q < nv) acc[q] += t * Xv[(long)q * N + base + b];
+    }
+  }
+  // y sweep: Ty[j][b] broadcast, x[i,b,k] coalesced
+  {
+    const long base = i + (long)nx * ny * k;
+    const double* trow = ty + (long)j * ny;
+    for (int b = 0; b < ny; ++b) {
+      const double t = trow[b];
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+        if (q < nv) acc[q] += t * Xv[(long)q * N + base + (long)nx * b];
+    }
+  }
+  // z sweep: Tz[k][b] broadcast, x[i,j,b] coalesced
+  {
+    const long base = i + (long)nx * j;
+    const long sz = (long)nx * ny;
+    const double* trow = tz + (long)k * nz;
+    for (int b = 0; b < nz; ++b) {
+      const double t = trow[b];
+#pragma unroll
+      for (int q = 0; q < NV; ++q)
+        if (q < nv) acc[q] += t * Xv[(long)q * N + base + sz * b];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    if (q < nv) Y[(long)(v0 + q) * N + g] = acc[q];
+}
+
+}  // namespace
+
+namespace pg {
+pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st);
+}
+
+extern "C" pg_status pg_hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
+                           void* stream) {
+  PG_ARG(g && v && x && y && nvec >= 0, "pg_hx: bad arguments");
+  PG_ARG(x != y, "pg_hx: X and Y must not alias");
+  if (nvec == 0) return PG_OK;
+  cudaStream_t st = pg::as_stream(stream);
+  if (precision == PG_MIXED) return pg::hx_mixed(g, v, x, y, nvec, st);
+  PG_ARG(precision == PG_FP64, "pg_hx: unknown precision %d", precision);
+  constexpr int NV = 4;
+  dim3 grid((unsigned)((g->N + 255) / 256), (unsigned)((nvec + NV - 1) / NV));
+  k_hx_fp64<NV><<<grid, 256, 0, st>>>(g->n[0], g->n[1], g->n[2], g->t_dev[0].p, g->t_dev[1].p, g->t_dev[2].p, v, x,
+                                     y, nvec);
+  return pg::check_launch("k_hx_fp64");
+}

@@ -1,0 +1,223 @@
+// Deterministic skinny FP64 kernels for the Davidson subspace (see pg_linalg.cuh).
+#include "pg_linalg.cuh"
+
+namespace pg {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kTP = 32;  // points per shared-memory tile in k_gram
+
+// True in exactly one block: the last to arrive.  Partial results written
+// before the call are visible to it.
+__device__ __forceinline__ bool arrive_last(unsigned* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return last;
+}
+
+long chunk_for(long N, int blocks, int align) {
+  long c = (N + blocks - 1) / blocks;
+  c = (c + align - 1) / align * align;
+  return c > 0 ? c : align;
+}
+
+__global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* __restrict__ P, int na,
+                                             const double* __restrict__ Q, int nb, double* __restrict__ partial,
+                                             unsigned* __restrict__ counter, double* __restrict__ out) {
+  extern __shared__ double sm[];
+  double* Ps = sm;                       // na x (kTP+1)
+  double* Qs = sm + na * (kTP + 1);      // nb x (kTP+1)
+  const int no = na * nb;
+  double acc[kMaxGramOut / kT];
+#pragma unroll
+  for (int s = 0; s < kMaxGramOut / kT; ++s) acc[s] = 0;
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  for (long g0 = g_begin; g0 < g_end; g0 += kTP) {
+    const int cnt = g_end - g0 < kTP ? (int)(g_end - g0) : kTP;
+    for (int e = threadIdx.x; e < na * kTP; e += kT) {
+      const int a = e / kTP, p = e % kTP;
+      Ps[a * (kTP + 1) + p] = p < cnt ? P[(long)a * N + g0 + p] : 0.0;
+    }
+    for (int e = threadIdx.x; e < nb * kTP; e += kT) {
+      const int b = e / kTP, p = e % kTP;
+      Qs[b * (kTP + 1) + p] = p < cnt ? Q[(long)b * N + g0 + p] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < kMaxGramOut / kT; ++s) {
+      const int o = threadIdx.x + s * kT;
+      if (o < no) {
+        const double* pa = Ps + (o / nb) * (kTP + 1);
+        const double* qb = Qs + (o % nb) * (kTP + 1);
+        double a = acc[s];
+        for (int p = 0; p < kTP; ++p) a += pa[p] * qb[p];
+        acc[s] = a;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int s = 0; s < kMaxGramOut / kT; ++s) {
+    const int o = threadIdx.x + s * kT;
+    if (o < no) partial[(long)blockIdx.x * no + o] = acc[s];
+  }
+  if (arrive_last(counter)) {
+    for (int o = threadIdx.x; o < no; o += kT) {
+      double s = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += partial[(long)b * no + o];
+      out[o] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double* __restrict__ P, int na,
+                                                const double* __restrict__ C, int ldc, double cscale, const double* X,
+                                                const double* __restrict__ alpha, int inv_sqrt, double* Y, int nr,
+                                                double* __restrict__ partial, unsigned* __restrict__ counter,
+                                                double* __restrict__ sq) {
+  extern __shared__ double sm[];
+  double* Cs = sm;                 // na x nr
+  __shared__ double al[kMaxCombine];
+  __shared__ double red[kT / 32][kMaxCombine];
+  for (int e = threadIdx.x; e < na * nr; e += kT) Cs[e] = cscale * C[(e / nr) + (long)(e % nr) * ldc];
+  if (threadIdx.x < nr) {
+    double a = 0;
+    if (alpha) a = inv_sqrt ? 1.0 / sqrt(alpha[threadIdx.x]) : alpha[threadIdx.x];
+    al[threadIdx.x] = a;
+  }
+  __syncthreads();
+  double sacc[kMaxCombine];
+#pragma unroll
+  for (int r = 0; r < kMaxCombine; ++r) sacc[r] = 0;
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
+    double acc[kMaxCombine];
+#pragma unroll
+    for (int r = 0; r < kMaxCombine; ++r) acc[r] = (r < nr && X && alpha) ? al[r] * X[(long)r * N + g] : 0.0;
+    for (int a = 0; a < na; ++a) {
+      const double p = P[(long)a * N + g];
+      const double* c = Cs + a * nr;
+#pragma unroll
+      for (int r = 0; r < kMaxCombine; ++r)
+        if (r < nr) acc[r] += p * c[r];
+    }
+#pragma unroll
+    for (int r = 0; r < kMaxCombine; ++r)
+      if (r < nr) {
+        Y[(long)r * N + g] = acc[r];
+        sacc[r] += acc[r] * acc[r];
+      }
+  }
+  if (!sq) return;
+  // block reduction of the squared norms (fixed order)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < kMaxCombine; ++r) {
+    double v = sacc[r];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    double s = 0;
+    for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
+    partial[(long)blockIdx.x * nr + threadIdx.x] = s;
+  }
+  if (arrive_last(counter)) {
+    if (threadIdx.x < nr) {
+      double s = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += partial[(long)b * nr + threadIdx.x];
+      sq[threadIdx.x] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_sqnorms(long N, long chunk, const double* __restrict__ X, int nr,
+                                                double* __restrict__ partial, unsigned* __restrict__ counter,
+                                                double* __restrict__ sq) {
+  __shared__ double red[kT / 32];
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = 0; r < nr; ++r) {
+    double s = 0;
+    for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
+      const double x = X[(long)r * N + g];
+      s += x * x;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int w = 0; w < kT / 32; ++w) t += red[w];
+      partial[(long)blockIdx.x * nr + r] = t;
+    }
+    __syncthreads();
+  }
+  if (arrive_last(counter)) {
+    for (int r = threadIdx.x; r < nr; r += kT) {
+      double s = 0;
+      for (unsigned b = 0; b < gridDim.x; ++b) s += partial[(long)b * nr + r];
+      sq[r] = s;
+    }
+    if (threadIdx.x == 0) *counter = 0;
+  }
+}
+
+}  // namespace
+
+pg_status RedScratch::ensure() {
+  if (!partial.p) {
+    PG_TRY(partial.alloc((size_t)kRedBlocks * kMaxGramOut));
+    PG_TRY(counter.alloc(4));
+    PG_CUDA_TRY(cudaMemset(counter.p, 0, 4 * sizeof(unsigned)));
+  }
+  return PG_OK;
+}
+
+pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs,
+               cudaStream_t st) {
+  PG_ARG(na > 0 && nb > 0 && na * nb <= kMaxGramOut, "gram: %d x %d outputs exceed %d", na, nb, kMaxGramOut);
+  PG_TRY(rs.ensure());
+  const long chunk = chunk_for(N, kRedBlocks, kTP);
+  const int blocks = (int)((N + chunk - 1) / chunk);
+  const size_t smem = sizeof(double) * (size_t)(na + nb) * (kTP + 1);
+  if (smem > 48 * 1024) PG_CUDA_TRY(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p, rs.counter.p, out);
+  return check_launch("k_gram");
+}
+
+pg_status combine(long N, const double* P, int na, const double* C, int ldc, double cscale, const double* X,
+                  const double* alpha,
+                  bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs, cudaStream_t st) {
+  PG_ARG(nr > 0 && nr <= kMaxCombine && na >= 0, "combine: bad sizes na=%d nr=%d", na, nr);
+  PG_TRY(rs.ensure());
+  const long chunk = chunk_for(N, kRedBlocks, kT);
+  const int blocks = (int)((N + chunk - 1) / chunk);
+  const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
+  if (smem > 48 * 1024)
+    PG_CUDA_TRY(cudaFuncSetAttribute(k_combine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_combine<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ldc, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, rs.partial.p,
+                                      rs.counter.p + 1, sq);
+  return check_launch("k_combine");
+}
+
+pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st) {
+  PG_ARG(nr > 0 && nr <= kMaxGramOut, "sqnorms: bad count %d", nr);
+  PG_TRY(rs.ensure());
+  const long chunk = chunk_for(N, kRedBlocks, kT);
+  const int blocks = (int)((N + chunk - 1) / chunk);
+  k_sqnorms<<<blocks, kT, 0, st>>>(N, chunk, X, nr, rs.partial.p, rs.counter.p + 2, sq);
+  return check_launch("k_sqnorms");
+}
+
+}  // namespace pg

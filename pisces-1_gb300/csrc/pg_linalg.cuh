@@ -1,0 +1,37 @@
+// Skinny FP64 linear algebra of the Davidson subspace on the device.
+//
+// Every reduction is deterministic: blocks write partial sums, and the last
+// block to finish (found with a device-scope counter) adds the partials in
+// block order.  Results therefore do not depend on scheduling, which keeps a
+// solve bit-identical whether it runs alone or next to other solves.
+#pragma once
+
+#include "pg_common.cuh"
+
+namespace pg {
+
+constexpr int kRedBlocks = 296;  // partial-sum blocks of a reduction (2 per SM on 148+ SMs)
+constexpr int kMaxGramOut = 2048;
+constexpr int kMaxCombine = 16;  // columns produced by one combine launch
+
+// Scratch for reductions; one per stream of work.
+struct RedScratch {
+  DevBuf<double> partial;     // kRedBlocks * kMaxGramOut
+  DevBuf<unsigned> counter;   // 4 independent counters, zero between launches
+  pg_status ensure();
+};
+
+// out[a*nb + b] = sum_g P[a*N + g] * Q[b*N + g]     (a < na, b < nb; na*nb <= kMaxGramOut)
+pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs, cudaStream_t st);
+
+// Y[r*N + g] = alpha_r * X[r*N + g] + cscale * sum_a P[a*N + g] * C[a + r*ldc]   (r < nr <= kMaxCombine)
+// alpha_r: 0 if alpha is null; alpha[r] if inv_sqrt is false; 1/sqrt(alpha[r]) if true.
+// X may equal Y.  If sq is not null, sq[r] = |Y_r|^2.
+pg_status combine(long N, const double* P, int na, const double* C, int ldc, double cscale, const double* X,
+                  const double* alpha,
+                  bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs, cudaStream_t st);
+
+// sq[r] = |X_r|^2 for r < nr.
+pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st);
+
+}  // namespace pg

@@ -1,0 +1,201 @@
+"""GPU parity: the CUDA path through the C ABI against the golden vectors of
+the reference CPU code and against the CPU oracle on the same inputs.
+
+Tolerances: V(r) and diag(H) 1e-13 relative to max|V| (the kernel evaluates
+the reference's expressions in its order without fused multiply-adds; exp
+may differ in the last place); FP64 H*X 1e-13 relative to max|Y|;
+eigenvalues of the FP64 path 1e-8 Eh of the reference, eigenvector overlap
+>= 1 - 1e-8.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available(), "GPU tests need a CUDA device"
+    return t
+
+
+def dev(torch, a):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("tag", ["w6", "w24"])
+def test_potential_from_reference_tables(pg, torch, tag):
+    g = golden(f"dpp_{tag}.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    t = pg.WaterTables.from_lists(g["sites"], g["charges"], g["charge_site"], g["dipoles"], g["dipole_site"])
+    v, parts = grid.potential(t, parts=True)
+    scale = np.max(np.abs(g["v"]))
+    assert np.max(np.abs(host(v) - g["v"])) / scale < 1e-13
+    for k, name in enumerate(["v_pc", "v_ind", "v_rep", "v_pol"]):
+        assert np.max(np.abs(host(parts[k]) - g[name])) / scale < 1e-13, name
+    assert rel(host(grid.diagonal(v)), g["diag"]) < 1e-13
+
+
+@pytest.mark.parametrize("tag", ["w6", "w24"])
+def test_potential_from_own_site_producer(pg, torch, tag):
+    g = golden(f"dpp_{tag}.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    v = grid.potential(pg.WaterTables(g["waters"]))
+    assert rel(host(v), g["v"]) < 1e-12
+
+
+def test_potential_ions(pg, torch):
+    g = golden("ions_small.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    v = grid.potential(pg.WaterTables(g["waters"]))
+    grid.add_ions(v, g["ion_sites"], g["ion_charges"])
+    assert rel(host(v), g["v"]) < 1e-12
+
+
+def test_potential_point_on_a_site(pg, orc, torch):
+    # a grid point exactly on a site exercises the damped branches (R < r0)
+    # and the R = 0 limits of every term (src/Potential.cpp:1191, 1252, 1357)
+    g = golden("dpp_w6.npz")
+    n, L = (9, 9, 9), (10.0, 10.0, 10.0)
+    ogrid = orc.Grid(n, L)
+    sites = np.array(g["sites"], dtype=np.float64)
+    sites[0:3] = [ogrid.x[0][4], ogrid.x[1][4], ogrid.x[2][4]]      # O of water 0 on the centre point
+    sites[12 + 9:12 + 12] = [ogrid.x[0][2], ogrid.x[1][6], ogrid.x[2][3]]  # M of water 1 on a grid point
+    ref = ogrid.potential_dpp(sites, g["charges"], g["charge_site"], g["dipoles"], g["dipole_site"])
+    assert np.all(np.isfinite(ref))
+    grid = pg.Grid(n, L)
+    t = pg.WaterTables.from_lists(sites, g["charges"], g["charge_site"], g["dipoles"], g["dipole_site"])
+    assert rel(host(grid.potential(t)), ref) < 1e-13
+
+
+def test_spherical_potential(pg, orc, torch):
+    n, L = (11, 12, 13), (12.0, 13.0, 14.0)
+    assert rel(host(pg.Grid(n, L).spherical(0.1)), orc.Grid(n, L).spherical(0.1)) < 1e-15
+
+
+@pytest.mark.parametrize("name", ["dpp_w6.npz", "dpp_w24.npz", "small_w6.npz", "ions_small.npz"])
+def test_hx_fp64_matches_reference(pg, torch, name):
+    g = golden(name)
+    grid = pg.Grid(g["n"], g["L"])
+    y = grid.hx(dev(torch, g["v"]), dev(torch, g["mv_x"]))
+    assert rel(host(y), g["mv_y"]) < 1e-13
+
+
+def test_hx_fp64_block_matches_oracle(pg, orc, torch):
+    # 7 vectors: exercises the 4-vector register groups and a ragged tail
+    n, L = (24, 20, 28), (20.0, 18.0, 22.0)
+    rng = np.random.default_rng(5)
+    v = rng.normal(size=int(np.prod(n)))
+    X = rng.normal(size=(7, int(np.prod(n))))
+    grid = pg.Grid(n, L)
+    Y = host(grid.hx(dev(torch, v), dev(torch, X))).reshape(7, -1)
+    og = orc.Grid(n, L)
+    for r in range(7):
+        assert rel(Y[r], og.matvec(v, X[r])) < 1e-13
+
+
+def test_hx_fp64_properties_at_64cubed(pg, orc, torch):
+    # full C2 grid: symmetry <x, H y> = <H x, y>, linearity, and one vector vs the oracle
+    g = golden("dpp_w24.npz")
+    n, L = (64, 64, 64), (40.0, 40.0, 40.0)
+    grid = pg.Grid(n, L)
+    v = grid.potential(pg.WaterTables(g["waters"]))
+    rng = np.random.default_rng(11)
+    X = dev(torch, rng.normal(size=(2, grid.N)))
+    Y = grid.hx(v, X).view(2, -1)
+    a = float((X[0] * Y[1]).sum())
+    b = float((Y[0] * X[1]).sum())
+    assert abs(a - b) < 1e-11 * (abs(a) + abs(b))
+    Z = grid.hx(v, (2.0 * X[0] - 3.0 * X[1]).contiguous())
+    assert float((Z - (2.0 * Y[0] - 3.0 * Y[1])).abs().max()) < 1e-11 * float(Y.abs().max())
+    og = orc.Grid(n, L)
+    assert rel(host(Y[0]), og.matvec(host(v), host(X[0]))) < 1e-13
+
+
+def test_solve_fp64_two_states(pg, torch):
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    ev, vec, st = grid.solve(dev(torch, g["v"]), nroots=2, ptol=8)
+    assert st["nconv"] == 2
+    assert np.max(np.abs(ev - g["evals"])) < 1e-8
+    W = g["wavefn"].reshape(2, -1)
+    V = host(vec)
+    for r in range(2):
+        assert abs(V[r] @ W[r]) / np.linalg.norm(V[r]) / np.linalg.norm(W[r]) > 1 - 1e-8
+
+
+def test_solve_fp64_c1(pg, torch):
+    # (H2O)6, 32^3 over 30 bohr, lowest state, from water coordinates
+    g = golden("c1.npz")
+    ev, vec, st = pg.cluster_solve(g["n"], g["L"], g["waters"], nroots=1, ptol=8)
+    assert abs(ev[0] - g["evals"][0]) < 1e-8
+    w = g["wavefn32"].astype(np.float64)
+    assert abs(vec[0] @ w) / np.linalg.norm(vec[0]) / np.linalg.norm(w) > 1 - 1e-8
+
+
+def test_solve_fp64_matches_oracle_iteration_count(pg, orc, torch):
+    # same start vectors, same algorithm: the matvec counts agree closely
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    ev, vec, st = grid.solve(dev(torch, g["v"]), nroots=2, ptol=8)
+    _, ev_o, _, nmv_o = orc.Grid(g["n"], g["L"]).solve(g["v"], nstates=2, ptol=8)
+    assert np.max(np.abs(ev - ev_o)) < 1e-10
+    assert abs(st["n_matvec"] - nmv_o) <= max(8, nmv_o // 20)
+
+
+def test_solve_analytic(pg, torch):
+    g = golden("analytic.npz")
+    grid = pg.Grid(g["box_n"], g["box_L"])
+    v0 = torch.zeros(grid.N, dtype=torch.float64, device="cuda")
+    ev, _, _ = grid.solve(v0, nroots=1, ptol=8)
+    assert abs(ev[0] - sum((3.14159265358979 / L) ** 2 / 2 for L in g["box_L"])) < 1e-9
+    grid = pg.Grid(g["harm_n"], g["harm_L"])
+    ev, _, _ = grid.solve(grid.spherical(float(g["harm_k"])), nroots=1, ptol=8)
+    assert abs(ev[0] - g["harm_evals"][0]) < 1e-9
+    grid = pg.Grid(g["full_n"], g["full_L"])
+    ev, _, _ = grid.solve(dev(torch, g["full_v"]), nroots=3, ptol=8, maxsub=40)
+    assert np.max(np.abs(ev - g["full_evals"][:3])) < 1e-9
+
+
+def test_solve_not_converged_is_a_status(pg, torch):
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    with pytest.raises(pg.NotConverged):
+        grid.solve(dev(torch, g["v"]), nroots=2, ptol=8, maxiter=1)
+
+
+def test_reverse_communication_drop_in(pg, torch):
+    # Drive pg_davidson_rci exactly as DVR::davdriver drives Davidson()
+    # (src/davdriver.cpp:58-86), with pg_hx as the matvec callback.
+    import ctypes
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    N, nroots, maxsub = grid.N, 2, 20
+    v = dev(torch, g["v"])
+    B = torch.zeros(maxsub * N, dtype=torch.float64, device="cuda")
+    Z = torch.zeros_like(B)
+    work = torch.zeros(pg.Davidson.work_size(N, maxsub, nroots, 1), dtype=torch.float64, device="cuda")
+    diag = grid.diagonal(v)
+    B[:N] = grid.piab()
+    B[N:2 * N] = dev(torch, np.random.default_rng(3).uniform(-1, 1, N))
+    evals = np.zeros(nroots)
+    nconv = ctypes.c_int(0)
+    inout = np.zeros(3, dtype=np.int32)
+    dav = pg.Davidson()
+    ret, calls = 1, 0
+    while ret != 0:
+        s, ret = dav.step(N, maxsub, nroots, 100, 8, 1, evals, nconv, B, Z, diag, work, inout)
+        assert s == pg.PG_OK
+        if ret == 1:
+            i0, z0, k = (int(a) for a in inout)
+            grid.hx(v, B[i0 * N:(i0 + k) * N], nvec=k, out=Z[z0 * N:(z0 + k) * N])
+            calls += 1
+    assert nconv.value == 2 and calls > 5
+    assert np.max(np.abs(evals - g["evals"])) < 1e-8
