@@ -157,6 +157,13 @@ typedef struct pg_davidson pg_davidson;
 pg_status pg_davidson_create(pg_davidson** out);
 pg_status pg_davidson_destroy(pg_davidson* d);
 
+/* The subspace eigensolver of the Davidson iteration (host): the k lowest
+ * eigenpairs of the symmetric m x m matrix whose upper triangle is stored in
+ * S (column-major, leading dimension ld); eigenvalues ascending in w[k],
+ * eigenvectors in the columns of V (leading dimension ldv).  Takes the place
+ * of the dsyev call of src/Davidson.cpp:224, which computes all m pairs. */
+pg_status pg_subspace_lowest(int m, const double* S_host, int ld, int k, double* w_host, double* V_host, int ldv);
+
 /* Work-array length in doubles (DavidsonWorkSize, src/Davidson.cpp:46-52). */
 long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag);
 

@@ -84,6 +84,7 @@ SYMBOLS = {
     "pg_davidson_create": (C.c_int, [C.POINTER(_vp)]),
     "pg_davidson_destroy": (C.c_int, [_vp]),
     "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    "pg_subspace_lowest": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, _dp, _dp, C.c_int]),
     "pg_davidson_rci": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
                                   _vp, _vp, _ip, _ip, _vp]),
     "pg_solve": (C.c_int, [_vp, _vp, C.POINTER(SolveParams), _dp, _vp, C.POINTER(SolveStats), _vp]),
@@ -342,6 +343,17 @@ def cluster_solve(n, L, waters_angstrom, ions=None, nroots=1, maxsub=20, maxiter
                                _stream(stream) if stream is not None else None)
     _check(s)
     return ev, (vec.reshape(nroots, N) if want_vectors else None), st.as_dict(nroots)
+
+
+def subspace_lowest(S, k):
+    """k lowest eigenpairs of a symmetric matrix (upper triangle read) with the
+    library's subspace eigensolver."""
+    S = np.asfortranarray(S, dtype=np.float64)
+    m = S.shape[0]
+    w = np.empty(k)
+    V = np.empty((m, k), order="F")
+    _check(lib().pg_subspace_lowest(m, S.ctypes.data_as(_dp), m, k, _d(w), V.ctypes.data_as(_dp), m))
+    return w, V
 
 
 def glibc_rand_stream(count):

@@ -15,8 +15,10 @@
 //     normalise), where the reference projects and renormalises against one
 //     basis vector at a time, twice each (src/Davidson.cpp:447-474); both
 //     produce the normalised component of v orthogonal to span(B);
-//   - the subspace eigenproblem uses a cyclic Jacobi solver (LAPACK dsyev in
-//     the reference, src/Davidson.cpp:224) on the same upper triangle.
+//   - the subspace eigenproblem (LAPACK dsyev of all m pairs in the
+//     reference, src/Davidson.cpp:224) computes only the nroots lowest pairs,
+//     the only ones the iteration reads (pg_subspace.cpp), from the same
+//     upper triangle.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -41,6 +43,9 @@ struct pg_davidson {
 };
 
 namespace pg {
+
+// pg_subspace.cpp
+bool lowest_eigenpairs(int m, const double* S, int ld, int k, double* w, double* V, int ldv);
 
 namespace {
 
@@ -91,60 +96,6 @@ __global__ void k_jd_finish(long N, double* __restrict__ r, const double* __rest
   const double f = dots[0] / dots[1];
   for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x)
     r[g] += f * jd[g];
-}
-
-// Cyclic Jacobi on the upper triangle of the m x m matrix S (leading
-// dimension ld); eigenvalues ascending into w, eigenvectors into V (ld).
-bool small_syev(int m, const double* S, int ld, double* w, double* V) {
-  std::vector<double> a((size_t)m * m);
-  for (int j = 0; j < m; ++j)
-    for (int i = 0; i <= j; ++i) a[i + (size_t)j * m] = a[j + (size_t)i * m] = S[i + (size_t)j * ld];
-  std::vector<double> v((size_t)m * m, 0.0);
-  for (int i = 0; i < m; ++i) v[i + (size_t)i * m] = 1.0;
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0, tot = 0;
-    for (int j = 0; j < m; ++j)
-      for (int i = 0; i < m; ++i) {
-        const double e = a[i + (size_t)j * m] * a[i + (size_t)j * m];
-        tot += e;
-        if (i != j) off += e;
-      }
-    if (off == 0 || off <= 1e-32 * tot) break;
-    for (int p = 0; p < m - 1; ++p)
-      for (int q = p + 1; q < m; ++q) {
-        const double apq = a[p + (size_t)q * m];
-        if (apq == 0) continue;
-        const double th = (a[q + (size_t)q * m] - a[p + (size_t)p * m]) / (2 * apq);
-        const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1));
-        const double c = 1 / sqrt(t * t + 1), s = t * c;
-        for (int k = 0; k < m; ++k) {
-          const double akp = a[k + (size_t)p * m], akq = a[k + (size_t)q * m];
-          a[k + (size_t)p * m] = c * akp - s * akq;
-          a[k + (size_t)q * m] = s * akp + c * akq;
-        }
-        for (int k = 0; k < m; ++k) {
-          const double apk = a[p + (size_t)k * m], aqk = a[q + (size_t)k * m];
-          a[p + (size_t)k * m] = c * apk - s * aqk;
-          a[q + (size_t)k * m] = s * apk + c * aqk;
-        }
-        for (int k = 0; k < m; ++k) {
-          const double vkp = v[k + (size_t)p * m], vkq = v[k + (size_t)q * m];
-          v[k + (size_t)p * m] = c * vkp - s * vkq;
-          v[k + (size_t)q * m] = s * vkp + c * vkq;
-        }
-      }
-  }
-  std::vector<int> order(m);
-  for (int i = 0; i < m; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return a[x + (size_t)x * m] < a[y + (size_t)y * m]; });
-  for (int c = 0; c < m; ++c) {
-    const int o = order[c];
-    w[c] = a[o + (size_t)o * m];
-    if (!std::isfinite(w[c])) return false;
-    for (int k = 0; k < m; ++k) V[k + (size_t)c * ld] = v[k + (size_t)o * m];
-  }
-  return true;
 }
 
 }  // namespace
@@ -279,7 +230,7 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       d->s_valid = m;
     }
     d->nsub = m;
-    if (!small_syev(m, d->S.data(), ms, d->sse.data(), d->V.data())) {
+    if (!lowest_eigenpairs(m, d->S.data(), ms, nroots, d->sse.data(), d->V.data(), ms)) {
       set_error("pg_davidson_rci: subspace eigensolve produced a non-finite value");
       d->status = 0;
       return PG_NUMERIC;
@@ -514,7 +465,7 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
     std::vector<double> Sc((size_t)nr * nr);  // gram gives [i*nr + j] = Z_i . B_j = S(i,j)
     for (int i = 0; i < nr; ++i)
       for (int j = 0; j < nr; ++j) Sc[i + (size_t)j * nr] = S[(size_t)i * nr + j];
-    if (!small_syev(nr, Sc.data(), nr, w.data(), V.data())) return PG_NUMERIC;
+    if (!lowest_eigenpairs(nr, Sc.data(), nr, nr, w.data(), V.data(), nr)) return PG_NUMERIC;
     PG_CUDA_TRY(cudaMemcpyAsync(d.dcoef.p, V.data(), sizeof(double) * nr * nr, cudaMemcpyHostToDevice, st));
     PG_TRY(combine(N, B.p, nr, d.dcoef.p, nr, 1.0, nullptr, nullptr, false, evecs, nr, nullptr, d.rs, st));
     for (int r = 0; r < nr; ++r) evals[r] = w[r];

@@ -76,3 +76,27 @@ def test_random_start_stream_is_c_library_rand(pg):
     libc.srand(1)
     exp = [libc.rand() for _ in range(2000)]
     assert list(pg.glibc_rand_stream(2000)) == exp
+
+
+@pytest.mark.parametrize("m,k", [(1, 1), (2, 1), (3, 2), (20, 4), (60, 4), (96, 16)])
+def test_subspace_eigensolver(pg, m, k):
+    rng = np.random.default_rng(m * 31 + k)
+    A = rng.normal(size=(m, m))
+    S = (A + A.T) / 2
+    w, V = pg.subspace_lowest(np.triu(S), k)   # only the upper triangle is read
+    wr = np.linalg.eigvalsh(S)[:k]
+    assert np.max(np.abs(w - wr)) < 1e-12 * max(1.0, np.abs(wr).max())
+    assert np.max(np.abs(S @ V - V * w)) < 1e-10
+    assert np.max(np.abs(V.T @ V - np.eye(k))) < 1e-10
+
+
+def test_subspace_eigensolver_degenerate(pg):
+    # a cluster of equal eigenvalues (the box and harmonic spectra have them)
+    rng = np.random.default_rng(2)
+    Q, _ = np.linalg.qr(rng.normal(size=(30, 30)))
+    lam = np.concatenate([[-1.0, 0.5, 0.5, 0.5, 0.5000001], np.linspace(1, 3, 25)])
+    S = (Q * lam) @ Q.T
+    w, V = pg.subspace_lowest(S, 5)
+    assert np.max(np.abs(w - lam[:5])) < 1e-12
+    assert np.max(np.abs(S @ V - V * w)) < 1e-10
+    assert np.max(np.abs(V.T @ V - np.eye(5))) < 1e-10
