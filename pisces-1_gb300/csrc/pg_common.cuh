@@ -95,4 +95,13 @@ struct pg_grid {
   pg::DevBuf<float> t_hi[3];       // TF32-rounded high part (stored as fp32)
   pg::DevBuf<float> t_lo[3];       // TF32-rounded remainder T - hi
   pg::DevBuf<double> x_dev[3];     // grid points on the device
+  pg::DevBuf<int> tc_err;          // set by the tensor-core H*X kernels if a completion wait times out
 };
+
+namespace pg {
+// H*X without the public call's synchronous status check (pg_hx.cu); the
+// caller checks check_tc_error() at its own synchronisation points.
+pg_status hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
+             cudaStream_t st);
+pg_status check_tc_error(const pg_grid* g, cudaStream_t st);
+}  // namespace pg

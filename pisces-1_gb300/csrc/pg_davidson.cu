@@ -448,15 +448,16 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
     if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
     if (ret == 1) {
       // the whole block in one launch (the reference multiplies vector by vector)
-      PG_TRY(pg_hx(g, v, B.p + (long)inout[0] * N, Z.p + (long)inout[1] * N, inout[2], p->precision, st));
+      PG_TRY(hx(g, v, B.p + (long)inout[0] * N, Z.p + (long)inout[1] * N, inout[2], p->precision, st));
       nmv += inout[2];
     }
   }
   const pg_status conv_status = s;
+  if (p->precision == PG_MIXED) PG_TRY(check_tc_error(g, st));
   if (p->precision == PG_MIXED && p->refine) {
     // FP64 Rayleigh-Ritz on the converged vectors: Z = H B with the FP64
     // operator, S = B^T Z, eigenpairs of S rotate the vectors.
-    PG_TRY(pg_hx(g, v, B.p, Z.p, nr, PG_FP64, st));
+    PG_TRY(hx(g, v, B.p, Z.p, nr, PG_FP64, st));
     nmv += nr;
     PG_TRY(gram(N, Z.p, nr, B.p, nr, d.dcoef.p, d.rs, st));
     std::vector<double> S((size_t)nr * nr), w(nr), V((size_t)nr * nr);

@@ -166,6 +166,11 @@ extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid**
       return PG_CUDA;
     }
   }
+  if (g->tc_err.alloc(1) != PG_OK || cudaMemset(g->tc_err.p, 0, sizeof(int)) != cudaSuccess) {
+    pg::set_error("pg_grid_create: allocation of the status word failed");
+    delete g;
+    return PG_OOM;
+  }
   *out = g;
   return PG_OK;
 }

@@ -77,20 +77,29 @@ __global__ void __launch_bounds__(256) k_hx_fp64(int nx, int ny, int nz, const d
 }  // namespace
 
 namespace pg {
-pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st);
-}
 
-extern "C" pg_status pg_hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
-                           void* stream) {
+pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
+                   bool check);
+
+pg_status hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
+             cudaStream_t st) {
   PG_ARG(g && v && x && y && nvec >= 0, "pg_hx: bad arguments");
   PG_ARG(x != y, "pg_hx: X and Y must not alias");
   if (nvec == 0) return PG_OK;
-  cudaStream_t st = pg::as_stream(stream);
-  if (precision == PG_MIXED) return pg::hx_mixed(g, v, x, y, nvec, st);
+  if (precision == PG_MIXED) return hx_mixed(g, v, x, y, nvec, st, false);
   PG_ARG(precision == PG_FP64, "pg_hx: unknown precision %d", precision);
   constexpr int NV = 4;
   dim3 grid((unsigned)((g->N + 255) / 256), (unsigned)((nvec + NV - 1) / NV));
   k_hx_fp64<NV><<<grid, 256, 0, st>>>(g->n[0], g->n[1], g->n[2], g->t_dev[0].p, g->t_dev[1].p, g->t_dev[2].p, v, x,
                                      y, nvec);
-  return pg::check_launch("k_hx_fp64");
+  return check_launch("k_hx_fp64");
+}
+
+}  // namespace pg
+
+extern "C" pg_status pg_hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
+                           void* stream) {
+  cudaStream_t st = pg::as_stream(stream);
+  PG_TRY(pg::hx(g, v, x, y, nvec, precision, st));
+  return precision == PG_MIXED ? pg::check_tc_error(g, st) : PG_OK;
 }

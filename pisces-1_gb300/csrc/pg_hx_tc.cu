@@ -1,11 +1,306 @@
-// Mixed-precision H*X (split-TF32 tensor-core kinetic contractions): placeholder
-// until the tcgen05 kernel lands.
+// Y = H X, mixed form: kinetic contractions on the 5th-generation tensor
+// cores (tcgen05, TF32 inputs, FP32 accumulation in tensor memory) as
+// split-precision products, V*X and the accumulation into Y in FP64.
+//
+// Each axis contraction is a batched GEMM.  With the "columns" c of an axis
+// being all points of the other two axes and all vectors, the transposed
+// product  D[c, i] = sum_b X[b, c] * T[i, b]  has M = columns (128 per tile),
+// N = n_axis (padded to 16) and K = n_axis (padded to 8): A is a 128-column
+// tile of X^T, B is the kinetic matrix, which stays in shared memory for the
+// whole (persistent) kernel.  Both are split into TF32 high and low parts,
+// D = Ah*Bh + Ah*Bl + Al*Bh (error ~2^-21 relative per term; Al*Bl dropped),
+// accumulated in FP32 in TMEM.  X is split on the fly from FP64 with integer
+// operations only (the FP64 pipe is two orders of magnitude slower on this
+// part).  Three passes: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X; X stays L2
+// resident between passes for the grids of the eigensolve workloads.
+//
+// Operand layout in shared memory: no-swizzle K-major core matrices
+// (8 rows x 16 bytes); K-adjacent core matrices 128 B apart (leading byte
+// offset), 8-row groups kpad/4*128 B apart (stride byte offset).
+// One thread issues the MMAs and commits them to an mbarrier; every wait is
+// bounded and a timeout is reported through an error word.
+#include <cstdint>
+
 #include "pg_common.cuh"
 
-namespace pg {
-pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st) {
-  (void)g; (void)v; (void)x; (void)y; (void)nvec; (void)st;
-  set_error("pg_hx: mixed precision is not built yet");
-  return PG_UNSUPPORTED;
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kTileM = 128;
+constexpr int kMaxN = 112;  // n_axis handled with the whole K extent resident in shared memory
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint32_t kmajor_off(int r, int k, int kpad) {
+  return (uint32_t)(((r >> 3) * (kpad >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// FP64 -> (hi, lo) TF32 pair with integer operations: truncate to FP32,
+// round the mantissa to 10 bits for hi, lo = the exact FP32 remainder
+// (rounded to TF32 by the tensor core).  Values below 2^-126 flush to zero.
+__device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t h = (uint32_t)(b >> 32);
+  const int e = (int)((h >> 20) & 0x7ff) - 1023 + 127;
+  uint32_t f = 0;
+  if (e > 0) f = (h & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+  const uint32_t hb = (f + 0x1000u) & 0xffffe000u;
+  const float xf = __uint_as_float(f);
+  hi = __uint_as_float(hb);
+  lo = xf - hi;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  for (long it = 0; it < (1L << 26); ++it) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(phase)
+                 : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) out[j] = __uint_as_float(r[j]);
+}
+
+struct AxisMap {
+  int n;          // length of the contracted axis
+  long stride;    // element stride along the axis
+  long ncols;     // columns: N * nvec / n
+};
+
+// base address (element index into X/Y) of column c, and the grid point of
+// its first element, for each axis
+template <int AXIS>
+__device__ __forceinline__ long col_base(long c, int nx, int ny, long N) {
+  if (AXIS == 0) return (long)nx * c;
+  if (AXIS == 1) {
+    const long q = c / nx;
+    return (c - q * nx) + (long)nx * ny * q;
+  }
+  const long plane = (long)nx * ny;
+  const long vv = c / plane;
+  return (c - vv * plane) + N * vv;
+}
+
+template <int AXIS>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kpad, uint32_t tmem_cols,
+            const float* __restrict__ t_hi, const float* __restrict__ t_lo, const double* __restrict__ v,
+            const double* __restrict__ X, double* __restrict__ Y, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int n = am.n;
+  const uint32_t b_bytes = (uint32_t)npad * kpad * 4;
+  const uint32_t a_bytes = (uint32_t)kTileM * kpad * 4;
+  unsigned char* sBh = smem;
+  unsigned char* sBl = smem + b_bytes;
+  unsigned char* sAh = smem + 2 * b_bytes;
+  unsigned char* sAl = sAh + a_bytes;
+  __shared__ __align__(8) uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x;
+  const long N = (long)nx * ny * nz;
+  const long ntiles = (am.ncols + kTileM - 1) / kTileM;
+
+  // kinetic matrix (B operand, rows = output index i, K = b), both halves
+  for (int e = tid; e < npad * kpad; e += kThreads) {
+    const int r = e / kpad, k = e - (e / kpad) * kpad;
+    const bool in = r < n && k < n;
+    *(float*)(sBh + kmajor_off(r, k, kpad)) = in ? t_hi[r * n + k] : 0.f;
+    *(float*)(sBl + kmajor_off(r, k, kpad)) = in ? t_lo[r * n + k] : 0.f;
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (tid < 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(npad >> 3) << 17) |
+                         ((uint32_t)(kTileM >> 4) << 24);
+  const uint32_t lbo = 128, sbo = (uint32_t)(kpad >> 2) * 128;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int quarter = warp & 3;      // TMEM lanes 32*quarter .. +31
+  const int half = warp >> 2;        // which 16-column chunks this warp reads
+  uint32_t phase = 0;
+  bool ok = true;
+
+  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long c0 = tile * kTileM;
+    // ---- A operand: 128 columns x K, split into TF32 hi/lo
+    if (AXIS == 0) {  // a column is a contiguous line: read along K
+      for (int e = tid; e < kTileM * kpad; e += kThreads) {
+        const int m = e / kpad, k = e - (e / kpad) * kpad;
+        const long c = c0 + m;
+        float h = 0.f, l = 0.f;
+        if (k < n && c < am.ncols) split_tf32(X[(long)nx * c + k], h, l);
+        *(float*)(sAh + kmajor_off(m, k, kpad)) = h;
+        *(float*)(sAl + kmajor_off(m, k, kpad)) = l;
+      }
+    } else {  // consecutive columns are consecutive addresses: read across columns
+      for (int e = tid; e < kTileM * kpad; e += kThreads) {
+        const int m = e & (kTileM - 1), k = e >> 7;
+        const long c = c0 + m;
+        float h = 0.f, l = 0.f;
+        if (k < n && c < am.ncols) split_tf32(X[col_base<AXIS>(c, nx, ny, N) + (long)k * am.stride], h, l);
+        *(float*)(sAh + kmajor_off(m, k, kpad)) = h;
+        *(float*)(sAl + kmajor_off(m, k, kpad)) = l;
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (tid == 0) {
+      const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
+      for (int kk = 0; kk < kpad / 8; ++kk) {
+        const uint32_t off = (uint32_t)kk * 256;  // 8 K-elements = two core matrices
+        const uint64_t dah = smem_desc(ah + off, lbo, sbo), dal = smem_desc(al + off, lbo, sbo);
+        const uint64_t dbh = smem_desc(bh + off, lbo, sbo), dbl = smem_desc(bl + off, lbo, sbo);
+        // small terms first, then the leading product
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                     " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                     "l"(dal), "l"(dbh), "r"(idesc), "r"(kk > 0 ? 1u : 0u));
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                     " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                     "l"(dah), "l"(dbl), "r"(idesc), "r"(1u));
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                     " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                     "l"(dah), "l"(dbh), "r"(idesc), "r"(1u));
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar)));
+    }
+    const bool waited = mbar_wait(smem_u32(&mbar), phase);
+    phase ^= 1u;
+    if (!__syncthreads_and(waited ? 1 : 0)) {
+      ok = false;
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // ---- epilogue: thread (quarter, lane) owns column c = c0 + 32*quarter + lane
+    const int m = 32 * quarter + lane;
+    const long c = c0 + m;
+    const bool cvalid = c < am.ncols;
+    const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
+    for (int chunk = half; chunk * 16 < npad; chunk += 2) {
+      float d[16];
+      tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(chunk * 16), d);
+      if (cvalid) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int i = chunk * 16 + j;
+          if (i < n) {
+            const long a = base + (long)i * am.stride;
+            double prev;
+            if (AXIS == 0) {
+              const long g = a % N;
+              prev = v[g] * X[a];
+            } else {
+              prev = Y[a];
+            }
+            Y[a] = prev + (double)d[j];
+          }
+        }
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();  // A buffers and the accumulator are free for the next tile
+  }
+  if (!ok && tid == 0) atomicExch(err, 1);
+  if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols));
+}
+
+}  // namespace
+
+namespace pg {
+
+static int g_num_sms = 0;
+
+// Launches the three axis passes on st.  The tensor-core completion waits
+// report a timeout through g->tc_err; with check, the call waits for the
+// stream and returns PG_DEVICE_TIMEOUT if one occurred (the eigensolver checks
+// the word itself at its own synchronisation points).
+pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
+                   bool check) {
+  for (int a = 0; a < 3; ++a)
+    if (g->n[a] > kMaxN) {
+      set_error("pg_hx: mixed form supports n <= %d per axis (got %d)", kMaxN, g->n[a]);
+      return PG_UNSUPPORTED;
+    }
+  if (!g_num_sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 148;
+  }
+  int* err = g->tc_err.p;
+  const long N = g->N;
+  for (int a = 0; a < 3; ++a) {
+    const int n = g->n[a];
+    AxisMap am;
+    am.n = n;
+    am.stride = a == 0 ? 1 : (a == 1 ? g->n[0] : (long)g->n[0] * g->n[1]);
+    am.ncols = N / n * nvec;
+    const int npad = (n + 15) / 16 * 16;
+    const int kpad = (n + 7) / 8 * 8;
+    uint32_t cols = 32;
+    while (cols < (uint32_t)npad) cols <<= 1;
+    const size_t smem = (size_t)2 * npad * kpad * 4 + (size_t)2 * kTileM * kpad * 4;
+    const long tiles = (am.ncols + kTileM - 1) / kTileM;
+    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+    switch (a) {
+      case 0:
+        PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, g->t_hi[0].p,
+                                                 g->t_lo[0].p, v, x, y, err);
+        break;
+      case 1:
+        PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, g->t_hi[1].p,
+                                                 g->t_lo[1].p, v, x, y, err);
+        break;
+      default:
+        PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, g->t_hi[2].p,
+                                                 g->t_lo[2].p, v, x, y, err);
+    }
+    PG_TRY(check_launch("k_hx_tc"));
+  }
+  return check ? check_tc_error(g, st) : PG_OK;
+}
+
+pg_status check_tc_error(const pg_grid* g, cudaStream_t st) {
+  int herr = 0;
+  PG_CUDA_TRY(cudaMemcpyAsync(&herr, g->tc_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  PG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr) {
+    set_error("pg_hx: tensor-core completion wait timed out");
+    return PG_DEVICE_TIMEOUT;
+  }
+  return PG_OK;
+}
+
 }  // namespace pg

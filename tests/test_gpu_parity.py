@@ -199,3 +199,47 @@ def test_reverse_communication_drop_in(pg, torch):
             calls += 1
     assert nconv.value == 2 and calls > 5
     assert np.max(np.abs(evals - g["evals"])) < 1e-8
+
+
+# ---------------------------------------------------------------- mixed form
+# split-TF32 tensor-core kinetic contractions, FP32 accumulation: each output
+# carries an absolute error of about 2^-21 * sum_b |T_ib x_b|, so the bound is
+# stated against max|Y| of the FP64 product.
+MIXED_HX_TOL = 2e-5
+
+
+@pytest.mark.parametrize("n,L,nvec", [((24, 20, 28), (20.0, 18.0, 22.0), 7), ((64, 64, 64), (40.0, 40.0, 40.0), 4),
+                                      ((33, 48, 17), (30.0, 40.0, 16.0), 3), ((96, 96, 96), (48.0, 48.0, 48.0), 1)])
+def test_hx_mixed_matches_fp64(pg, torch, n, L, nvec):
+    grid = pg.Grid(n, L)
+    rng = np.random.default_rng(7)
+    v = dev(torch, rng.normal(size=grid.N))
+    X = dev(torch, rng.normal(size=nvec * grid.N))
+    y64 = host(grid.hx(v, X, precision=pg.PG_FP64))
+    ymx = host(grid.hx(v, X, precision=pg.PG_MIXED))
+    assert np.max(np.abs(ymx - y64)) / np.max(np.abs(y64)) < MIXED_HX_TOL
+
+
+def test_hx_mixed_smooth_vector(pg, torch):
+    # an eigenfunction-like input: the kinetic sums cancel strongly
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    v = dev(torch, g["v"])
+    W = dev(torch, g["wavefn"])
+    y64 = host(grid.hx(v, W, precision=pg.PG_FP64))
+    ymx = host(grid.hx(v, W, precision=pg.PG_MIXED))
+    assert np.max(np.abs(ymx - y64)) / np.max(np.abs(y64)) < MIXED_HX_TOL
+    # Rayleigh quotients agree far better than the pointwise bound
+    Wh = g["wavefn"].reshape(2, -1)
+    for r in range(2):
+        a = Wh[r] @ y64.reshape(2, -1)[r] / (Wh[r] @ Wh[r])
+        b = Wh[r] @ ymx.reshape(2, -1)[r] / (Wh[r] @ Wh[r])
+        assert abs(a - b) < 1e-7
+
+
+def test_solve_mixed_c1_within_1e6(pg, torch):
+    g = golden("c1.npz")
+    ev, vec, st = pg.cluster_solve(g["n"], g["L"], g["waters"], nroots=1, ptol=6, precision=pg.PG_MIXED, refine=1)
+    assert abs(ev[0] - g["evals"][0]) < 1e-6
+    w = g["wavefn32"].astype(np.float64)
+    assert abs(vec[0] @ w) / np.linalg.norm(vec[0]) / np.linalg.norm(w) > 1 - 1e-8
