@@ -128,7 +128,7 @@ def run_ours(args, ws, rank, local):
     def step():
         v = grid.potential(tables, stream=sptr)
         return grid.solve(v, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=ptol, precision=precision,
-                          refine=1, stream=sptr)
+                          corrflag=args.corrflag, refine=1, stream=sptr)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
@@ -137,7 +137,7 @@ def run_ours(args, ws, rank, local):
         if precision == pg.PG_MIXED:  # FP64 answer of the same problem, for the error statement
             v = grid.potential(tables, stream=sptr)
             ev_ref, _, st_ref = grid.solve(v, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=wl["ptol"],
-                                           precision=pg.PG_FP64, stream=sptr)
+                                           precision=pg.PG_FP64, corrflag=args.corrflag, stream=sptr)
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
@@ -180,7 +180,7 @@ def run_ours(args, ws, rank, local):
         reps = max(1, min(args.steps, 3))
         for _ in range(reps):
             pg.cluster_solve(wl["n"], wl["L"], waters, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=ptol,
-                             precision=precision, refine=1, want_vectors=True)
+                             precision=precision, corrflag=args.corrflag, refine=1, want_vectors=True)
         e2e_ms = (time.perf_counter() - t0) * 1000 / reps
 
     # dominant kernel: H*X on a block of nroots vectors, timed with CUDA events on its stream
@@ -265,6 +265,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--corrflag", type=int, default=1, choices=[1, 3],
+                    help="1: the reference's diagonal (Davidson) correction; 3: exact-kinetic preconditioner")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -307,7 +309,8 @@ def main():
     line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+tf32x3",
-            "data": "synthetic", "config": dict(cfg, precision=args.precision, residual_tol=10.0 ** -r["ptol"]),
+            "data": "synthetic", "config": dict(cfg, precision=args.precision, residual_tol=10.0 ** -r["ptol"],
+                                                  corrflag=args.corrflag),
             "latency_ms": {"p50": p50, "p99": p99},
             "eigenvalues": r["evals"], "max_abs_dE_vs_fp64": r["de"],
             "solve": {k: r["stats"][k] for k in ("n_matvec", "n_iter", "n_restart", "nconv")},

@@ -157,6 +157,15 @@ typedef struct pg_davidson pg_davidson;
 pg_status pg_davidson_create(pg_davidson** out);
 pg_status pg_davidson_destroy(pg_davidson* d);
 
+/* Enables corrflag 3 on this handle: the correction vector of a root with
+ * Ritz value lambda is (T - lambda)^-1 r, T the grid's kinetic operator,
+ * applied exactly in its DST-I eigenbasis (three axis contractions, a
+ * diagonal scale, three more; precision as pg_hx).  Not in the reference,
+ * whose corrections use diag(H) only (src/Davidson.cpp:557-566); it changes
+ * the convergence rate, not the converged eigenpairs.  g must outlive the
+ * solve. */
+pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int precision);
+
 /* The subspace eigensolver of the Davidson iteration (host): the k lowest
  * eigenpairs of the symmetric m x m matrix whose upper triangle is stored in
  * S (column-major, leading dimension ld); eigenvalues ascending in w[k],
@@ -184,7 +193,7 @@ typedef struct {
   int maxsub;     /* max subspace (maxSubspace, default 20) */
   int maxiter;    /* max macro iterations (maxIter, default 100) */
   int ptol;       /* residual threshold 10^-ptol (pTol) */
-  int corrflag;   /* 0 residual, 1 Davidson (default), 2 Jacobi-Davidson */
+  int corrflag;   /* 0 residual, 1 Davidson (default), 2 Jacobi-Davidson, 3 exact-kinetic preconditioner */
   int precision;  /* pg_precision of the H*X products */
   int startvec;   /* 0: start vectors given in evecs_dev; 1: PiaB + random; 2: random */
   int refine;     /* PG_MIXED only: finish with FP64 H*X Rayleigh-Ritz on the converged vectors */

@@ -96,9 +96,19 @@ struct pg_grid {
   pg::DevBuf<float> t_lo[3];       // TF32-rounded remainder T - hi
   pg::DevBuf<double> x_dev[3];     // grid points on the device
   pg::DevBuf<int> tc_err;          // set by the tensor-core H*X kernels if a completion wait times out
+  // eigenbasis of the kinetic matrices (the orthonormal DST-I, symmetric),
+  // for the kinetic preconditioner: FP64, TF32 hi/lo, and the eigenvalues
+  pg::DevBuf<double> q_dev[3];
+  pg::DevBuf<float> q_hi[3], q_lo[3];
+  pg::DevBuf<double> d_dev[3];
 };
 
 namespace pg {
+// Single-axis contraction Y = A x_axis X for nvec vectors, A an n_axis x
+// n_axis matrix given in both FP64 and split-TF32 form; mode 0: Y = A X,
+// mode 1: Y += A X.  FP64 or tensor-core arithmetic per precision.
+pg_status axis_apply(const pg_grid* g, int axis, const double* A64, const float* Ahi, const float* Alo,
+                     const double* x, double* y, int nvec, int mode, int precision, cudaStream_t st);
 // H*X without the public call's synchronous status check (pg_hx.cu); the
 // caller checks check_tc_error() at its own synchronisation points.
 pg_status hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,

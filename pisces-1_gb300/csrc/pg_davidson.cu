@@ -37,7 +37,12 @@ struct pg_davidson {
   std::vector<int> ccode, bindex;
   pg::RedScratch rs;
   pg::DevBuf<double> dcoef;  // maxsub * maxsub coefficients / Gram blocks
-  pg::DevBuf<double> dsq;    // squared norms / scalars (4 * maxsub)
+  pg::DevBuf<double> dsq;    // device scalars (norms, Ritz values, constants)
+  pg::DevBuf<double> dgram;  // small Gram matrices of the Cholesky-QR step
+  // kinetic preconditioner (corrflag 3): grid, arithmetic, work blocks
+  const pg_grid* pc_grid = nullptr;
+  int pc_precision = PG_FP64;
+  pg::DevBuf<double> pc_w1, pc_w2;
   // counters for the solve statistics
   long n_iter = 0, n_restart = 0;
 };
@@ -90,6 +95,25 @@ __global__ void k_jd_prep(long N, double* __restrict__ r, double* __restrict__ j
   }
 }
 
+// Diagonal of the kinetic preconditioner in the DST-I eigenbasis:
+// y_v(i,j,k) /= (dx_i + dy_j + dz_k - sigma_v), the denominator kept at
+// least `floor` in magnitude.
+__global__ void k_kin_scale(int nx, int ny, int nz, const double* __restrict__ dx, const double* __restrict__ dy,
+                            const double* __restrict__ dz, const double* __restrict__ sigma, double floor,
+                            double* __restrict__ Y, int nvec) {
+  const long N = (long)nx * ny * nz;
+  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
+    const int i = (int)(g % nx);
+    const long r = g / nx;
+    const double dk = dx[i] + dy[(int)(r % ny)] + dz[(int)(r / ny)];
+    for (int v = 0; v < nvec; ++v) {
+      double den = dk - sigma[v];
+      if (fabs(den) < floor) den = den < 0 ? -floor : floor;
+      Y[(long)v * N + g] /= den;
+    }
+  }
+}
+
 // r += f jd with f = dots[0] / dots[1]  (src/Davidson.cpp:547-548)
 __global__ void k_jd_finish(long N, double* __restrict__ r, const double* __restrict__ jd,
                             const double* __restrict__ dots) {
@@ -112,6 +136,13 @@ extern "C" pg_status pg_davidson_destroy(pg_davidson* d) {
   return PG_OK;
 }
 
+extern "C" pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int precision) {
+  PG_ARG(d && (precision == PG_FP64 || precision == PG_MIXED), "pg_davidson_set_preconditioner: bad arguments");
+  d->pc_grid = g;
+  d->pc_precision = precision;
+  return PG_OK;
+}
+
 extern "C" long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag) {
   // DavidsonWorkSize (src/Davidson.cpp:46-52); same layout of the work array.
   if (corrflag == 2) return 2L * maxsub * maxsub + 11L * maxsub + (2L * nroots + 1) * ndim;
@@ -121,34 +152,104 @@ extern "C" long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corr
 namespace pg {
 namespace {
 
+// Device scalars of one Davidson handle (offsets into pg_davidson::dsq).
+constexpr int kUsq = 0;     // |U_r|^2 and 1/|U_r| (2 x 16)
+constexpr int kLam = 32;    // Ritz values (16)
+constexpr int kRsq = 64;    // |r_r|^2 and 1/|r_r| (2 x 16)
+constexpr int kOnes = 96;   // 1.0 (16), the "keep X" coefficients of combine
+constexpr int kDots = 112;  // Jacobi-Davidson dot products (2)
+constexpr int kSigma = 128; // shifts of the kinetic preconditioner (16)
+constexpr int kScalars = 256;
+
 pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
   if (d->ndim == ndim && d->maxsub >= maxsub && d->nroots >= nroots && d->dcoef.p) return PG_OK;
   PG_TRY(d->dcoef.alloc((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
-  PG_TRY(d->dsq.alloc((size_t)4 * std::max(maxsub, 16)));
+  PG_TRY(d->dgram.alloc((size_t)kMaxGramOut));
+  PG_TRY(d->dsq.alloc(kScalars));
+  std::vector<double> init(kScalars, 0.0);
+  for (int i = 0; i < 16; ++i) init[kOnes + i] = 1.0;
+  PG_CUDA_TRY(cudaMemcpy(d->dsq.p, init.data(), sizeof(double) * kScalars, cudaMemcpyHostToDevice));
   d->ndim = ndim;
   d->maxsub = maxsub;
   d->nroots = nroots;
   return PG_OK;
 }
 
-// The one combine that must keep X: v <- 1*v - B c.
-pg_status cgs_pass(pg_davidson* d, long N, const double* B, int nbas, double* vec, cudaStream_t st) {
-  double* c = d->dcoef.p;
-  double* one = d->dsq.p + 3 * std::max(d->maxsub, 16);
-  PG_TRY(gram(N, B, nbas, vec, 1, c, d->rs, st));
-  PG_TRY(combine(N, B, nbas, c, nbas, -1.0, vec, one, false, vec, 1, nullptr, d->rs, st));
+// C = L^-T for the Cholesky factor of the k x k Gram matrix G (row-major,
+// G[a*k+b] = R_a . R_b), so that R C has orthonormal columns and, C being
+// upper triangular, the same nested spans as Gram-Schmidt.  One thread; a
+// pivot is floored at 1e-300 so that a numerically dependent vector yields a
+// (normalised) noise direction, as the reference's normalisation does.
+__global__ void k_cholinv(const double* __restrict__ G, int k, double* __restrict__ C) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double L[kMaxCombine][kMaxCombine];
+  for (int j = 0; j < k; ++j) {
+    double s = G[j * k + j];
+    for (int p = 0; p < j; ++p) s -= L[j][p] * L[j][p];
+    const double piv = sqrt(s > 1e-300 ? s : 1e-300);
+    L[j][j] = piv;
+    for (int i = j + 1; i < k; ++i) {
+      double t = G[i * k + j];
+      for (int p = 0; p < j; ++p) t -= L[i][p] * L[j][p];
+      L[i][j] = t / piv;
+    }
+  }
+  // C = L^-T: solve L^T C = I column by column (C upper triangular)
+  for (int c = 0; c < k; ++c)
+    for (int i = k - 1; i >= 0; --i) {
+      double s = i == c ? 1.0 : 0.0;
+      for (int p = i + 1; p < k; ++p) s -= L[p][i] * C[p * k + c];
+      C[i * k + c] = i > c ? 0.0 : s / L[i][i];
+    }
+}
+
+// Kinetic preconditioner on the k contiguous vectors R: R <- (T - sigma_j)^-1 R
+// with T = Qx Qy Qz diag(d) Qz Qy Qx (the DST-I eigenbasis of the sine DVR),
+// i.e. three axis contractions, a diagonal scale and three contractions.
+pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* sigma_dev, cudaStream_t st) {
+  const pg_grid* g = d->pc_grid;
+  const long N = g->N;
+  if (d->pc_w1.n < (size_t)k * N) {
+    PG_TRY(d->pc_w1.alloc((size_t)d->nroots * N));
+    PG_TRY(d->pc_w2.alloc((size_t)d->nroots * N));
+  }
+  double *w1 = d->pc_w1.p, *w2 = d->pc_w2.p;
+  const int pr = d->pc_precision;
+  PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, R, w1, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w1, w2, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 0, g->q_dev[0].p, g->q_hi[0].p, g->q_lo[0].p, w2, w1, k, 0, pr, st));
+  // the smallest kinetic level, a scale for the denominator floor
+  double dmin = 0;
+  for (int a = 0; a < 3; ++a) dmin += 0.5 * (M_PI / g->L[a]) * (M_PI / g->L[a]);
+  k_kin_scale<<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], g->d_dev[0].p, g->d_dev[1].p, g->d_dev[2].p,
+                                            sigma_dev, 0.1 * dmin, w1, k);
+  PG_TRY(check_launch("k_kin_scale"));
+  PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, w1, w2, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w2, w1, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 0, g->q_dev[0].p, g->q_hi[0].p, g->q_lo[0].p, w1, R, k, 0, pr, st));
   return PG_OK;
 }
 
-pg_status orthonormalise(pg_davidson* d, long N, double* vec, const double* B, int nbas, double* out,
-                         cudaStream_t st) {
-  if (nbas > 0) {
-    PG_TRY(cgs_pass(d, N, B, nbas, vec, st));
-    PG_TRY(cgs_pass(d, N, B, nbas, vec, st));
+// Orthonormalise the k vectors R (contiguous, R[j*N]) against the first nbas
+// columns of B (block classical Gram-Schmidt, two passes), then among
+// themselves (Cholesky-QR, two passes); the result goes to out (k vectors,
+// may equal R).  Same spans as the reference's vector-by-vector
+// orthogonalisation (src/Davidson.cpp:447-514).
+pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, const double* B, int nbas, double* out,
+                               cudaStream_t st) {
+  double* c = d->dcoef.p;
+  double* ones = d->dsq.p + kOnes;
+  for (int pass = 0; nbas > 0 && pass < 2; ++pass) {
+    // c[a*k + j] = B_a . R_j ;  R_j <- R_j - sum_a B_a c[a*k + j]
+    PG_TRY(gram(N, B, nbas, R, k, c, d->rs, st));
+    PG_TRY(combine(N, B, nbas, c, k, 1, -1.0, R, ones, false, R, k, nullptr, d->rs, st));
   }
-  double* sq = d->dsq.p;
-  PG_TRY(sqnorms(N, vec, 1, sq, d->rs, st));
-  PG_TRY(combine(N, nullptr, 0, nullptr, 1, 0.0, vec, sq, true, out, 1, nullptr, d->rs, st));
+  for (int pass = 0; pass < 2; ++pass) {
+    PG_TRY(gram(N, R, k, R, k, d->dgram.p, d->rs, st));
+    k_cholinv<<<1, 32, 0, st>>>(d->dgram.p, k, c);
+    PG_TRY(check_launch("k_cholinv"));
+    PG_TRY(combine(N, R, k, c, k, 1, 1.0, nullptr, nullptr, false, pass == 1 ? out : R, k, nullptr, d->rs, st));
+  }
   return PG_OK;
 }
 
@@ -170,7 +271,12 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
   double* ritz = work + 2L * ms * ms + 11L * ms;
   double* res = ritz + N * nroots;
   double* jd = res + N * nroots;
-  if (corrflag < 0 || corrflag > 2) corrflag = 1;
+  if (corrflag == 3 && !d->pc_grid) {
+    set_error("pg_davidson_rci: corrflag 3 needs pg_davidson_set_preconditioner");
+    return PG_BAD_ARG;
+  }
+  if (corrflag < 0 || corrflag > 3) corrflag = 1;
+  if (corrflag == 3) PG_ARG(d->pc_grid->N == ndim, "pg_davidson_rci: preconditioner grid does not match ndim");
 
   if (d->status == 0) {  // first call (src/Davidson.cpp:145-193)
     PG_TRY(ensure_scratch(d, ndim, maxsub, nroots));
@@ -187,11 +293,8 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     d->ccode.assign(nroots, 0);
     d->bindex.assign(nroots, 0);
     d->n_iter = d->n_restart = 0;
-    const double one = 1.0;
-    PG_CUDA_TRY(cudaMemcpyAsync(d->dsq.p + 3 * std::max(d->maxsub, 16), &one, sizeof(double),
-                                cudaMemcpyHostToDevice, st));
     // orthonormalise the start vectors (GramSchmidt, src/Davidson.cpp:482-514)
-    for (int i = 0; i < nroots; ++i) PG_TRY(orthonormalise(d, N, B + i * N, B, i, B + i * N, st));
+    PG_TRY(block_orthonormalise(d, N, B, nroots, B, 0, B, st));
     d->status = 1;
   }
   PG_ARG(d->status == 1 && d->ndim == ndim, "pg_davidson_rci: state does not match this problem");
@@ -244,13 +347,13 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     // Ritz vectors u = B v (renormalised) and residuals Z v - lambda u
     // (src/Davidson.cpp:240-269), all roots in one pass
     double* dV = d->dcoef.p;
-    double* dlam = d->dsq.p + ms;
-    double* usq = d->dsq.p;
-    double* rsq = d->dsq.p + 2 * ms;
+    double* dlam = d->dsq.p + kLam;
+    double* usq = d->dsq.p + kUsq;
+    double* rsq = d->dsq.p + kRsq;
     PG_CUDA_TRY(cudaMemcpyAsync(dV, d->V.data(), sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
     PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->sse.data(), sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
-    PG_TRY(combine(N, B, m, dV, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st));
-    PG_TRY(combine(N, Z, m, dV, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st));
+    PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st));
+    PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st));
     k_ritz_residual<<<blocks_for(N), kT, 0, st>>>(N, nroots, ritz, res, usq, dlam);
     PG_TRY(check_launch("k_ritz_residual"));
     PG_TRY(sqnorms(N, res, nroots, rsq, d->rs, st));
@@ -305,8 +408,8 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       for (int r = 0; r < nroots; ++r)
         if (d->ccode[r] > 0) {
           const int jz = d->bindex[r];
-          PG_TRY(combine(N, Z, d->nsub, dV + (size_t)r * ms, ms, 1.0, nullptr, nullptr, false, ritz + (long)jz * N, 1,
-                         nullptr, d->rs, st));
+          PG_TRY(combine(N, Z, d->nsub, dV + (size_t)r * ms, 1, ms, 1.0, nullptr, nullptr, false,
+                         ritz + (long)jz * N, 1, nullptr, d->rs, st));
         }
       const long first = *nconv - newly;
       const long cnt = (long)(d->nnewB + newly);
@@ -327,11 +430,18 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         return PG_NOT_CONVERGED;
       }
     }
-    // correction vectors (src/Davidson.cpp:353-371)
-    d->nnewB = 0;
+    // correction vectors (src/Davidson.cpp:353-371): the unconverged roots in
+    // order while the subspace has room, preconditioned, compacted to the
+    // front of the residual block, orthonormalised as one block and appended
+    // to B
+    std::vector<int> sel;
     for (int r = 0; r < nroots; ++r) {
-      if (d->nsub + d->nnewB == ms) break;
+      if (d->nsub + (int)sel.size() == ms) break;
       if (d->ccode[r] < 2) continue;
+      sel.push_back(r);
+    }
+    for (size_t j = 0; j < sel.size(); ++j) {
+      const int r = sel[j];
       double* rv = res + (long)r * N;
       if (corrflag == 1) {
         k_precond<<<blocks_for(N), kT, 0, st>>>(N, rv, diag, d->sse[r]);
@@ -339,16 +449,25 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       } else if (corrflag == 2) {
         k_jd_prep<<<blocks_for(N), kT, 0, st>>>(N, rv, jd, ritz + (long)r * N, diag, d->sse[r]);
         PG_TRY(check_launch("k_jd_prep"));
-        double* dots = d->dsq.p + 2 * ms;  // (u . r, u . jd)
+        double* dots = d->dsq.p + kDots;  // (u . r, u . jd)
         PG_TRY(gram(N, ritz + (long)r * N, 1, rv, 1, dots, d->rs, st));
         PG_TRY(gram(N, ritz + (long)r * N, 1, jd, 1, dots + 1, d->rs, st));
         k_jd_finish<<<blocks_for(N), kT, 0, st>>>(N, rv, jd, dots);
         PG_TRY(check_launch("k_jd_finish"));
       }
-      const int slot = d->nsub + d->nnewB;
-      PG_TRY(orthonormalise(d, N, rv, B, slot, B + (long)slot * N, st));
-      d->nnewB++;
+      if (r != (int)j)  // sel is increasing, so slot j is free or already moved
+        PG_CUDA_TRY(cudaMemcpyAsync(res + (long)j * N, rv, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
     }
+    d->nnewB = (int)sel.size();
+    if (corrflag == 3 && d->nnewB > 0) {
+      std::vector<double> sig(d->nnewB);
+      for (int j = 0; j < d->nnewB; ++j) sig[j] = d->sse[sel[j]];
+      double* dsig = d->dsq.p + kSigma;
+      PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig.data(), sizeof(double) * d->nnewB, cudaMemcpyHostToDevice, st));
+      PG_TRY(kinetic_precondition(d, res, d->nnewB, dsig, st));
+    }
+    if (d->nnewB > 0)
+      PG_TRY(block_orthonormalise(d, N, res, d->nnewB, B, d->nsub, B + (long)d->nsub * N, st));
   }
 }
 
@@ -439,6 +558,7 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
     PG_TRY(start_vectors(g, nr, p->startvec, B.p, st));
   PG_TRY(pg_diagonal(g, v, diag.p, st));
   pg_davidson d;
+  if (p->corrflag == 3) PG_TRY(pg_davidson_set_preconditioner(&d, g, p->precision));
   int inout[3] = {0, 0, 0}, nconv = 0, ret = 1;
   long nmv = 0;
   pg_status s = PG_OK;
@@ -468,7 +588,7 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
       for (int j = 0; j < nr; ++j) Sc[i + (size_t)j * nr] = S[(size_t)i * nr + j];
     if (!lowest_eigenpairs(nr, Sc.data(), nr, nr, w.data(), V.data(), nr)) return PG_NUMERIC;
     PG_CUDA_TRY(cudaMemcpyAsync(d.dcoef.p, V.data(), sizeof(double) * nr * nr, cudaMemcpyHostToDevice, st));
-    PG_TRY(combine(N, B.p, nr, d.dcoef.p, nr, 1.0, nullptr, nullptr, false, evecs, nr, nullptr, d.rs, st));
+    PG_TRY(combine(N, B.p, nr, d.dcoef.p, 1, nr, 1.0, nullptr, nullptr, false, evecs, nr, nullptr, d.rs, st));
     for (int r = 0; r < nr; ++r) evals[r] = w[r];
   } else {
     PG_CUDA_TRY(cudaMemcpyAsync(evecs, B.p, sizeof(double) * N * nr, cudaMemcpyDeviceToDevice, st));

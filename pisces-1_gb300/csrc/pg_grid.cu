@@ -166,6 +166,34 @@ extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid**
       return PG_CUDA;
     }
   }
+  // Eigenbasis of the sine-DVR kinetic matrix: the DVR is the
+  // particle-in-a-box basis, so T = Q diag(d) Q with the orthonormal DST-I
+  // matrix Q[i][k] = sqrt(2/(n+1)) sin(pi (i+1)(k+1)/(n+1)) and
+  // d_k = (pi (k+1) / L)^2 / 2 (src/sine_dvr.cpp:1-12).
+  for (int a = 0; a < 3; ++a) {
+    const int m = n[a];
+    std::vector<double> q((size_t)m * m), d(m);
+    std::vector<float> qh((size_t)m * m), ql((size_t)m * m);
+    const double s = sqrt(2.0 / (m + 1));
+    for (int i = 0; i < m; ++i)
+      for (int k = 0; k < m; ++k) {
+        const double v = s * sin(M_PI * (double)((long)(i + 1) * (k + 1) % (2 * (m + 1))) / (m + 1));
+        q[(size_t)i * m + k] = v;
+        qh[(size_t)i * m + k] = to_tf32((float)v);
+        ql[(size_t)i * m + k] = to_tf32((float)(v - (double)qh[(size_t)i * m + k]));
+      }
+    for (int k = 0; k < m; ++k) d[k] = 0.5 * (M_PI * (k + 1) / L[a]) * (M_PI * (k + 1) / L[a]);
+    if (g->q_dev[a].alloc((size_t)m * m) != PG_OK || g->q_hi[a].alloc((size_t)m * m) != PG_OK ||
+        g->q_lo[a].alloc((size_t)m * m) != PG_OK || g->d_dev[a].alloc(m) != PG_OK ||
+        cudaMemcpy(g->q_dev[a].p, q.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->q_hi[a].p, qh.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->q_lo[a].p, ql.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->d_dev[a].p, d.data(), sizeof(double) * m, cudaMemcpyHostToDevice) != cudaSuccess) {
+      pg::set_error("pg_grid_create: kinetic eigenbasis upload failed");
+      delete g;
+      return PG_OOM;
+    }
+  }
   if (g->tc_err.alloc(1) != PG_OK || cudaMemset(g->tc_err.p, 0, sizeof(int)) != cudaSuccess) {
     pg::set_error("pg_grid_create: allocation of the status word failed");
     delete g;

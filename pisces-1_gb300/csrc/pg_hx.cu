@@ -74,9 +74,55 @@ __global__ void __launch_bounds__(256) k_hx_fp64(int nx, int ny, int nz, const d
     if (q < nv) Y[(long)(v0 + q) * N + g] = acc[q];
 }
 
+// Y (mode) A x_axis X: one axis contraction in FP64, mode 0 write, 1 add.
+template <int NV>
+__global__ void __launch_bounds__(256) k_axis_fp64(int nx, int ny, int nz, int axis, const double* __restrict__ A,
+                                                   const double* __restrict__ X, double* __restrict__ Y, int nvec,
+                                                   int mode) {
+  const long N = (long)nx * ny * nz;
+  const long g = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int v0 = blockIdx.y * NV;
+  if (g >= N) return;
+  const int i = (int)(g % nx);
+  const long r = g / nx;
+  const int j = (int)(r % ny);
+  const int k = (int)(r / ny);
+  const int na = axis == 0 ? nx : (axis == 1 ? ny : nz);
+  const int idx = axis == 0 ? i : (axis == 1 ? j : k);
+  const long stride = axis == 0 ? 1 : (axis == 1 ? nx : (long)nx * ny);
+  const long base = g - (long)idx * stride;
+  const int nv = nvec - v0 < NV ? nvec - v0 : NV;
+  double acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; ++q) acc[q] = (q < nv && mode == 1) ? Y[(long)(v0 + q) * N + g] : 0.0;
+  const double* arow = A + (long)idx * na;
+  for (int b = 0; b < na; ++b) {
+    const double t = arow[b];
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+      if (q < nv) acc[q] += t * X[(long)(v0 + q) * N + base + (long)b * stride];
+  }
+#pragma unroll
+  for (int q = 0; q < NV; ++q)
+    if (q < nv) Y[(long)(v0 + q) * N + g] = acc[q];
+}
+
 }  // namespace
 
 namespace pg {
+
+pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* v, const double* x,
+                  double* y, int nvec, int mode, cudaStream_t st);
+
+pg_status axis_apply(const pg_grid* g, int axis, const double* A64, const float* Ahi, const float* Alo,
+                     const double* x, double* y, int nvec, int mode, int precision, cudaStream_t st) {
+  PG_ARG(g && x && y && x != y && axis >= 0 && axis < 3 && (mode == 0 || mode == 1), "axis_apply: bad arguments");
+  if (precision == PG_MIXED) return tc_axis(g, axis, Ahi, Alo, nullptr, x, y, nvec, mode, st);
+  constexpr int NV = 4;
+  dim3 grid((unsigned)((g->N + 255) / 256), (unsigned)((nvec + NV - 1) / NV));
+  k_axis_fp64<NV><<<grid, 256, 0, st>>>(g->n[0], g->n[1], g->n[2], axis, A64, x, y, nvec, mode);
+  return check_launch("k_axis_fp64");
+}
 
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
                    bool check);

@@ -103,7 +103,8 @@ template <int AXIS>
 __global__ void __launch_bounds__(kThreads, 1)
     k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kpad, uint32_t tmem_cols,
             const float* __restrict__ t_hi, const float* __restrict__ t_lo, const double* __restrict__ v,
-            const double* __restrict__ X, double* __restrict__ Y, int* __restrict__ err) {
+            const double* __restrict__ X, double* __restrict__ Y, int mode, int* __restrict__ err) {
+  // mode 0: Y = D;  1: Y += D;  2: Y = V X + D   (D = the axis contraction)
   extern __shared__ __align__(1024) unsigned char smem[];
   const int n = am.n;
   const uint32_t b_bytes = (uint32_t)npad * kpad * 4;
@@ -214,13 +215,9 @@ __global__ void __launch_bounds__(kThreads, 1)
           const int i = chunk * 16 + j;
           if (i < n) {
             const long a = base + (long)i * am.stride;
-            double prev;
-            if (AXIS == 0) {
-              const long g = a % N;
-              prev = v[g] * X[a];
-            } else {
-              prev = Y[a];
-            }
+            double prev = 0.0;
+            if (mode == 2) prev = v[a % N] * X[a];
+            else if (mode == 1) prev = Y[a];
             Y[a] = prev + (double)d[j];
           }
         }
@@ -239,56 +236,60 @@ namespace pg {
 
 static int g_num_sms = 0;
 
-// Launches the three axis passes on st.  The tensor-core completion waits
-// report a timeout through g->tc_err; with check, the call waits for the
-// stream and returns PG_DEVICE_TIMEOUT if one occurred (the eigensolver checks
-// the word itself at its own synchronisation points).
-pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
-                   bool check) {
-  for (int a = 0; a < 3; ++a)
-    if (g->n[a] > kMaxN) {
-      set_error("pg_hx: mixed form supports n <= %d per axis (got %d)", kMaxN, g->n[a]);
-      return PG_UNSUPPORTED;
-    }
+// One axis contraction on the tensor cores: Y (mode) D with D = A x_axis X,
+// A given as TF32 hi/lo halves (n_axis x n_axis, row-major).
+pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* v, const double* x,
+                  double* y, int nvec, int mode, cudaStream_t st) {
+  if (g->n[a] > kMaxN) {
+    set_error("mixed form supports n <= %d per axis (got %d)", kMaxN, g->n[a]);
+    return PG_UNSUPPORTED;
+  }
   if (!g_num_sms) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 148;
   }
-  int* err = g->tc_err.p;
   const long N = g->N;
-  for (int a = 0; a < 3; ++a) {
-    const int n = g->n[a];
-    AxisMap am;
-    am.n = n;
-    am.stride = a == 0 ? 1 : (a == 1 ? g->n[0] : (long)g->n[0] * g->n[1]);
-    am.ncols = N / n * nvec;
-    const int npad = (n + 15) / 16 * 16;
-    const int kpad = (n + 7) / 8 * 8;
-    uint32_t cols = 32;
-    while (cols < (uint32_t)npad) cols <<= 1;
-    const size_t smem = (size_t)2 * npad * kpad * 4 + (size_t)2 * kTileM * kpad * 4;
-    const long tiles = (am.ncols + kTileM - 1) / kTileM;
-    const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
-    switch (a) {
-      case 0:
-        PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, g->t_hi[0].p,
-                                                 g->t_lo[0].p, v, x, y, err);
-        break;
-      case 1:
-        PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, g->t_hi[1].p,
-                                                 g->t_lo[1].p, v, x, y, err);
-        break;
-      default:
-        PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, g->t_hi[2].p,
-                                                 g->t_lo[2].p, v, x, y, err);
-    }
-    PG_TRY(check_launch("k_hx_tc"));
+  const int n = g->n[a];
+  AxisMap am;
+  am.n = n;
+  am.stride = a == 0 ? 1 : (a == 1 ? g->n[0] : (long)g->n[0] * g->n[1]);
+  am.ncols = N / n * nvec;
+  const int npad = (n + 15) / 16 * 16;
+  const int kpad = (n + 7) / 8 * 8;
+  uint32_t cols = 32;
+  while (cols < (uint32_t)npad) cols <<= 1;
+  const size_t smem = (size_t)2 * npad * kpad * 4 + (size_t)2 * kTileM * kpad * 4;
+  const long tiles = (am.ncols + kTileM - 1) / kTileM;
+  const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+  int* err = g->tc_err.p;
+  switch (a) {
+    case 0:
+      PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, v, x, y,
+                                               mode, err);
+      break;
+    case 1:
+      PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, v, x, y,
+                                               mode, err);
+      break;
+    default:
+      PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, v, x, y,
+                                               mode, err);
   }
+  return check_launch("k_hx_tc");
+}
+
+// Launches the three axis passes on st: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X.
+// The tensor-core completion waits report a timeout through g->tc_err; with
+// check, the call waits for the stream and returns PG_DEVICE_TIMEOUT if one
+// occurred (the eigensolver checks the word at its own synchronisation points).
+pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
+                   bool check) {
+  for (int a = 0; a < 3; ++a) PG_TRY(tc_axis(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, a == 0 ? 2 : 1, st));
   return check ? check_tc_error(g, st) : PG_OK;
 }
 

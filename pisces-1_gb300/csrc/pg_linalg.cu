@@ -1,4 +1,8 @@
 // Deterministic skinny FP64 kernels for the Davidson subspace (see pg_linalg.cuh).
+//
+// Every reduction runs in two launches: blocks of the first write partial
+// sums (one per output), the second reduces the partials of each output with
+// one warp, in a fixed order.  No atomics, no dependence on scheduling.
 #include "pg_linalg.cuh"
 
 namespace pg {
@@ -8,26 +12,31 @@ namespace {
 constexpr int kT = 256;
 constexpr int kTP = 32;  // points per shared-memory tile in k_gram
 
-// True in exactly one block: the last to arrive.  Partial results written
-// before the call are visible to it.
-__device__ __forceinline__ bool arrive_last(unsigned* counter) {
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  __syncthreads();
-  return last;
-}
-
 long chunk_for(long N, int blocks, int align) {
   long c = (N + blocks - 1) / blocks;
   c = (c + align - 1) / align * align;
   return c > 0 ? c : align;
 }
 
+// out[o] = sum_b partial[b*no + o] over nb partial rows; one warp per output,
+// lanes stride over the rows, then a fixed shuffle tree.  inv_sqrt_out: also
+// store 1/sqrt(out[o]) at out[no + o] (used to normalise vectors on device).
+__global__ void __launch_bounds__(kT) k_reduce_partials(const double* __restrict__ partial, int nb, int no,
+                                                        double* __restrict__ out, int sqrt_mode) {
+  const int warp = (blockIdx.x * kT + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= no) return;
+  double s = 0;
+  for (int b = lane; b < nb; b += 32) s += partial[(long)b * no + warp];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    out[warp] = s;
+    if (sqrt_mode) out[no + warp] = 1.0 / sqrt(s);
+  }
+}
+
 __global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* __restrict__ P, int na,
-                                             const double* __restrict__ Q, int nb, double* __restrict__ partial,
-                                             unsigned* __restrict__ counter, double* __restrict__ out) {
+                                             const double* __restrict__ Q, int nb, double* __restrict__ partial) {
   extern __shared__ double sm[];
   double* Ps = sm;                       // na x (kTP+1)
   double* Qs = sm + na * (kTP + 1);      // nb x (kTP+1)
@@ -54,9 +63,15 @@ __global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* _
       if (o < no) {
         const double* pa = Ps + (o / nb) * (kTP + 1);
         const double* qb = Qs + (o % nb) * (kTP + 1);
-        double a = acc[s];
-        for (int p = 0; p < kTP; ++p) a += pa[p] * qb[p];
-        acc[s] = a;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;  // four chains hide the DFMA latency
+#pragma unroll
+        for (int p = 0; p < kTP; p += 4) {
+          a0 += pa[p] * qb[p];
+          a1 += pa[p + 1] * qb[p + 1];
+          a2 += pa[p + 2] * qb[p + 2];
+          a3 += pa[p + 3] * qb[p + 3];
+        }
+        acc[s] += (a0 + a1) + (a2 + a3);
       }
     }
     __syncthreads();
@@ -66,26 +81,18 @@ __global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* _
     const int o = threadIdx.x + s * kT;
     if (o < no) partial[(long)blockIdx.x * no + o] = acc[s];
   }
-  if (arrive_last(counter)) {
-    for (int o = threadIdx.x; o < no; o += kT) {
-      double s = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += partial[(long)b * no + o];
-      out[o] = s;
-    }
-    if (threadIdx.x == 0) *counter = 0;
-  }
 }
 
-__global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double* __restrict__ P, int na,
-                                                const double* __restrict__ C, int ldc, double cscale, const double* X,
+__global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double* P, int na,
+                                                const double* __restrict__ C, int ca, int cr, double cscale,
+                                                const double* X,
                                                 const double* __restrict__ alpha, int inv_sqrt, double* Y, int nr,
-                                                double* __restrict__ partial, unsigned* __restrict__ counter,
-                                                double* __restrict__ sq) {
+                                                double* __restrict__ partial) {
   extern __shared__ double sm[];
   double* Cs = sm;                 // na x nr
   __shared__ double al[kMaxCombine];
   __shared__ double red[kT / 32][kMaxCombine];
-  for (int e = threadIdx.x; e < na * nr; e += kT) Cs[e] = cscale * C[(e / nr) + (long)(e % nr) * ldc];
+  for (int e = threadIdx.x; e < na * nr; e += kT) Cs[e] = cscale * C[(long)(e / nr) * ca + (long)(e % nr) * cr];
   if (threadIdx.x < nr) {
     double a = 0;
     if (alpha) a = inv_sqrt ? 1.0 / sqrt(alpha[threadIdx.x]) : alpha[threadIdx.x];
@@ -115,8 +122,7 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
         sacc[r] += acc[r] * acc[r];
       }
   }
-  if (!sq) return;
-  // block reduction of the squared norms (fixed order)
+  if (!partial) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int r = 0; r < kMaxCombine; ++r) {
@@ -130,57 +136,48 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
     for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
     partial[(long)blockIdx.x * nr + threadIdx.x] = s;
   }
-  if (arrive_last(counter)) {
-    if (threadIdx.x < nr) {
-      double s = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += partial[(long)b * nr + threadIdx.x];
-      sq[threadIdx.x] = s;
-    }
-    if (threadIdx.x == 0) *counter = 0;
-  }
 }
 
 __global__ void __launch_bounds__(kT) k_sqnorms(long N, long chunk, const double* __restrict__ X, int nr,
-                                                double* __restrict__ partial, unsigned* __restrict__ counter,
-                                                double* __restrict__ sq) {
-  __shared__ double red[kT / 32];
+                                                double* __restrict__ partial) {
+  __shared__ double red[kT / 32][kMaxCombine];
   const long g_begin = blockIdx.x * chunk;
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int r = 0; r < nr; ++r) {
-    double s = 0;
-    for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
-      const double x = X[(long)r * N + g];
-      s += x * x;
-    }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lane == 0) red[warp] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int w = 0; w < kT / 32; ++w) t += red[w];
-      partial[(long)blockIdx.x * nr + r] = t;
-    }
-    __syncthreads();
+  double s[kMaxCombine];
+#pragma unroll
+  for (int r = 0; r < kMaxCombine; ++r) s[r] = 0;
+  for (long g = g_begin + threadIdx.x; g < g_end; g += kT)
+#pragma unroll
+    for (int r = 0; r < kMaxCombine; ++r)
+      if (r < nr) {
+        const double x = X[(long)r * N + g];
+        s[r] += x * x;
+      }
+#pragma unroll
+  for (int r = 0; r < kMaxCombine; ++r) {
+    double v = s[r];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][r] = v;
   }
-  if (arrive_last(counter)) {
-    for (int r = threadIdx.x; r < nr; r += kT) {
-      double s = 0;
-      for (unsigned b = 0; b < gridDim.x; ++b) s += partial[(long)b * nr + r];
-      sq[r] = s;
-    }
-    if (threadIdx.x == 0) *counter = 0;
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    double t = 0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w][threadIdx.x];
+    partial[(long)blockIdx.x * nr + threadIdx.x] = t;
   }
+}
+
+pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
+  const int blocks = (no * 32 + kT - 1) / kT;
+  k_reduce_partials<<<blocks, kT, 0, st>>>(partial, nb, no, out, sqrt_mode ? 1 : 0);
+  return check_launch("k_reduce_partials");
 }
 
 }  // namespace
 
 pg_status RedScratch::ensure() {
-  if (!partial.p) {
-    PG_TRY(partial.alloc((size_t)kRedBlocks * kMaxGramOut));
-    PG_TRY(counter.alloc(4));
-    PG_CUDA_TRY(cudaMemset(counter.p, 0, 4 * sizeof(unsigned)));
-  }
+  if (!partial.p) PG_TRY(partial.alloc((size_t)kRedBlocks * kMaxGramOut));
   return PG_OK;
 }
 
@@ -192,13 +189,14 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
   const int blocks = (int)((N + chunk - 1) / chunk);
   const size_t smem = sizeof(double) * (size_t)(na + nb) * (kTP + 1);
   if (smem > 48 * 1024) PG_CUDA_TRY(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p, rs.counter.p, out);
-  return check_launch("k_gram");
+  k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
+  PG_TRY(check_launch("k_gram"));
+  return reduce(rs.partial.p, blocks, na * nb, out, false, st);
 }
 
-pg_status combine(long N, const double* P, int na, const double* C, int ldc, double cscale, const double* X,
-                  const double* alpha,
-                  bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs, cudaStream_t st) {
+pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
+                  const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
+                  cudaStream_t st) {
   PG_ARG(nr > 0 && nr <= kMaxCombine && na >= 0, "combine: bad sizes na=%d nr=%d", na, nr);
   PG_TRY(rs.ensure());
   const long chunk = chunk_for(N, kRedBlocks, kT);
@@ -206,18 +204,20 @@ pg_status combine(long N, const double* P, int na, const double* C, int ldc, dou
   const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
   if (smem > 48 * 1024)
     PG_CUDA_TRY(cudaFuncSetAttribute(k_combine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_combine<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ldc, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, rs.partial.p,
-                                      rs.counter.p + 1, sq);
-  return check_launch("k_combine");
+  k_combine<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr,
+                                      sq ? rs.partial.p : nullptr);
+  PG_TRY(check_launch("k_combine"));
+  return sq ? reduce(rs.partial.p, blocks, nr, sq, true, st) : PG_OK;
 }
 
 pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st) {
-  PG_ARG(nr > 0 && nr <= kMaxGramOut, "sqnorms: bad count %d", nr);
+  PG_ARG(nr > 0 && nr <= kMaxCombine, "sqnorms: bad count %d", nr);
   PG_TRY(rs.ensure());
   const long chunk = chunk_for(N, kRedBlocks, kT);
   const int blocks = (int)((N + chunk - 1) / chunk);
-  k_sqnorms<<<blocks, kT, 0, st>>>(N, chunk, X, nr, rs.partial.p, rs.counter.p + 2, sq);
-  return check_launch("k_sqnorms");
+  k_sqnorms<<<blocks, kT, 0, st>>>(N, chunk, X, nr, rs.partial.p);
+  PG_TRY(check_launch("k_sqnorms"));
+  return reduce(rs.partial.p, blocks, nr, sq, true, st);
 }
 
 }  // namespace pg

@@ -24,14 +24,15 @@ struct RedScratch {
 // out[a*nb + b] = sum_g P[a*N + g] * Q[b*N + g]     (a < na, b < nb; na*nb <= kMaxGramOut)
 pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs, cudaStream_t st);
 
-// Y[r*N + g] = alpha_r * X[r*N + g] + cscale * sum_a P[a*N + g] * C[a + r*ldc]   (r < nr <= kMaxCombine)
+// Y[r*N + g] = alpha_r * X[r*N + g] + cscale * sum_a P[a*N + g] * C[a*ca + r*cr]   (r < nr <= kMaxCombine)
 // alpha_r: 0 if alpha is null; alpha[r] if inv_sqrt is false; 1/sqrt(alpha[r]) if true.
-// X may equal Y.  If sq is not null, sq[r] = |Y_r|^2.
-pg_status combine(long N, const double* P, int na, const double* C, int ldc, double cscale, const double* X,
-                  const double* alpha,
-                  bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs, cudaStream_t st);
+// X and P may equal Y (each point is read before it is written).  If sq is
+// not null, sq[r] = |Y_r|^2 and sq[nr + r] = 1/|Y_r|.
+pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
+                  const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
+                  cudaStream_t st);
 
-// sq[r] = |X_r|^2 for r < nr.
+// sq[r] = |X_r|^2 and sq[nr + r] = 1/|X_r| for r < nr.
 pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st);
 
 }  // namespace pg

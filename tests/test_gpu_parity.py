@@ -240,6 +240,32 @@ def test_hx_mixed_smooth_vector(pg, torch):
         assert abs(a - b) < 1e-7
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_solve_kinetic_preconditioner(pg, torch, precision):
+    # corrflag 3 (exact kinetic preconditioner) converges to the same
+    # eigenpairs as the reference algorithm, in far fewer products
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    prec = pg.PG_FP64 if precision == "fp64" else pg.PG_MIXED
+    ptol = 8 if precision == "fp64" else 6
+    ev3, vec3, st3 = grid.solve(dev(torch, g["v"]), nroots=2, ptol=ptol, corrflag=3, precision=prec)
+    ev1, _, st1 = grid.solve(dev(torch, g["v"]), nroots=2, ptol=ptol, corrflag=1, precision=prec)
+    assert np.max(np.abs(ev3 - g["evals"])) < (1e-8 if precision == "fp64" else 1e-6)
+    assert st3["n_matvec"] < st1["n_matvec"]
+    W = g["wavefn"].reshape(2, -1)
+    V = host(vec3)
+    for r in range(2):
+        assert abs(V[r] @ W[r]) / np.linalg.norm(V[r]) / np.linalg.norm(W[r]) > 1 - 1e-8
+
+
+def test_solve_kinetic_preconditioner_c1(pg, torch):
+    g = golden("c1.npz")
+    ev, vec, st = pg.cluster_solve(g["n"], g["L"], g["waters"], nroots=1, ptol=8, corrflag=3)
+    assert abs(ev[0] - g["evals"][0]) < 1e-8
+    w = g["wavefn32"].astype(np.float64)
+    assert abs(vec[0] @ w) / np.linalg.norm(vec[0]) / np.linalg.norm(w) > 1 - 1e-8
+
+
 def test_solve_mixed_c1_within_1e6(pg, torch):
     g = golden("c1.npz")
     ev, vec, st = pg.cluster_solve(g["n"], g["L"], g["waters"], nroots=1, ptol=6, precision=pg.PG_MIXED, refine=1)
