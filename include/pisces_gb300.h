@@ -206,6 +206,8 @@ typedef struct {
   int n_restart;
   double residual[64];   /* final |r| per root (first min(nroots,64)) */
   double seconds;        /* wall time of the solve */
+  double host_eig_seconds;     /* of which in the host subspace eigensolver */
+  double device_wait_seconds;  /* of which waiting for device results at the two per-iteration reads */
 } pg_solve_stats;
 
 /* Full eigensolve on the device: start vectors (DVR::Diagonalize,

@@ -53,11 +53,13 @@ class SolveParams(C.Structure):
 
 class SolveStats(C.Structure):
     _fields_ = [("nconv", C.c_int), ("n_matvec", C.c_int), ("n_iter", C.c_int), ("n_restart", C.c_int),
-                ("residual", C.c_double * 64), ("seconds", C.c_double)]
+                ("residual", C.c_double * 64), ("seconds", C.c_double), ("host_eig_seconds", C.c_double),
+                ("device_wait_seconds", C.c_double)]
 
     def as_dict(self, nroots):
         return {"nconv": self.nconv, "n_matvec": self.n_matvec, "n_iter": self.n_iter, "n_restart": self.n_restart,
-                "residual": list(self.residual[:nroots]), "seconds": self.seconds}
+                "residual": list(self.residual[:nroots]), "seconds": self.seconds,
+                "host_eig_seconds": self.host_eig_seconds, "device_wait_seconds": self.device_wait_seconds}
 
 
 _lib = None

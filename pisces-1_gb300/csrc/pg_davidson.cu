@@ -45,6 +45,7 @@ struct pg_davidson {
   pg::DevBuf<double> pc_w1, pc_w2;
   // counters for the solve statistics
   long n_iter = 0, n_restart = 0;
+  double t_eig = 0, t_wait = 0;  // host seconds in the subspace eigensolver / waiting for the device
 };
 
 namespace pg {
@@ -293,6 +294,7 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     d->ccode.assign(nroots, 0);
     d->bindex.assign(nroots, 0);
     d->n_iter = d->n_restart = 0;
+    d->t_eig = d->t_wait = 0;
     // orthonormalise the start vectors (GramSchmidt, src/Davidson.cpp:482-514)
     PG_TRY(block_orthonormalise(d, N, B, nroots, B, 0, B, st));
     d->status = 1;
@@ -322,7 +324,9 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       }
       std::vector<double> cols((size_t)m * nc);
       PG_CUDA_TRY(cudaMemcpyAsync(cols.data(), d->dcoef.p, sizeof(double) * m * nc, cudaMemcpyDeviceToHost, st));
+      const auto w0 = std::chrono::steady_clock::now();
       PG_CUDA_TRY(cudaStreamSynchronize(st));
+      d->t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
       // gram output is [a*nb + b] per chunk: a = Z column i, b = new B column
       for (int cb = 0; cb < nc; cb += per) {
         const int k = std::min(per, nc - cb);
@@ -333,7 +337,10 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       d->s_valid = m;
     }
     d->nsub = m;
-    if (!lowest_eigenpairs(m, d->S.data(), ms, nroots, d->sse.data(), d->V.data(), ms)) {
+    const auto e0 = std::chrono::steady_clock::now();
+    const bool eig_ok = lowest_eigenpairs(m, d->S.data(), ms, nroots, d->sse.data(), d->V.data(), ms);
+    d->t_eig += std::chrono::duration<double>(std::chrono::steady_clock::now() - e0).count();
+    if (!eig_ok) {
       set_error("pg_davidson_rci: subspace eigensolve produced a non-finite value");
       d->status = 0;
       return PG_NUMERIC;
@@ -359,7 +366,9 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     PG_TRY(sqnorms(N, res, nroots, rsq, d->rs, st));
     std::vector<double> hr(nroots);
     PG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsq, sizeof(double) * nroots, cudaMemcpyDeviceToHost, st));
+    const auto w1 = std::chrono::steady_clock::now();
     PG_CUDA_TRY(cudaStreamSynchronize(st));
+    d->t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - w1).count();
     for (int r = 0; r < nroots; ++r) {
       d->residuals[r] = sqrt(hr[r]);
       if (!std::isfinite(d->residuals[r])) {
@@ -602,6 +611,8 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
     stats->n_restart = (int)d.n_restart;
     for (int r = 0; r < nr && r < 64; ++r) stats->residual[r] = r < (int)d.residuals.size() ? d.residuals[r] : 0;
     stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    stats->host_eig_seconds = d.t_eig;
+    stats->device_wait_seconds = d.t_wait;
   }
   return conv_status;
 }
