@@ -157,6 +157,13 @@ typedef struct pg_davidson pg_davidson;
 pg_status pg_davidson_create(pg_davidson** out);
 pg_status pg_davidson_destroy(pg_davidson* d);
 
+/* Arithmetic of the subspace products of this handle (S = Z^T B, the Ritz
+ * and residual combinations, the block orthogonalisation): PG_FP64 (default,
+ * IEEE FP64 throughout) or PG_MIXED, double-float (two FP32 numbers,
+ * ~2^-48 relative) on the FP32 pipe.  The subspace eigensolve, the Cholesky
+ * factors and the residual norms stay FP64 either way. */
+pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision);
+
 /* Enables corrflag 3 on this handle: the correction vector of a root with
  * Ritz value lambda is (T - lambda)^-1 r, T the grid's kinetic operator,
  * applied exactly in its DST-I eigenbasis (three axis contractions, a

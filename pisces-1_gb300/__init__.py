@@ -88,6 +88,7 @@ SYMBOLS = {
     "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
     "pg_subspace_lowest": (C.c_int, [C.c_int, _dp, C.c_int, C.c_int, _dp, _dp, C.c_int]),
     "pg_davidson_set_preconditioner": (C.c_int, [_vp, _vp, C.c_int]),
+    "pg_davidson_set_arithmetic": (C.c_int, [_vp, C.c_int]),
     "pg_davidson_rci": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _dp, _ip, _vp, _vp,
                                   _vp, _vp, _ip, _ip, _vp]),
     "pg_solve": (C.c_int, [_vp, _vp, C.POINTER(SolveParams), _dp, _vp, C.POINTER(SolveStats), _vp]),

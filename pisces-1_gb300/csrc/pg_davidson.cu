@@ -42,6 +42,9 @@ struct pg_davidson {
   // kinetic preconditioner (corrflag 3): grid, arithmetic, work blocks
   const pg_grid* pc_grid = nullptr;
   int pc_precision = PG_FP64;
+  // subspace products (S, Ritz/residual combinations, orthogonalisation) in
+  // double-float arithmetic on the FP32 pipe instead of FP64 (mixed form)
+  bool dfloat = false;
   pg::DevBuf<double> pc_w1, pc_w2;
   // counters for the solve statistics
   long n_iter = 0, n_restart = 0;
@@ -134,6 +137,12 @@ extern "C" pg_status pg_davidson_create(pg_davidson** out) {
 
 extern "C" pg_status pg_davidson_destroy(pg_davidson* d) {
   delete d;
+  return PG_OK;
+}
+
+extern "C" pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision) {
+  PG_ARG(d && (precision == PG_FP64 || precision == PG_MIXED), "pg_davidson_set_arithmetic: bad arguments");
+  d->dfloat = precision == PG_MIXED;
   return PG_OK;
 }
 
@@ -242,14 +251,15 @@ pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, const d
   double* ones = d->dsq.p + kOnes;
   for (int pass = 0; nbas > 0 && pass < 2; ++pass) {
     // c[a*k + j] = B_a . R_j ;  R_j <- R_j - sum_a B_a c[a*k + j]
-    PG_TRY(gram(N, B, nbas, R, k, c, d->rs, st));
-    PG_TRY(combine(N, B, nbas, c, k, 1, -1.0, R, ones, false, R, k, nullptr, d->rs, st));
+    PG_TRY(gram(N, B, nbas, R, k, c, d->rs, st, d->dfloat));
+    PG_TRY(combine(N, B, nbas, c, k, 1, -1.0, R, ones, false, R, k, nullptr, d->rs, st, d->dfloat));
   }
   for (int pass = 0; pass < 2; ++pass) {
-    PG_TRY(gram(N, R, k, R, k, d->dgram.p, d->rs, st));
+    PG_TRY(gram(N, R, k, R, k, d->dgram.p, d->rs, st, d->dfloat));
     k_cholinv<<<1, 32, 0, st>>>(d->dgram.p, k, c);
     PG_TRY(check_launch("k_cholinv"));
-    PG_TRY(combine(N, R, k, c, k, 1, 1.0, nullptr, nullptr, false, pass == 1 ? out : R, k, nullptr, d->rs, st));
+    PG_TRY(combine(N, R, k, c, k, 1, 1.0, nullptr, nullptr, false, pass == 1 ? out : R, k, nullptr, d->rs, st,
+                   d->dfloat));
   }
   return PG_OK;
 }
@@ -317,10 +327,10 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     {
       const int c0 = d->s_valid;
       const int nc = m - c0;
-      const int per = std::max(1, kMaxGramOut / m);
+      const int per = std::max(1, std::min(kMaxGramOut / m, std::min(16, 144 - m)));
       for (int cb = 0; cb < nc; cb += per) {
         const int k = std::min(per, nc - cb);
-        PG_TRY(gram(N, Z, m, B + (long)(c0 + cb) * N, k, d->dcoef.p + (size_t)cb * m, d->rs, st));
+        PG_TRY(gram(N, Z, m, B + (long)(c0 + cb) * N, k, d->dcoef.p + (size_t)cb * m, d->rs, st, d->dfloat));
       }
       std::vector<double> cols((size_t)m * nc);
       PG_CUDA_TRY(cudaMemcpyAsync(cols.data(), d->dcoef.p, sizeof(double) * m * nc, cudaMemcpyDeviceToHost, st));
@@ -359,8 +369,8 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     double* rsq = d->dsq.p + kRsq;
     PG_CUDA_TRY(cudaMemcpyAsync(dV, d->V.data(), sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
     PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->sse.data(), sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
-    PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st));
-    PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st));
+    PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat));
+    PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat));
     k_ritz_residual<<<blocks_for(N), kT, 0, st>>>(N, nroots, ritz, res, usq, dlam);
     PG_TRY(check_launch("k_ritz_residual"));
     PG_TRY(sqnorms(N, res, nroots, rsq, d->rs, st));
@@ -418,7 +428,7 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         if (d->ccode[r] > 0) {
           const int jz = d->bindex[r];
           PG_TRY(combine(N, Z, d->nsub, dV + (size_t)r * ms, 1, ms, 1.0, nullptr, nullptr, false,
-                         ritz + (long)jz * N, 1, nullptr, d->rs, st));
+                         ritz + (long)jz * N, 1, nullptr, d->rs, st, d->dfloat));
         }
       const long first = *nconv - newly;
       const long cnt = (long)(d->nnewB + newly);
@@ -568,6 +578,7 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
   PG_TRY(pg_diagonal(g, v, diag.p, st));
   pg_davidson d;
   if (p->corrflag == 3) PG_TRY(pg_davidson_set_preconditioner(&d, g, p->precision));
+  d.dfloat = p->precision == PG_MIXED;
   int inout[3] = {0, 0, 0}, nconv = 0, ret = 1;
   long nmv = 0;
   pg_status s = PG_OK;

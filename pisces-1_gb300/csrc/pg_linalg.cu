@@ -3,6 +3,8 @@
 // Every reduction runs in two launches: blocks of the first write partial
 // sums (one per output), the second reduces the partials of each output with
 // one warp, in a fixed order.  No atomics, no dependence on scheduling.
+#include <cstdint>
+
 #include "pg_linalg.cuh"
 
 namespace pg {
@@ -168,6 +170,192 @@ __global__ void __launch_bounds__(kT) k_sqnorms(long N, long chunk, const double
   }
 }
 
+// ------------------------------------------------------------------------
+// Double-float (two FP32 numbers, hi + lo) arithmetic for the mixed form's
+// subspace products.  The FP32 pipe of this part retires ~67 TFLOP/s against
+// ~1 TFLOP/s for FP64; a double-float multiply-accumulate costs ~11 FP32
+// operations and keeps ~48 significant bits (Dekker 1971, Knuth TwoSum).
+
+// x = hi + lo exactly up to 2^-53 |x|, with integer operations only (the FP64
+// pipe is not touched).  |x| < 2^-126 flushes to zero.
+__device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t h = (uint32_t)(b >> 32);
+  const int e = (int)((h >> 20) & 0x7ff);
+  const int ef = e - 1023 + 127;
+  if (ef <= 0) {
+    hi = 0.f;
+    lo = 0.f;
+    return;
+  }
+  const uint32_t sign = h & 0x80000000u;
+  hi = __uint_as_float(sign | ((uint32_t)ef << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
+  const uint32_t rem = (uint32_t)(b & 0x1fffffffu);  // the 29 mantissa bits below hi
+  const int el = e - 1075 + 127;                      // exponent of one unit of rem
+  float scale = el > 0 ? __uint_as_float((uint32_t)el << 23) : 0.f;
+  const float l = __uint2float_rn(rem) * scale;
+  lo = sign ? -l : l;
+}
+
+// (sh, sl) += a * b with a = (ah, al), b = (bh, bl)
+__device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al, float bh, float bl) {
+  const float p = ah * bh;
+  float e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+  const float t = sh + p;
+  const float bp = t - sh;
+  const float err = (sh - (t - bp)) + (p - bp);
+  sl += err + e;
+  sh = t;
+}
+
+// (sh, sl) += (ph, pl)
+__device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl) {
+  const float t = sh + ph;
+  const float bp = t - sh;
+  const float err = (sh - (t - bp)) + (ph - bp);
+  sl += err + pl;
+  sh = t;
+}
+
+// Gram partials in double-float: same contract as k_gram; partial sums are
+// written as double (hi + lo).
+__global__ void __launch_bounds__(kT) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
+                                                const double* __restrict__ Q, int nb, double* __restrict__ partial) {
+  extern __shared__ float smf[];
+  float* Ph = smf;                         // na x (kTP+1)
+  float* Pl = Ph + na * (kTP + 1);
+  float* Qh = Pl + na * (kTP + 1);         // nb x (kTP+1)
+  float* Ql = Qh + nb * (kTP + 1);
+  const int no = na * nb;
+  float ah[kMaxGramOut / kT], al[kMaxGramOut / kT];
+#pragma unroll
+  for (int s = 0; s < kMaxGramOut / kT; ++s) ah[s] = al[s] = 0.f;
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  for (long g0 = g_begin; g0 < g_end; g0 += kTP) {
+    const int cnt = g_end - g0 < kTP ? (int)(g_end - g0) : kTP;
+    for (int e = threadIdx.x; e < na * kTP; e += kT) {
+      const int a = e / kTP, p = e % kTP;
+      float h = 0.f, l = 0.f;
+      if (p < cnt) df_split(P[(long)a * N + g0 + p], h, l);
+      Ph[a * (kTP + 1) + p] = h;
+      Pl[a * (kTP + 1) + p] = l;
+    }
+    for (int e = threadIdx.x; e < nb * kTP; e += kT) {
+      const int b = e / kTP, p = e % kTP;
+      float h = 0.f, l = 0.f;
+      if (p < cnt) df_split(Q[(long)b * N + g0 + p], h, l);
+      Qh[b * (kTP + 1) + p] = h;
+      Ql[b * (kTP + 1) + p] = l;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < kMaxGramOut / kT; ++s) {
+      const int o = threadIdx.x + s * kT;
+      if (o < no) {
+        const int a = o / nb, b = o % nb;
+        const float* pah = Ph + a * (kTP + 1);
+        const float* pal = Pl + a * (kTP + 1);
+        const float* qbh = Qh + b * (kTP + 1);
+        const float* qbl = Ql + b * (kTP + 1);
+        float th = 0.f, tl = 0.f, uh = 0.f, ul = 0.f;  // two chains for latency
+#pragma unroll
+        for (int p = 0; p < kTP; p += 2) {
+          df_fma(th, tl, pah[p], pal[p], qbh[p], qbl[p]);
+          df_fma(uh, ul, pah[p + 1], pal[p + 1], qbh[p + 1], qbl[p + 1]);
+        }
+        df_add(th, tl, uh, ul);
+        df_add(ah[s], al[s], th, tl);
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int s = 0; s < kMaxGramOut / kT; ++s) {
+    const int o = threadIdx.x + s * kT;
+    if (o < no) partial[(long)blockIdx.x * no + o] = (double)ah[s] + (double)al[s];
+  }
+}
+
+// Combine in double-float: same contract as k_combine (coefficients and
+// alpha are FP64 and split once per block; Y is written as double).
+__global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const double* P, int na,
+                                                   const double* __restrict__ C, int ca, int cr, double cscale,
+                                                   const double* X, const double* __restrict__ alpha, int inv_sqrt,
+                                                   double* Y, int nr, double* __restrict__ partial) {
+  extern __shared__ float smf[];
+  float* Ch = smf;              // na x nr
+  float* Cl = smf + na * nr;
+  __shared__ float alh[kMaxCombine], all[kMaxCombine];
+  __shared__ double red[kT / 32][kMaxCombine];
+  for (int e = threadIdx.x; e < na * nr; e += kT) {
+    float h, l;
+    df_split(cscale * C[(long)(e / nr) * ca + (long)(e % nr) * cr], h, l);
+    Ch[e] = h;
+    Cl[e] = l;
+  }
+  if (threadIdx.x < nr) {
+    double a = 0;
+    if (alpha) a = inv_sqrt ? 1.0 / sqrt(alpha[threadIdx.x]) : alpha[threadIdx.x];
+    float h, l;
+    df_split(a, h, l);
+    alh[threadIdx.x] = h;
+    all[threadIdx.x] = l;
+  }
+  __syncthreads();
+  double sacc[kMaxCombine];
+#pragma unroll
+  for (int r = 0; r < kMaxCombine; ++r) sacc[r] = 0;
+  const bool keep = X && alpha;
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
+    float sh[kMaxCombine], sl[kMaxCombine];
+#pragma unroll
+    for (int r = 0; r < kMaxCombine; ++r) {
+      sh[r] = 0.f;
+      sl[r] = 0.f;
+      if (r < nr && keep) {
+        float xh, xl;
+        df_split(X[(long)r * N + g], xh, xl);
+        df_fma(sh[r], sl[r], alh[r], all[r], xh, xl);
+      }
+    }
+    for (int a = 0; a < na; ++a) {
+      float ph, pl;
+      df_split(P[(long)a * N + g], ph, pl);
+      const float* ch = Ch + a * nr;
+      const float* cl = Cl + a * nr;
+#pragma unroll
+      for (int r = 0; r < kMaxCombine; ++r)
+        if (r < nr) df_fma(sh[r], sl[r], ph, pl, ch[r], cl[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kMaxCombine; ++r)
+      if (r < nr) {
+        const double y = (double)sh[r] + (double)sl[r];
+        Y[(long)r * N + g] = y;
+        sacc[r] += y * y;
+      }
+  }
+  if (!partial) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < kMaxCombine; ++r) {
+    double v = sacc[r];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    double s = 0;
+    for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
+    partial[(long)blockIdx.x * nr + threadIdx.x] = s;
+  }
+}
+
 pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
   const int blocks = (no * 32 + kT - 1) / kT;
   k_reduce_partials<<<blocks, kT, 0, st>>>(partial, nb, no, out, sqrt_mode ? 1 : 0);
@@ -181,32 +369,60 @@ pg_status RedScratch::ensure() {
   return PG_OK;
 }
 
+// Dynamic shared-memory opt-in, once per kernel (the largest size any call
+// needs: 112 + 16 vectors of 33 doubles for the Gram kernels).
+static pg_status opt_in_smem() {
+  static bool done = false;
+  if (done) return PG_OK;
+  const int big = (int)(sizeof(double) * (size_t)(128 + 16) * (kTP + 1));
+  PG_CUDA_TRY(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PG_CUDA_TRY(cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PG_CUDA_TRY(cudaFuncSetAttribute(k_combine, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  PG_CUDA_TRY(cudaFuncSetAttribute(k_combine_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  done = true;
+  return PG_OK;
+}
+
 pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs,
-               cudaStream_t st) {
-  PG_ARG(na > 0 && nb > 0 && na * nb <= kMaxGramOut, "gram: %d x %d outputs exceed %d", na, nb, kMaxGramOut);
+               cudaStream_t st, bool dfloat) {
+  PG_ARG(na > 0 && nb > 0 && na * nb <= kMaxGramOut && na + nb <= 144, "gram: %d x %d outputs exceed the limits",
+         na, nb);
   PG_TRY(rs.ensure());
+  PG_TRY(opt_in_smem());
   const long chunk = chunk_for(N, kRedBlocks, kTP);
   const int blocks = (int)((N + chunk - 1) / chunk);
-  const size_t smem = sizeof(double) * (size_t)(na + nb) * (kTP + 1);
-  if (smem > 48 * 1024) PG_CUDA_TRY(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
-  PG_TRY(check_launch("k_gram"));
+  if (dfloat) {
+    const size_t smem = sizeof(float) * 2 * (size_t)(na + nb) * (kTP + 1);
+    k_gram_df<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
+    PG_TRY(check_launch("k_gram_df"));
+  } else {
+    const size_t smem = sizeof(double) * (size_t)(na + nb) * (kTP + 1);
+    k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
+    PG_TRY(check_launch("k_gram"));
+  }
   return reduce(rs.partial.p, blocks, na * nb, out, false, st);
 }
 
 pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
-                  cudaStream_t st) {
-  PG_ARG(nr > 0 && nr <= kMaxCombine && na >= 0, "combine: bad sizes na=%d nr=%d", na, nr);
+                  cudaStream_t st, bool dfloat) {
+  PG_ARG(nr > 0 && nr <= kMaxCombine && na >= 0 && na * nr <= 128 * kMaxCombine, "combine: bad sizes na=%d nr=%d",
+         na, nr);
   PG_TRY(rs.ensure());
+  PG_TRY(opt_in_smem());
   const long chunk = chunk_for(N, kRedBlocks, kT);
   const int blocks = (int)((N + chunk - 1) / chunk);
-  const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
-  if (smem > 48 * 1024)
-    PG_CUDA_TRY(cudaFuncSetAttribute(k_combine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_combine<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr,
-                                      sq ? rs.partial.p : nullptr);
-  PG_TRY(check_launch("k_combine"));
+  if (dfloat) {
+    const size_t smem = sizeof(float) * 2 * (size_t)(na > 0 ? na : 1) * nr;
+    k_combine_df<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr,
+                                           sq ? rs.partial.p : nullptr);
+    PG_TRY(check_launch("k_combine_df"));
+  } else {
+    const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
+    k_combine<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr,
+                                        sq ? rs.partial.p : nullptr);
+    PG_TRY(check_launch("k_combine"));
+  }
   return sq ? reduce(rs.partial.p, blocks, nr, sq, true, st) : PG_OK;
 }
 

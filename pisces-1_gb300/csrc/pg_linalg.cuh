@@ -22,7 +22,10 @@ struct RedScratch {
 };
 
 // out[a*nb + b] = sum_g P[a*N + g] * Q[b*N + g]     (a < na, b < nb; na*nb <= kMaxGramOut)
-pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs, cudaStream_t st);
+// dfloat: products and sums in double-float (two-FP32) arithmetic, ~2^-48
+// relative, on the FP32 pipe instead of the FP64 pipe.
+pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs, cudaStream_t st,
+               bool dfloat = false);
 
 // Y[r*N + g] = alpha_r * X[r*N + g] + cscale * sum_a P[a*N + g] * C[a*ca + r*cr]   (r < nr <= kMaxCombine)
 // alpha_r: 0 if alpha is null; alpha[r] if inv_sqrt is false; 1/sqrt(alpha[r]) if true.
@@ -30,7 +33,7 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
 // not null, sq[r] = |Y_r|^2 and sq[nr + r] = 1/|Y_r|.
 pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
-                  cudaStream_t st);
+                  cudaStream_t st, bool dfloat = false);
 
 // sq[r] = |X_r|^2 and sq[nr + r] = 1/|X_r| for r < nr.
 pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st);
