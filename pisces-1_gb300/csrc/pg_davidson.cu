@@ -101,14 +101,24 @@ __global__ void k_jd_prep(long N, double* __restrict__ r, double* __restrict__ j
 
 // Diagonal of the kinetic preconditioner in the DST-I eigenbasis:
 // y_v(i,j,k) /= (dx_i + dy_j + dz_k - sigma_v), the denominator kept at
-// least `floor` in magnitude.
+// least `floor` in magnitude.  fast: the scale factor in FP32 (it only sets
+// the convergence rate; the mixed form uses it to stay off the FP64 pipe).
 __global__ void k_kin_scale(int nx, int ny, int nz, const double* __restrict__ dx, const double* __restrict__ dy,
                             const double* __restrict__ dz, const double* __restrict__ sigma, double floor,
-                            double* __restrict__ Y, int nvec) {
+                            double* __restrict__ Y, int nvec, int fast) {
   const long N = (long)nx * ny * nz;
   for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
     const int i = (int)(g % nx);
     const long r = g / nx;
+    if (fast) {
+      const float dk = (float)dx[i] + (float)dy[(int)(r % ny)] + (float)dz[(int)(r / ny)];
+      for (int v = 0; v < nvec; ++v) {
+        float den = dk - (float)sigma[v];
+        if (fabsf(den) < (float)floor) den = den < 0 ? -(float)floor : (float)floor;
+        Y[(long)v * N + g] *= (double)(1.0f / den);
+      }
+      continue;
+    }
     const double dk = dx[i] + dy[(int)(r % ny)] + dz[(int)(r / ny)];
     for (int v = 0; v < nvec; ++v) {
       double den = dk - sigma[v];
@@ -232,7 +242,7 @@ pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* s
   double dmin = 0;
   for (int a = 0; a < 3; ++a) dmin += 0.5 * (M_PI / g->L[a]) * (M_PI / g->L[a]);
   k_kin_scale<<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], g->d_dev[0].p, g->d_dev[1].p, g->d_dev[2].p,
-                                            sigma_dev, 0.1 * dmin, w1, k);
+                                            sigma_dev, 0.1 * dmin, w1, k, pr == PG_MIXED ? 1 : 0);
   PG_TRY(check_launch("k_kin_scale"));
   PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, w1, w2, k, 0, pr, st));
   PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w2, w1, k, 0, pr, st));

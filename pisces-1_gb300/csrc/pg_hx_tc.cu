@@ -28,6 +28,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kTileM = 128;
 constexpr int kMaxN = 112;  // n_axis handled with the whole K extent resident in shared memory
+constexpr int kBatch = 8;   // global loads a thread keeps in flight while filling A
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -151,23 +152,31 @@ __global__ void __launch_bounds__(kThreads, 1)
   for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long c0 = tile * kTileM;
     // ---- A operand: 128 columns x K, split into TF32 hi/lo
-    if (AXIS == 0) {  // a column is a contiguous line: read along K
-      for (int e = tid; e < kTileM * kpad; e += kThreads) {
-        const int m = e / kpad, k = e - (e / kpad) * kpad;
+    // eight loads per thread in flight, then split and store
+    for (int e0 = tid; e0 < kTileM * kpad; e0 += kBatch * kThreads) {
+      double xv[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * kThreads;
+        // AXIS 0: a column is a contiguous line, read along K;
+        // AXIS 1, 2: consecutive columns are consecutive addresses, read across columns
+        const int m = AXIS == 0 ? e / kpad : (e & (kTileM - 1));
+        const int k = AXIS == 0 ? e - (e / kpad) * kpad : (e >> 7);
         const long c = c0 + m;
-        float h = 0.f, l = 0.f;
-        if (k < n && c < am.ncols) split_tf32(X[(long)nx * c + k], h, l);
-        *(float*)(sAh + kmajor_off(m, k, kpad)) = h;
-        *(float*)(sAl + kmajor_off(m, k, kpad)) = l;
+        const bool in = e < kTileM * kpad && k < n && c < am.ncols;
+        xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)k * am.stride] : 0.0;
       }
-    } else {  // consecutive columns are consecutive addresses: read across columns
-      for (int e = tid; e < kTileM * kpad; e += kThreads) {
-        const int m = e & (kTileM - 1), k = e >> 7;
-        const long c = c0 + m;
-        float h = 0.f, l = 0.f;
-        if (k < n && c < am.ncols) split_tf32(X[col_base<AXIS>(c, nx, ny, N) + (long)k * am.stride], h, l);
-        *(float*)(sAh + kmajor_off(m, k, kpad)) = h;
-        *(float*)(sAl + kmajor_off(m, k, kpad)) = l;
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * kThreads;
+        if (e < kTileM * kpad) {
+          const int m = AXIS == 0 ? e / kpad : (e & (kTileM - 1));
+          const int k = AXIS == 0 ? e - (e / kpad) * kpad : (e >> 7);
+          float h, l;
+          split_tf32(xv[u], h, l);
+          *(float*)(sAh + kmajor_off(m, k, kpad)) = h;
+          *(float*)(sAl + kmajor_off(m, k, kpad)) = l;
+        }
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -206,20 +215,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     const long c = c0 + m;
     const bool cvalid = c < am.ncols;
     const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
+    const long gshift = cvalid ? (c / (N / n)) * N : 0;  // vector offset: grid point = address - gshift
     for (int chunk = half; chunk * 16 < npad; chunk += 2) {
       float d[16];
       tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(chunk * 16), d);
       if (cvalid) {
+        // all loads of the chunk first (16 in flight), then the stores
+        double prev[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int i = chunk * 16 + j;
+          const long a = base + (long)i * am.stride;
+          prev[j] = 0.0;
           if (i < n) {
-            const long a = base + (long)i * am.stride;
-            double prev = 0.0;
-            if (mode == 2) prev = v[a % N] * X[a];
-            else if (mode == 1) prev = Y[a];
-            Y[a] = prev + (double)d[j];
+            if (mode == 2) prev[j] = v[a - gshift] * X[a];
+            else if (mode == 1) prev[j] = Y[a];
           }
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int i = chunk * 16 + j;
+          if (i < n) Y[base + (long)i * am.stride] = prev[j] + (double)d[j];
         }
       }
     }

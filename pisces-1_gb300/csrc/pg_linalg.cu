@@ -12,7 +12,8 @@ namespace pg {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kTP = 32;  // points per shared-memory tile in k_gram
+constexpr int kTP = 32;     // points per shared-memory tile in k_gram
+constexpr int kBatch = 8;   // global loads a thread keeps in flight
 
 long chunk_for(long N, int blocks, int align) {
   long c = (N + blocks - 1) / blocks;
@@ -50,13 +51,22 @@ __global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* _
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
   for (long g0 = g_begin; g0 < g_end; g0 += kTP) {
     const int cnt = g_end - g0 < kTP ? (int)(g_end - g0) : kTP;
-    for (int e = threadIdx.x; e < na * kTP; e += kT) {
-      const int a = e / kTP, p = e % kTP;
-      Ps[a * (kTP + 1) + p] = p < cnt ? P[(long)a * N + g0 + p] : 0.0;
-    }
-    for (int e = threadIdx.x; e < nb * kTP; e += kT) {
-      const int b = e / kTP, p = e % kTP;
-      Qs[b * (kTP + 1) + p] = p < cnt ? Q[(long)b * N + g0 + p] : 0.0;
+    // rows 0..na-1 from P, na..na+nb-1 from Q (Qs follows Ps); batched loads
+    const int tot = (na + nb) * kTP;
+    for (int e0 = threadIdx.x; e0 < tot; e0 += kBatch * kT) {
+      double v[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * kT;
+        const int row = e / kTP, p = e % kTP;
+        const double* src = row < na ? P + (long)row * N : Q + (long)(row - na) * N;
+        v[u] = (e < tot && p < cnt) ? src[g0 + p] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * kT;
+        if (e < tot) Ps[(e / kTP) * (kTP + 1) + e % kTP] = v[u];
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -110,12 +120,19 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
     double acc[kMaxCombine];
 #pragma unroll
     for (int r = 0; r < kMaxCombine; ++r) acc[r] = (r < nr && X && alpha) ? al[r] * X[(long)r * N + g] : 0.0;
-    for (int a = 0; a < na; ++a) {
-      const double p = P[(long)a * N + g];
-      const double* c = Cs + a * nr;
+    // eight independent loads in flight before they are consumed
+    for (int a0 = 0; a0 < na; a0 += kBatch) {
+      double pv[kBatch];
 #pragma unroll
-      for (int r = 0; r < kMaxCombine; ++r)
-        if (r < nr) acc[r] += p * c[r];
+      for (int u = 0; u < kBatch; ++u) pv[u] = a0 + u < na ? P[(long)(a0 + u) * N + g] : 0.0;
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        if (a0 + u >= na) break;
+        const double* c = Cs + (a0 + u) * nr;
+#pragma unroll
+        for (int r = 0; r < kMaxCombine; ++r)
+          if (r < nr) acc[r] += pv[u] * c[r];
+      }
     }
 #pragma unroll
     for (int r = 0; r < kMaxCombine; ++r)
@@ -224,10 +241,12 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl)
 __global__ void __launch_bounds__(kT) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
                                                 const double* __restrict__ Q, int nb, double* __restrict__ partial) {
   extern __shared__ float smf[];
-  float* Ph = smf;                         // na x (kTP+1)
-  float* Pl = Ph + na * (kTP + 1);
-  float* Qh = Pl + na * (kTP + 1);         // nb x (kTP+1)
-  float* Ql = Qh + nb * (kTP + 1);
+  float* Hs = smf;                          // high parts, (na + nb) x (kTP+1): P rows then Q rows
+  float* Ls = smf + (na + nb) * (kTP + 1);  // low parts, same layout
+  const float* Ph = Hs;
+  const float* Pl = Ls;
+  const float* Qh = Hs + na * (kTP + 1);
+  const float* Ql = Ls + na * (kTP + 1);
   const int no = na * nb;
   float ah[kMaxGramOut / kT], al[kMaxGramOut / kT];
 #pragma unroll
@@ -236,19 +255,26 @@ __global__ void __launch_bounds__(kT) k_gram_df(long N, long chunk, const double
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
   for (long g0 = g_begin; g0 < g_end; g0 += kTP) {
     const int cnt = g_end - g0 < kTP ? (int)(g_end - g0) : kTP;
-    for (int e = threadIdx.x; e < na * kTP; e += kT) {
-      const int a = e / kTP, p = e % kTP;
-      float h = 0.f, l = 0.f;
-      if (p < cnt) df_split(P[(long)a * N + g0 + p], h, l);
-      Ph[a * (kTP + 1) + p] = h;
-      Pl[a * (kTP + 1) + p] = l;
-    }
-    for (int e = threadIdx.x; e < nb * kTP; e += kT) {
-      const int b = e / kTP, p = e % kTP;
-      float h = 0.f, l = 0.f;
-      if (p < cnt) df_split(Q[(long)b * N + g0 + p], h, l);
-      Qh[b * (kTP + 1) + p] = h;
-      Ql[b * (kTP + 1) + p] = l;
+    const int tot = (na + nb) * kTP;
+    for (int e0 = threadIdx.x; e0 < tot; e0 += kBatch * kT) {
+      double v[kBatch];
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * kT;
+        const int row = e / kTP, p = e % kTP;
+        const double* src = row < na ? P + (long)row * N : Q + (long)(row - na) * N;
+        v[u] = (e < tot && p < cnt) ? src[g0 + p] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        const int e = e0 + u * kT;
+        if (e < tot) {
+          float h, l;
+          df_split(v[u], h, l);
+          Hs[(e / kTP) * (kTP + 1) + e % kTP] = h;
+          Ls[(e / kTP) * (kTP + 1) + e % kTP] = l;
+        }
+      }
     }
     __syncthreads();
 #pragma unroll
@@ -323,14 +349,21 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
         df_fma(sh[r], sl[r], alh[r], all[r], xh, xl);
       }
     }
-    for (int a = 0; a < na; ++a) {
-      float ph, pl;
-      df_split(P[(long)a * N + g], ph, pl);
-      const float* ch = Ch + a * nr;
-      const float* cl = Cl + a * nr;
+    for (int a0 = 0; a0 < na; a0 += kBatch) {
+      double pv[kBatch];
 #pragma unroll
-      for (int r = 0; r < kMaxCombine; ++r)
-        if (r < nr) df_fma(sh[r], sl[r], ph, pl, ch[r], cl[r]);
+      for (int u = 0; u < kBatch; ++u) pv[u] = a0 + u < na ? P[(long)(a0 + u) * N + g] : 0.0;
+#pragma unroll
+      for (int u = 0; u < kBatch; ++u) {
+        if (a0 + u >= na) break;
+        float ph, pl;
+        df_split(pv[u], ph, pl);
+        const float* ch = Ch + (a0 + u) * nr;
+        const float* cl = Cl + (a0 + u) * nr;
+#pragma unroll
+        for (int r = 0; r < kMaxCombine; ++r)
+          if (r < nr) df_fma(sh[r], sl[r], ph, pl, ch[r], cl[r]);
+      }
     }
 #pragma unroll
     for (int r = 0; r < kMaxCombine; ++r)
