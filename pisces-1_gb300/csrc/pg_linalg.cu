@@ -14,6 +14,7 @@ namespace {
 constexpr int kT = 256;
 constexpr int kTP = 32;     // points per shared-memory tile in k_gram
 constexpr int kBatch = 8;   // global loads a thread keeps in flight
+constexpr int kStreamBlocks = 4 * kRedBlocks;  // blocks of the streaming kernels (about one point per thread)
 
 long chunk_for(long N, int blocks, int align) {
   long c = (N + blocks - 1) / blocks;
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* _
   }
 }
 
+template <int NR>
 __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double* P, int na,
                                                 const double* __restrict__ C, int ca, int cr, double cscale,
                                                 const double* X,
@@ -102,8 +104,8 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
                                                 double* __restrict__ partial) {
   extern __shared__ double sm[];
   double* Cs = sm;                 // na x nr
-  __shared__ double al[kMaxCombine];
-  __shared__ double red[kT / 32][kMaxCombine];
+  __shared__ double al[NR];
+  __shared__ double red[kT / 32][NR];
   for (int e = threadIdx.x; e < na * nr; e += kT) Cs[e] = cscale * C[(long)(e / nr) * ca + (long)(e % nr) * cr];
   if (threadIdx.x < nr) {
     double a = 0;
@@ -111,15 +113,15 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
     al[threadIdx.x] = a;
   }
   __syncthreads();
-  double sacc[kMaxCombine];
+  double sacc[NR];
 #pragma unroll
-  for (int r = 0; r < kMaxCombine; ++r) sacc[r] = 0;
+  for (int r = 0; r < NR; ++r) sacc[r] = 0;
   const long g_begin = blockIdx.x * chunk;
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
   for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
-    double acc[kMaxCombine];
+    double acc[NR];
 #pragma unroll
-    for (int r = 0; r < kMaxCombine; ++r) acc[r] = (r < nr && X && alpha) ? al[r] * X[(long)r * N + g] : 0.0;
+    for (int r = 0; r < NR; ++r) acc[r] = (r < nr && X && alpha) ? al[r] * X[(long)r * N + g] : 0.0;
     // eight independent loads in flight before they are consumed
     for (int a0 = 0; a0 < na; a0 += kBatch) {
       double pv[kBatch];
@@ -130,12 +132,12 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
         if (a0 + u >= na) break;
         const double* c = Cs + (a0 + u) * nr;
 #pragma unroll
-        for (int r = 0; r < kMaxCombine; ++r)
+        for (int r = 0; r < NR; ++r)
           if (r < nr) acc[r] += pv[u] * c[r];
       }
     }
 #pragma unroll
-    for (int r = 0; r < kMaxCombine; ++r)
+    for (int r = 0; r < NR; ++r)
       if (r < nr) {
         Y[(long)r * N + g] = acc[r];
         sacc[r] += acc[r] * acc[r];
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
   if (!partial) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int r = 0; r < kMaxCombine; ++r) {
+  for (int r = 0; r < NR; ++r) {
     double v = sacc[r];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp][r] = v;
@@ -307,6 +309,7 @@ __global__ void __launch_bounds__(kT) k_gram_df(long N, long chunk, const double
 
 // Combine in double-float: same contract as k_combine (coefficients and
 // alpha are FP64 and split once per block; Y is written as double).
+template <int NR>
 __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const double* P, int na,
                                                    const double* __restrict__ C, int ca, int cr, double cscale,
                                                    const double* X, const double* __restrict__ alpha, int inv_sqrt,
@@ -314,8 +317,8 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
   extern __shared__ float smf[];
   float* Ch = smf;              // na x nr
   float* Cl = smf + na * nr;
-  __shared__ float alh[kMaxCombine], all[kMaxCombine];
-  __shared__ double red[kT / 32][kMaxCombine];
+  __shared__ float alh[NR], all[NR];
+  __shared__ double red[kT / 32][NR];
   for (int e = threadIdx.x; e < na * nr; e += kT) {
     float h, l;
     df_split(cscale * C[(long)(e / nr) * ca + (long)(e % nr) * cr], h, l);
@@ -331,16 +334,16 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
     all[threadIdx.x] = l;
   }
   __syncthreads();
-  double sacc[kMaxCombine];
+  double sacc[NR];
 #pragma unroll
-  for (int r = 0; r < kMaxCombine; ++r) sacc[r] = 0;
+  for (int r = 0; r < NR; ++r) sacc[r] = 0;
   const bool keep = X && alpha;
   const long g_begin = blockIdx.x * chunk;
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
   for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
-    float sh[kMaxCombine], sl[kMaxCombine];
+    float sh[NR], sl[NR];
 #pragma unroll
-    for (int r = 0; r < kMaxCombine; ++r) {
+    for (int r = 0; r < NR; ++r) {
       sh[r] = 0.f;
       sl[r] = 0.f;
       if (r < nr && keep) {
@@ -361,12 +364,12 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
         const float* ch = Ch + (a0 + u) * nr;
         const float* cl = Cl + (a0 + u) * nr;
 #pragma unroll
-        for (int r = 0; r < kMaxCombine; ++r)
+        for (int r = 0; r < NR; ++r)
           if (r < nr) df_fma(sh[r], sl[r], ph, pl, ch[r], cl[r]);
       }
     }
 #pragma unroll
-    for (int r = 0; r < kMaxCombine; ++r)
+    for (int r = 0; r < NR; ++r)
       if (r < nr) {
         const double y = (double)sh[r] + (double)sl[r];
         Y[(long)r * N + g] = y;
@@ -376,7 +379,7 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
   if (!partial) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int r = 0; r < kMaxCombine; ++r) {
+  for (int r = 0; r < NR; ++r) {
     double v = sacc[r];
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp][r] = v;
@@ -410,8 +413,6 @@ static pg_status opt_in_smem() {
   const int big = (int)(sizeof(double) * (size_t)(128 + 16) * (kTP + 1));
   PG_CUDA_TRY(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   PG_CUDA_TRY(cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PG_CUDA_TRY(cudaFuncSetAttribute(k_combine, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PG_CUDA_TRY(cudaFuncSetAttribute(k_combine_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
   done = true;
   return PG_OK;
 }
@@ -443,17 +444,31 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
          na, nr);
   PG_TRY(rs.ensure());
   PG_TRY(opt_in_smem());
-  const long chunk = chunk_for(N, kRedBlocks, kT);
+  const long chunk = chunk_for(N, kStreamBlocks, kT);
   const int blocks = (int)((N + chunk - 1) / chunk);
   if (dfloat) {
     const size_t smem = sizeof(float) * 2 * (size_t)(na > 0 ? na : 1) * nr;
-    k_combine_df<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr,
-                                           sq ? rs.partial.p : nullptr);
+#define PG_COMBINE_DF(NRV) \
+  k_combine_df<NRV><<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, \
+                                              sq ? rs.partial.p : nullptr)
+    if (nr <= 1) PG_COMBINE_DF(1);
+    else if (nr <= 2) PG_COMBINE_DF(2);
+    else if (nr <= 4) PG_COMBINE_DF(4);
+    else if (nr <= 8) PG_COMBINE_DF(8);
+    else PG_COMBINE_DF(16);
+#undef PG_COMBINE_DF
     PG_TRY(check_launch("k_combine_df"));
   } else {
     const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
-    k_combine<<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr,
-                                        sq ? rs.partial.p : nullptr);
+#define PG_COMBINE(NRV) \
+  k_combine<NRV><<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, \
+                                           sq ? rs.partial.p : nullptr)
+    if (nr <= 1) PG_COMBINE(1);
+    else if (nr <= 2) PG_COMBINE(2);
+    else if (nr <= 4) PG_COMBINE(4);
+    else if (nr <= 8) PG_COMBINE(8);
+    else PG_COMBINE(16);
+#undef PG_COMBINE
     PG_TRY(check_launch("k_combine"));
   }
   return sq ? reduce(rs.partial.p, blocks, nr, sq, true, st) : PG_OK;
