@@ -235,6 +235,76 @@ pg_status pg_cluster_solve(const int n[3], const double L[3], int nw, const doub
                            const double* ions_angstrom_q, const pg_solve_params* p, double* evals_host,
                            double* evecs_host, pg_solve_stats* stats, void* stream);
 
+/* ---- Serving engine ------------------------------------------------------
+ * A request loop for streams of single points (geometry-optimisation and
+ * MD-snapshot streams): the role of the reference's repeated
+ * ClusterAnion::EnergyFromConfiguration calls (src/ClusterAnion.cpp:192-290,
+ * warm start istartvec = 0 after the first solve at :291), which the
+ * reference runs one at a time.  Requests of different clusters, grids and
+ * state counts are admitted while slots and device memory allow, run
+ * concurrently on their own streams, warm-start from the last converged
+ * eigenvectors of the same key, and have their mixed-form H*X products on a
+ * shared grid merged into one tensor-core launch per axis. */
+typedef struct pg_engine pg_engine;
+
+typedef struct {
+  int device;             /* CUDA device of the engine (-1: the calling thread's current device) */
+  int slots;              /* solves in flight at once, one worker thread + stream each (default 8) */
+  double memory_budget;   /* bytes of device memory admitted solves may need together (<= 0: 80% of free) */
+  int batch_matvecs;      /* 1: merge concurrent mixed-form H*X products on the same grid */
+  int batch_window_us;    /* how long a product waits for partners on its grid (default 200) */
+  int warm_start;         /* 1: start from the cached eigenvectors of the request's key */
+} pg_engine_config;
+
+typedef struct {
+  int n[3];
+  double L[3];
+  int nw;                       /* waters, 9 doubles each (O, H, H in Angstrom) */
+  const double* waters;
+  int nions;                    /* ions, 4 doubles each (x, y, z in Angstrom, charge) */
+  const double* ions;
+  pg_solve_params params;       /* startvec 1 or 2: used when no cached vectors exist */
+  long key;                     /* warm-start key (e.g. base cluster id); < 0: none */
+  double* evecs_host;           /* optional: receives nroots*N eigenvector values */
+} pg_request;
+
+typedef struct {
+  long id;
+  pg_status status;
+  int nroots;
+  int warm_started;             /* 1 if the solve started from cached vectors */
+  double evals[64];
+  pg_solve_stats stats;
+  double queue_seconds;         /* submit -> start */
+  double latency_seconds;       /* submit -> result */
+  char error[256];
+} pg_result;
+
+typedef struct {
+  long submitted, completed, failed;
+  long warm_starts;
+  long batches;                 /* merged H*X launches (one per axis counts once) */
+  long batched_products;        /* products that went through them */
+  int peak_in_flight;
+  double peak_bytes;            /* largest admitted footprint sum */
+} pg_engine_stats;
+
+/* Footprint of one request in device bytes: the solve buffers (basis and
+ * product blocks, work array, diagonal, potential, eigenvectors). */
+double pg_request_footprint(const pg_request* r);
+pg_status pg_engine_create(const pg_engine_config* c, pg_engine** out);
+/* Copies the request's host data; returns at once.  PG_OOM if the request
+ * alone exceeds the memory budget. */
+pg_status pg_engine_submit(pg_engine* e, const pg_request* r, long* id);
+/* Blocks until request id is done (timeout_s < 0: no limit) and hands over
+ * its result; PG_DEVICE_TIMEOUT when the limit passes first. */
+pg_status pg_engine_wait(pg_engine* e, long id, pg_result* out, double timeout_s);
+/* Hands over up to max finished results in completion order. */
+pg_status pg_engine_poll(pg_engine* e, pg_result* out, int max, int* nout);
+pg_status pg_engine_get_stats(pg_engine* e, pg_engine_stats* out);
+/* Finishes the admitted solves, fails the queued ones, joins the workers. */
+pg_status pg_engine_destroy(pg_engine* e);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,29 @@ class SolveStats(C.Structure):
                 "host_eig_seconds": self.host_eig_seconds, "device_wait_seconds": self.device_wait_seconds}
 
 
+class EngineConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("memory_budget", C.c_double),
+                ("batch_matvecs", C.c_int), ("batch_window_us", C.c_int), ("warm_start", C.c_int)]
+
+
+class Request(C.Structure):
+    _fields_ = [("n", C.c_int * 3), ("L", C.c_double * 3), ("nw", C.c_int), ("waters", _dp),
+                ("nions", C.c_int), ("ions", _dp), ("params", SolveParams), ("key", C.c_long),
+                ("evecs_host", _dp)]
+
+
+class Result(C.Structure):
+    _fields_ = [("id", C.c_long), ("status", C.c_int), ("nroots", C.c_int), ("warm_started", C.c_int),
+                ("evals", C.c_double * 64), ("stats", SolveStats), ("queue_seconds", C.c_double),
+                ("latency_seconds", C.c_double), ("error", C.c_char * 256)]
+
+
+class EngineStats(C.Structure):
+    _fields_ = [("submitted", C.c_long), ("completed", C.c_long), ("failed", C.c_long),
+                ("warm_starts", C.c_long), ("batches", C.c_long), ("batched_products", C.c_long),
+                ("peak_in_flight", C.c_int), ("peak_bytes", C.c_double)]
+
+
 _lib = None
 
 # exported C-ABI symbols (also checked by the CPU tests against the header)
@@ -95,6 +118,13 @@ SYMBOLS = {
     "pg_cluster_solve": (C.c_int, [_ip, _dp, C.c_int, _dp, C.c_int, _dp, C.POINTER(SolveParams), _dp, _dp,
                                    C.POINTER(SolveStats), _vp]),
     "pg_glibc_rand_check": (C.c_int, [C.c_int, _ip]),
+    "pg_request_footprint": (C.c_double, [C.POINTER(Request)]),
+    "pg_engine_create": (C.c_int, [C.POINTER(EngineConfig), C.POINTER(_vp)]),
+    "pg_engine_submit": (C.c_int, [_vp, C.POINTER(Request), C.POINTER(C.c_long)]),
+    "pg_engine_wait": (C.c_int, [_vp, C.c_long, C.POINTER(Result), C.c_double]),
+    "pg_engine_poll": (C.c_int, [_vp, C.POINTER(Result), C.c_int, _ip]),
+    "pg_engine_get_stats": (C.c_int, [_vp, C.POINTER(EngineStats)]),
+    "pg_engine_destroy": (C.c_int, [_vp]),
 }
 
 
@@ -365,3 +395,98 @@ def glibc_rand_stream(count):
     out = np.empty(count, dtype=np.int32)
     lib().pg_glibc_rand_check(count, _i(out))
     return out
+
+
+def _result_dict(r: Result):
+    nr = r.nroots
+    return {"id": r.id, "status": r.status, "evals": list(r.evals[:nr]), "warm_started": bool(r.warm_started),
+            "stats": r.stats.as_dict(nr), "queue_seconds": r.queue_seconds, "latency_seconds": r.latency_seconds,
+            "error": r.error.decode(errors="replace")}
+
+
+class Engine:
+    """The serving engine (pg_engine_*): concurrent single points with
+    footprint admission, warm start per key and merged mixed-form H*X."""
+
+    def __init__(self, slots=8, memory_budget=0.0, batch_matvecs=True, batch_window_us=200, warm_start=True,
+                 device=-1):
+        self._h = _vp()
+        self.config = EngineConfig(device, slots, memory_budget, int(batch_matvecs), batch_window_us,
+                                   int(warm_start))
+        _check(lib().pg_engine_create(C.byref(self.config), C.byref(self._h)))
+        self._keep = {}  # host arrays that must live until their request is done
+
+    def close(self):
+        if self._h:
+            lib().pg_engine_destroy(self._h)
+            self._h = _vp()
+            self._keep.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def request(n, L, waters_angstrom, ions=None, nroots=1, maxsub=20, maxiter=100, ptol=5, corrflag=1,
+                precision=PG_FP64, startvec=1, refine=1, key=-1, want_vectors=False):
+        """A request with its host arrays (kept alive by the returned tuple)."""
+        n = [int(x) for x in np.broadcast_to(n, 3)]
+        L = [float(x) for x in np.broadcast_to(L, 3)]
+        w = np.ascontiguousarray(waters_angstrom, dtype=np.float64).reshape(-1)
+        io = np.ascontiguousarray(ions if ions is not None else np.zeros((0, 4)), dtype=np.float64).reshape(-1)
+        vec = np.empty(nroots * n[0] * n[1] * n[2]) if want_vectors else None
+        r = Request((C.c_int * 3)(*n), (C.c_double * 3)(*L), len(w) // 9, _d(w) if len(w) else None,
+                    len(io) // 4, _d(io) if len(io) else None,
+                    SolveParams(nroots, maxsub, maxiter, ptol, corrflag, precision, startvec, refine), key,
+                    _d(vec) if want_vectors else None)
+        return r, (w, io, vec)
+
+    @staticmethod
+    def footprint(req):
+        """Device bytes the engine admits the request with."""
+        r = req[0] if isinstance(req, tuple) else req
+        return lib().pg_request_footprint(C.byref(r))
+
+    def submit(self, req):
+        """Submit a request made by Engine.request; returns its id."""
+        r, keep = req
+        rid = C.c_long(0)
+        _check(lib().pg_engine_submit(self._h, C.byref(r), C.byref(rid)))
+        self._keep[rid.value] = keep
+        return rid.value
+
+    def wait(self, rid, timeout=-1.0):
+        """Result of request rid (a dict; 'vectors' holds the eigenvectors when asked for)."""
+        out = Result()
+        _check(lib().pg_engine_wait(self._h, rid, C.byref(out), timeout))
+        d = _result_dict(out)
+        keep = self._keep.pop(rid, None)
+        if keep is not None and keep[2] is not None:
+            d["vectors"] = keep[2].reshape(out.nroots, -1)
+        return d
+
+    def poll(self, max_results=64):
+        buf = (Result * max_results)()
+        k = C.c_int(0)
+        _check(lib().pg_engine_poll(self._h, buf, max_results, C.byref(k)))
+        res = []
+        for i in range(k.value):
+            d = _result_dict(buf[i])
+            keep = self._keep.pop(buf[i].id, None)
+            if keep is not None and keep[2] is not None:
+                d["vectors"] = keep[2].reshape(buf[i].nroots, -1)
+            res.append(d)
+        return res
+
+    def stats(self):
+        s = EngineStats()
+        _check(lib().pg_engine_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in EngineStats._fields_}

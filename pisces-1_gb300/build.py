@@ -74,7 +74,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         raise RuntimeError("build failed:\n" + "\n".join(errors))
     objs = [o for o, _ in results]
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs, "-lcuda"]
+        cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", LIB, *objs, "-lpthread", "-lcuda"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             # libcuda is only needed for driver-API entry points; link without it if absent

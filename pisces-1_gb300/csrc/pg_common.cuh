@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -74,6 +75,9 @@ struct DevBuf {
     n = count;
     return PG_OK;
   }
+  // Grow-only: keeps the buffer if it already holds count elements (a
+  // long-lived owner then allocates, and frees, only while it grows).
+  pg_status ensure(size_t count) { return n >= count && p ? PG_OK : alloc(count); }
   void release() {
     if (p) cudaFree(p);
     p = nullptr;
@@ -101,6 +105,10 @@ struct pg_grid {
   pg::DevBuf<double> q_dev[3];
   pg::DevBuf<float> q_hi[3], q_lo[3];
   pg::DevBuf<double> d_dev[3];
+  // random start columns (Randm11 from seed 1; the same values for every
+  // solve on this grid), generated once and grown on demand
+  mutable std::mutex start_m;
+  mutable pg::DevBuf<double> start_rand;
 };
 
 namespace pg {

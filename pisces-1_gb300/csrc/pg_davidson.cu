@@ -23,9 +23,11 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "pg_linalg.cuh"
+#include "pg_solve.cuh"
 
 struct pg_davidson {
   int status = 0;
@@ -182,13 +184,15 @@ constexpr int kSigma = 128; // shifts of the kinetic preconditioner (16)
 constexpr int kScalars = 256;
 
 pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
-  if (d->ndim == ndim && d->maxsub >= maxsub && d->nroots >= nroots && d->dcoef.p) return PG_OK;
-  PG_TRY(d->dcoef.alloc((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
-  PG_TRY(d->dgram.alloc((size_t)kMaxGramOut));
-  PG_TRY(d->dsq.alloc(kScalars));
-  std::vector<double> init(kScalars, 0.0);
-  for (int i = 0; i < 16; ++i) init[kOnes + i] = 1.0;
-  PG_CUDA_TRY(cudaMemcpy(d->dsq.p, init.data(), sizeof(double) * kScalars, cudaMemcpyHostToDevice));
+  // grow-only scratch: a reused handle allocates only while its problems grow
+  PG_TRY(d->dcoef.ensure((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
+  PG_TRY(d->dgram.ensure((size_t)kMaxGramOut));
+  if (!d->dsq.p) {
+    PG_TRY(d->dsq.alloc(kScalars));
+    std::vector<double> init(kScalars, 0.0);
+    for (int i = 0; i < 16; ++i) init[kOnes + i] = 1.0;
+    PG_CUDA_TRY(cudaMemcpy(d->dsq.p, init.data(), sizeof(double) * kScalars, cudaMemcpyHostToDevice));
+  }
   d->ndim = ndim;
   d->maxsub = maxsub;
   d->nroots = nroots;
@@ -229,10 +233,8 @@ __global__ void k_cholinv(const double* __restrict__ G, int k, double* __restric
 pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* sigma_dev, cudaStream_t st) {
   const pg_grid* g = d->pc_grid;
   const long N = g->N;
-  if (d->pc_w1.n < (size_t)k * N) {
-    PG_TRY(d->pc_w1.alloc((size_t)d->nroots * N));
-    PG_TRY(d->pc_w2.alloc((size_t)d->nroots * N));
-  }
+  PG_TRY(d->pc_w1.ensure((size_t)d->nroots * N));
+  PG_TRY(d->pc_w2.ensure((size_t)d->nroots * N));
   double *w1 = d->pc_w1.p, *w2 = d->pc_w2.p;
   const int pr = d->pc_precision;
   PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, R, w1, k, 0, pr, st));
@@ -542,16 +544,23 @@ pg_status start_vectors(const pg_grid* g, int nroots, int startvec, double* B, c
     istart = 1;
   }
   if (istart < nroots) {
-    // Randm11 (src/DVR.cpp:52-59): sign draw, then magnitude draw
-    GlibcRand rnd(1);
-    std::vector<double> h((size_t)(nroots - istart) * N);
-    for (auto& x : h) {
-      if (rnd() > kRandMax / 2) x = (double)rnd() / kRandMax;
-      else x = -(double)rnd() / kRandMax;
+    // Randm11 (src/DVR.cpp:52-59): sign draw, then magnitude draw.  The
+    // sequence restarts at seed 1 for every solve, so the grid keeps it.
+    const size_t cnt = (size_t)(nroots - istart) * N;
+    std::lock_guard<std::mutex> l(g->start_m);
+    if (g->start_rand.n < cnt) {
+      GlibcRand rnd(1);
+      std::vector<double> h(cnt);
+      for (auto& x : h) {
+        if (rnd() > kRandMax / 2) x = (double)rnd() / kRandMax;
+        else x = -(double)rnd() / kRandMax;
+      }
+      PG_TRY(g->start_rand.alloc(cnt));
+      PG_CUDA_TRY(cudaMemcpyAsync(g->start_rand.p, h.data(), sizeof(double) * cnt, cudaMemcpyHostToDevice, st));
     }
-    PG_CUDA_TRY(cudaMemcpyAsync(B + (long)istart * N, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice,
-                                st));
-    PG_CUDA_TRY(cudaStreamSynchronize(st));
+    PG_CUDA_TRY(cudaMemcpyAsync(B + (long)istart * N, g->start_rand.p, sizeof(double) * cnt,
+                                cudaMemcpyDeviceToDevice, st));
+    PG_CUDA_TRY(cudaStreamSynchronize(st));  // before another solve may regrow the cache
   }
   return PG_OK;
 }
@@ -565,28 +574,45 @@ extern "C" int pg_glibc_rand_check(int count, int* out) {
   return 0;
 }
 
-extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_params* p, double* evals,
-                              double* evecs, pg_solve_stats* stats, void* stream) {
-  using namespace pg;
+namespace pg {
+
+// Buffers of one eigensolve, kept by a long-lived caller (a serving worker)
+// so that repeated solves allocate only while their sizes grow.
+struct SolveWorkspace {
+  DevBuf<double> B, Z, diag, work;
+  pg_davidson d;
+};
+
+SolveWorkspace* workspace_create() { return new SolveWorkspace(); }
+void workspace_destroy(SolveWorkspace* w) { delete w; }
+
+// The device eigensolve of pg_solve with the H*X product supplied by the
+// caller (the serving engine routes it through its cross-solve batcher).
+pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p, double* evals, double* evecs,
+                     pg_solve_stats* stats, cudaStream_t st,
+                     const std::function<pg_status(const double*, double*, int)>& matvec, SolveWorkspace* wsp) {
   PG_ARG(g && v && p && evals && evecs, "pg_solve: null argument");
   PG_ARG(p->nroots > 0 && p->maxsub > p->nroots && p->maxiter > 0 && p->ptol > 0, "pg_solve: bad parameters");
   PG_ARG(p->precision == PG_FP64 || p->precision == PG_MIXED, "pg_solve: unknown precision");
   PG_ARG(g->N < (1L << 31), "pg_solve: grid too large for the reverse-communication interface");
   auto t0 = std::chrono::steady_clock::now();
-  cudaStream_t st = as_stream(stream);
   const long N = g->N;
   const int ms = p->maxsub, nr = p->nroots;
-  DevBuf<double> B, Z, diag, work;
-  PG_TRY(B.alloc((size_t)ms * N));
-  PG_TRY(Z.alloc((size_t)ms * N));
-  PG_TRY(diag.alloc(N));
-  PG_TRY(work.alloc((size_t)pg_davidson_work_size((int)N, ms, nr, p->corrflag)));
+  SolveWorkspace local;
+  SolveWorkspace& ws = wsp ? *wsp : local;
+  DevBuf<double>&B = ws.B, &Z = ws.Z, &diag = ws.diag, &work = ws.work;
+  PG_TRY(B.ensure((size_t)ms * N));
+  PG_TRY(Z.ensure((size_t)ms * N));
+  PG_TRY(diag.ensure(N));
+  PG_TRY(work.ensure((size_t)pg_davidson_work_size((int)N, ms, nr, p->corrflag)));
   if (p->startvec == 0)
     PG_CUDA_TRY(cudaMemcpyAsync(B.p, evecs, sizeof(double) * N * nr, cudaMemcpyDeviceToDevice, st));
   else
     PG_TRY(start_vectors(g, nr, p->startvec, B.p, st));
   PG_TRY(pg_diagonal(g, v, diag.p, st));
-  pg_davidson d;
+  pg_davidson& d = ws.d;
+  d.status = 0;  // a fresh solve, whatever the last one left behind
+  d.pc_grid = nullptr;
   if (p->corrflag == 3) PG_TRY(pg_davidson_set_preconditioner(&d, g, p->precision));
   d.dfloat = p->precision == PG_MIXED;
   int inout[3] = {0, 0, 0}, nconv = 0, ret = 1;
@@ -598,11 +624,13 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
     if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
     if (ret == 1) {
       // the whole block in one launch (the reference multiplies vector by vector)
-      PG_TRY(hx(g, v, B.p + (long)inout[0] * N, Z.p + (long)inout[1] * N, inout[2], p->precision, st));
+      PG_TRY(matvec(B.p + (long)inout[0] * N, Z.p + (long)inout[1] * N, inout[2]));
       nmv += inout[2];
     }
   }
   const pg_status conv_status = s;
+  if (nconv < nr)  // not converged: report the current Ritz values
+    for (int r = 0; r < nr && r < (int)d.sse.size(); ++r) evals[r] = d.sse[r];
   if (p->precision == PG_MIXED) PG_TRY(check_tc_error(g, st));
   if (p->precision == PG_MIXED && p->refine) {
     // FP64 Rayleigh-Ritz on the converged vectors: Z = H B with the FP64
@@ -638,6 +666,47 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
   return conv_status;
 }
 
+// V(r) of a water cluster (default model) plus Bloomfield ions, on the device.
+pg_status cluster_potential(const pg_grid* g, int nw, const double* waters, int nions, const double* ions, double* v,
+                            cudaStream_t st) {
+  const long N = g->N;
+  if (nw > 0) {
+    std::vector<double> sites(12 * (size_t)nw), q(3 * (size_t)nw), dip(9 * (size_t)nw), sto(8 * (size_t)nw),
+        pa(nw);
+    std::vector<int> qs(3 * (size_t)nw), ds(3 * (size_t)nw), ss(4 * (size_t)nw), ps(nw);
+    int it = 0;
+    PG_TRY(pg_water_sites(nw, waters, sites.data(), q.data(), qs.data(), dip.data(), ds.data(), &it));
+    pg_sites t;
+    PG_TRY(pg_water_default_tables(nw, sites.data(), q.data(), qs.data(), dip.data(), ds.data(), sto.data(),
+                                   ss.data(), pa.data(), ps.data(), &t));
+    PG_TRY(pg_potential_eval(g, &t, v, nullptr, st));
+  } else {
+    PG_CUDA_TRY(cudaMemsetAsync(v, 0, sizeof(double) * N, st));
+  }
+  if (nions > 0) {
+    std::vector<double> pos(3 * (size_t)nions), qi(nions);
+    const double a2b = 1.0 / 0.52917720859;
+    for (int i = 0; i < nions; ++i) {
+      for (int c = 0; c < 3; ++c) pos[3 * i + c] = ions[4 * i + c] * a2b;
+      qi[i] = ions[4 * i + 3];
+    }
+    PG_TRY(pg_potential_ions_add(g, nions, pos.data(), qi.data(), 2.9, 1.0, v, st));
+  }
+  return PG_OK;
+}
+
+}  // namespace pg
+
+extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_params* p, double* evals,
+                              double* evecs, pg_solve_stats* stats, void* stream) {
+  using namespace pg;
+  cudaStream_t st = as_stream(stream);
+  const int prec = p ? p->precision : PG_FP64;
+  return solve_with(
+      g, v, p, evals, evecs, stats, st,
+      [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, prec, st); }, nullptr);
+}
+
 extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw, const double* waters, int nions,
                                       const double* ions, const pg_solve_params* p, double* evals, double* evecs_host,
                                       pg_solve_stats* stats, void* stream) {
@@ -654,28 +723,7 @@ extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw,
   DevBuf<double> v, vec;
   PG_TRY(v.alloc(N));
   PG_TRY(vec.alloc((size_t)N * p->nroots));
-  if (nw > 0) {
-    std::vector<double> sites(12 * (size_t)nw), q(3 * (size_t)nw), dip(9 * (size_t)nw), sto(8 * (size_t)nw),
-        pa(nw);
-    std::vector<int> qs(3 * (size_t)nw), ds(3 * (size_t)nw), ss(4 * (size_t)nw), ps(nw);
-    int it = 0;
-    PG_TRY(pg_water_sites(nw, waters, sites.data(), q.data(), qs.data(), dip.data(), ds.data(), &it));
-    pg_sites t;
-    PG_TRY(pg_water_default_tables(nw, sites.data(), q.data(), qs.data(), dip.data(), ds.data(), sto.data(),
-                                   ss.data(), pa.data(), ps.data(), &t));
-    PG_TRY(pg_potential_eval(g, &t, v.p, nullptr, st));
-  } else {
-    PG_CUDA_TRY(cudaMemsetAsync(v.p, 0, sizeof(double) * N, st));
-  }
-  if (nions > 0) {
-    std::vector<double> pos(3 * (size_t)nions), qi(nions);
-    const double a2b = 1.0 / 0.52917720859;
-    for (int i = 0; i < nions; ++i) {
-      for (int c = 0; c < 3; ++c) pos[3 * i + c] = ions[4 * i + c] * a2b;
-      qi[i] = ions[4 * i + 3];
-    }
-    PG_TRY(pg_potential_ions_add(g, nions, pos.data(), qi.data(), 2.9, 1.0, v.p, st));
-  }
+  PG_TRY(cluster_potential(g, nw, waters, nions, ions, v.p, st));
   pg_status s = pg_solve(g, v.p, p, evals, vec.p, stats, stream);
   if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
   if (evecs_host)

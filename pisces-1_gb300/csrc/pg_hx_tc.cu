@@ -21,7 +21,7 @@
 // bounded and a timeout is reported through an error word.
 #include <cstdint>
 
-#include "pg_common.cuh"
+#include "pg_solve.cuh"
 
 namespace {
 
@@ -100,11 +100,37 @@ __device__ __forceinline__ long col_base(long c, int nx, int ny, long N) {
   return (c - vv * plane) + N * vv;
 }
 
+}  // namespace
+
+namespace pg {
+// One launch serves up to kMaxTcJobs solves on the same grid: job j owns the
+// tiles [tile0_j, tile0_{j+1}) of the launch, with its own X, Y and V.
+constexpr int kMaxTcJobs = 16;
+static_assert(kMaxTcJobs == kMaxBatchJobs, "batcher and kernel job tables differ");
+struct TcJob {
+  const double* x;
+  double* y;
+  const double* v;
+  long ncols;  // columns of this job: N * nvec / n_axis
+  long tile0;  // first tile of this job in the launch
+};
+struct TcJobs {
+  TcJob j[kMaxTcJobs];
+  int n;
+  long ntiles;
+};
+}  // namespace pg
+
+namespace {
+
+using pg::TcJob;
+using pg::TcJobs;
+
 template <int AXIS>
 __global__ void __launch_bounds__(kThreads, 1)
     k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kpad, uint32_t tmem_cols,
-            const float* __restrict__ t_hi, const float* __restrict__ t_lo, const double* __restrict__ v,
-            const double* __restrict__ X, double* __restrict__ Y, int mode, int* __restrict__ err) {
+            const float* __restrict__ t_hi, const float* __restrict__ t_lo, const __grid_constant__ TcJobs jobs,
+            int mode, int* __restrict__ err) {
   // mode 0: Y = D;  1: Y += D;  2: Y = V X + D   (D = the axis contraction)
   extern __shared__ __align__(1024) unsigned char smem[];
   const int n = am.n;
@@ -118,7 +144,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x;
   const long N = (long)nx * ny * nz;
-  const long ntiles = (am.ncols + kTileM - 1) / kTileM;
+  const long ntiles = jobs.ntiles;
 
   // kinetic matrix (B operand, rows = output index i, K = b), both halves
   for (int e = tid; e < npad * kpad; e += kThreads) {
@@ -150,7 +176,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   bool ok = true;
 
   for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long c0 = tile * kTileM;
+    int jb = 0;
+    while (jb + 1 < jobs.n && tile >= jobs.j[jb + 1].tile0) ++jb;
+    const double* __restrict__ X = jobs.j[jb].x;
+    double* __restrict__ Y = jobs.j[jb].y;
+    const double* __restrict__ v = jobs.j[jb].v;
+    const long ncols = jobs.j[jb].ncols;
+    const long c0 = (tile - jobs.j[jb].tile0) * kTileM;
     // ---- A operand: 128 columns x K, split into TF32 hi/lo
     // eight loads per thread in flight, then split and store
     for (int e0 = tid; e0 < kTileM * kpad; e0 += kBatch * kThreads) {
@@ -163,7 +195,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int m = AXIS == 0 ? e / kpad : (e & (kTileM - 1));
         const int k = AXIS == 0 ? e - (e / kpad) * kpad : (e >> 7);
         const long c = c0 + m;
-        const bool in = e < kTileM * kpad && k < n && c < am.ncols;
+        const bool in = e < kTileM * kpad && k < n && c < ncols;
         xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)k * am.stride] : 0.0;
       }
 #pragma unroll
@@ -213,7 +245,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---- epilogue: thread (quarter, lane) owns column c = c0 + 32*quarter + lane
     const int m = 32 * quarter + lane;
     const long c = c0 + m;
-    const bool cvalid = c < am.ncols;
+    const bool cvalid = c < ncols;
     const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
     const long gshift = cvalid ? (c / (N / n)) * N : 0;  // vector offset: grid point = address - gshift
     for (int chunk = half; chunk * 16 < npad; chunk += 2) {
@@ -252,51 +284,84 @@ namespace pg {
 
 static int g_num_sms = 0;
 
-// One axis contraction on the tensor cores: Y (mode) D with D = A x_axis X,
-// A given as TF32 hi/lo halves (n_axis x n_axis, row-major).
-pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* v, const double* x,
-                  double* y, int nvec, int mode, cudaStream_t st) {
+// One axis contraction on the tensor cores for a list of jobs on the same
+// grid: Y_j (mode) D_j with D_j = A x_axis X_j, A given as TF32 hi/lo halves
+// (n_axis x n_axis, row-major).  Each job covers nvec_j vectors.
+pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* const* v,
+                       const double* const* x, double* const* y, const int* nvec, int njobs, int mode,
+                       cudaStream_t st) {
+  PG_ARG(njobs > 0 && njobs <= kMaxTcJobs, "tc_axis: %d jobs (at most %d)", njobs, kMaxTcJobs);
   if (g->n[a] > kMaxN) {
     set_error("mixed form supports n <= %d per axis (got %d)", kMaxN, g->n[a]);
     return PG_UNSUPPORTED;
   }
-  if (!g_num_sms) {
+  // once per process (thread-safe static initialisation): SM count and the
+  // 227 KB dynamic shared-memory opt-in of the three axis kernels
+  static const cudaError_t init = [] {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (g_num_sms <= 0) g_num_sms = 148;
-  }
+    cudaError_t e = cudaFuncSetAttribute(k_hx_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_hx_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_hx_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    return e;
+  }();
+  PG_CUDA_TRY(init);
   const long N = g->N;
   const int n = g->n[a];
   AxisMap am;
   am.n = n;
   am.stride = a == 0 ? 1 : (a == 1 ? g->n[0] : (long)g->n[0] * g->n[1]);
-  am.ncols = N / n * nvec;
+  am.ncols = 0;
+  TcJobs jobs;
+  jobs.n = njobs;
+  long tiles = 0;
+  for (int j = 0; j < njobs; ++j) {
+    jobs.j[j].x = x[j];
+    jobs.j[j].y = y[j];
+    jobs.j[j].v = v ? v[j] : nullptr;
+    jobs.j[j].ncols = N / n * nvec[j];
+    jobs.j[j].tile0 = tiles;
+    tiles += (jobs.j[j].ncols + kTileM - 1) / kTileM;
+  }
+  jobs.ntiles = tiles;
   const int npad = (n + 15) / 16 * 16;
   const int kpad = (n + 7) / 8 * 8;
   uint32_t cols = 32;
   while (cols < (uint32_t)npad) cols <<= 1;
   const size_t smem = (size_t)2 * npad * kpad * 4 + (size_t)2 * kTileM * kpad * 4;
-  const long tiles = (am.ncols + kTileM - 1) / kTileM;
   const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
   int* err = g->tc_err.p;
   switch (a) {
     case 0:
-      PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, v, x, y,
-                                               mode, err);
+      k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, jobs, mode,
+                                               err);
       break;
     case 1:
-      PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, v, x, y,
-                                               mode, err);
+      k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, jobs, mode,
+                                               err);
       break;
     default:
-      PG_CUDA_TRY(cudaFuncSetAttribute(k_hx_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, v, x, y,
-                                               mode, err);
+      k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, jobs, mode,
+                                               err);
   }
   return check_launch("k_hx_tc");
+}
+
+pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* v, const double* x,
+                  double* y, int nvec, int mode, cudaStream_t st) {
+  return tc_axis_jobs(g, a, Ahi, Alo, v ? &v : nullptr, &x, &y, &nvec, 1, mode, st);
+}
+
+// Mixed H*X of several solves on the same grid in one launch per axis.
+pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
+                         const int* nvec, int njobs, cudaStream_t st) {
+  for (int a = 0; a < 3; ++a)
+    PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 2 : 1, st));
+  return PG_OK;
 }
 
 // Launches the three axis passes on st: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X.

@@ -408,12 +408,13 @@ pg_status RedScratch::ensure() {
 // Dynamic shared-memory opt-in, once per kernel (the largest size any call
 // needs: 112 + 16 vectors of 33 doubles for the Gram kernels).
 static pg_status opt_in_smem() {
-  static bool done = false;
-  if (done) return PG_OK;
-  const int big = (int)(sizeof(double) * (size_t)(128 + 16) * (kTP + 1));
-  PG_CUDA_TRY(cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  PG_CUDA_TRY(cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  done = true;
+  static const cudaError_t init = [] {  // thread-safe static initialisation
+    const int big = (int)(sizeof(double) * (size_t)(128 + 16) * (kTP + 1));
+    cudaError_t e = cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    return e;
+  }();
+  PG_CUDA_TRY(init);
   return PG_OK;
 }
 

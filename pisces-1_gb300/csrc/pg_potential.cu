@@ -261,10 +261,12 @@ extern "C" pg_status pg_potential_eval(const pg_grid* g, const pg_sites* t, doub
   // order reproduces that order only if every list is sorted by site.
   for (int s = 0; s < ns; ++s) rec[(size_t)s * kRec + R_FLAGS] = (double)(flags[s] | ((nsto[s] > 2 ? 2 : nsto[s]) << 3));
 
-  pg::DevBuf<double> drec;
-  pg::DevBuf<int> derr;
-  PG_TRY(drec.alloc(rec.size()));
-  PG_TRY(derr.alloc(1));
+  // per-thread, grow-only device copies of the site records (the call waits
+  // for its stream before returning, so the next call may overwrite them)
+  static thread_local pg::DevBuf<double> drec;
+  static thread_local pg::DevBuf<int> derr;
+  PG_TRY(drec.ensure(rec.size()));
+  PG_TRY(derr.ensure(1));
   cudaStream_t st = pg::as_stream(stream);
   PG_CUDA_TRY(cudaMemcpyAsync(drec.p, rec.data(), rec.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   PG_CUDA_TRY(cudaMemsetAsync(derr.p, 0, sizeof(int), st));
@@ -298,15 +300,15 @@ extern "C" pg_status pg_potential_ions_add(const pg_grid* g, int nions, const do
     for (int c = 0; c < 3; ++c) ion[4 * s + c] = pos[3 * s + c];
     ion[4 * s + 3] = q[s];
   }
-  pg::DevBuf<double> d;
-  PG_TRY(d.alloc(ion.size()));
+  static thread_local pg::DevBuf<double> d;  // per-thread, grow-only; idle again on return
+  PG_TRY(d.ensure(ion.size()));
   cudaStream_t st = pg::as_stream(stream);
   PG_CUDA_TRY(cudaMemcpyAsync(d.p, ion.data(), ion.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   k_potential_ions<<<grid_stride_blocks(g->N), 256, 0, st>>>(g->n[0], g->n[1], g->n[2], g->x_dev[0].p,
                                                              g->x_dev[1].p, g->x_dev[2].p, d.p, nions,
                                                              1.0 / r_cation, 1.0 / r_anion, v);
   PG_TRY(pg::check_launch("k_potential_ions"));
-  PG_CUDA_TRY(cudaStreamSynchronize(st));  // d is released on return
+  PG_CUDA_TRY(cudaStreamSynchronize(st));
   return PG_OK;
 }
 

@@ -1,0 +1,31 @@
+// Internal interfaces between the eigensolver (pg_davidson.cu), the
+// tensor-core H*X (pg_hx_tc.cu) and the serving engine (pg_serve.cu).
+#pragma once
+
+#include <functional>
+
+#include "pg_common.cuh"
+
+namespace pg {
+
+struct SolveWorkspace;
+SolveWorkspace* workspace_create();
+void workspace_destroy(SolveWorkspace* w);
+
+// pg_solve with the H*X product supplied by the caller; ws (may be null)
+// holds the solve buffers across calls.
+pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p, double* evals, double* evecs,
+                     pg_solve_stats* stats, cudaStream_t st,
+                     const std::function<pg_status(const double*, double*, int)>& matvec, SolveWorkspace* ws);
+
+// V(r) of a water cluster (default model) plus Bloomfield ions on the device.
+pg_status cluster_potential(const pg_grid* g, int nw, const double* waters, int nions, const double* ions, double* v,
+                            cudaStream_t st);
+
+constexpr int kMaxBatchJobs = 16;  // job-table entries of one tensor-core launch
+
+// Mixed-form H*X of up to kMaxBatchJobs solves on the same grid: one launch per axis.
+pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
+                         const int* nvec, int njobs, cudaStream_t st);
+
+}  // namespace pg
