@@ -19,6 +19,7 @@
 // offset), 8-row groups kpad/4*128 B apart (stride byte offset).
 // One thread issues the MMAs and commits them to an mbarrier; every wait is
 // bounded and a timeout is reported through an error word.
+#include <algorithm>
 #include <cstdint>
 
 #include "pg_solve.cuh"
@@ -296,17 +297,25 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     return PG_UNSUPPORTED;
   }
   // once per process (thread-safe static initialisation): SM count and the
-  // 227 KB dynamic shared-memory opt-in of the three axis kernels
+  // dynamic shared-memory opt-in of the three axis kernels, set to the most
+  // the device allows beside each kernel's static shared memory
+  static int g_max_dyn = 0;
   static const cudaError_t init = [] {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (g_num_sms <= 0) g_num_sms = 148;
-    cudaError_t e = cudaFuncSetAttribute(k_hx_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_hx_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_hx_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    const void* fns[3] = {(const void*)k_hx_tc<0>, (const void*)k_hx_tc<1>, (const void*)k_hx_tc<2>};
+    int lim = optin;
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+      cudaFuncAttributes fa;
+      e = cudaFuncGetAttributes(&fa, fns[k]);
+      if (e == cudaSuccess) lim = std::min(lim, optin - (int)fa.sharedSizeBytes);
+    }
+    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+      e = cudaFuncSetAttribute(fns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    g_max_dyn = lim;
     return e;
   }();
   PG_CUDA_TRY(init);
@@ -333,6 +342,10 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
   uint32_t cols = 32;
   while (cols < (uint32_t)npad) cols <<= 1;
   const size_t smem = (size_t)2 * npad * kpad * 4 + (size_t)2 * kTileM * kpad * 4;
+  if ((long)smem > (long)g_max_dyn) {
+    set_error("tc_axis: %zu bytes of shared memory needed, the device allows %d", smem, g_max_dyn);
+    return PG_UNSUPPORTED;
+  }
   const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
   int* err = g->tc_err.p;
   switch (a) {

@@ -64,7 +64,8 @@ def test_alone_equals_in_the_mix(pg, torch, mix, precision):
         res, _ = _run(pg, [r], slots=1, warm_start=False)
         alone.append(res[0])
     together, stats = _run(pg, _requests(pg, mix, precision), slots=8, warm_start=False, batch_window_us=2000)
-    assert stats["completed"] == len(mix) and stats["failed"] == 0
+    assert all(a["status"] == 0 for a in alone), [a["error"] for a in alone]
+    assert stats["completed"] == len(mix) and stats["failed"] == 0, [b["error"] for b in together]
     assert stats["peak_in_flight"] > 1
     if precision == 1:
         # products of the four 40^3 solves went through merged launches
