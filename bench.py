@@ -40,6 +40,13 @@ WORKLOADS = {
 }
 MIXED_PTOL = 6  # residual threshold of the mixed form before the FP64 Rayleigh-Ritz step
 
+# Serving stream: 16 seeded base clusters (H2O)n, n uniform in 8..64, O sites
+# in a sphere of radius 9 A (n/24)^(1/3); each request jitters one base by
+# 0.1 A / 5 degrees, takes a grid from {48,64,80,96}^3 at spacing 0.615 bohr
+# (L = 0.615 (n+1)) and 1-4 states; it warm-starts from its base's vectors.
+C4 = dict(nreq=512, nbase=16, grids=(48, 64, 80, 96), spacing=0.615, max_roots=4, maxsub=40, seed=4,
+          base_seed=1000, ptol_fp64=8, corrflag=3)
+
 
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -257,6 +264,99 @@ def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
                       f"of a full solve", "seconds_per_matvec": per, "potential_s": t_pot}
 
 
+def c4_stream(clusters, nreq, seed=C4["seed"]):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    sizes = [int(x) for x in rng.integers(8, 65, size=C4["nbase"])]
+    bases = [clusters.water_cluster(n, 9.0 * (n / 24.0) ** (1.0 / 3.0), seed=C4["base_seed"] + i)
+             for i, n in enumerate(sizes)]
+    reqs = []
+    for _ in range(nreq):
+        b = int(rng.integers(C4["nbase"]))
+        n = int(rng.choice(C4["grids"]))
+        nr = int(rng.integers(1, C4["max_roots"] + 1))
+        reqs.append(dict(base=b, n=n, L=C4["spacing"] * (n + 1), nroots=nr, waters=clusters.jitter(bases[b], rng)))
+    return sizes, reqs
+
+
+def serve_stream(pg, reqs, precision, rate, slots, batch, window_us):
+    """Submits reqs to a fresh engine at Poisson arrivals of the given rate
+    (None: all at once) and waits for all; returns results and timings."""
+    ptol = MIXED_PTOL if precision == pg.PG_MIXED else C4["ptol_fp64"]
+    rng = np.random.Generator(np.random.PCG64(99))
+    gaps = rng.exponential(1.0 / rate, size=len(reqs)) if rate else np.zeros(len(reqs))
+    arrivals = np.cumsum(gaps) - gaps[0]
+    launches0 = pg.lib().pg_kernel_launches()
+    with pg.Engine(slots=slots, batch_matvecs=batch, batch_window_us=window_us) as eng:
+        made = [pg.Engine.request(q["n"], q["L"], q["waters"], nroots=q["nroots"], maxsub=C4["maxsub"], maxiter=400,
+                                  ptol=ptol, corrflag=C4["corrflag"], precision=precision, key=q["base"])
+                for q in reqs]
+        t0 = time.perf_counter()
+        ids = []
+        for r, ta in zip(made, arrivals):
+            dt = ta - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            ids.append(eng.submit(r))
+        res = [eng.wait(i, timeout=600.0) for i in ids]
+        wall = time.perf_counter() - t0
+        stats = eng.stats()
+    lat = sorted(r["latency_seconds"] * 1000.0 for r in res)
+    return dict(results=res, wall=wall, solves_per_s=len(reqs) / wall, p50=float(np.percentile(lat, 50)),
+                p99=float(np.percentile(lat, 99)), stats=stats, failed=sum(r["status"] != 0 for r in res),
+                launches=pg.lib().pg_kernel_launches() - launches0,
+                n_matvec=sum(r["stats"]["n_matvec"] for r in res))
+
+
+def run_c4(args):
+    """The serving stream through the engine (pg_engine_*): mixed form at
+    saturation and at Poisson arrivals, FP64 at saturation, same requests."""
+    import torch
+    pg = entry.load_package()
+    import importlib
+    clusters = importlib.import_module("pisces_gb300.clusters")
+    torch.cuda.set_device(0)
+    nreq = args.requests
+    sizes, reqs = c4_stream(clusters, nreq)
+    _, warm = c4_stream(clusters, max(3, args.warmup) * 8, seed=C4["seed"] + 1)
+    slots, window = args.slots, args.window_us
+    for prec in (pg.PG_MIXED, pg.PG_FP64):  # warm-up: kernels, grids, allocator
+        serve_stream(pg, warm, prec, None, slots, True, window)
+    clocks = ClockSampler(0)
+    clocks.start()
+    mixed = serve_stream(pg, reqs, pg.PG_MIXED, None, slots, True, window)
+    clk = clocks.stop()
+    fp64 = serve_stream(pg, reqs, pg.PG_FP64, None, slots, True, window)
+    unbatched = serve_stream(pg, reqs, pg.PG_MIXED, None, slots, False, window)
+    rate = 0.7 * mixed["solves_per_s"]
+    poisson = serve_stream(pg, reqs, pg.PG_MIXED, rate, slots, True, window)
+    de = max(abs(a - b) for rm, rf in zip(mixed["results"], fp64["results"])
+             for a, b in zip(rm["evals"], rf["evals"]))
+    h2d = sum(q["waters"].size * 8 for q in reqs) / nreq
+    d2h = sum(q["nroots"] * 8 for q in reqs) / nreq
+    cfg = {"workload": f"c4: {nreq} single points from {C4['nbase']} base (H2O)n clusters (n = {sorted(sizes)}), "
+                       f"grids {list(C4['grids'])}^3 at {C4['spacing']} bohr, 1-{C4['max_roots']} states, "
+                       f"maxsub {C4['maxsub']}, warm start per base cluster",
+           "seed": C4["seed"], "slots": slots, "batch_window_us": window, "corrflag": C4["corrflag"],
+           "precision": "mixed", "residual_tol": 10.0 ** -MIXED_PTOL, "fp64_residual_tol": 10.0 ** -C4["ptol_fp64"],
+           "l2": "per-solve working sets of 48^3-96^3 grids; no flush (requests differ)"}
+    line = {"metric": "solves/s", "value": mixed["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": nreq,
+            "warmup": len(warm), "ms_per_step": 1000.0 * mixed["wall"] / nreq, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+tf32x3", "data": "synthetic", "config": cfg,
+            "latency_ms": {"p50": mixed["p50"], "p99": mixed["p99"], "at": "saturation (all submitted at once)"},
+            "poisson": {"rate_per_s": rate, "solves_per_s": poisson["solves_per_s"], "p50_ms": poisson["p50"],
+                        "p99_ms": poisson["p99"]},
+            "fp64_gpu": {"solves_per_s": fp64["solves_per_s"], "p50_ms": fp64["p50"], "p99_ms": fp64["p99"],
+                         "n_matvec": fp64["n_matvec"]},
+            "mixed_over_fp64": mixed["solves_per_s"] / fp64["solves_per_s"],
+            "unbatched_mixed_solves_per_s": unbatched["solves_per_s"],
+            "max_abs_dE_vs_fp64": de, "failed": mixed["failed"] + fp64["failed"],
+            "engine": mixed["stats"], "n_matvec": mixed["n_matvec"], "clocks": clk, "gpu_launches": mixed["launches"],
+            "e2e": {"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "note": "the engine takes host coordinates and returns host "
+                                                      "eigenvalues: value is already end to end"}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -264,7 +364,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c4"])
+    ap.add_argument("--requests", type=int, default=C4["nreq"], help="c4: requests in the timed stream")
+    ap.add_argument("--slots", type=int, default=16, help="c4: engine slots")
+    ap.add_argument("--window-us", type=int, default=200, help="c4: matvec batching window")
     ap.add_argument("--corrflag", type=int, default=1, choices=[1, 3],
                     help="1: the reference's diagonal (Davidson) correction; 3: exact-kinetic preconditioner")
     ap.add_argument("--maxsub", type=int, default=0, help="override the workload's subspace size")
@@ -272,6 +375,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "c4":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the serving stream has no reference counterpart "
+                                                                  "(the reference solves one point at a time)"}))
+            return
+        if rank == 0:
+            run_c4(args)
+        return
     wl = dict(WORKLOADS[args.workload])
     if args.maxsub:
         wl["maxsub"] = args.maxsub

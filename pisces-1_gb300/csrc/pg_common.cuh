@@ -85,6 +85,17 @@ struct DevBuf {
   }
 };
 
+// Byte offset of element (r, k) of a tensor-core operand tile in shared
+// memory: no-swizzle K-major core matrices of 8 rows x 16 bytes (4 FP32/TF32
+// values), K-adjacent core matrices 128 bytes apart, 8-row groups kpad/4 *
+// 128 bytes apart.  The grid keeps its kinetic matrices in this layout
+// (rows padded to 16, K to 8) so that a kernel copies them in one piece.
+inline __host__ __device__ unsigned tc_kmajor_off(int r, int k, int kpad) {
+  return (unsigned)(((r >> 3) * (kpad >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
+}
+inline __host__ __device__ int tc_npad(int n) { return (n + 15) / 16 * 16; }
+inline __host__ __device__ int tc_kpad(int n) { return (n + 7) / 8 * 8; }
+
 }  // namespace pg
 
 // The grid handle: sizes, host copies of the 1-D data and device kinetic matrices.
@@ -96,14 +107,16 @@ struct pg_grid {
   std::vector<double> x[3];        // grid points per axis
   std::vector<double> t[3];        // full symmetric kinetic matrices, n x n row-major (host)
   pg::DevBuf<double> t_dev[3];     // same, FP64, on the device
-  pg::DevBuf<float> t_hi[3];       // TF32-rounded high part (stored as fp32)
-  pg::DevBuf<float> t_lo[3];       // TF32-rounded remainder T - hi
+  // TF32-rounded high part and the TF32-rounded remainder T - hi, each as a
+  // tensor-core operand image (tc_kmajor_off layout, tc_npad x tc_kpad)
+  pg::DevBuf<float> t_hi[3];
+  pg::DevBuf<float> t_lo[3];
   pg::DevBuf<double> x_dev[3];     // grid points on the device
   pg::DevBuf<int> tc_err;          // set by the tensor-core H*X kernels if a completion wait times out
   // eigenbasis of the kinetic matrices (the orthonormal DST-I, symmetric),
   // for the kinetic preconditioner: FP64, TF32 hi/lo, and the eigenvalues
   pg::DevBuf<double> q_dev[3];
-  pg::DevBuf<float> q_hi[3], q_lo[3];
+  pg::DevBuf<float> q_hi[3], q_lo[3];  // operand images, as t_hi / t_lo
   pg::DevBuf<double> d_dev[3];
   // random start columns (Randm11 from seed 1; the same values for every
   // solve on this grid), generated once and grown on demand

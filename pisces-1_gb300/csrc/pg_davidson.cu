@@ -67,15 +67,54 @@ int blocks_for(long N) {
   return (int)(b < 152L * 8 ? (b > 0 ? b : 1) : 152L * 8);
 }
 
-// ritz_r = U_r / |U_r|;  res_r = W_r - lambda_r ritz_r   (src/Davidson.cpp:240-260)
-__global__ void k_ritz_residual(long N, int nr, double* __restrict__ U, double* __restrict__ W,
-                                const double* __restrict__ usq, const double* __restrict__ lam) {
-  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x)
-    for (int r = 0; r < nr; ++r) {
-      const double u = U[(long)r * N + g] * (1.0 / sqrt(usq[r]));
-      U[(long)r * N + g] = u;
-      W[(long)r * N + g] = W[(long)r * N + g] + (-lam[r]) * u;
-    }
+// ritz_r = U_r / |U_r|;  res_r = W_r - lambda_r ritz_r   (src/Davidson.cpp:240-260),
+// with per-block partial sums of |res_r|^2 (reduced by reduce_partials).
+// uinv[r] = 1/|U_r| (written by the combine that formed U).
+template <int NR>
+__global__ void __launch_bounds__(kT) k_ritz_residual(long N, long chunk, int nr, double* __restrict__ U,
+                                                      double* __restrict__ W, const double* __restrict__ uinv,
+                                                      const double* __restrict__ lam, double* __restrict__ partial) {
+  __shared__ double red[kT / 32][NR];
+  double inv[NR], nl[NR], acc[NR];
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    inv[r] = r < nr ? uinv[r] : 0.0;
+    nl[r] = r < nr ? -lam[r] : 0.0;
+    acc[r] = 0.0;
+  }
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
+    double u[NR], w[NR];  // all loads of the point first, then the arithmetic and stores
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+      if (r < nr) {
+        u[r] = U[(long)r * N + g];
+        w[r] = W[(long)r * N + g];
+      }
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+      if (r < nr) {
+        u[r] = u[r] * inv[r];
+        w[r] = w[r] + nl[r] * u[r];
+        acc[r] += w[r] * w[r];
+        U[(long)r * N + g] = u[r];
+        W[(long)r * N + g] = w[r];
+      }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    double v = acc[r];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][r] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nr) {
+    double t = 0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w][threadIdx.x];
+    partial[(long)blockIdx.x * nr + threadIdx.x] = t;
+  }
 }
 
 // Davidson correction (lambda - diag H)^-1 r with the 1e-12 floor
@@ -105,27 +144,38 @@ __global__ void k_jd_prep(long N, double* __restrict__ r, double* __restrict__ j
 // y_v(i,j,k) /= (dx_i + dy_j + dz_k - sigma_v), the denominator kept at
 // least `floor` in magnitude.  fast: the scale factor in FP32 (it only sets
 // the convergence rate; the mixed form uses it to stay off the FP64 pipe).
-__global__ void k_kin_scale(int nx, int ny, int nz, const double* __restrict__ dx, const double* __restrict__ dy,
-                            const double* __restrict__ dz, const double* __restrict__ sigma, double floor,
-                            double* __restrict__ Y, int nvec, int fast) {
-  const long N = (long)nx * ny * nz;
-  for (long g = blockIdx.x * (long)blockDim.x + threadIdx.x; g < N; g += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(g % nx);
-    const long r = g / nx;
+template <int NR>
+__global__ void __launch_bounds__(kT) k_kin_scale(int nx, int ny, int nz, const double* __restrict__ dx,
+                                                  const double* __restrict__ dy, const double* __restrict__ dz,
+                                                  const double* __restrict__ sigma, double floor,
+                                                  double* __restrict__ Y, int nvec, int fast) {
+  // 32-bit index arithmetic (the grid has fewer than 2^31 points)
+  const unsigned N = (unsigned)nx * ny * nz;
+  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < N; g += gridDim.x * blockDim.x) {
+    const unsigned i = g % (unsigned)nx;
+    const unsigned r = g / (unsigned)nx;
+    double y[NR];  // all loads of the point first
+#pragma unroll
+    for (int v = 0; v < NR; ++v)
+      if (v < nvec) y[v] = Y[(size_t)v * N + g];
     if (fast) {
-      const float dk = (float)dx[i] + (float)dy[(int)(r % ny)] + (float)dz[(int)(r / ny)];
-      for (int v = 0; v < nvec; ++v) {
-        float den = dk - (float)sigma[v];
-        if (fabsf(den) < (float)floor) den = den < 0 ? -(float)floor : (float)floor;
-        Y[(long)v * N + g] *= (double)(1.0f / den);
-      }
-      continue;
-    }
-    const double dk = dx[i] + dy[(int)(r % ny)] + dz[(int)(r / ny)];
-    for (int v = 0; v < nvec; ++v) {
-      double den = dk - sigma[v];
-      if (fabs(den) < floor) den = den < 0 ? -floor : floor;
-      Y[(long)v * N + g] /= den;
+      const float dk = (float)dx[i] + (float)dy[r % (unsigned)ny] + (float)dz[r / (unsigned)ny];
+#pragma unroll
+      for (int v = 0; v < NR; ++v)
+        if (v < nvec) {
+          float den = dk - (float)sigma[v];
+          if (fabsf(den) < (float)floor) den = den < 0 ? -(float)floor : (float)floor;
+          Y[(size_t)v * N + g] = y[v] * (double)(1.0f / den);
+        }
+    } else {
+      const double dk = dx[i] + dy[r % (unsigned)ny] + dz[r / (unsigned)ny];
+#pragma unroll
+      for (int v = 0; v < NR; ++v)
+        if (v < nvec) {
+          double den = dk - sigma[v];
+          if (fabs(den) < floor) den = den < 0 ? -floor : floor;
+          Y[(size_t)v * N + g] = y[v] / den;
+        }
     }
   }
 }
@@ -187,6 +237,7 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
   // grow-only scratch: a reused handle allocates only while its problems grow
   PG_TRY(d->dcoef.ensure((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
   PG_TRY(d->dgram.ensure((size_t)kMaxGramOut));
+  PG_TRY(d->rs.ensure());
   if (!d->dsq.p) {
     PG_TRY(d->dsq.alloc(kScalars));
     std::vector<double> init(kScalars, 0.0);
@@ -201,30 +252,38 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
 
 // C = L^-T for the Cholesky factor of the k x k Gram matrix G (row-major,
 // G[a*k+b] = R_a . R_b), so that R C has orthonormal columns and, C being
-// upper triangular, the same nested spans as Gram-Schmidt.  One thread; a
-// pivot is floored at 1e-300 so that a numerically dependent vector yields a
-// (normalised) noise direction, as the reference's normalisation does.
-__global__ void k_cholinv(const double* __restrict__ G, int k, double* __restrict__ C) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double L[kMaxCombine][kMaxCombine];
+// upper triangular, the same nested spans as Gram-Schmidt.  One warp: lane i
+// updates row i of L at each column step, then lane c solves column c of C.
+// A pivot is floored at 1e-300 so that a numerically dependent vector yields
+// a (normalised) noise direction, as the reference's normalisation does.
+__global__ void __launch_bounds__(32) k_cholinv(const double* __restrict__ G, int k, double* __restrict__ C) {
+  __shared__ double L[kMaxCombine][kMaxCombine + 1];
+  const int lane = threadIdx.x;
+  for (int e = lane; e < k * k; e += 32) L[e / k][e % k] = G[e];
+  __syncwarp();
   for (int j = 0; j < k; ++j) {
-    double s = G[j * k + j];
-    for (int p = 0; p < j; ++p) s -= L[j][p] * L[j][p];
-    const double piv = sqrt(s > 1e-300 ? s : 1e-300);
-    L[j][j] = piv;
-    for (int i = j + 1; i < k; ++i) {
-      double t = G[i * k + j];
-      for (int p = 0; p < j; ++p) t -= L[i][p] * L[j][p];
-      L[i][j] = t / piv;
+    if (lane == 0) {
+      double s = L[j][j];
+      for (int p = 0; p < j; ++p) s -= L[j][p] * L[j][p];
+      L[j][j] = sqrt(s > 1e-300 ? s : 1e-300);
     }
+    __syncwarp();
+    if (lane > j && lane < k) {
+      double t = L[lane][j];
+      for (int p = 0; p < j; ++p) t -= L[lane][p] * L[j][p];
+      L[lane][j] = t / L[j][j];
+    }
+    __syncwarp();
   }
-  // C = L^-T: solve L^T C = I column by column (C upper triangular)
-  for (int c = 0; c < k; ++c)
+  // C = L^-T: solve L^T C = I, column c on lane c (C upper triangular)
+  if (lane < k) {
+    const int c = lane;
     for (int i = k - 1; i >= 0; --i) {
       double s = i == c ? 1.0 : 0.0;
       for (int p = i + 1; p < k; ++p) s -= L[p][i] * C[p * k + c];
       C[i * k + c] = i > c ? 0.0 : s / L[i][i];
     }
+  }
 }
 
 // Kinetic preconditioner on the k contiguous vectors R: R <- (T - sigma_j)^-1 R
@@ -243,8 +302,15 @@ pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* s
   // the smallest kinetic level, a scale for the denominator floor
   double dmin = 0;
   for (int a = 0; a < 3; ++a) dmin += 0.5 * (M_PI / g->L[a]) * (M_PI / g->L[a]);
-  k_kin_scale<<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], g->d_dev[0].p, g->d_dev[1].p, g->d_dev[2].p,
-                                            sigma_dev, 0.1 * dmin, w1, k, pr == PG_MIXED ? 1 : 0);
+#define PG_KIN_SCALE(NRV)                                                                                  \
+  k_kin_scale<NRV><<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], g->d_dev[0].p, g->d_dev[1].p,   \
+                                                 g->d_dev[2].p, sigma_dev, 0.1 * dmin, w1, k, pr == PG_MIXED ? 1 : 0)
+  if (k <= 1) PG_KIN_SCALE(1);
+  else if (k <= 2) PG_KIN_SCALE(2);
+  else if (k <= 4) PG_KIN_SCALE(4);
+  else if (k <= 8) PG_KIN_SCALE(8);
+  else PG_KIN_SCALE(16);
+#undef PG_KIN_SCALE
   PG_TRY(check_launch("k_kin_scale"));
   PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, w1, w2, k, 0, pr, st));
   PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w2, w1, k, 0, pr, st));
@@ -383,9 +449,20 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->sse.data(), sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
     PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat));
     PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat));
-    k_ritz_residual<<<blocks_for(N), kT, 0, st>>>(N, nroots, ritz, res, usq, dlam);
-    PG_TRY(check_launch("k_ritz_residual"));
-    PG_TRY(sqnorms(N, res, nroots, rsq, d->rs, st));
+    {
+      const long chunk = (N + kRedBlocks - 1) / kRedBlocks;
+      const int nblk = (int)((N + chunk - 1) / chunk);
+#define PG_RITZ(NRV) \
+  k_ritz_residual<NRV><<<nblk, kT, 0, st>>>(N, chunk, nroots, ritz, res, usq + nroots, dlam, d->rs.partial.p)
+      if (nroots <= 1) PG_RITZ(1);
+      else if (nroots <= 2) PG_RITZ(2);
+      else if (nroots <= 4) PG_RITZ(4);
+      else if (nroots <= 8) PG_RITZ(8);
+      else PG_RITZ(16);
+#undef PG_RITZ
+      PG_TRY(check_launch("k_ritz_residual"));
+      PG_TRY(reduce_partials(d->rs.partial.p, nblk, nroots, rsq, true, st));
+    }
     std::vector<double> hr(nroots);
     PG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsq, sizeof(double) * nroots, cudaMemcpyDeviceToHost, st));
     const auto w1 = std::chrono::steady_clock::now();
@@ -536,6 +613,11 @@ struct GlibcRand {
 
 constexpr int kRandMax = 2147483647;
 
+}  // namespace
+
+// Start vectors of DVR::Diagonalize (src/DVR.cpp:405-453): startvec 1 puts
+// the particle-in-a-box product in column 0, the other columns (all of them
+// for startvec 2) are uniform in [-1, 1] from the C library generator.
 pg_status start_vectors(const pg_grid* g, int nroots, int startvec, double* B, cudaStream_t st) {
   const long N = g->N;
   int istart = 0;
@@ -565,7 +647,6 @@ pg_status start_vectors(const pg_grid* g, int nroots, int startvec, double* B, c
   return PG_OK;
 }
 
-}  // namespace
 }  // namespace pg
 
 extern "C" int pg_glibc_rand_check(int count, int* out) {

@@ -68,6 +68,16 @@ extern "C" pg_status pg_sine_dvr(int n, double mu, double x0, double xNp1, doubl
 namespace {
 
 // Round to the TF32 grid (10 explicit mantissa bits), nearest-even, as fp32.
+// Row-major n x n matrix -> tensor-core operand image (rows padded to 16,
+// K to 8, zero fill).
+std::vector<float> tc_image(const std::vector<float>& M, int n) {
+  const int npad = pg::tc_npad(n), kpad = pg::tc_kpad(n);
+  std::vector<float> img((size_t)npad * kpad, 0.f);
+  for (int r = 0; r < n; ++r)
+    for (int k = 0; k < n; ++k) img[pg::tc_kmajor_off(r, k, kpad) / 4] = M[(size_t)r * n + k];
+  return img;
+}
+
 float to_tf32(float f) {
   unsigned u;
   memcpy(&u, &f, 4);
@@ -152,14 +162,17 @@ extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid**
       hi[e] = to_tf32((float)g->t[a][e]);
       lo[e] = to_tf32((float)(g->t[a][e] - (double)hi[e]));
     }
-    if ((s = g->t_dev[a].alloc((size_t)m * m)) != PG_OK || (s = g->t_hi[a].alloc((size_t)m * m)) != PG_OK ||
-        (s = g->t_lo[a].alloc((size_t)m * m)) != PG_OK || (s = g->x_dev[a].alloc(m)) != PG_OK) {
+    const std::vector<float> hi_img = tc_image(hi, m), lo_img = tc_image(lo, m);
+    if ((s = g->t_dev[a].alloc((size_t)m * m)) != PG_OK || (s = g->t_hi[a].alloc(hi_img.size())) != PG_OK ||
+        (s = g->t_lo[a].alloc(lo_img.size())) != PG_OK || (s = g->x_dev[a].alloc(m)) != PG_OK) {
       delete g;
       return s;
     }
     if (cudaMemcpy(g->t_dev[a].p, g->t[a].data(), sizeof(double) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->t_hi[a].p, hi.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->t_lo[a].p, lo.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->t_hi[a].p, hi_img.data(), sizeof(float) * hi_img.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(g->t_lo[a].p, lo_img.data(), sizeof(float) * lo_img.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
         cudaMemcpy(g->x_dev[a].p, g->x[a].data(), sizeof(double) * m, cudaMemcpyHostToDevice) != cudaSuccess) {
       pg::set_error("pg_grid_create: upload failed: %s", cudaGetErrorString(cudaGetLastError()));
       delete g;
@@ -183,11 +196,14 @@ extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid**
         ql[(size_t)i * m + k] = to_tf32((float)(v - (double)qh[(size_t)i * m + k]));
       }
     for (int k = 0; k < m; ++k) d[k] = 0.5 * (M_PI * (k + 1) / L[a]) * (M_PI * (k + 1) / L[a]);
-    if (g->q_dev[a].alloc((size_t)m * m) != PG_OK || g->q_hi[a].alloc((size_t)m * m) != PG_OK ||
-        g->q_lo[a].alloc((size_t)m * m) != PG_OK || g->d_dev[a].alloc(m) != PG_OK ||
+    const std::vector<float> qh_img = tc_image(qh, m), ql_img = tc_image(ql, m);
+    if (g->q_dev[a].alloc((size_t)m * m) != PG_OK || g->q_hi[a].alloc(qh_img.size()) != PG_OK ||
+        g->q_lo[a].alloc(ql_img.size()) != PG_OK || g->d_dev[a].alloc(m) != PG_OK ||
         cudaMemcpy(g->q_dev[a].p, q.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->q_hi[a].p, qh.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->q_lo[a].p, ql.data(), sizeof(float) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(g->q_hi[a].p, qh_img.data(), sizeof(float) * qh_img.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
+        cudaMemcpy(g->q_lo[a].p, ql_img.data(), sizeof(float) * ql_img.size(), cudaMemcpyHostToDevice) !=
+            cudaSuccess ||
         cudaMemcpy(g->d_dev[a].p, d.data(), sizeof(double) * m, cudaMemcpyHostToDevice) != cudaSuccess) {
       pg::set_error("pg_grid_create: kinetic eigenbasis upload failed");
       delete g;

@@ -29,13 +29,11 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kTileM = 128;
 constexpr int kMaxN = 112;  // n_axis handled with the whole K extent resident in shared memory
-constexpr int kBatch = 8;   // global loads a thread keeps in flight while filling A
+constexpr int kBatch = 16;  // global loads a thread keeps in flight while filling A
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ uint32_t kmajor_off(int r, int k, int kpad) {
-  return (uint32_t)(((r >> 3) * (kpad >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
-}
+__device__ __forceinline__ uint32_t kmajor_off(int r, int k, int kpad) { return pg::tc_kmajor_off(r, k, kpad); }
 
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
@@ -147,16 +145,28 @@ __global__ void __launch_bounds__(kThreads, 1)
   const long N = (long)nx * ny * nz;
   const long ntiles = jobs.ntiles;
 
-  // kinetic matrix (B operand, rows = output index i, K = b), both halves
-  for (int e = tid; e < npad * kpad; e += kThreads) {
-    const int r = e / kpad, k = e - (e / kpad) * kpad;
-    const bool in = r < n && k < n;
-    *(float*)(sBh + kmajor_off(r, k, kpad)) = in ? t_hi[r * n + k] : 0.f;
-    *(float*)(sBl + kmajor_off(r, k, kpad)) = in ? t_lo[r * n + k] : 0.f;
-  }
+  // kinetic matrix (B operand, rows = output index i, K = b): both halves are
+  // operand images in global memory, brought in by two bulk copies that
+  // overlap the first A fill
+  __shared__ __align__(8) uint64_t mbar_b;
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_b)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(smem_u32(&mbar_b)), "r"(2 * b_bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sBh)),
+                 "l"(t_hi), "r"(b_bytes), "r"(smem_u32(&mbar_b))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sBl)),
+                 "l"(t_lo), "r"(b_bytes), "r"(smem_u32(&mbar_b))
+                 : "memory");
   }
   if (tid < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -175,6 +185,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int half = warp >> 2;        // which 16-column chunks this warp reads
   uint32_t phase = 0;
   bool ok = true;
+  bool b_ready = false;
 
   for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     int jb = 0;
@@ -214,7 +225,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
+    if (!b_ready) b_ready = mbar_wait(smem_u32(&mbar_b), 0);  // the B images have landed (first tile only)
+    if (!__syncthreads_and(b_ready ? 1 : 0)) {
+      ok = false;
+      break;
+    }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (tid == 0) {
       const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
@@ -249,26 +264,28 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool cvalid = c < ncols;
     const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
     const long gshift = cvalid ? (c / (N / n)) * N : 0;  // vector offset: grid point = address - gshift
-    for (int chunk = half; chunk * 16 < npad; chunk += 2) {
-      float d[16];
-      tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(chunk * 16), d);
+    // two 16-row chunks per round: 32 loads in flight, then the stores
+    for (int c0k = half; c0k * 16 < npad; c0k += 4) {
+      const bool second = (c0k + 2) * 16 < npad;
+      float d[32];
+      tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(c0k * 16), d);
+      if (second) tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)((c0k + 2) * 16), d + 16);
       if (cvalid) {
-        // all loads of the chunk first (16 in flight), then the stores
-        double prev[16];
+        double prev[32];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int i = chunk * 16 + j;
+        for (int j = 0; j < 32; ++j) {
+          const int i = (c0k + 2 * (j >> 4)) * 16 + (j & 15);
           const long a = base + (long)i * am.stride;
           prev[j] = 0.0;
-          if (i < n) {
+          if (i < n && (j < 16 || second)) {
             if (mode == 2) prev[j] = v[a - gshift] * X[a];
             else if (mode == 1) prev[j] = Y[a];
           }
         }
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int i = chunk * 16 + j;
-          if (i < n) Y[base + (long)i * am.stride] = prev[j] + (double)d[j];
+        for (int j = 0; j < 32; ++j) {
+          const int i = (c0k + 2 * (j >> 4)) * 16 + (j & 15);
+          if (i < n && (j < 16 || second)) Y[base + (long)i * am.stride] = prev[j] + (double)d[j];
         }
       }
     }

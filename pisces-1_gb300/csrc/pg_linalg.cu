@@ -3,6 +3,7 @@
 // Every reduction runs in two launches: blocks of the first write partial
 // sums (one per output), the second reduces the partials of each output with
 // one warp, in a fixed order.  No atomics, no dependence on scheduling.
+#include <algorithm>
 #include <cstdint>
 
 #include "pg_linalg.cuh"
@@ -31,7 +32,16 @@ __global__ void __launch_bounds__(kT) k_reduce_partials(const double* __restrict
   const int lane = threadIdx.x & 31;
   if (warp >= no) return;
   double s = 0;
-  for (int b = lane; b < nb; b += 32) s += partial[(long)b * no + warp];
+  for (int b0 = 0; b0 < nb; b0 += 8 * 32) {  // eight independent loads in flight per lane
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int b = b0 + u * 32 + lane;
+      v[u] = b < nb ? partial[(long)b * no + warp] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += v[u];
+  }
   for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
   if (lane == 0) {
     out[warp] = s;
@@ -159,36 +169,6 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
   }
 }
 
-__global__ void __launch_bounds__(kT) k_sqnorms(long N, long chunk, const double* __restrict__ X, int nr,
-                                                double* __restrict__ partial) {
-  __shared__ double red[kT / 32][kMaxCombine];
-  const long g_begin = blockIdx.x * chunk;
-  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double s[kMaxCombine];
-#pragma unroll
-  for (int r = 0; r < kMaxCombine; ++r) s[r] = 0;
-  for (long g = g_begin + threadIdx.x; g < g_end; g += kT)
-#pragma unroll
-    for (int r = 0; r < kMaxCombine; ++r)
-      if (r < nr) {
-        const double x = X[(long)r * N + g];
-        s[r] += x * x;
-      }
-#pragma unroll
-  for (int r = 0; r < kMaxCombine; ++r) {
-    double v = s[r];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp][r] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < nr) {
-    double t = 0;
-    for (int w = 0; w < kT / 32; ++w) t += red[w][threadIdx.x];
-    partial[(long)blockIdx.x * nr + threadIdx.x] = t;
-  }
-}
-
 // ------------------------------------------------------------------------
 // Double-float (two FP32 numbers, hi + lo) arithmetic for the mixed form's
 // subspace products.  The FP32 pipe of this part retires ~67 TFLOP/s against
@@ -238,72 +218,120 @@ __device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl)
   sh = t;
 }
 
-// Gram partials in double-float: same contract as k_gram; partial sums are
-// written as double (hi + lo).
-__global__ void __launch_bounds__(kT) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
-                                                const double* __restrict__ Q, int nb, double* __restrict__ partial) {
-  extern __shared__ float smf[];
-  float* Hs = smf;                          // high parts, (na + nb) x (kTP+1): P rows then Q rows
-  float* Ls = smf + (na + nb) * (kTP + 1);  // low parts, same layout
-  const float* Ph = Hs;
-  const float* Pl = Ls;
-  const float* Qh = Hs + na * (kTP + 1);
-  const float* Ql = Ls + na * (kTP + 1);
-  const int no = na * nb;
-  float ah[kMaxGramOut / kT], al[kMaxGramOut / kT];
-#pragma unroll
-  for (int s = 0; s < kMaxGramOut / kT; ++s) ah[s] = al[s] = 0.f;
+// Gram partials in double-float, written as double (hi + lo): same contract
+// as k_gram.  A thread owns a kGA x kGB block of outputs (kGA rows of P
+// against kGB rows of Q) for one slice of the points of each tile, so every
+// point value it reads from shared memory feeds kGB or kGA products.  Tiles of
+// tp points of all na + nb rows stream through kGStages shared-memory stages
+// with cp.async (each thread converts the doubles it copied to (hi, lo) pairs
+// in place once they land), keeping two tiles in flight behind the one being
+// multiplied.  At the end the slices of each output block are summed in a
+// fixed order.
+constexpr int kGA = 4, kGB = 4, kGStages = 3;
+constexpr int kGramSmemMax = 112 * 1024;
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_stages() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(kGStages - 2) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
+                                                   const double* __restrict__ Q, int nb, int tp_log2, int S, int ablk,
+                                                   int nblk, double* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char gsm[];
+  const int tp = 1 << tp_log2;
+  const int rows = na + nb;
+  const int stage_elems = rows * tp;
+  double* stage0 = reinterpret_cast<double*>(gsm);
   const long g_begin = blockIdx.x * chunk;
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
-  for (long g0 = g_begin; g0 < g_end; g0 += kTP) {
-    const int cnt = g_end - g0 < kTP ? (int)(g_end - g0) : kTP;
-    const int tot = (na + nb) * kTP;
-    for (int e0 = threadIdx.x; e0 < tot; e0 += kBatch * kT) {
-      double v[kBatch];
+  const int ntiles = g_end > g_begin ? (int)((g_end - g_begin + tp - 1) >> tp_log2) : 0;
+  const int tid = threadIdx.x;
+  const int blk = tid / S, slice = tid - blk * S;
+  const bool active = blk < nblk;
+  const int a0 = (blk % ablk) * kGA, b0 = (blk / ablk) * kGB;
+  int ra[kGA], rb[kGB];  // stage rows of this thread's outputs (clamped; extra outputs are discarded)
 #pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int e = e0 + u * kT;
-        const int row = e / kTP, p = e % kTP;
+  for (int i = 0; i < kGA; ++i) ra[i] = (a0 + i < na ? a0 + i : na - 1) * tp;
+#pragma unroll
+  for (int j = 0; j < kGB; ++j) rb[j] = (na + (b0 + j < nb ? b0 + j : nb - 1)) * tp;
+  float sh[kGA][kGB], sl[kGA][kGB];
+#pragma unroll
+  for (int i = 0; i < kGA; ++i)
+#pragma unroll
+    for (int j = 0; j < kGB; ++j) sh[i][j] = sl[i][j] = 0.f;
+
+  auto issue = [&](int tile) {
+    double* dst = stage0 + (size_t)(tile % kGStages) * stage_elems;
+    const long g0 = g_begin + ((long)tile << tp_log2);
+    const int cnt = g_end - g0 < tp ? (int)(g_end - g0) : tp;
+    for (int e = tid; e < stage_elems; e += kT) {
+      const int row = e >> tp_log2, p = e & (tp - 1);
+      if (p < cnt) {
         const double* src = row < na ? P + (long)row * N : Q + (long)(row - na) * N;
-        v[u] = (e < tot && p < cnt) ? src[g0 + p] : 0.0;
-      }
-#pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int e = e0 + u * kT;
-        if (e < tot) {
-          float h, l;
-          df_split(v[u], h, l);
-          Hs[(e / kTP) * (kTP + 1) + e % kTP] = h;
-          Ls[(e / kTP) * (kTP + 1) + e % kTP] = l;
-        }
+        cp_async8(dst + e, src + g0 + p);
+      } else {
+        dst[e] = 0.0;
       }
     }
-    __syncthreads();
-#pragma unroll
-    for (int s = 0; s < kMaxGramOut / kT; ++s) {
-      const int o = threadIdx.x + s * kT;
-      if (o < no) {
-        const int a = o / nb, b = o % nb;
-        const float* pah = Ph + a * (kTP + 1);
-        const float* pal = Pl + a * (kTP + 1);
-        const float* qbh = Qh + b * (kTP + 1);
-        const float* qbl = Ql + b * (kTP + 1);
-        float th = 0.f, tl = 0.f, uh = 0.f, ul = 0.f;  // two chains for latency
-#pragma unroll
-        for (int p = 0; p < kTP; p += 2) {
-          df_fma(th, tl, pah[p], pal[p], qbh[p], qbl[p]);
-          df_fma(uh, ul, pah[p + 1], pal[p + 1], qbh[p + 1], qbl[p + 1]);
-        }
-        df_add(th, tl, uh, ul);
-        df_add(ah[s], al[s], th, tl);
-      }
-    }
-    __syncthreads();
+  };
+  for (int t = 0; t < kGStages - 1; ++t) {
+    if (t < ntiles) issue(t);
+    cp_async_commit();
   }
+  for (int it = 0; it < ntiles; ++it) {
+    cp_async_wait_stages();  // this thread's copies of tile `it` have landed
+    double* cur = stage0 + (size_t)(it % kGStages) * stage_elems;
+    float2* cur2 = reinterpret_cast<float2*>(cur);
+    for (int e = tid; e < stage_elems; e += kT) {  // the elements this thread copied
+      float h, l;
+      df_split(cur[e], h, l);
+      cur2[e] = make_float2(h, l);
+    }
+    __syncthreads();  // tile `it` converted; everyone is done with tile it-1
+    if (it + kGStages - 1 < ntiles) issue(it + kGStages - 1);
+    cp_async_commit();
+    if (active) {
+      const long g0 = g_begin + ((long)it << tp_log2);
+      const int cnt = g_end - g0 < tp ? (int)(g_end - g0) : tp;
+      for (int p = slice; p < cnt; p += S) {
+        float2 x[kGA], y[kGB];
 #pragma unroll
-  for (int s = 0; s < kMaxGramOut / kT; ++s) {
-    const int o = threadIdx.x + s * kT;
-    if (o < no) partial[(long)blockIdx.x * no + o] = (double)ah[s] + (double)al[s];
+        for (int i = 0; i < kGA; ++i) x[i] = cur2[ra[i] + p];
+#pragma unroll
+        for (int j = 0; j < kGB; ++j) y[j] = cur2[rb[j] + p];
+#pragma unroll
+        for (int i = 0; i < kGA; ++i)
+#pragma unroll
+          for (int j = 0; j < kGB; ++j) df_fma(sh[i][j], sl[i][j], x[i].x, x[i].y, y[j].x, y[j].y);
+      }
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // slices -> one partial per output, summed in slice order
+  double* red = reinterpret_cast<double*>(gsm);
+  if (active) {
+#pragma unroll
+    for (int i = 0; i < kGA; ++i)
+#pragma unroll
+      for (int j = 0; j < kGB; ++j)
+        red[((size_t)slice * nblk + blk) * (kGA * kGB) + i * kGB + j] = (double)sh[i][j] + (double)sl[i][j];
+  }
+  __syncthreads();
+  const int no = na * nb;
+  for (int o = tid; o < no; o += kT) {
+    const int a = o / nb, b = o - (o / nb) * nb;
+    const int bo = a / kGA + (b / kGB) * ablk;
+    const int k = (a % kGA) * kGB + (b % kGB);
+    double acc = 0;
+    for (int q = 0; q < S; ++q) acc += red[((size_t)q * nblk + bo) * (kGA * kGB) + k];
+    partial[(long)blockIdx.x * no + o] = acc;
   }
 }
 
@@ -392,6 +420,16 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
   }
 }
 
+pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st);
+
+}  // namespace
+
+pg_status reduce_partials(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
+  return reduce(partial, nb, no, out, sqrt_mode, st);
+}
+
+namespace {
+
 pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
   const int blocks = (no * 32 + kT - 1) / kT;
   k_reduce_partials<<<blocks, kT, 0, st>>>(partial, nb, no, out, sqrt_mode ? 1 : 0);
@@ -411,7 +449,8 @@ static pg_status opt_in_smem() {
   static const cudaError_t init = [] {  // thread-safe static initialisation
     const int big = (int)(sizeof(double) * (size_t)(128 + 16) * (kTP + 1));
     cudaError_t e = cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmemMax);
     return e;
   }();
   PG_CUDA_TRY(init);
@@ -427,9 +466,19 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
   const long chunk = chunk_for(N, kRedBlocks, kTP);
   const int blocks = (int)((N + chunk - 1) / chunk);
   if (dfloat) {
-    const size_t smem = sizeof(float) * 2 * (size_t)(na + nb) * (kTP + 1);
-    k_gram_df<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
+    const int ablk = (na + kGA - 1) / kGA, nblk = ablk * ((nb + kGB - 1) / kGB);
+    PG_ARG(nblk <= kT, "gram: %d output blocks", nblk);  // at most ~160 within the limits above
+    const int S = kT / nblk;
+    const int rows = na + nb;
+    int tp_log2 = 8;          // largest tile with kGStages stages in kGramSmemMax
+    while (tp_log2 > 5 && (size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8 > (size_t)kGramSmemMax) --tp_log2;
+    const long dchunk = chunk_for(N, kRedBlocks, 1 << tp_log2);
+    const int dblocks = (int)((N + dchunk - 1) / dchunk);
+    const size_t smem = std::max((size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8,
+                                 (size_t)S * nblk * kGA * kGB * 8);
+    k_gram_df<<<dblocks, kT, smem, st>>>(N, dchunk, P, na, Q, nb, tp_log2, S, ablk, nblk, rs.partial.p);
     PG_TRY(check_launch("k_gram_df"));
+    return reduce(rs.partial.p, dblocks, na * nb, out, false, st);
   } else {
     const size_t smem = sizeof(double) * (size_t)(na + nb) * (kTP + 1);
     k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
@@ -475,14 +524,5 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
   return sq ? reduce(rs.partial.p, blocks, nr, sq, true, st) : PG_OK;
 }
 
-pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st) {
-  PG_ARG(nr > 0 && nr <= kMaxCombine, "sqnorms: bad count %d", nr);
-  PG_TRY(rs.ensure());
-  const long chunk = chunk_for(N, kRedBlocks, kT);
-  const int blocks = (int)((N + chunk - 1) / chunk);
-  k_sqnorms<<<blocks, kT, 0, st>>>(N, chunk, X, nr, rs.partial.p);
-  PG_TRY(check_launch("k_sqnorms"));
-  return reduce(rs.partial.p, blocks, nr, sq, true, st);
-}
 
 }  // namespace pg

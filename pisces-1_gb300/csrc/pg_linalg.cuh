@@ -1,9 +1,9 @@
 // Skinny FP64 linear algebra of the Davidson subspace on the device.
 //
-// Every reduction is deterministic: blocks write partial sums, and the last
-// block to finish (found with a device-scope counter) adds the partials in
-// block order.  Results therefore do not depend on scheduling, which keeps a
-// solve bit-identical whether it runs alone or next to other solves.
+// Every reduction is deterministic: blocks write partial sums, and a second
+// launch adds the partials of each output in a fixed order.  Results
+// therefore do not depend on scheduling, which keeps a solve bit-identical
+// whether it runs alone or next to other solves.
 #pragma once
 
 #include "pg_common.cuh"
@@ -17,9 +17,12 @@ constexpr int kMaxCombine = 16;  // columns produced by one combine launch
 // Scratch for reductions; one per stream of work.
 struct RedScratch {
   DevBuf<double> partial;     // kRedBlocks * kMaxGramOut
-  DevBuf<unsigned> counter;   // 4 independent counters, zero between launches
   pg_status ensure();
 };
+
+// out[o] = sum over b < nb of partial[b*no + o], in a fixed order; with
+// sqrt_mode also out[no + o] = 1/sqrt(out[o]).
+pg_status reduce_partials(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st);
 
 // out[a*nb + b] = sum_g P[a*N + g] * Q[b*N + g]     (a < na, b < nb; na*nb <= kMaxGramOut)
 // dfloat: products and sums in double-float (two-FP32) arithmetic, ~2^-48
@@ -34,8 +37,5 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
 pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
                   cudaStream_t st, bool dfloat = false);
-
-// sq[r] = |X_r|^2 and sq[nr + r] = 1/|X_r| for r < nr.
-pg_status sqnorms(long N, const double* X, int nr, double* sq, RedScratch& rs, cudaStream_t st);
 
 }  // namespace pg

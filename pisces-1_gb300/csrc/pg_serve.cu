@@ -12,8 +12,9 @@
 //     solves plus the head's stays within the budget (head-of-line order:
 //     a large request is not starved by smaller ones behind it);
 //   - warm start: converged eigenvectors are kept on the device per
-//     (key, grid); a request with a cached entry of at least its state count
-//     starts from it (startvec 0), otherwise from the start vectors it asks for;
+//     (key, grid), as many states as any solve of that pair produced; a
+//     request starts from the cached vectors (startvec 0), its own start
+//     vectors filling any further columns;
 //   - matvec batching: mixed-form H*X products of solves in flight on the same
 //     grid go to one batcher thread, which merges up to 16 of them into one
 //     tensor-core launch per axis (the job table of k_hx_tc).  Ordering between
@@ -285,10 +286,14 @@ void pg_engine::run_job(Job& job, cudaStream_t st, pg::SolveWorkspace* ws, pg::D
   if (use_cache) {
     std::lock_guard<std::mutex> l(cm);
     auto it = cache.find({r.key, gk});
-    if (it != cache.end() && it->second->nroots >= p.nroots) {
+    if (it != cache.end() && it->second->nroots > 0) {
+      const int k = std::min(it->second->nroots, p.nroots);
+      // fewer cached vectors than states: the request's own start vectors
+      // fill the columns the cache does not cover
+      if (k < p.nroots && (s = pg::start_vectors(g, p.nroots, p.startvec, evecs.p, st)) != PG_OK) return fail(s);
       // copy under the lock and wait for it: the entry may be rewritten next
-      if (cudaMemcpyAsync(evecs.p, it->second->vecs.p, sizeof(double) * N * p.nroots, cudaMemcpyDeviceToDevice,
-                          st) != cudaSuccess ||
+      if (cudaMemcpyAsync(evecs.p, it->second->vecs.p, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st) !=
+              cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess) {
         pg::set_error("warm-start copy failed: %s", cudaGetErrorString(cudaGetLastError()));
         return fail(PG_CUDA);
@@ -320,22 +325,34 @@ void pg_engine::run_job(Job& job, cudaStream_t st, pg::SolveWorkspace* ws, pg::D
     if (s != PG_NOT_CONVERGED) return;
   }
   if (s == PG_OK && use_cache) {
+    // keep the most states any solve of this key and grid produced: a solve
+    // with fewer states refreshes the leading vectors only
     std::lock_guard<std::mutex> l(cm);
     auto& e = cache[{r.key, gk}];
     if (!e) e.reset(new CacheEntry());
-    pg_status cs = e->vecs.ensure((size_t)N * p.nroots);
+    const int keep = std::max(e->nroots, p.nroots);
+    pg_status cs = PG_OK;
+    if (e->vecs.n < (size_t)N * keep) {
+      pg::DevBuf<double> grown;
+      cs = grown.alloc((size_t)N * keep);
+      if (cs == PG_OK && e->nroots > 0 &&
+          cudaMemcpyAsync(grown.p, e->vecs.p, sizeof(double) * N * e->nroots, cudaMemcpyDeviceToDevice, st) !=
+              cudaSuccess)
+        cs = PG_CUDA;
+      if (cs == PG_OK) std::swap(grown.p, e->vecs.p), std::swap(grown.n, e->vecs.n);
+      if (cs == PG_OK && cudaStreamSynchronize(st) != cudaSuccess) cs = PG_CUDA;  // before `grown` frees the old one
+    }
     if (cs == PG_OK &&
         (cudaMemcpyAsync(e->vecs.p, evecs.p, sizeof(double) * N * p.nroots, cudaMemcpyDeviceToDevice, st) !=
              cudaSuccess ||
-         cudaStreamSynchronize(st) != cudaSuccess)) {
-      pg::set_error("warm-start store failed: %s", cudaGetErrorString(cudaGetLastError()));
+         cudaStreamSynchronize(st) != cudaSuccess))
       cs = PG_CUDA;
-    }
     if (cs != PG_OK) {
+      if (cs == PG_CUDA) pg::set_error("warm-start store failed: %s", cudaGetErrorString(cudaGetLastError()));
       cache.erase({r.key, gk});
       return fail(cs);
     }
-    e->nroots = p.nroots;
+    e->nroots = keep;
   }
   if (r.evecs_host) {
     if (cudaMemcpyAsync(r.evecs_host, evecs.p, sizeof(double) * N * p.nroots, cudaMemcpyDeviceToHost, st) !=

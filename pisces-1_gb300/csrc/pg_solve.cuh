@@ -18,6 +18,10 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
                      pg_solve_stats* stats, cudaStream_t st,
                      const std::function<pg_status(const double*, double*, int)>& matvec, SolveWorkspace* ws);
 
+// Start vectors of the reference (startvec 1: box product + random, 2: random)
+// into B (nroots * N doubles); waits for st.
+pg_status start_vectors(const pg_grid* g, int nroots, int startvec, double* B, cudaStream_t st);
+
 // V(r) of a water cluster (default model) plus Bloomfield ions on the device.
 pg_status cluster_potential(const pg_grid* g, int nw, const double* waters, int nions, const double* ions, double* v,
                             cudaStream_t st);

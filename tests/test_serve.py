@@ -157,3 +157,21 @@ def test_poll_and_wait_hand_over_once(pg, torch, mix):
         with pytest.raises(pg.PiscesError):
             eng.wait(ids[1], timeout=1.0)
     assert got == set(ids)
+
+
+def test_warm_start_fills_missing_states(pg, torch, clusters):
+    """A cached entry with fewer states than asked for seeds the leading
+    columns; the request's own start vectors fill the rest."""
+    w = clusters.water_cluster(10, 7.0, seed=43)
+    kw = dict(maxsub=40, ptol=6, precision=1)
+    cold, _ = _run(pg, [pg.Engine.request(GRID, L40, w, nroots=3, key=-1, **kw)], slots=1)
+    with pg.Engine(slots=1) as eng:
+        one = eng.wait(eng.submit(pg.Engine.request(GRID, L40, w, nroots=1, key=9, **kw)), timeout=300.0)
+        three = eng.wait(eng.submit(pg.Engine.request(GRID, L40, w, nroots=3, key=9, **kw)), timeout=300.0)
+        again = eng.wait(eng.submit(pg.Engine.request(GRID, L40, w, nroots=1, key=9, **kw)), timeout=300.0)
+    assert not one["warm_started"] and three["warm_started"] and again["warm_started"]
+    assert three["status"] == 0
+    assert max(abs(x - y) for x, y in zip(cold[0]["evals"], three["evals"])) <= 1e-6
+    assert abs(again["evals"][0] - cold[0]["evals"][0]) <= 1e-6
+    # the same geometry again: the cached vectors are already converged
+    assert again["stats"]["n_matvec"] < one["stats"]["n_matvec"]
