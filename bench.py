@@ -1,15 +1,25 @@
 """Benchmark of the GB300 eigensolve path (one JSON line on rank 0).
 
-Workload (default): (H2O)24 in a 9 A sphere (seed 2), 64^3 sine-DVR grid over
-40 bohr, lowest 4 states, block 4 (all unconverged roots per H*X launch),
-60-vector subspace.  A step is one complete single point: V(r) on the grid
-from the water-site tables, diag(H), and the Davidson eigensolve to
-convergence.  The FP64 form converges to residual 1e-8 (|dE| far below
-1e-8 Eh); the mixed form converges to a looser residual with split-TF32
-tensor-core H*X and finishes with an FP64 Rayleigh-Ritz step.
+Workload (default, c2): (H2O)24 in a 9 A sphere (seed 2), 64^3 sine-DVR grid
+over 40 bohr, lowest 4 states, block 4 (all unconverged roots per H*X
+launch), 60-vector subspace.  A step is one complete single point with the
+inputs resident on the device: V(r) on the grid from the water-site tables,
+diag(H), and the Davidson eigensolve to convergence.
 
-  python bench.py [--steps K] [--warmup W] [--precision mixed|fp64]
+Default form: mixed precision (split-TF32 tensor-core H*X, double-float
+subspace products, FP64 subspace eigensolve, Cholesky factors and residual
+norms) converged to residual 1e-6, then an FP64 Rayleigh-Ritz step with the
+FP64 operator; corrections from the exact-kinetic preconditioner (corrflag 3).
+The same run also times the plain FP64 form (residual 1e-8) on the same
+problem -- with the same corrections and with the reference's diagonal
+correction (corrflag 1) -- and reports |dE| of the mixed eigenvalues against
+the FP64 ones.  `value` is mixed solves/s; `e2e` is the same through
+pg_cluster_solve with host buffers.
+
+  python bench.py [--steps K] [--warmup W] [--precision mixed|fp64] [--corrflag 1|3]
+  python bench.py --workload c4         # the serving stream through pg_engine_*
   python bench.py --impl reference      # the reference algorithm on the host cores
+  python bench.py --roofline-only       # the dominant kernels alone (for ncu captures)
 
 Multi-GPU (torchrun, one rank per GPU): replicas only -- every rank solves
 its own stream of single points, no data-path collective; value is the
@@ -39,6 +49,9 @@ WORKLOADS = {
     "c1": dict(nw=6, radius=6.0, seed=1, n=(32, 32, 32), L=(30.0, 30.0, 30.0), nroots=1, maxsub=20, ptol=8),
 }
 MIXED_PTOL = 6  # residual threshold of the mixed form before the FP64 Rayleigh-Ritz step
+# single-vector H*x products of a full solve by the reference algorithm
+# (diagonal correction, FP64), counted by the oracle on the same input
+REFERENCE_MATVECS = {"c2": 4500, "c1": 700}
 
 # Serving stream: 16 seeded base clusters (H2O)n, n uniform in 8..64, O sites
 # in a sphere of radius 9 A (n/24)^(1/3); each request jitters one base by
@@ -132,103 +145,153 @@ def run_ours(args, ws, rank, local):
     sptr = stream.cuda_stream
     nroots = wl["nroots"]
 
-    def step():
+    def step(prec=precision, corr=args.corrflag, tol=ptol):
         v = grid.potential(tables, stream=sptr)
-        return grid.solve(v, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=ptol, precision=precision,
-                          corrflag=args.corrflag, refine=1, stream=sptr)
+        return grid.solve(v, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=tol, precision=prec,
+                          corrflag=corr, refine=1, stream=sptr)
+
+    def timed(nsteps, **kw):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        lat = []
+        a.record(stream)
+        for _ in range(nsteps):
+            x = torch.cuda.Event(enable_timing=True)
+            y = torch.cuda.Event(enable_timing=True)
+            x.record(stream)
+            out = step(**kw)
+            y.record(stream)
+            lat.append((x, y))
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), [x.elapsed_time(y) for x, y in lat], out
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            ev, vec, st = step()
-        ev_ref, _, st_ref = ev, vec, st
-        if precision == pg.PG_MIXED:  # FP64 answer of the same problem, for the error statement
-            v = grid.potential(tables, stream=sptr)
-            ev_ref, _, st_ref = grid.solve(v, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=wl["ptol"],
-                                           precision=pg.PG_FP64, corrflag=args.corrflag, stream=sptr)
+            step()
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
         clocks = ClockSampler(local)
         clocks.start()
         launches0 = pg.lib().pg_kernel_launches()
-        lat = []
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            ev, vec, st = step()
-            b.record(stream)
-            lat.append((a, b))
-        e1.record(stream)
-        torch.cuda.synchronize()
+        total_ms, lat_ms, (ev, vec, st) = timed(args.steps)
         launches = pg.lib().pg_kernel_launches() - launches0
         clk = clocks.stop()
-    total_ms = e0.elapsed_time(e1)
-    lat_ms = [a.elapsed_time(b) for a, b in lat]
+        if ws > 1:
+            torch.distributed.barrier()
+        # the plain FP64 form on the same problem in the same run: same
+        # corrections, residual 10^-ptol of the workload (the drop-in form)
+        fp64 = None
+        if precision == pg.PG_MIXED:
+            step(pg.PG_FP64, args.corrflag, wl["ptol"])
+            k = max(1, min(args.steps, 5))
+            ms, _, (ev64, _, st64) = timed(k, prec=pg.PG_FP64, tol=wl["ptol"])
+            fp64 = {"solves_per_s": 1000.0 * k / ms, "corrflag": args.corrflag, "residual_tol": 10.0 ** -wl["ptol"],
+                    "n_matvec": st64["n_matvec"], "eigenvalues": list(map(float, ev64))}
+        else:
+            ev64, st64 = ev, st
+        # the reference's own algorithm (diagonal correction) in FP64 on the GPU, once
+        refalg = None
+        if not args.no_refalg and not (precision == pg.PG_FP64 and args.corrflag == 1):
+            ms, _, (evr, _, str_) = timed(1, prec=pg.PG_FP64, corr=1, tol=wl["ptol"])
+            refalg = {"solves_per_s": 1000.0 / ms, "corrflag": 1, "n_matvec": str_["n_matvec"],
+                      "n_iter": str_["n_iter"], "eigenvalues": list(map(float, evr))}
+        elif precision == pg.PG_FP64 and args.corrflag == 1:
+            refalg = {"solves_per_s": 1000.0 * args.steps / total_ms, "corrflag": 1, "n_matvec": st["n_matvec"],
+                      "n_iter": st["n_iter"], "eigenvalues": list(map(float, ev))}
     max_ms = total_ms
     if ws > 1:
         t = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         max_ms = float(t.item())
-    de = float(np.max(np.abs(np.asarray(ev) - np.asarray(ev_ref))))
+    de = float(np.max(np.abs(np.asarray(ev) - np.asarray(ev64))))
 
     # end to end through the public host-buffer API: water coordinates in,
     # eigenvalues and eigenvectors out (pg_cluster_solve)
     e2e_ms = None
-    d2h = nroots * N * 8
+    d2h = nroots * N * 8 + nroots * 8
     h2d = waters.size * 8
     if not args.no_e2e:
         torch.cuda.synchronize()
+        cs = lambda: pg.cluster_solve(wl["n"], wl["L"], waters, nroots=nroots, maxsub=wl["maxsub"], maxiter=400,
+                                      ptol=ptol, precision=precision, corrflag=args.corrflag, refine=1,
+                                      want_vectors=True)
+        cs()
         t0 = time.perf_counter()
-        reps = max(1, min(args.steps, 3))
+        reps = max(1, min(args.steps, 5))
         for _ in range(reps):
-            pg.cluster_solve(wl["n"], wl["L"], waters, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=ptol,
-                             precision=precision, corrflag=args.corrflag, refine=1, want_vectors=True)
+            cs()
         e2e_ms = (time.perf_counter() - t0) * 1000 / reps
 
-    # dominant kernel: H*X on a block of nroots vectors, timed with CUDA events on its stream
-    roof = hx_roofline(pg, torch, grid, tables, nroots, precision, stream)
-    return dict(total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev_ref)),
-                de=de, stats=st, stats_fp64=st_ref, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h,
-                roofline=roof, N=N, precision=args.precision, ptol=ptol)
+    roof = kernel_rooflines(pg, torch, grid, tables, nroots, precision, stream)
+    return dict(total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
+                de=de, stats=st, fp64=fp64, refalg=refalg, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d,
+                d2h=d2h, roofline=roof, N=N, precision=args.precision, ptol=ptol)
 
 
-def hx_roofline(pg, torch, grid, tables, nb, precision, stream):
-    v = grid.potential(tables, stream=stream.cuda_stream)
-    X = torch.randn(nb * grid.N, dtype=torch.float64, device="cuda")
-    Y = torch.empty_like(X)
-    nx, ny, nz = grid.n
-    reps = 20
+GRAM_SHAPE = (40, 4)  # P rows x Q rows of the timed Gram launch: mid-solve basis against a new block
+
+
+def _time_launches(torch, stream, fn, reps=20, warm=3):
     with torch.cuda.stream(stream):
-        for _ in range(3):
-            grid.hx(v, X, nvec=nb, precision=precision, out=Y, stream=stream.cuda_stream)
+        for _ in range(warm):
+            fn()
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
         for _ in range(reps):
-            grid.hx(v, X, nvec=nb, precision=precision, out=Y, stream=stream.cuda_stream)
+            fn()
         b.record(stream)
         torch.cuda.synchronize()
-    ms = a.elapsed_time(b) / reps
-    N = grid.N
-    flops = N * nb * (2 * (nx + ny + nz) + 2)
-    bytes_ = 8 * N * (2 * nb + 1)
+    return a.elapsed_time(b) / reps
+
+
+def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
+    """The dominant kernel of the solve (the subspace Gram, k_gram_df in the
+    mixed form) and the H*X product, each timed alone with CUDA events on its
+    stream.  Algorithmic bytes: every input vector read once (Gram); X read,
+    Y written, V read once (H*X)."""
     peaks, which = measured_peaks()
+    N = grid.N
+    g = torch.Generator(device="cuda").manual_seed(5)
+    na, nq = GRAM_SHAPE
+    P = torch.randn(na, N, dtype=torch.float64, device="cuda", generator=g)
+    Q = torch.randn(nq, N, dtype=torch.float64, device="cuda", generator=g)
+    out = torch.empty(na * nq, dtype=torch.float64, device="cuda")
+    ms = _time_launches(torch, stream, lambda: pg.block_gram(P, Q, precision=precision, out=out,
+                                                             stream=stream.cuda_stream))
+    gbytes = 8.0 * N * (na + nq)
+    # one k_gram_df launch plus its partial-sum reduction; traffic from the ncu
+    # capture of this shape (dram read + write of k_gram_df, one launch)
+    gram = {"kernel": "k_gram_df" if precision == pg.PG_MIXED else "k_gram", "bound": "hbm",
+            "achieved": gbytes / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": gbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "peak_source": which,
+            "traffic": GRAM_TRAFFIC.get((tuple(grid.n), na, nq, precision)), "ms_per_launch": ms,
+            "algorithmic_bytes": gbytes, "shape": f"{na} x {nq} vectors of {N} points"}
+    v = grid.potential(tables, stream=stream.cuda_stream)
+    X = torch.randn(nb * N, dtype=torch.float64, device="cuda", generator=g)
+    Y = torch.empty_like(X)
+    ms = _time_launches(torch, stream, lambda: grid.hx(v, X, nvec=nb, precision=precision, out=Y,
+                                                       stream=stream.cuda_stream))
+    nx, ny, nz = grid.n
+    hbytes = 8.0 * N * (2 * nb + 1)
+    flops = N * nb * (2 * (nx + ny + nz) + 2)
+    hx = {"kernel": "pg_hx mixed: 3 x k_hx_tc (split-TF32 tcgen05)" if precision == pg.PG_MIXED else "k_hx_fp64",
+          "bound": "hbm" if precision == pg.PG_MIXED else "fp64", "ms_per_launch": ms, "algorithmic_bytes": hbytes,
+          "vectors_per_launch": nb}
     if precision == pg.PG_MIXED:
-        achieved = bytes_ / (ms * 1e-3) / 1e9
-        peak = peaks["hbm_gbs"]
-        return {"kernel": "pg_hx mixed (split-TF32 tcgen05)", "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_source": which, "traffic": None,
-                "ms_per_launch": ms, "algorithmic_bytes": bytes_, "vectors_per_launch": nb}
-    achieved = flops / (ms * 1e-3) / 1e12
-    peak = 1.0  # FP64 FMA pipe of this GB300, measured (DFMA loop, 1.00-1.01 TFLOP/s)
-    return {"kernel": "k_hx_fp64", "bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "peak_source": "measured FP64 DFMA throughput (not in MEASURED_PEAKS.json)",
-            "traffic": None, "ms_per_launch": ms, "algorithmic_flops": flops, "vectors_per_launch": nb}
+        hx.update(achieved=hbytes / (ms * 1e-3) / 1e9, peak=peaks["hbm_gbs"], unit="GB/s",
+                  frac=hbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], peak_source=which)
+    else:
+        hx.update(achieved=flops / (ms * 1e-3) / 1e12, peak=1.0, unit="TFLOP/s", frac=flops / (ms * 1e-3) / 1e12,
+                  peak_source="FP64 FMA pipe of this GB300, measured with a DFMA loop (not in MEASURED_PEAKS.json)")
+    return gram, hx
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
+# capture of `python bench.py --roofline-only` (profiles/k_gram_df_c2.md)
+GRAM_TRAFFIC = {((64, 64, 64), 40, 4, 1): 92320512 + 2397952}
 
 
 def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
@@ -360,16 +423,19 @@ def run_c4(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS) + ["c4"])
     ap.add_argument("--requests", type=int, default=C4["nreq"], help="c4: requests in the timed stream")
     ap.add_argument("--slots", type=int, default=16, help="c4: engine slots")
     ap.add_argument("--window-us", type=int, default=200, help="c4: matvec batching window")
-    ap.add_argument("--corrflag", type=int, default=1, choices=[1, 3],
+    ap.add_argument("--corrflag", type=int, default=3, choices=[1, 3],
                     help="1: the reference's diagonal (Davidson) correction; 3: exact-kinetic preconditioner")
+    ap.add_argument("--no-refalg", action="store_true",
+                    help="skip the FP64 solve with the reference's diagonal correction")
+    ap.add_argument("--roofline-only", action="store_true", help="time the dominant kernels only")
     ap.add_argument("--maxsub", type=int, default=0, help="override the workload's subspace size")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -396,9 +462,9 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # matvec count of a full solve of this workload (reference algorithm,
-        # FP64); measured by the GPU FP64 path, which follows the same algorithm
-        n_full = 3656 if args.workload == "c2" else 700
+        # single-vector H*x products of a full solve of this workload by the
+        # reference algorithm (diagonal correction), counted by the oracle
+        n_full = REFERENCE_MATVECS[args.workload]
         steps = []
         for _ in range(args.warmup + args.steps):
             steps.append(cpu_baseline(args, wl, n_full, budget_s=8.0))
@@ -413,6 +479,17 @@ def main():
         return
 
     import torch
+    if args.roofline_only:
+        pg = entry.load_package()
+        import importlib
+        clusters = importlib.import_module("pisces_gb300.clusters")
+        torch.cuda.set_device(local)
+        grid = pg.Grid(wl["n"], wl["L"])
+        tables = pg.WaterTables(clusters.water_cluster(wl["nw"], wl["radius"], wl["seed"]))
+        prec = pg.PG_MIXED if args.precision == "mixed" else pg.PG_FP64
+        gram, hx = kernel_rooflines(pg, torch, grid, tables, wl["nroots"], prec, torch.cuda.Stream())
+        print(json.dumps({"roofline": gram, "roofline_hx": hx, "config": cfg}))
+        return
     if ws > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     r = run_ours(args, ws, rank, local)
@@ -430,12 +507,20 @@ def main():
             "eigenvalues": r["evals"], "max_abs_dE_vs_fp64": r["de"],
             "solve": {k: r["stats"][k] for k in ("n_matvec", "n_iter", "n_restart", "nconv", "seconds",
                                                  "host_eig_seconds", "device_wait_seconds")},
-            "roofline": r["roofline"], "clocks": r["clocks"], "gpu_launches": r["launches"]}
+            "roofline": r["roofline"][0], "roofline_hx": r["roofline"][1], "clocks": r["clocks"],
+            "gpu_launches": r["launches"]}
+    if r["fp64"]:
+        line["fp64_gpu"] = dict(r["fp64"], solves_per_s=ws * r["fp64"]["solves_per_s"])
+        line["mixed_over_fp64"] = value / line["fp64_gpu"]["solves_per_s"]
+    if r["refalg"]:
+        line["fp64_gpu_reference_algorithm"] = dict(r["refalg"], solves_per_s=ws * r["refalg"]["solves_per_s"])
     if r["e2e_ms"] is not None:
         line["e2e"] = {"value": ws * 1000.0 / r["e2e_ms"], "unit": "solves/s", "h2d_bytes_per_step": r["h2d"],
-                       "d2h_bytes_per_step": r["d2h"]}
+                       "d2h_bytes_per_step": r["d2h"],
+                       "path": "pg_cluster_solve: host water coordinates in, host eigenvalues and eigenvectors out"}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args, WORKLOADS[args.workload], r["stats_fp64"]["n_matvec"])
+        nfull = r["refalg"]["n_matvec"] if r["refalg"] else REFERENCE_MATVECS.get(args.workload)
+        line["cpu_baseline"] = cpu_baseline(args, WORKLOADS[args.workload], nfull)
     if ws > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:

@@ -180,6 +180,18 @@ pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int p
  * of the dsyev call of src/Davidson.cpp:224, which computes all m pairs. */
 pg_status pg_subspace_lowest(int m, const double* S_host, int ld, int k, double* w_host, double* V_host, int ldv);
 
+/* Block products of the Davidson subspace (device arrays, vectors stored
+ * contiguously, vector a at P_dev + a*n), the skinny GEMMs of the reference's
+ * S = Z^T B build (src/Davidson.cpp:220, 385-393) and Ritz combinations
+ * (src/Davidson.cpp:240-260).  Deterministic (fixed reduction order).
+ * precision PG_FP64: FP64; PG_MIXED: double-float on the FP32 pipe.
+ *   pg_block_gram:    out[a*nq + b] = P_a . Q_b   (np*nq <= 2048, np+nq <= 144)
+ *   pg_block_combine: Y_r = sum_a P_a C[a*ny + r]   (ny <= 16, np*ny <= 2048) */
+pg_status pg_block_gram(long n, const double* P_dev, int np, const double* Q_dev, int nq, double* out_dev,
+                        int precision, void* stream);
+pg_status pg_block_combine(long n, const double* P_dev, int np, const double* C_dev, int ny, double* Y_dev,
+                           int precision, void* stream);
+
 /* Work-array length in doubles (DavidsonWorkSize, src/Davidson.cpp:46-52). */
 long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag);
 

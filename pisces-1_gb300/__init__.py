@@ -118,6 +118,8 @@ SYMBOLS = {
     "pg_cluster_solve": (C.c_int, [_ip, _dp, C.c_int, _dp, C.c_int, _dp, C.POINTER(SolveParams), _dp, _dp,
                                    C.POINTER(SolveStats), _vp]),
     "pg_glibc_rand_check": (C.c_int, [C.c_int, _ip]),
+    "pg_block_gram": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
+    "pg_block_combine": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_request_footprint": (C.c_double, [C.POINTER(Request)]),
     "pg_engine_create": (C.c_int, [C.POINTER(EngineConfig), C.POINTER(_vp)]),
     "pg_engine_submit": (C.c_int, [_vp, C.POINTER(Request), C.POINTER(C.c_long)]),
@@ -377,6 +379,29 @@ def cluster_solve(n, L, waters_angstrom, ions=None, nroots=1, maxsub=20, maxiter
                                _stream(stream) if stream is not None else None)
     _check(s)
     return ev, (vec.reshape(nroots, N) if want_vectors else None), st.as_dict(nroots)
+
+
+def block_gram(P, Q, precision=PG_FP64, out=None, stream=None):
+    """out[a, b] = P_a . Q_b for torch CUDA float64 blocks P (np x n), Q (nq x n)."""
+    import torch
+    np_, n = P.shape
+    nq = Q.shape[0]
+    if out is None:
+        out = torch.empty(np_ * nq, dtype=torch.float64, device=P.device)
+    _check(lib().pg_block_gram(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
+    return out.view(np_, nq)
+
+
+def block_combine(P, Cm, precision=PG_FP64, out=None, stream=None):
+    """Y_r = sum_a P_a C[a, r] for torch CUDA float64 P (np x n), C (np x ny)."""
+    import torch
+    np_, n = P.shape
+    ny = Cm.shape[1]
+    if out is None:
+        out = torch.empty(ny, n, dtype=torch.float64, device=P.device)
+    Cc = Cm.contiguous()
+    _check(lib().pg_block_combine(n, _dev(P), np_, _dev(Cc), ny, _dev(out), precision, _stream(stream)))
+    return out
 
 
 def subspace_lowest(S, k):

@@ -24,6 +24,11 @@
 #include <cmath>
 #include <cstring>
 #include <functional>
+#include <tuple>
+#include <mutex>
+#include <memory>
+#include <map>
+#include <deque>
 #include <vector>
 
 #include "pg_linalg.cuh"
@@ -788,6 +793,50 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
       [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, prec, st); }, nullptr);
 }
 
+namespace pg {
+namespace {
+
+// Grids of pg_cluster_solve, kept per (device, n, L) so that a stream of
+// single points on one grid builds its kinetic matrices once (at most
+// kGridCacheMax grids; the oldest is dropped when a new one does not fit).
+constexpr size_t kGridCacheMax = 16;
+struct GridCache {
+  std::mutex m;
+  std::map<std::tuple<int, int, int, int, double, double, double>, std::shared_ptr<pg_grid>> grids;
+  std::deque<std::tuple<int, int, int, int, double, double, double>> order;
+};
+GridCache& grid_cache() {
+  static GridCache c;
+  return c;
+}
+
+pg_status cached_grid(const int n[3], const double L[3], std::shared_ptr<pg_grid>* out) {
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev));
+  const auto key = std::make_tuple(dev, n[0], n[1], n[2], L[0], L[1], L[2]);
+  GridCache& c = grid_cache();
+  std::lock_guard<std::mutex> l(c.m);
+  auto it = c.grids.find(key);
+  if (it != c.grids.end()) {
+    *out = it->second;
+    return PG_OK;
+  }
+  pg_grid* g = nullptr;
+  PG_TRY(pg_grid_create(n, L, &g));
+  std::shared_ptr<pg_grid> sp(g, [](pg_grid* q) { pg_grid_destroy(q); });
+  if (c.order.size() >= kGridCacheMax) {  // in-flight users keep their shared_ptr
+    c.grids.erase(c.order.front());
+    c.order.pop_front();
+  }
+  c.grids[key] = sp;
+  c.order.push_back(key);
+  *out = sp;
+  return PG_OK;
+}
+
+}  // namespace
+}  // namespace pg
+
 extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw, const double* waters, int nions,
                                       const double* ions, const pg_solve_params* p, double* evals, double* evecs_host,
                                       pg_solve_stats* stats, void* stream) {
@@ -796,16 +845,23 @@ extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw,
   PG_ARG(nw == 0 || waters, "pg_cluster_solve: null water coordinates");
   PG_ARG(nions == 0 || ions, "pg_cluster_solve: null ion list");
   PG_ARG(p->startvec != 0, "pg_cluster_solve: start vectors 0 need pg_solve");
+  PG_ARG(p->nroots > 0, "pg_cluster_solve: bad parameters");
   cudaStream_t st = as_stream(stream);
-  pg_grid* g = nullptr;
-  PG_TRY(pg_grid_create(n, L, &g));
-  struct GridGuard { pg_grid* g; ~GridGuard() { pg_grid_destroy(g); } } guard{g};
+  std::shared_ptr<pg_grid> gs;
+  PG_TRY(cached_grid(n, L, &gs));
+  const pg_grid* g = gs.get();
   const long N = g->N;
-  DevBuf<double> v, vec;
-  PG_TRY(v.alloc(N));
-  PG_TRY(vec.alloc((size_t)N * p->nroots));
+  // per-thread, grow-only buffers: repeated single points allocate nothing
+  static thread_local SolveWorkspace ws;
+  static thread_local DevBuf<double> v, vec;
+  PG_TRY(v.ensure(N));
+  PG_TRY(vec.ensure((size_t)N * p->nroots));
   PG_TRY(cluster_potential(g, nw, waters, nions, ions, v.p, st));
-  pg_status s = pg_solve(g, v.p, p, evals, vec.p, stats, stream);
+  const int prec = p->precision;
+  const double* vp = v.p;
+  pg_status s = solve_with(
+      g, vp, p, evals, vec.p, stats, st,
+      [&](const double* x, double* y, int nvec) { return hx(g, vp, x, y, nvec, prec, st); }, &ws);
   if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
   if (evecs_host)
     PG_CUDA_TRY(cudaMemcpyAsync(evecs_host, vec.p, sizeof(double) * N * p->nroots, cudaMemcpyDeviceToHost, st));

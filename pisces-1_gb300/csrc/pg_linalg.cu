@@ -526,3 +526,20 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
 
 
 }  // namespace pg
+
+extern "C" pg_status pg_block_gram(long n, const double* P, int np, const double* Q, int nq, double* out,
+                                   int precision, void* stream) {
+  PG_ARG(n > 0 && P && Q && out && np > 0 && nq > 0, "pg_block_gram: bad arguments");
+  PG_ARG(precision == PG_FP64 || precision == PG_MIXED, "pg_block_gram: unknown precision");
+  static thread_local pg::RedScratch rs;
+  return pg::gram(n, P, np, Q, nq, out, rs, pg::as_stream(stream), precision == PG_MIXED);
+}
+
+extern "C" pg_status pg_block_combine(long n, const double* P, int np, const double* C, int ny, double* Y,
+                                      int precision, void* stream) {
+  PG_ARG(n > 0 && P && C && Y && np > 0 && ny > 0, "pg_block_combine: bad arguments");
+  PG_ARG(precision == PG_FP64 || precision == PG_MIXED, "pg_block_combine: unknown precision");
+  static thread_local pg::RedScratch rs;
+  return pg::combine(n, P, np, C, ny, 1, 1.0, nullptr, nullptr, false, Y, ny, nullptr, rs, pg::as_stream(stream),
+                     precision == PG_MIXED);
+}

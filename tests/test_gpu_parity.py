@@ -272,3 +272,39 @@ def test_solve_mixed_c1_within_1e6(pg, torch):
     assert abs(ev[0] - g["evals"][0]) < 1e-6
     w = g["wavefn32"].astype(np.float64)
     assert abs(vec[0] @ w) / np.linalg.norm(vec[0]) / np.linalg.norm(w) > 1 - 1e-8
+
+
+# ---------------------------------------------------------------- block products
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("n,na,nb", [(64 ** 3, 40, 4), (33 ** 3, 5, 5), (1000, 1, 128), (4097, 16, 16)])
+def test_block_gram(pg, torch, precision, n, na, nb):
+    """S = P Q^T against torch FP64; the double-float form within 1e-12 of
+    the largest |entry| scale (|P_a| |Q_b|)."""
+    g = torch.Generator(device="cuda").manual_seed(11)
+    P = torch.randn(na, n, dtype=torch.float64, device="cuda", generator=g)
+    Q = torch.randn(nb, n, dtype=torch.float64, device="cuda", generator=g)
+    ref = P @ Q.T
+    out = pg.block_gram(P, Q, precision=precision)
+    torch.cuda.synchronize()
+    scale = float(P.norm(dim=1).max() * Q.norm(dim=1).max())
+    err = float((out - ref).abs().max()) / scale
+    assert err <= (1e-14 if precision == 0 else 1e-12), err
+    again = pg.block_gram(P, Q, precision=precision)
+    assert torch.equal(out, again)  # deterministic
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("n,na,ny", [(64 ** 3, 40, 4), (33 ** 3, 7, 16), (999, 128, 1)])
+def test_block_combine(pg, torch, precision, n, na, ny):
+    g = torch.Generator(device="cuda").manual_seed(12)
+    P = torch.randn(na, n, dtype=torch.float64, device="cuda", generator=g)
+    Cm = torch.randn(na, ny, dtype=torch.float64, device="cuda", generator=g)
+    ref = Cm.T @ P
+    out = pg.block_combine(P, Cm, precision=precision)
+    torch.cuda.synchronize()
+    scale = float(Cm.abs().sum(dim=0).max()) * float(P.abs().max())
+    err = float((out - ref).abs().max()) / scale
+    assert err <= (1e-14 if precision == 0 else 1e-12), err
