@@ -192,6 +192,20 @@ pg_status pg_block_gram(long n, const double* P_dev, int np, const double* Q_dev
 pg_status pg_block_combine(long n, const double* P_dev, int np, const double* C_dev, int ny, double* Y_dev,
                            int precision, void* stream);
 
+/* pg_block_gram without any device allocation; no counterpart in the
+ * reference.  For callers that must not allocate device memory: a framework
+ * may already hold the free memory in its own caching allocator, so a
+ * cudaMalloc would fail, or a cudaFree would synchronise the whole device
+ * under a latency budget.  The reduction partials go to a fixed file-scope
+ * device array of 256 x 296 doubles (592 KiB), so np * nq <= 256
+ * (PG_BAD_ARG with a message otherwise).  The first call on a device looks up
+ * that array's address and should come before any stream capture.  Nothing in
+ * the array has to start at zero.  Calls that overlap in time (other streams
+ * or threads) share the one array and race: serialise them.  Results are
+ * bit-identical to pg_block_gram's. */
+pg_status pg_block_gram_noalloc(long n, const double* P_dev, int np, const double* Q_dev, int nq, double* out_dev,
+                                int precision, void* stream);
+
 /* Work-array length in doubles (DavidsonWorkSize, src/Davidson.cpp:46-52). */
 long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag);
 

@@ -120,6 +120,7 @@ SYMBOLS = {
     "pg_glibc_rand_check": (C.c_int, [C.c_int, _ip]),
     "pg_block_gram": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_block_combine": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
+    "pg_block_gram_noalloc": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_request_footprint": (C.c_double, [C.POINTER(Request)]),
     "pg_engine_create": (C.c_int, [C.POINTER(EngineConfig), C.POINTER(_vp)]),
     "pg_engine_submit": (C.c_int, [_vp, C.POINTER(Request), C.POINTER(C.c_long)]),
@@ -389,6 +390,15 @@ def block_gram(P, Q, precision=PG_FP64, out=None, stream=None):
     if out is None:
         out = torch.empty(np_ * nq, dtype=torch.float64, device=P.device)
     _check(lib().pg_block_gram(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
+    return out.view(np_, nq)
+
+
+def block_gram_noalloc(P, Q, out, precision=PG_FP64, stream=None):
+    """block_gram through pg_block_gram_noalloc: the library allocates nothing
+    (out must be given; np * nq <= 256)."""
+    np_, n = P.shape
+    nq = Q.shape[0]
+    _check(lib().pg_block_gram_noalloc(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
     return out.view(np_, nq)
 
 

@@ -5,6 +5,7 @@
 // one warp, in a fixed order.  No atomics, no dependence on scheduling.
 #include <algorithm>
 #include <cstdint>
+#include <mutex>
 
 #include "pg_linalg.cuh"
 
@@ -542,4 +543,79 @@ extern "C" pg_status pg_block_combine(long n, const double* P, int np, const dou
   static thread_local pg::RedScratch rs;
   return pg::combine(n, P, np, C, ny, 1, 1.0, nullptr, nullptr, false, Y, ny, nullptr, rs, pg::as_stream(stream),
                      precision == PG_MIXED);
+}
+
+// ---------------------------------------------------------------------------
+// pg_block_gram_noalloc: pg_block_gram for callers that may not allocate
+// device memory.  The per-block partial sums live in a fixed file-scope
+// device array instead of a cudaMalloc'd buffer; the kernels and the
+// reduction order are pg_block_gram's, so the results are bit-identical.
+namespace {
+
+constexpr int kNoAllocMaxOut = 256;  // np * nq limit of this entry point
+constexpr long kNoAllocPartials = (long)pg::kRedBlocks * kNoAllocMaxOut;  // 75,776 doubles = 592 KiB
+
+// Nothing here needs to start at zero: each call writes every partial it
+// reads back.  One array per device, shared by every caller of the entry point.
+__device__ __align__(256) double g_noalloc_partial[kNoAllocPartials];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_m;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+}  // namespace
+
+extern "C" pg_status pg_block_gram_noalloc(long n, const double* P, int np, const double* Q, int nq, double* out,
+                                           int precision, void* stream) {
+  using namespace pg;
+  PG_ARG(n > 0 && P && Q && out && np > 0 && nq > 0, "pg_block_gram_noalloc: bad arguments");
+  PG_ARG(precision == PG_FP64 || precision == PG_MIXED, "pg_block_gram_noalloc: unknown precision");
+  PG_ARG((long)np * nq <= kNoAllocMaxOut,
+         "pg_block_gram_noalloc: %d x %d = %ld outputs exceed this entry point's fixed scratch (at most %d "
+         "outputs; use pg_block_gram)",
+         np, nq, (long)np * nq, kNoAllocMaxOut);
+  PG_ARG(np + nq <= 144, "pg_block_gram_noalloc: np + nq = %d exceeds 144", np + nq);
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev));
+  PG_ARG(dev >= 0 && dev < kNoAllocMaxDevices, "pg_block_gram_noalloc: device %d out of range", dev);
+  double* partial = nullptr;
+  {
+    // first call on a device: the address of the scratch array in this
+    // device's context (no allocation; done before any stream capture)
+    std::lock_guard<std::mutex> l(g_noalloc_m);
+    if (!g_noalloc_ptr[dev]) {
+      void* addr = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&addr, g_noalloc_partial);
+      if (e != cudaSuccess || !addr) {
+        set_error("pg_block_gram_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        return PG_CUDA;
+      }
+      g_noalloc_ptr[dev] = static_cast<double*>(addr);
+    }
+    partial = g_noalloc_ptr[dev];
+  }
+  PG_TRY(opt_in_smem());
+  cudaStream_t st = as_stream(stream);
+  const int no = np * nq;
+  if (precision == PG_MIXED) {
+    const int ablk = (np + kGA - 1) / kGA, nblk = ablk * ((nq + kGB - 1) / kGB);
+    PG_ARG(nblk <= kT, "pg_block_gram_noalloc: %d output blocks", nblk);
+    const int S = kT / nblk;
+    const int rows = np + nq;
+    int tp_log2 = 8;
+    while (tp_log2 > 5 && (size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8 > (size_t)kGramSmemMax) --tp_log2;
+    const long chunk = chunk_for(n, pg::kRedBlocks, 1 << tp_log2);
+    const int blocks = (int)((n + chunk - 1) / chunk);
+    const size_t smem = std::max((size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8,
+                                 (size_t)S * nblk * kGA * kGB * 8);
+    k_gram_df<<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, tp_log2, S, ablk, nblk, partial);
+    PG_TRY(check_launch("k_gram_df"));
+    return reduce(partial, blocks, no, out, false, st);
+  }
+  const long chunk = chunk_for(n, pg::kRedBlocks, kTP);
+  const int blocks = (int)((n + chunk - 1) / chunk);
+  const size_t smem = sizeof(double) * (size_t)(np + nq) * (kTP + 1);
+  k_gram<<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, partial);
+  PG_TRY(check_launch("k_gram"));
+  return reduce(partial, blocks, no, out, false, st);
 }
