@@ -58,6 +58,15 @@ long pg_kernel_launches(void);
  * same arguments and meaning (the verbose flag is dropped).  Host-only. */
 pg_status pg_sine_dvr(int n, double mu, double x0, double xNp1, double* x_host, double* ekin_host, int ldt);
 
+/* Periodic FFT kinetic term of DVRType 3: the grid points and the plane-wave
+ * energies ekin[n] = (dK k)^2 / (2 mu), dK = 2 pi / (n dx), k = a or a - n
+ * (Tdiag, src/KE_diag.cpp:33-80, same arguments without ldt/verbose); and,
+ * if t_host is not NULL, the n x n matrix of the per-axis operator
+ * ifft(ekin * fft(.)) / n that VectorFFT::apply applies
+ * (src/VectorFFTW.cpp:56-112), a real symmetric circulant.  Host-only. */
+pg_status pg_fft_kinetic(int n, double mu, double x0, double xNp1, double* x_host, double* ekin_host,
+                         double* t_host);
+
 /* --------------------------------------------------------------------- grid */
 
 typedef struct pg_grid pg_grid;
@@ -67,6 +76,13 @@ typedef struct pg_grid pg_grid;
  * split-TF32 copies of the mixed form) in device memory.  Replaces
  * DVR::SetupDVR with DVRType 0 (src/DVR.cpp:64-161, 524-651). */
 pg_status pg_grid_create(const int n[3], const double L[3], pg_grid** out);
+/* The same with the kinetic term chosen as the reference's DVRType: 2 = sine
+ * DVR (pg_grid_create), 3 = periodic FFT kinetic (VectorFFT, src/DVR.cpp:
+ * 138-142, 596-630), applied here as three per-axis dense circulant
+ * contractions, exactly the operator the 3-D FFT applies, by the same H*X
+ * kernels.  The reference's FFT path assumes cubic grids
+ * (src/VectorFFTW.cpp:83); this one is the separable operator for any box. */
+pg_status pg_grid_create_dvr(const int n[3], const double L[3], int dvrtype, pg_grid** out);
 pg_status pg_grid_destroy(pg_grid* g);
 /* Number of grid points (n0*n1*n2). */
 long pg_grid_npoints(const pg_grid* g);
@@ -165,12 +181,15 @@ pg_status pg_davidson_destroy(pg_davidson* d);
 pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision);
 
 /* Enables corrflag 3 on this handle: the correction vector of a root with
- * Ritz value lambda is (T - lambda)^-1 r, T the grid's kinetic operator,
- * applied exactly in its DST-I eigenbasis (three axis contractions, a
- * diagonal scale, three more; precision as pg_hx).  Not in the reference,
- * whose corrections use diag(H) only (src/Davidson.cpp:557-566); it changes
- * the convergence rate, not the converged eigenpairs.  g must outlive the
- * solve. */
+ * Ritz vector u, Ritz value lambda and residual r is M r, M = (T - lambda)^-1,
+ * T the grid's kinetic operator applied exactly in its eigenbasis (DST-I for
+ * the sine DVR, the real Fourier basis for the periodic FFT kinetic term:
+ * three axis contractions, a diagonal scale, three more; precision as
+ * pg_hx).  Where V is identically zero M r equals u and adds nothing, so the
+ * Olsen form -M r + (u.M r / u.M u) M u is used there (detected from diag(H)
+ * at the first call).  Not in the reference, whose corrections use diag(H)
+ * only (src/Davidson.cpp:530-566); it changes the convergence rate, not the
+ * converged eigenpairs.  g must outlive the solve. */
 pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int precision);
 
 /* The subspace eigensolver of the Davidson iteration (host): the k lowest

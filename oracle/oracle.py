@@ -168,6 +168,54 @@ class Grid:
         return st, ev, B[: self.N * nstates].reshape(nstates, self.N), nmv.value
 
 
+# ------------------------------------------------------------ FFT kinetic path
+# numpy restatement of the reference's DVRType 3 (periodic FFT kinetic term).
+# FFTW is not part of the reference tree, so the reference's own FFT path is
+# not built here; numpy's FFT stands in for FFTW (same unnormalised forward /
+# backward pair up to numpy's 1/N on the inverse).  Parity for this path is
+# therefore against this restatement and analytic spectra, not against a run
+# of the reference.
+
+REF_PI = 3.14159265358979  # src/KE_diag.cpp:28-30
+
+
+def fft_tdiag(n: int, mu: float, x0: float, xNp1: float):
+    """Tdiag (src/KE_diag.cpp:33-80): interior grid points and plane-wave
+    energies (dK kpoint)^2 / (2 mu), dK = 2 f2 / dx, f2 = pi / n."""
+    dx = (xNp1 - x0) / (n + 1)
+    x = np.array([x0 + dx * (j + 1) for j in range(n)])
+    f2 = REF_PI / n
+    dk = 2.0 * f2 / dx
+    e = np.empty(n)
+    for a in range(n):
+        kp = a - n if a >= n // 2 else a
+        e[a] = (dk * kp) ** 2 / (2.0 * mu)
+    return x, e
+
+
+def fft_ke_diag(n3, L3):
+    """KE_diag[xa1*n1*n2 + ya2*n2 + za3] = e0[xa1] + e1[ya2] + e2[za3]
+    (src/DVR.cpp:617-630), with e_a from Tdiag on the walls -L/2, L/2."""
+    e = [fft_tdiag(int(n3[a]), 1.0, -0.5 * L3[a], 0.5 * L3[a])[1] for a in range(3)]
+    return (e[0][:, None, None] + e[1][None, :, None] + e[2][None, None, :]).reshape(-1)
+
+
+def fft_apply(x, v_diag, n3, ke_diag):
+    """VectorFFT::apply (src/VectorFFTW.cpp:56-112): y = V x + ifft(K fft(x)) / N.
+    FFTW's 3-D r2c sees the array as [n0][n1][n2] (n2 fastest, dims
+    n_1dbas); the half spectrum element [i][j] (i over n0*n1, j < n2/2+1) is
+    multiplied by KE_diag[ng*i + j] with ng = n_1dbas[0] (cubic grids)."""
+    n0, n1, n2 = (int(a) for a in n3)
+    ng = n0
+    ng_h = n2 // 2 + 1
+    phi = np.fft.rfftn(np.asarray(x, dtype=np.float64).reshape(n0, n1, n2))
+    flat = phi.reshape(n0 * n1, ng_h)
+    idx = ng * np.arange(n0 * n1)[:, None] + np.arange(ng_h)[None, :]
+    flat *= np.asarray(ke_diag)[idx]
+    back = np.fft.irfftn(flat.reshape(n0, n1, ng_h), s=(n0, n1, n2), axes=(0, 1, 2))  # includes the 1/N
+    return np.asarray(v_diag) * np.asarray(x) + back.reshape(-1)
+
+
 def dpp_sites(waters_angstrom):
     """Rigid-water DPP site tables (sites, charges, charge_site, dipoles, dipole_site, iters)."""
     w = np.ascontiguousarray(waters_angstrom, dtype=np.float64).reshape(-1)

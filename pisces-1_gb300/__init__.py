@@ -94,6 +94,8 @@ SYMBOLS = {
     "pg_kernel_launches": (C.c_long, []),
     "pg_sine_dvr": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "pg_grid_create": (C.c_int, [_ip, _dp, C.POINTER(_vp)]),
+    "pg_grid_create_dvr": (C.c_int, [_ip, _dp, C.c_int, C.POINTER(_vp)]),
+    "pg_fft_kinetic": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]),
     "pg_grid_destroy": (C.c_int, [_vp]),
     "pg_grid_npoints": (C.c_long, [_vp]),
     "pg_grid_points": (C.c_int, [_vp, _dp, _dp, _dp]),
@@ -177,6 +179,14 @@ def _stream(stream):
     return C.c_void_p(int(stream))
 
 
+def fft_kinetic(n, L, mu=1.0):
+    """Periodic FFT kinetic term on (-L/2, L/2): grid points, plane-wave
+    energies and the n x n circulant matrix of the per-axis operator."""
+    x, e, t = np.empty(n), np.empty(n), np.empty(n * n)
+    _check(lib().pg_fft_kinetic(n, mu, -0.5 * L, 0.5 * L, _d(x), _d(e), _d(t)))
+    return x, e, t.reshape(n, n)
+
+
 def sine_dvr(n, L, mu=1.0, packed=True):
     """1-D sine DVR on (-L/2, L/2): grid points and kinetic matrix (packed or full)."""
     x = np.empty(n)
@@ -237,13 +247,15 @@ class WaterTables:
 
 
 class Grid:
-    """3-D sine-DVR grid on the current CUDA device (pg_grid)."""
+    """3-D grid on the current CUDA device (pg_grid): dvrtype 2 = sine DVR,
+    3 = periodic FFT kinetic term (the reference's DVRType values)."""
 
-    def __init__(self, n, L):
-        n = np.ascontiguousarray(n, dtype=np.int32)
-        L = np.ascontiguousarray(L, dtype=np.float64)
+    def __init__(self, n, L, dvrtype=2):
+        n = np.ascontiguousarray(np.broadcast_to(n, 3), dtype=np.int32)
+        L = np.ascontiguousarray(np.broadcast_to(L, 3), dtype=np.float64)
         h = _vp()
-        _check(lib().pg_grid_create(_i(n), _d(L), C.byref(h)))
+        _check(lib().pg_grid_create_dvr(_i(n), _d(L), int(dvrtype), C.byref(h)))
+        self.dvrtype = int(dvrtype)
         self._h = h
         self.n = tuple(int(v) for v in n)
         self.L = tuple(float(v) for v in L)

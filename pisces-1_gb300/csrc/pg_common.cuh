@@ -15,10 +15,13 @@ namespace pg {
 void set_error(const char* fmt, ...);
 const char* last_error();
 
+// On failure the runtime's last-error slot is cleared as well, so that a
+// failed call is not reported again by the next launch check.
 #define PG_CUDA_TRY(expr)                                                                  \
   do {                                                                                     \
     cudaError_t e_ = (expr);                                                               \
     if (e_ != cudaSuccess) {                                                               \
+      cudaGetLastError();                                                                  \
       ::pg::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr, cudaGetErrorString(e_)); \
       return PG_CUDA;                                                                      \
     }                                                                                      \
@@ -100,6 +103,7 @@ inline __host__ __device__ int tc_kpad(int n) { return (n + 7) / 8 * 8; }
 
 // The grid handle: sizes, host copies of the 1-D data and device kinetic matrices.
 struct pg_grid {
+  int dvrtype = 2;                 // 2: sine DVR; 3: periodic FFT kinetic (as dense circulant matrices)
   int n[3];
   double L[3];
   long N;
@@ -116,8 +120,13 @@ struct pg_grid {
   // eigenbasis of the kinetic matrices (the orthonormal DST-I, symmetric),
   // for the kinetic preconditioner: FP64, TF32 hi/lo, and the eigenvalues
   pg::DevBuf<double> q_dev[3];
-  pg::DevBuf<float> q_hi[3], q_lo[3];  // operand images, as t_hi / t_lo
+  // forward transform Q^T (q_*) and backward transform Q (qb_*): FP64 and
+  // operand images, as t_hi / t_lo; the same matrix for the symmetric DST-I
+  pg::DevBuf<float> q_hi[3], q_lo[3];
+  pg::DevBuf<double> qb_dev[3];
+  pg::DevBuf<float> qb_hi[3], qb_lo[3];
   pg::DevBuf<double> d_dev[3];
+  std::vector<double> ekin[3];     // FFT grids: plane-wave energies per axis (Tdiag)
   // random start columns (Randm11 from seed 1; the same values for every
   // solve on this grid), generated once and grown on demand
   mutable std::mutex start_m;

@@ -52,7 +52,11 @@ struct pg_davidson {
   // subspace products (S, Ritz/residual combinations, orthogonalisation) in
   // double-float arithmetic on the FP32 pipe instead of FP64 (mixed form)
   bool dfloat = false;
-  pg::DevBuf<double> pc_w1, pc_w2;
+  pg::DevBuf<double> pc_w1, pc_w2, pc_ru;
+  // corrflag 3 on a grid where V is identically zero: the plain correction
+  // M r is the Ritz vector itself there, so the Olsen form is used instead
+  bool pc_olsen = false;
+  pg::DevBuf<int> pc_flag;
   // counters for the solve statistics
   long n_iter = 0, n_restart = 0;
   double t_eig = 0, t_wait = 0;  // host seconds in the subspace eigensolver / waiting for the device
@@ -235,7 +239,7 @@ constexpr int kLam = 32;    // Ritz values (16)
 constexpr int kRsq = 64;    // |r_r|^2 and 1/|r_r| (2 x 16)
 constexpr int kOnes = 96;   // 1.0 (16), the "keep X" coefficients of combine
 constexpr int kDots = 112;  // Jacobi-Davidson dot products (2)
-constexpr int kSigma = 128; // shifts of the kinetic preconditioner (16)
+constexpr int kSigma = 128; // shifts of the kinetic preconditioner (2 x 16)
 constexpr int kScalars = 256;
 
 pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
@@ -291,14 +295,49 @@ __global__ void __launch_bounds__(32) k_cholinv(const double* __restrict__ G, in
   }
 }
 
+// flag = 1 if diag(H) differs anywhere from the kinetic diagonal, i.e. V is
+// not identically zero (any nonzero difference sets the same value).
+__global__ void k_potential_nonzero(int nx, int ny, int nz, const double* __restrict__ diag,
+                                    const double* __restrict__ tx, const double* __restrict__ ty,
+                                    const double* __restrict__ tz, int* __restrict__ flag) {
+  const unsigned N = (unsigned)nx * ny * nz;
+  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < N; g += gridDim.x * blockDim.x) {
+    const unsigned i = g % (unsigned)nx, r = g / (unsigned)nx;
+    const unsigned j = r % (unsigned)ny, k = r / (unsigned)ny;
+    double t = 0.0;
+    t = __dadd_rn(t, tx[(size_t)i * nx + i]);
+    t = __dadd_rn(t, ty[(size_t)j * ny + j]);
+    t = __dadd_rn(t, tz[(size_t)k * nz + k]);
+    if (diag[g] != t) *flag = 1;
+  }
+}
+
+// Coefficients of the Olsen correction c_j = -M r_j + (u_j.M r_j / u_j.M u_j) M u_j
+// from the Gram block G[j*2k + b] = u_j . [M R, M U]_b, as a 2k x k matrix
+// C[a*k + j] for a combine over [M R, M U].
+__global__ void k_olsen_coef(const double* __restrict__ G, int k, double* __restrict__ C) {
+  for (int e = threadIdx.x; e < 2 * k * k; e += blockDim.x) {
+    const int a = e / k, j = e % k;
+    double c = 0.0;
+    if (a == j) {
+      c = -1.0;
+    } else if (a == k + j) {
+      const double den = G[(long)j * 2 * k + k + j];
+      c = den != 0.0 ? G[(long)j * 2 * k + j] / den : 0.0;
+    }
+    C[e] = c;
+  }
+}
+
 // Kinetic preconditioner on the k contiguous vectors R: R <- (T - sigma_j)^-1 R
-// with T = Qx Qy Qz diag(d) Qz Qy Qx (the DST-I eigenbasis of the sine DVR),
-// i.e. three axis contractions, a diagonal scale and three contractions.
+// with T = Q diag(d) Q^T per axis (DST-I for the sine DVR, the real Fourier
+// basis for the periodic FFT kinetic term): three forward contractions
+// (Q^T), a diagonal scale and three backward contractions (Q).
 pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* sigma_dev, cudaStream_t st) {
   const pg_grid* g = d->pc_grid;
   const long N = g->N;
-  PG_TRY(d->pc_w1.ensure((size_t)d->nroots * N));
-  PG_TRY(d->pc_w2.ensure((size_t)d->nroots * N));
+  PG_TRY(d->pc_w1.ensure((size_t)k * N));
+  PG_TRY(d->pc_w2.ensure((size_t)k * N));
   double *w1 = d->pc_w1.p, *w2 = d->pc_w2.p;
   const int pr = d->pc_precision;
   PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, R, w1, k, 0, pr, st));
@@ -307,19 +346,23 @@ pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* s
   // the smallest kinetic level, a scale for the denominator floor
   double dmin = 0;
   for (int a = 0; a < 3; ++a) dmin += 0.5 * (M_PI / g->L[a]) * (M_PI / g->L[a]);
-#define PG_KIN_SCALE(NRV)                                                                                  \
-  k_kin_scale<NRV><<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], g->d_dev[0].p, g->d_dev[1].p,   \
-                                                 g->d_dev[2].p, sigma_dev, 0.1 * dmin, w1, k, pr == PG_MIXED ? 1 : 0)
-  if (k <= 1) PG_KIN_SCALE(1);
-  else if (k <= 2) PG_KIN_SCALE(2);
-  else if (k <= 4) PG_KIN_SCALE(4);
-  else if (k <= 8) PG_KIN_SCALE(8);
-  else PG_KIN_SCALE(16);
+  for (int v0 = 0; v0 < k; v0 += 16) {  // at most 16 vectors per launch
+    const int kk = std::min(16, k - v0);
+#define PG_KIN_SCALE(NRV)                                                                                     \
+  k_kin_scale<NRV><<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], g->d_dev[0].p, g->d_dev[1].p,      \
+                                                 g->d_dev[2].p, sigma_dev + v0, 0.1 * dmin, w1 + (long)v0 * N, \
+                                                 kk, pr == PG_MIXED ? 1 : 0)
+    if (kk <= 1) PG_KIN_SCALE(1);
+    else if (kk <= 2) PG_KIN_SCALE(2);
+    else if (kk <= 4) PG_KIN_SCALE(4);
+    else if (kk <= 8) PG_KIN_SCALE(8);
+    else PG_KIN_SCALE(16);
 #undef PG_KIN_SCALE
-  PG_TRY(check_launch("k_kin_scale"));
-  PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, w1, w2, k, 0, pr, st));
-  PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w2, w1, k, 0, pr, st));
-  PG_TRY(axis_apply(g, 0, g->q_dev[0].p, g->q_hi[0].p, g->q_lo[0].p, w1, R, k, 0, pr, st));
+    PG_TRY(check_launch("k_kin_scale"));
+  }
+  PG_TRY(axis_apply(g, 2, g->qb_dev[2].p, g->qb_hi[2].p, g->qb_lo[2].p, w1, w2, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 1, g->qb_dev[1].p, g->qb_hi[1].p, g->qb_lo[1].p, w2, w1, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 0, g->qb_dev[0].p, g->qb_hi[0].p, g->qb_lo[0].p, w1, R, k, 0, pr, st));
   return PG_OK;
 }
 
@@ -374,6 +417,19 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
 
   if (d->status == 0) {  // first call (src/Davidson.cpp:145-193)
     PG_TRY(ensure_scratch(d, ndim, maxsub, nroots));
+    d->pc_olsen = false;
+    if (corrflag == 3) {  // is V identically zero? (diag(H) equals the kinetic diagonal)
+      const pg_grid* g = d->pc_grid;
+      PG_TRY(d->pc_flag.ensure(1));
+      PG_CUDA_TRY(cudaMemsetAsync(d->pc_flag.p, 0, sizeof(int), st));
+      k_potential_nonzero<<<blocks_for(N), kT, 0, st>>>(g->n[0], g->n[1], g->n[2], diag, g->t_dev[0].p,
+                                                         g->t_dev[1].p, g->t_dev[2].p, d->pc_flag.p);
+      PG_TRY(check_launch("k_potential_nonzero"));
+      int nonzero = 1;
+      PG_CUDA_TRY(cudaMemcpyAsync(&nonzero, d->pc_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+      PG_CUDA_TRY(cudaStreamSynchronize(st));
+      d->pc_olsen = nonzero == 0;
+    }
     d->jmacro = 1;
     d->nsub = 0;
     d->nnewB = nroots;
@@ -481,12 +537,27 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         return PG_NUMERIC;
       }
     }
-    // convergence and locking (src/Davidson.cpp:272-289)
+    // convergence and locking (src/Davidson.cpp:272-289).  The reference
+    // skips a root whose overlap with the converged space exceeds 0.95; at
+    // most nconv roots can (their squared overlaps sum to at most nconv), and
+    // with separated eigenvalues exactly the nconv locked ones do.  Inside a
+    // degenerate set the rotation of the Ritz vectors can leave every overlap
+    // below 0.95, and the reference would lock the same state again (nConv
+    // past nroots).  Here the nconv roots of largest overlap are the ones
+    // skipped: the same choice whenever the reference's is well defined.
+    std::vector<char> in_conv(nroots, 0);
+    {
+      std::vector<int> order(nroots);
+      for (int r = 0; r < nroots; ++r) order[r] = r;
+      std::stable_sort(order.begin(), order.end(),
+                       [&](int a, int b) { return d->conv_w[a] > d->conv_w[b]; });
+      for (int c = 0; c < *nconv && c < nroots; ++c) in_conv[order[c]] = 1;
+    }
     int newly = 0;
     for (int r = 0; r < nroots; ++r) {
-      if (d->conv_w[r] > 0.95) {
+      if (in_conv[r] || d->conv_w[r] > 0.95) {
         d->ccode[r] = 0;
-      } else if (d->residuals[r] < d->thresh) {
+      } else if (d->residuals[r] < d->thresh && *nconv < nroots) {
         d->ccode[r] = 1;
         d->bindex[r] = *nconv;
         PG_CUDA_TRY(cudaMemcpyAsync(B + (long)(*nconv) * N, ritz + (long)r * N, sizeof(double) * N,
@@ -506,7 +577,8 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       return PG_OK;
     }
     // restart (src/Davidson.cpp:303-346)
-    if (d->nsub == ms || newly > 0) {
+    const bool restarted = d->nsub == ms || newly > 0;
+    if (restarted) {
       d->n_restart++;
       d->nnewB = 0;
       for (int r = 0; r < nroots; ++r)
@@ -572,12 +644,38 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         PG_CUDA_TRY(cudaMemcpyAsync(res + (long)j * N, rv, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
     }
     d->nnewB = (int)sel.size();
-    if (corrflag == 3 && d->nnewB > 0) {
+    if (corrflag == 3 && d->nnewB > 0 && !d->pc_olsen) {
+      // exact-kinetic correction M r_j, M = (T - lambda_j)^-1
       std::vector<double> sig(d->nnewB);
       for (int j = 0; j < d->nnewB; ++j) sig[j] = d->sse[sel[j]];
       double* dsig = d->dsq.p + kSigma;
       PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig.data(), sizeof(double) * d->nnewB, cudaMemcpyHostToDevice, st));
       PG_TRY(kinetic_precondition(d, res, d->nnewB, dsig, st));
+    } else if (corrflag == 3 && d->nnewB > 0) {
+      // Olsen correction with M = (T - lambda_j)^-1 applied exactly:
+      // c_j = -M r_j + (u_j.M r_j / u_j.M u_j) M u_j, orthogonal to u_j.  With
+      // V = 0, M r_j is u_j itself and would add no direction.
+      const int k = d->nnewB;
+      PG_TRY(d->pc_ru.ensure((size_t)3 * nroots * N));
+      double* RU = d->pc_ru.p;             // [R (k), U (k), U again (k)]
+      double* Uc = RU + (long)2 * k * N;
+      PG_CUDA_TRY(cudaMemcpyAsync(RU, res, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
+      for (int j = 0; j < k; ++j) {
+        // after a restart the Ritz block holds Z v; the Ritz vector is in B
+        const double* u = restarted ? B + (long)d->bindex[sel[j]] * N : ritz + (long)sel[j] * N;
+        PG_CUDA_TRY(cudaMemcpyAsync(RU + (long)(k + j) * N, u, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+      }
+      PG_CUDA_TRY(cudaMemcpyAsync(Uc, RU + (long)k * N, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
+      std::vector<double> sig(2 * k);
+      for (int j = 0; j < k; ++j) sig[j] = sig[k + j] = d->sse[sel[j]];
+      double* dsig = d->dsq.p + kSigma;
+      PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig.data(), sizeof(double) * 2 * k, cudaMemcpyHostToDevice, st));
+      PG_TRY(kinetic_precondition(d, RU, 2 * k, dsig, st));  // RU = [M R, M U]
+      PG_TRY(gram(N, Uc, k, RU, 2 * k, d->dgram.p, d->rs, st, d->dfloat));
+      k_olsen_coef<<<1, 256, 0, st>>>(d->dgram.p, k, d->dcoef.p);
+      PG_TRY(check_launch("k_olsen_coef"));
+      PG_TRY(combine(N, RU, 2 * k, d->dcoef.p, k, 1, 1.0, nullptr, nullptr, false, res, k, nullptr, d->rs, st,
+                     d->dfloat));
     }
     if (d->nnewB > 0)
       PG_TRY(block_orthonormalise(d, N, res, d->nnewB, B, d->nsub, B + (long)d->nsub * N, st));

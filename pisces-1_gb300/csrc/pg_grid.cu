@@ -1,9 +1,10 @@
-// Grid handle, sine-DVR kinetic builder, diag(H) and the particle-in-a-box
-// start vector.
+// Grid handle, kinetic builders (sine DVR; periodic FFT kinetic), diag(H)
+// and the particle-in-a-box start vector.
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
+#include <vector>
 
 #include "pg_common.cuh"
 
@@ -62,6 +63,37 @@ extern "C" pg_status pg_sine_dvr(int n, double mu, double x0, double xNp1, doubl
   if (ldt > 0)
     for (int a = 0; a < n; ++a)
       for (int b = 0; b < a; ++b) ekin[b + (long)a * ldt] = ekin[a + (long)b * ldt];
+  return PG_OK;
+}
+
+extern "C" pg_status pg_fft_kinetic(int n, double mu, double x0, double xNp1, double* x, double* ekin, double* t) {
+  PG_ARG(n > 1 && x && ekin && mu > 0 && xNp1 > x0, "pg_fft_kinetic: bad arguments");
+  // Tdiag (src/KE_diag.cpp:33-80): the same interior points as the sine DVR
+  // and, for the periodic FFT kinetic term, the plane-wave energies
+  // (dK kpoint)^2 / (2 mu) with dK = 2 pi / (n dx) and kpoint = a for
+  // a < n/2, a - n otherwise (the reference's 15-digit pi).
+  const double dx = (xNp1 - x0) / (double)(n + 1);
+  for (int j = 0; j < n; ++j) x[j] = x0 + dx * (double)(j + 1);
+  const double f2 = pg::kRefPi / (double)n;
+  const double dk = 2.0 * f2 / dx;
+  for (int a = 0; a < n; ++a) {
+    const int kp = a >= n / 2 ? a - n : a;
+    const double q = dk * kp;
+    ekin[a] = q * q / (2.0 * mu);
+  }
+  // The operator VectorFFT::apply uses per axis, ifft(ekin * fft(.)) / n
+  // (src/VectorFFTW.cpp:56-112), as a real symmetric circulant matrix:
+  // T[p][q] = (1/n) sum_m ekin[m] cos(2 pi m (p - q) / n).
+  if (t) {
+    std::vector<double> c(n);
+    for (int d = 0; d < n; ++d) {
+      double s = 0;
+      for (int m = 0; m < n; ++m) s += ekin[m] * cos(2.0 * M_PI * (double)(((long)m * d) % n) / (double)n);
+      c[d] = s / (double)n;
+    }
+    for (int p = 0; p < n; ++p)
+      for (int q = 0; q < n; ++q) t[(long)p * n + q] = c[(p - q + n) % n];
+  }
   return PG_OK;
 }
 
@@ -139,13 +171,19 @@ int grid_blocks(long N, int threads) {
 }  // namespace
 
 extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid** out) {
+  return pg_grid_create_dvr(n, L, 2, out);
+}
+
+extern "C" pg_status pg_grid_create_dvr(const int n[3], const double L[3], int dvrtype, pg_grid** out) {
   PG_ARG(n && L && out, "pg_grid_create: null argument");
+  PG_ARG(dvrtype == 2 || dvrtype == 3, "pg_grid_create: dvrtype %d (2: sine DVR, 3: periodic FFT kinetic)", dvrtype);
   for (int a = 0; a < 3; ++a) {
     PG_ARG(n[a] >= 2 && n[a] <= 1024, "pg_grid_create: n[%d] = %d out of range [2, 1024]", a, n[a]);
     PG_ARG(L[a] > 0 && std::isfinite(L[a]), "pg_grid_create: L[%d] must be positive", a);
   }
   PG_ARG((double)n[0] * n[1] * n[2] < 2.0e9, "pg_grid_create: too many grid points");
   pg_grid* g = new pg_grid();
+  g->dvrtype = dvrtype;
   cudaGetDevice(&g->device);
   g->N = 1;
   for (int a = 0; a < 3; ++a) {
@@ -155,8 +193,12 @@ extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid**
     const int m = n[a];
     g->x[a].resize(m);
     g->t[a].resize((size_t)m * m);
-    pg_status s = pg_sine_dvr(m, 1.0, -0.5 * L[a], 0.5 * L[a], g->x[a].data(), g->t[a].data(), m);
+    std::vector<double> ek(m);
+    pg_status s = dvrtype == 3 ? pg_fft_kinetic(m, 1.0, -0.5 * L[a], 0.5 * L[a], g->x[a].data(), ek.data(),
+                                                g->t[a].data())
+                               : pg_sine_dvr(m, 1.0, -0.5 * L[a], 0.5 * L[a], g->x[a].data(), g->t[a].data(), m);
     if (s != PG_OK) { delete g; return s; }
+    g->ekin[a] = ek;
     std::vector<float> hi((size_t)m * m), lo((size_t)m * m);
     for (size_t e = 0; e < hi.size(); ++e) {
       hi[e] = to_tf32((float)g->t[a][e]);
@@ -179,31 +221,59 @@ extern "C" pg_status pg_grid_create(const int n[3], const double L[3], pg_grid**
       return PG_CUDA;
     }
   }
-  // Eigenbasis of the sine-DVR kinetic matrix: the DVR is the
-  // particle-in-a-box basis, so T = Q diag(d) Q with the orthonormal DST-I
-  // matrix Q[i][k] = sqrt(2/(n+1)) sin(pi (i+1)(k+1)/(n+1)) and
-  // d_k = (pi (k+1) / L)^2 / 2 (src/sine_dvr.cpp:1-12).
+  // Eigenbasis of the kinetic matrix of each axis, T = Q diag(d) Q^T, for the
+  // kinetic preconditioner (forward transform Q^T, backward Q).
+  //   sine DVR: the DVR is the particle-in-a-box basis, Q is the orthonormal
+  //     DST-I matrix Q[i][k] = sqrt(2/(n+1)) sin(pi (i+1)(k+1)/(n+1)) (symmetric,
+  //     Q^T = Q) and d_k = (pi (k+1) / L)^2 / 2 (src/sine_dvr.cpp:1-12);
+  //   periodic FFT kinetic: the real Fourier basis, columns 1/sqrt(n),
+  //     sqrt(2/n) cos(2 pi m i / n), sqrt(2/n) sin(2 pi m i / n) for
+  //     0 < m < n/2, and (-1)^i / sqrt(n) for even n; d = the plane-wave
+  //     energy of m.
   for (int a = 0; a < 3; ++a) {
     const int m = n[a];
-    std::vector<double> q((size_t)m * m), d(m);
-    std::vector<float> qh((size_t)m * m), ql((size_t)m * m);
-    const double s = sqrt(2.0 / (m + 1));
-    for (int i = 0; i < m; ++i)
-      for (int k = 0; k < m; ++k) {
-        const double v = s * sin(M_PI * (double)((long)(i + 1) * (k + 1) % (2 * (m + 1))) / (m + 1));
-        q[(size_t)i * m + k] = v;
-        qh[(size_t)i * m + k] = to_tf32((float)v);
-        ql[(size_t)i * m + k] = to_tf32((float)(v - (double)qh[(size_t)i * m + k]));
+    std::vector<double> q((size_t)m * m), qt((size_t)m * m), d(m);
+    if (dvrtype == 3) {
+      const std::vector<double>& ek = g->ekin[a];
+      int col = 0;
+      auto put = [&](int c, auto f, double e) {
+        for (int i = 0; i < m; ++i) q[(size_t)i * m + c] = f(i);
+        d[c] = e;
+      };
+      put(col++, [&](int) { return 1.0 / sqrt((double)m); }, ek[0]);
+      for (int f = 1; 2 * f < m; ++f) {
+        const double s2 = sqrt(2.0 / m);
+        put(col++, [&](int i) { return s2 * cos(2.0 * M_PI * (double)(((long)f * i) % m) / m); }, ek[f]);
+        put(col++, [&](int i) { return s2 * sin(2.0 * M_PI * (double)(((long)f * i) % m) / m); }, ek[f]);
       }
-    for (int k = 0; k < m; ++k) d[k] = 0.5 * (M_PI * (k + 1) / L[a]) * (M_PI * (k + 1) / L[a]);
-    const std::vector<float> qh_img = tc_image(qh, m), ql_img = tc_image(ql, m);
-    if (g->q_dev[a].alloc((size_t)m * m) != PG_OK || g->q_hi[a].alloc(qh_img.size()) != PG_OK ||
-        g->q_lo[a].alloc(ql_img.size()) != PG_OK || g->d_dev[a].alloc(m) != PG_OK ||
-        cudaMemcpy(g->q_dev[a].p, q.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(g->q_hi[a].p, qh_img.data(), sizeof(float) * qh_img.size(), cudaMemcpyHostToDevice) !=
-            cudaSuccess ||
-        cudaMemcpy(g->q_lo[a].p, ql_img.data(), sizeof(float) * ql_img.size(), cudaMemcpyHostToDevice) !=
-            cudaSuccess ||
+      if (m % 2 == 0) put(col++, [&](int i) { return (i % 2 ? -1.0 : 1.0) / sqrt((double)m); }, ek[m / 2]);
+    } else {
+      const double s = sqrt(2.0 / (m + 1));
+      for (int i = 0; i < m; ++i)
+        for (int k = 0; k < m; ++k)
+          q[(size_t)i * m + k] = s * sin(M_PI * (double)((long)(i + 1) * (k + 1) % (2 * (m + 1))) / (m + 1));
+      for (int k = 0; k < m; ++k) d[k] = 0.5 * (M_PI * (k + 1) / L[a]) * (M_PI * (k + 1) / L[a]);
+    }
+    for (int i = 0; i < m; ++i)
+      for (int k = 0; k < m; ++k) qt[(size_t)k * m + i] = q[(size_t)i * m + k];
+    // forward (Q^T) and backward (Q) transforms in FP64 and as TF32 operand images
+    auto upload = [&](const std::vector<double>& M, pg::DevBuf<double>& dv, pg::DevBuf<float>& hi,
+                      pg::DevBuf<float>& lo) -> bool {
+      std::vector<float> h((size_t)m * m), l((size_t)m * m);
+      for (size_t e = 0; e < M.size(); ++e) {
+        h[e] = to_tf32((float)M[e]);
+        l[e] = to_tf32((float)(M[e] - (double)h[e]));
+      }
+      const std::vector<float> hi_img = tc_image(h, m), lo_img = tc_image(l, m);
+      return dv.alloc((size_t)m * m) == PG_OK && hi.alloc(hi_img.size()) == PG_OK &&
+             lo.alloc(lo_img.size()) == PG_OK &&
+             cudaMemcpy(dv.p, M.data(), sizeof(double) * M.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemcpy(hi.p, hi_img.data(), sizeof(float) * hi_img.size(), cudaMemcpyHostToDevice) ==
+                 cudaSuccess &&
+             cudaMemcpy(lo.p, lo_img.data(), sizeof(float) * lo_img.size(), cudaMemcpyHostToDevice) == cudaSuccess;
+    };
+    if (!upload(qt, g->q_dev[a], g->q_hi[a], g->q_lo[a]) || !upload(q, g->qb_dev[a], g->qb_hi[a], g->qb_lo[a]) ||
+        g->d_dev[a].alloc(m) != PG_OK ||
         cudaMemcpy(g->d_dev[a].p, d.data(), sizeof(double) * m, cudaMemcpyHostToDevice) != cudaSuccess) {
       pg::set_error("pg_grid_create: kinetic eigenbasis upload failed");
       delete g;

@@ -136,7 +136,7 @@ extern "C" double pg_request_footprint(const pg_request* r) {
   const double N = (double)r->n[0] * r->n[1] * r->n[2];
   const double ms = r->params.maxsub, nr = r->params.nroots;
   const double work = r->params.corrflag == 2 ? 2 * nr + 1 : 2 * nr;  // pg_davidson_work_size
-  const double pc = r->params.corrflag == 3 ? 2 * nr : 0;            // preconditioner work blocks
+  const double pc = r->params.corrflag == 3 ? 7 * nr : 0;            // preconditioner blocks (2 x 2nr work, 3nr)
   // basis + products, work array, diagonal, potential, eigenvectors
   return 8.0 * (N * (2 * ms + work + 1 + 1 + nr + pc) + 2 * ms * ms + 11 * ms);
 }

@@ -352,3 +352,80 @@ def test_solve_c2_mixed_against_fp64_and_reference(pg, torch):
     ref = torch.tensor(gd["wavefn16"].astype(np.float64), device="cuda").reshape(4, -1)
     ov = torch.abs(torch.sum(X64 * ref, dim=1)) / (X64.norm(dim=1) * ref.norm(dim=1))
     assert float(ov.min()) >= 1 - 1e-3, ov
+
+
+# ---------------------------------------------------------------- FFT kinetic path (DVRType 3)
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("n,L,nvec", [(24, 20.0, 1), (32, 30.0, 4)])
+def test_hx_fft_grid_matches_reference_fft_apply(pg, orc, torch, precision, n, L, nvec):
+    """H*X on a DVRType 3 grid against the numpy restatement of
+    VectorFFT::apply (cubic grids): FP64 to round-off, mixed within the
+    mixed form's H*X bound (2e-5 of max |Y|, as for the sine DVR)."""
+    rng = np.random.Generator(np.random.PCG64(4))
+    grid = pg.Grid((n, n, n), (L, L, L), dvrtype=3)
+    N = grid.N
+    x = rng.standard_normal(nvec * N)
+    v = rng.standard_normal(N)
+    ke = orc.fft_ke_diag((n, n, n), (L, L, L))
+    ref = np.concatenate([orc.fft_apply(x[k * N:(k + 1) * N], v, (n, n, n), ke) for k in range(nvec)])
+    y = grid.hx(dev(torch, v), dev(torch, x), nvec=nvec, precision=precision)
+    err = np.max(np.abs(host(y) - ref)) / np.max(np.abs(ref))
+    assert err <= (1e-13 if precision == 0 else 2e-5), err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_fft_grid_plane_waves_are_eigenvectors(pg, torch, precision):
+    """V = 0 on a periodic grid: H applied to a product of axis plane waves
+    cos(2 pi m_a i_a / n_a) returns it times sum_a ekin_a[m_a] (known answer
+    of the FFT kinetic operator), for a non-cubic box; the ground state of
+    the empty box is the constant vector with energy 0."""
+    n3, L3 = (16, 12, 20), (15.0, 13.0, 17.0)
+    grid = pg.Grid(n3, L3, dvrtype=3)
+    ek = [pg.fft_kinetic(n3[a], L3[a])[1] for a in range(3)]
+    v = torch.zeros(grid.N, dtype=torch.float64, device="cuda")
+    for m in ((0, 0, 0), (1, 0, 0), (3, 2, 1), (8, 6, 10), (5, 11, 7)):
+        f = [np.cos(2 * np.pi * m[a] * np.arange(n3[a]) / n3[a]) for a in range(3)]
+        x = (f[2][:, None, None] * f[1][None, :, None] * f[0][None, None, :]).reshape(-1)
+        e = ek[0][m[0]] + ek[1][m[1]] + ek[2][m[2]]
+        y = host(grid.hx(v, dev(torch, x), nvec=1, precision=precision))
+        err = np.max(np.abs(y - e * x)) / sum(float(np.max(k)) for k in ek)  # relative to the kinetic scale
+        assert err <= (1e-12 if precision == 0 else 2e-5), (m, err)
+    for corr in (1, 3):
+        ev, _, _ = grid.solve(v, nroots=1, maxsub=20, maxiter=200, ptol=8, corrflag=corr)
+        assert abs(ev[0]) <= 1e-8, corr
+    # and the sine DVR on the same non-cubic box: the particle-in-a-box ground state
+    sine = pg.Grid(n3, L3)
+    e0 = sum(0.5 * (np.pi / L) ** 2 for L in L3)
+    for corr in (1, 3):
+        ev, _, _ = sine.solve(v, nroots=1, maxsub=20, maxiter=200, ptol=8, corrflag=corr)
+        assert abs(ev[0] - e0) <= 1e-8, (corr, ev, e0)
+
+
+@pytest.mark.gpu
+def test_fft_grid_cluster_solve_against_dense_reference_operator(pg, orc, torch, clusters):
+    """(H2O)4 on a periodic 12^3 grid: the two lowest eigenvalues of the device
+    Davidson (FP64, diagonal correction and kinetic preconditioner; mixed)
+    against numpy's dense eigensolver of the reference FFT operator, built
+    column by column with the restatement of VectorFFT::apply."""
+    n, L = 12, 14.0
+    w = clusters.water_cluster(4, 4.0, seed=5)
+    grid = pg.Grid((n, n, n), (L, L, L), dvrtype=3)
+    v = grid.potential(pg.WaterTables(w))
+    vh = host(v)
+    ke = orc.fft_ke_diag((n, n, n), (L, L, L))
+    N = grid.N
+    H = np.empty((N, N))
+    eye = np.zeros(N)
+    for c in range(N):
+        eye[c] = 1.0
+        H[:, c] = orc.fft_apply(eye, vh, (n, n, n), ke)
+        eye[c] = 0.0
+    ref = np.linalg.eigvalsh(0.5 * (H + H.T))[:2]
+    for corr in (1, 3):
+        ev, _, _ = grid.solve(v, nroots=2, maxsub=30, maxiter=300, ptol=8, corrflag=corr)
+        assert np.max(np.abs(np.asarray(ev) - ref)) <= 1e-8, (corr, ev, ref)
+    ev, _, _ = grid.solve(v, nroots=2, maxsub=30, maxiter=300, ptol=6, corrflag=3, precision=pg.PG_MIXED, refine=1)
+    assert np.max(np.abs(np.asarray(ev) - ref)) <= 1e-6

@@ -143,3 +143,35 @@ def test_start_vectors_random_stream_is_c_library_rand(orc):
         exp.append(m / 2147483647 if s > 2147483647 // 2 else -m / 2147483647)
     assert np.allclose(list(out), exp, rtol=0, atol=0)
     assert len(set(seq)) > 40
+
+
+# ---------------------------------------------------------------- FFT kinetic path
+
+def test_fft_kinetic_builder_matches_tdiag_restatement(orc, pg):
+    """pg_fft_kinetic (host) against the numpy restatement of Tdiag: the same
+    points and plane-wave energies, and its circulant matrix is the operator
+    ifft(ekin fft(.)) / n of one axis (applied to unit vectors)."""
+    for n, L in ((12, 9.0), (15, 11.0), (32, 30.0)):
+        x, e, t = pg.fft_kinetic(n, L)
+        xo, eo = orc.fft_tdiag(n, 1.0, -0.5 * L, 0.5 * L)
+        assert np.array_equal(x, xo)
+        assert np.allclose(e, eo, rtol=1e-15, atol=0)
+        eye = np.eye(n)
+        cols = np.real(np.fft.ifft(eo[:, None] * np.fft.fft(eye, axis=0), axis=0))
+        assert np.max(np.abs(t - cols)) <= 1e-13 * np.max(np.abs(t))
+
+
+def test_fft_apply_is_three_axis_circulants(orc, pg):
+    """The reference's 3-D FFT matvec equals V x plus the per-axis circulant
+    contractions (cubic grid, where the reference's KE_diag indexing is
+    consistent): the form the GPU kernels apply."""
+    n, L = 10, 8.0
+    rng = np.random.Generator(np.random.PCG64(3))
+    x = rng.standard_normal(n ** 3)
+    v = rng.standard_normal(n ** 3)
+    y = orc.fft_apply(x, v, (n, n, n), orc.fft_ke_diag((n, n, n), (L, L, L)))
+    _, _, t = pg.fft_kinetic(n, L)
+    X = x.reshape(n, n, n)  # [k][j][i], x fastest
+    ref = v * x + (np.einsum("ab,kjb->kja", t, X) + np.einsum("ab,kbi->kai", t, X)
+                   + np.einsum("ab,bji->aji", t, X)).reshape(-1)
+    assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
