@@ -47,11 +47,25 @@ WORKLOADS = {
     # name: waters, sphere radius (A), seed, n, L (bohr), nroots, maxsub, ptol
     "c2": dict(nw=24, radius=9.0, seed=2, n=(64, 64, 64), L=(40.0, 40.0, 40.0), nroots=4, maxsub=60, ptol=8),
     "c1": dict(nw=6, radius=6.0, seed=1, n=(32, 32, 32), L=(30.0, 30.0, 30.0), nroots=1, maxsub=20, ptol=8),
+    # (H2O)32 + Na+ + Cl- (ion sites seed 33, >= 2.8 A from every O), 96^3 over 48 bohr, 8 states
+    "c3": dict(nw=32, radius=10.0, seed=3, ion_seed=33, n=(96, 96, 96), L=(48.0, 48.0, 48.0), nroots=8, maxsub=64,
+               ptol=8),
+    # (H2O)128 in a 14 A sphere, 160^3 over 64 bohr (4.1M points), 16 states, block 16, maxsub 96
+    "c5": dict(nw=128, radius=14.0, seed=5, n=(160, 160, 160), L=(64.0, 64.0, 64.0), nroots=16, maxsub=96,
+               ptol=8),
 }
+A2B = 1.0 / 0.52917720859  # Angstrom -> bohr, the reference's constant
+
+
+def workload_ions(clusters, wl, waters):
+    """Ion list (x, y, z in Angstrom, q) of a workload, or None."""
+    if "ion_seed" not in wl:
+        return None
+    return clusters.place_ions(waters, wl["radius"], wl["ion_seed"])
 MIXED_PTOL = 6  # residual threshold of the mixed form before the FP64 Rayleigh-Ritz step
 # single-vector H*x products of a full solve by the reference algorithm
 # (diagonal correction, FP64), counted by the oracle on the same input
-REFERENCE_MATVECS = {"c2": 4500, "c1": 700}
+REFERENCE_MATVECS = {"c2": 4500, "c1": 700}  # c3: measured in the same run (the reference-algorithm solve)
 
 # Serving stream: 16 seeded base clusters (H2O)n, n uniform in 8..64, O sites
 # in a sphere of radius 9 A (n/24)^(1/3); each request jitters one base by
@@ -138,6 +152,7 @@ def run_ours(args, ws, rank, local):
     precision = pg.PG_MIXED if args.precision == "mixed" else pg.PG_FP64
     ptol = MIXED_PTOL if precision == pg.PG_MIXED else wl["ptol"]
     waters = clusters.water_cluster(wl["nw"], wl["radius"], wl["seed"])
+    ions = workload_ions(clusters, wl, waters)
     tables = pg.WaterTables(waters)
     grid = pg.Grid(wl["n"], wl["L"])
     N = grid.N
@@ -147,6 +162,8 @@ def run_ours(args, ws, rank, local):
 
     def step(prec=precision, corr=args.corrflag, tol=ptol):
         v = grid.potential(tables, stream=sptr)
+        if ions is not None:
+            grid.add_ions(v, ions[:, :3] * A2B, ions[:, 3], stream=sptr)
         return grid.solve(v, nroots=nroots, maxsub=wl["maxsub"], maxiter=400, ptol=tol, precision=prec,
                           corrflag=corr, refine=1, stream=sptr)
 
@@ -211,10 +228,11 @@ def run_ours(args, ws, rank, local):
     # eigenvalues and eigenvectors out (pg_cluster_solve)
     e2e_ms = None
     d2h = nroots * N * 8 + nroots * 8
-    h2d = waters.size * 8
+    h2d = waters.size * 8 + (ions.size * 8 if ions is not None else 0)
     if not args.no_e2e:
         torch.cuda.synchronize()
-        cs = lambda: pg.cluster_solve(wl["n"], wl["L"], waters, nroots=nroots, maxsub=wl["maxsub"], maxiter=400,
+        cs = lambda: pg.cluster_solve(wl["n"], wl["L"], waters, ions=ions, nroots=nroots, maxsub=wl["maxsub"],
+                                      maxiter=400,
                                       ptol=ptol, precision=precision, corrflag=args.corrflag, refine=1,
                                       want_vectors=True)
         cs()
@@ -303,10 +321,13 @@ def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
     entry.load_package()
     clusters = importlib.import_module("pisces_gb300.clusters")
     waters = clusters.water_cluster(wl["nw"], wl["radius"], wl["seed"])
+    ions = workload_ions(clusters, wl, waters)
     g = orc.Grid(wl["n"], wl["L"])
     s = orc.dpp_sites(waters)
     t0 = time.perf_counter()
     v = g.potential_dpp(*s[:5])
+    if ions is not None:
+        g.add_ions(v, (ions[:, :3] * A2B).reshape(-1), ions[:, 3])
     t_pot = time.perf_counter() - t0
     # calibrate: a short sample, then one sized to the budget
     sample = 40
@@ -453,7 +474,8 @@ def main():
     if args.maxsub:
         wl["maxsub"] = args.maxsub
     WORKLOADS[args.workload] = wl
-    cfg = {"workload": f"{args.workload}: (H2O){wl['nw']} {wl['n'][0]}^3 sine-DVR over {wl['L'][0]} bohr, "
+    cfg = {"workload": f"{args.workload}: (H2O){wl['nw']}{' + Na+ + Cl-' if 'ion_seed' in wl else ''} "
+                       f"{wl['n'][0]}^3 sine-DVR over {wl['L'][0]} bohr, "
                        f"{wl['nroots']} states, block {wl['nroots']}, maxsub {wl['maxsub']}",
            "grid": list(wl["n"]), "box_bohr": list(wl["L"]), "waters": wl["nw"], "seed": wl["seed"],
            "nroots": wl["nroots"], "maxsub": wl["maxsub"], "l2": "working set (B, Z: 2 x maxsub x N doubles) "
@@ -464,6 +486,10 @@ def main():
             return
         # single-vector H*x products of a full solve of this workload by the
         # reference algorithm (diagonal correction), counted by the oracle
+        if args.workload not in REFERENCE_MATVECS:
+            print(json.dumps({"impl": "reference", "unavailable": f"no reference H*x count recorded for "
+                                                                  f"{args.workload}; run bench.py (ours) for it"}))
+            return
         n_full = REFERENCE_MATVECS[args.workload]
         steps = []
         for _ in range(args.warmup + args.steps):

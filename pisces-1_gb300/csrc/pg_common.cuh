@@ -98,6 +98,16 @@ inline __host__ __device__ unsigned tc_kmajor_off(int r, int k, int kpad) {
 }
 inline __host__ __device__ int tc_npad(int n) { return (n + 15) / 16 * 16; }
 inline __host__ __device__ int tc_kpad(int n) { return (n + 7) / 8 * 8; }
+// K chunk of the tensor-core contraction: the B chunk (npad x kc) and the A
+// tile (128 x kc), both as TF32 hi/lo, must fit 220 KB of shared memory;
+// n <= 112 gives one chunk (kc = kpad).  The operand images are stored as
+// ceil(kpad / kc) consecutive chunk images of npad x kc.
+inline __host__ __device__ int tc_kchunk(int n) {
+  const int npad = tc_npad(n), kpad = tc_kpad(n);
+  const int kc_max = (220 * 1024 / (8 * (npad + 128))) / 8 * 8;
+  const int nch = (kpad + kc_max - 1) / kc_max;
+  return ((kpad + nch - 1) / nch + 7) / 8 * 8;
+}
 
 }  // namespace pg
 
@@ -111,8 +121,9 @@ struct pg_grid {
   std::vector<double> x[3];        // grid points per axis
   std::vector<double> t[3];        // full symmetric kinetic matrices, n x n row-major (host)
   pg::DevBuf<double> t_dev[3];     // same, FP64, on the device
-  // TF32-rounded high part and the TF32-rounded remainder T - hi, each as a
-  // tensor-core operand image (tc_kmajor_off layout, tc_npad x tc_kpad)
+  // TF32-rounded high part and the TF32-rounded remainder T - hi, each as
+  // tensor-core operand images (tc_kmajor_off layout, one tc_npad x tc_kchunk
+  // image per K chunk)
   pg::DevBuf<float> t_hi[3];
   pg::DevBuf<float> t_lo[3];
   pg::DevBuf<double> x_dev[3];     // grid points on the device

@@ -100,13 +100,16 @@ extern "C" pg_status pg_fft_kinetic(int n, double mu, double x0, double xNp1, do
 namespace {
 
 // Round to the TF32 grid (10 explicit mantissa bits), nearest-even, as fp32.
-// Row-major n x n matrix -> tensor-core operand image (rows padded to 16,
-// K to 8, zero fill).
+// Row-major n x n matrix -> tensor-core operand images: rows padded to 16,
+// K split into chunks of tc_kchunk(n) (zero fill past n), one K-major image
+// per chunk, stored one after the other.
 std::vector<float> tc_image(const std::vector<float>& M, int n) {
-  const int npad = pg::tc_npad(n), kpad = pg::tc_kpad(n);
-  std::vector<float> img((size_t)npad * kpad, 0.f);
+  const int npad = pg::tc_npad(n), kpad = pg::tc_kpad(n), kc = pg::tc_kchunk(n);
+  const int nch = (kpad + kc - 1) / kc;
+  std::vector<float> img((size_t)nch * npad * kc, 0.f);
   for (int r = 0; r < n; ++r)
-    for (int k = 0; k < n; ++k) img[pg::tc_kmajor_off(r, k, kpad) / 4] = M[(size_t)r * n + k];
+    for (int k = 0; k < n; ++k)
+      img[(size_t)(k / kc) * npad * kc + pg::tc_kmajor_off(r, k % kc, kc) / 4] = M[(size_t)r * n + k];
   return img;
 }
 

@@ -7,8 +7,9 @@
 // product  D[c, i] = sum_b X[b, c] * T[i, b]  has M = columns (128 per tile),
 // N = n_axis (padded to 16) and K = n_axis (padded to 8): A is a 128-column
 // tile of X^T, B is the kinetic matrix, which stays in shared memory for the
-// whole (persistent) kernel.  Both are split into TF32 high and low parts,
-// D = Ah*Bh + Ah*Bl + Al*Bh (error ~2^-21 relative per term; Al*Bl dropped),
+// whole (persistent) kernel when it fits (n <= 112); larger n (up to 256)
+// runs K in chunks, restaging each chunk of B per tile.  Both are split into
+// TF32 high and low parts, D = Ah*Bh + Ah*Bl + Al*Bh (error ~2^-21 relative per term; Al*Bl dropped),
 // accumulated in FP32 in TMEM.  X is split on the fly from FP64 with integer
 // operations only (the FP64 pipe is two orders of magnitude slower on this
 // part).  Three passes: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X; X stays L2
@@ -28,7 +29,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kTileM = 128;
-constexpr int kMaxN = 112;  // n_axis handled with the whole K extent resident in shared memory
+constexpr int kMaxN = 256;  // n_axis limit: the MMA N extent (rows of the axis matrix, padded to 16)
 constexpr int kBatch = 16;  // global loads a thread keeps in flight while filling A
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -127,33 +128,32 @@ using pg::TcJobs;
 
 template <int AXIS>
 __global__ void __launch_bounds__(kThreads, 1)
-    k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kpad, uint32_t tmem_cols,
+    k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kc, int nch, uint32_t tmem_cols,
             const float* __restrict__ t_hi, const float* __restrict__ t_lo, const __grid_constant__ TcJobs jobs,
             int mode, int* __restrict__ err) {
   // mode 0: Y = D;  1: Y += D;  2: Y = V X + D   (D = the axis contraction)
+  // K is processed in nch chunks of kc (one chunk for n <= 112): per chunk the
+  // A tile and the B chunk are staged, multiplied into the same accumulator,
+  // and the shared memory is reused once those MMAs have completed.
   extern __shared__ __align__(1024) unsigned char smem[];
   const int n = am.n;
-  const uint32_t b_bytes = (uint32_t)npad * kpad * 4;
-  const uint32_t a_bytes = (uint32_t)kTileM * kpad * 4;
+  const uint32_t b_bytes = (uint32_t)npad * kc * 4;  // one K chunk of one half of B
+  const uint32_t a_bytes = (uint32_t)kTileM * kc * 4;
   unsigned char* sBh = smem;
   unsigned char* sBl = smem + b_bytes;
   unsigned char* sAh = smem + 2 * b_bytes;
   unsigned char* sAl = sAh + a_bytes;
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar_b;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x;
   const long N = (long)nx * ny * nz;
   const long ntiles = jobs.ntiles;
 
-  // kinetic matrix (B operand, rows = output index i, K = b): both halves are
-  // operand images in global memory, brought in by two bulk copies that
-  // overlap the first A fill
-  __shared__ __align__(8) uint64_t mbar_b;
-  if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_b)));
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  // B (the kinetic matrix, rows = output index i, K = b): both halves are
+  // operand images in global memory, one per K chunk, brought in by bulk
+  // copies; with a single chunk B is loaded once and stays resident
+  auto load_b = [&](int ch) {  // one thread
     uint64_t state;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
                  : "=l"(state)
@@ -161,12 +161,19 @@ __global__ void __launch_bounds__(kThreads, 1)
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(sBh)),
-                 "l"(t_hi), "r"(b_bytes), "r"(smem_u32(&mbar_b))
+                 "l"(t_hi + (size_t)ch * npad * kc), "r"(b_bytes), "r"(smem_u32(&mbar_b))
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(sBl)),
-                 "l"(t_lo), "r"(b_bytes), "r"(smem_u32(&mbar_b))
+                 "l"(t_lo + (size_t)ch * npad * kc), "r"(b_bytes), "r"(smem_u32(&mbar_b))
                  : "memory");
+  };
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_b)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    load_b(0);  // overlaps the first A fill
   }
   if (tid < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
@@ -179,15 +186,16 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = tmem_base;
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(npad >> 3) << 17) |
                          ((uint32_t)(kTileM >> 4) << 24);
-  const uint32_t lbo = 128, sbo = (uint32_t)(kpad >> 2) * 128;
+  const uint32_t lbo = 128, sbo = (uint32_t)(kc >> 2) * 128;
   const int warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3;      // TMEM lanes 32*quarter .. +31
   const int half = warp >> 2;        // which 16-column chunks this warp reads
-  uint32_t phase = 0;
+  uint32_t phase = 0, b_phase = 0;
   bool ok = true;
-  bool b_ready = false;
+  bool b_ready = false;   // single chunk: B resident
+  bool first = true;      // the first chunk's B load was issued above
 
-  for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  for (long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
     int jb = 0;
     while (jb + 1 < jobs.n && tile >= jobs.j[jb + 1].tile0) ++jb;
     const double* __restrict__ X = jobs.j[jb].x;
@@ -195,69 +203,81 @@ __global__ void __launch_bounds__(kThreads, 1)
     const double* __restrict__ v = jobs.j[jb].v;
     const long ncols = jobs.j[jb].ncols;
     const long c0 = (tile - jobs.j[jb].tile0) * kTileM;
-    // ---- A operand: 128 columns x K, split into TF32 hi/lo
-    // eight loads per thread in flight, then split and store
-    for (int e0 = tid; e0 < kTileM * kpad; e0 += kBatch * kThreads) {
-      double xv[kBatch];
+    for (int ch = 0; ch < nch; ++ch) {
+      const int k0 = ch * kc;
+      if (nch > 1 && !first && tid == 0) load_b(ch);  // the previous chunk's MMAs have completed
+      first = false;
+      // ---- A operand: 128 columns x kc, split into TF32 hi/lo; kBatch loads
+      // per thread in flight, then split and store
+      for (int e0 = tid; e0 < kTileM * kc; e0 += kBatch * kThreads) {
+        double xv[kBatch];
 #pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int e = e0 + u * kThreads;
-        // AXIS 0: a column is a contiguous line, read along K;
-        // AXIS 1, 2: consecutive columns are consecutive addresses, read across columns
-        const int m = AXIS == 0 ? e / kpad : (e & (kTileM - 1));
-        const int k = AXIS == 0 ? e - (e / kpad) * kpad : (e >> 7);
-        const long c = c0 + m;
-        const bool in = e < kTileM * kpad && k < n && c < ncols;
-        xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)k * am.stride] : 0.0;
-      }
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * kThreads;
+          // AXIS 0: a column is a contiguous line, read along K;
+          // AXIS 1, 2: consecutive columns are consecutive addresses, read across columns
+          const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
+          const int k = k0 + (AXIS == 0 ? e - (e / kc) * kc : (e >> 7));
+          const long c = c0 + m;
+          const bool in = e < kTileM * kc && k < n && c < ncols;
+          xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)k * am.stride] : 0.0;
+        }
 #pragma unroll
-      for (int u = 0; u < kBatch; ++u) {
-        const int e = e0 + u * kThreads;
-        if (e < kTileM * kpad) {
-          const int m = AXIS == 0 ? e / kpad : (e & (kTileM - 1));
-          const int k = AXIS == 0 ? e - (e / kpad) * kpad : (e >> 7);
-          float h, l;
-          split_tf32(xv[u], h, l);
-          *(float*)(sAh + kmajor_off(m, k, kpad)) = h;
-          *(float*)(sAl + kmajor_off(m, k, kpad)) = l;
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * kThreads;
+          if (e < kTileM * kc) {
+            const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
+            const int k = AXIS == 0 ? e - (e / kc) * kc : (e >> 7);
+            float h, l;
+            split_tf32(xv[u], h, l);
+            *(float*)(sAh + kmajor_off(m, k, kc)) = h;
+            *(float*)(sAl + kmajor_off(m, k, kc)) = l;
+          }
         }
       }
-    }
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    if (!b_ready) b_ready = mbar_wait(smem_u32(&mbar_b), 0);  // the B images have landed (first tile only)
-    if (!__syncthreads_and(b_ready ? 1 : 0)) {
-      ok = false;
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (tid == 0) {
-      const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
-      for (int kk = 0; kk < kpad / 8; ++kk) {
-        const uint32_t off = (uint32_t)kk * 256;  // 8 K-elements = two core matrices
-        const uint64_t dah = smem_desc(ah + off, lbo, sbo), dal = smem_desc(al + off, lbo, sbo);
-        const uint64_t dbh = smem_desc(bh + off, lbo, sbo), dbl = smem_desc(bl + off, lbo, sbo);
-        // small terms first, then the leading product
-        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                     " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                     "l"(dal), "l"(dbh), "r"(idesc), "r"(kk > 0 ? 1u : 0u));
-        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                     " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                     "l"(dah), "l"(dbl), "r"(idesc), "r"(1u));
-        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                     " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-                     "l"(dah), "l"(dbh), "r"(idesc), "r"(1u));
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      bool bok = true;
+      if (nch > 1 || !b_ready) {  // this chunk's B images have landed
+        bok = mbar_wait(smem_u32(&mbar_b), b_phase);
+        b_phase ^= 1u;
+        b_ready = true;
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(&mbar)));
+      if (!__syncthreads_and(bok ? 1 : 0)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 0) {
+        const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
+        for (int kk = 0; kk < kc / 8; ++kk) {
+          const uint32_t off = (uint32_t)kk * 256;  // 8 K-elements = two core matrices
+          const uint64_t dah = smem_desc(ah + off, lbo, sbo), dal = smem_desc(al + off, lbo, sbo);
+          const uint64_t dbh = smem_desc(bh + off, lbo, sbo), dbl = smem_desc(bl + off, lbo, sbo);
+          const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
+          // small terms first, then the leading product
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                       "l"(dal), "l"(dbh), "r"(idesc), "r"(acc));
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                       "l"(dah), "l"(dbl), "r"(idesc), "r"(1u));
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                       " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+                       "l"(dah), "l"(dbh), "r"(idesc), "r"(1u));
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(&mbar)));
+      }
+      const bool waited = mbar_wait(smem_u32(&mbar), phase);
+      phase ^= 1u;
+      if (!__syncthreads_and(waited ? 1 : 0)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     }
-    const bool waited = mbar_wait(smem_u32(&mbar), phase);
-    phase ^= 1u;
-    if (!__syncthreads_and(waited ? 1 : 0)) {
-      ok = false;
-      break;
-    }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ok) break;
     // ---- epilogue: thread (quarter, lane) owns column c = c0 + 32*quarter + lane
     const int m = 32 * quarter + lane;
     const long c = c0 + m;
@@ -354,11 +374,13 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     tiles += (jobs.j[j].ncols + kTileM - 1) / kTileM;
   }
   jobs.ntiles = tiles;
-  const int npad = (n + 15) / 16 * 16;
-  const int kpad = (n + 7) / 8 * 8;
+  const int npad = pg::tc_npad(n);
+  const int kpad = pg::tc_kpad(n);
+  const int kc = pg::tc_kchunk(n);           // K chunk (the grid's operand images use the same split)
+  const int nch = (kpad + kc - 1) / kc;
   uint32_t cols = 32;
   while (cols < (uint32_t)npad) cols <<= 1;
-  const size_t smem = (size_t)2 * npad * kpad * 4 + (size_t)2 * kTileM * kpad * 4;
+  const size_t smem = (size_t)2 * npad * kc * 4 + (size_t)2 * kTileM * kc * 4;
   if ((long)smem > (long)g_max_dyn) {
     set_error("tc_axis: %zu bytes of shared memory needed, the device allows %d", smem, g_max_dyn);
     return PG_UNSUPPORTED;
@@ -367,15 +389,15 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
   int* err = g->tc_err.p;
   switch (a) {
     case 0:
-      k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, jobs, mode,
+      k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,
                                                err);
       break;
     case 1:
-      k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, jobs, mode,
+      k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,
                                                err);
       break;
     default:
-      k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kpad, cols, Ahi, Alo, jobs, mode,
+      k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,
                                                err);
   }
   return check_launch("k_hx_tc");

@@ -503,8 +503,8 @@ extern "C" pg_status pg_engine_submit(pg_engine* e, const pg_request* r, long* i
   PG_ARG(p.startvec == 1 || p.startvec == 2, "pg_engine_submit: startvec must be 1 or 2 (warm start is the engine's)");
   if (p.precision == PG_MIXED)
     for (int a = 0; a < 3; ++a)
-      if (r->n[a] > 112) {
-        pg::set_error("pg_engine_submit: the mixed form supports n <= 112 per axis (got %d)", r->n[a]);
+      if (r->n[a] > 256) {
+        pg::set_error("pg_engine_submit: the mixed form supports n <= 256 per axis (got %d)", r->n[a]);
         return PG_UNSUPPORTED;
       }
   std::unique_ptr<Job> job(new Job());

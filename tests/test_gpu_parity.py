@@ -429,3 +429,70 @@ def test_fft_grid_cluster_solve_against_dense_reference_operator(pg, orc, torch,
         assert np.max(np.abs(np.asarray(ev) - ref)) <= 1e-8, (corr, ev, ref)
     ev, _, _ = grid.solve(v, nroots=2, maxsub=30, maxiter=300, ptol=6, corrflag=3, precision=pg.PG_MIXED, refine=1)
     assert np.max(np.abs(np.asarray(ev) - ref)) <= 1e-6
+
+
+# ---------------------------------------------------------------- waters + ions (c3 model)
+
+@pytest.mark.gpu
+def test_solve_waters_and_ions_match_reference(pg, torch):
+    """(H2O)8 + Na+ + Cl- on a non-cubic 14 x 16 x 18 grid: V = DPP(waters) +
+    Bloomfield(ions), two states, against the reference run of the same
+    combined model (ions_small fixture): eigenvalues within 1e-8 Eh."""
+    gd = golden("ions_small.npz")
+    grid = pg.Grid(tuple(int(x) for x in gd["n"]), tuple(float(x) for x in gd["L"]))
+    v = grid.potential(pg.WaterTables(gd["waters"]))
+    grid.add_ions(v, gd["ion_sites"], gd["ion_charges"])
+    for corr in (1, 3):
+        ev, _, _ = grid.solve(v, nroots=2, maxsub=20, maxiter=200, ptol=8, corrflag=corr)
+        assert np.max(np.abs(np.asarray(ev) - gd["evals"][:2])) <= 1e-8, (corr, ev, gd["evals"])
+
+
+@pytest.mark.gpu
+def test_solve_c3_mixed_against_fp64(pg, torch, clusters):
+    """c3: (H2O)32 + Na+ + Cl-, 96^3 over 48 bohr, 8 states, block 8.  Mixed
+    form (with FP64 refinement) against the FP64 form: |dE| <= 1e-6 Eh per
+    eigenvalue and eigenvector overlap >= 1 - 1e-8."""
+    w = clusters.water_cluster(32, 10.0, 3)
+    ions = clusters.place_ions(w, 10.0, 33)
+    grid = pg.Grid((96, 96, 96), (48.0, 48.0, 48.0))
+    v = grid.potential(pg.WaterTables(w))
+    grid.add_ions(v, ions[:, :3] / 0.52917720859, ions[:, 3])
+    e64, x64, _ = grid.solve(v, nroots=8, maxsub=64, maxiter=400, ptol=8, corrflag=3)
+    emx, xmx, _ = grid.solve(v, nroots=8, maxsub=64, maxiter=400, ptol=6, corrflag=3, precision=pg.PG_MIXED,
+                             refine=1)
+    assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
+    ov = torch.abs(torch.sum(x64 * xmx, dim=1)) / (x64.norm(dim=1) * xmx.norm(dim=1))
+    assert float(ov.min()) >= 1 - 1e-8, ov
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [(160, 24, 20), (24, 136, 20), (20, 24, 200), (136, 136, 8)])
+def test_hx_mixed_k_chunked_axes(pg, torch, n):
+    """Axes longer than 112 points run the tensor-core contraction in K
+    chunks (the kinetic matrix restaged per chunk): mixed H*X against FP64
+    within the mixed form's bound (2e-5 of max |Y|), on each axis."""
+    rng = np.random.Generator(np.random.PCG64(6))
+    grid = pg.Grid(n, tuple(0.6 * (k + 1) for k in n))
+    N = grid.N
+    x = dev(torch, rng.standard_normal(3 * N))
+    v = dev(torch, rng.standard_normal(N))
+    y64 = host(grid.hx(v, x, nvec=3, precision=0))
+    ymx = host(grid.hx(v, x, nvec=3, precision=1))
+    assert np.max(np.abs(ymx - y64)) / np.max(np.abs(y64)) <= 2e-5
+
+
+@pytest.mark.gpu
+def test_solve_c5_mixed_against_fp64(pg, torch, clusters):
+    """c5: (H2O)128 in a 14 A sphere, 160^3 over 64 bohr (4.1M points), 16
+    states, block 16, maxsub 96 -- the K-chunked tensor-core path at full
+    size.  Mixed form (FP64 refinement) against the FP64 form: |dE| <= 1e-6
+    Eh per eigenvalue, eigenvector overlap >= 1 - 1e-8."""
+    w = clusters.water_cluster(128, 14.0, 5)
+    grid = pg.Grid((160, 160, 160), (64.0, 64.0, 64.0))
+    v = grid.potential(pg.WaterTables(w))
+    e64, x64, _ = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=8, corrflag=3)
+    emx, xmx, _ = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=6, corrflag=3, precision=pg.PG_MIXED,
+                             refine=1)
+    assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
+    ov = torch.abs(torch.sum(x64 * xmx, dim=1)) / (x64.norm(dim=1) * xmx.norm(dim=1))
+    assert float(ov.min()) >= 1 - 1e-8, ov

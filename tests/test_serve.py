@@ -133,7 +133,7 @@ def test_bad_requests(pg, torch, mix):
             eng.submit(pg.Engine.request(grid, L, bad, nroots=1))
         assert e.value.status == pg.PG_BAD_ARG
         with pytest.raises(pg.PiscesError) as e:
-            eng.submit(pg.Engine.request((120, 120, 120), 70.0, w, nroots=1, precision=1))
+            eng.submit(pg.Engine.request((260, 260, 260), 160.0, w, nroots=1, precision=1))
         assert e.value.status == pg.PG_UNSUPPORTED
         rid = eng.submit(pg.Engine.request(grid, L, w, nroots=2, maxiter=1, ptol=10))
         r = eng.wait(rid, timeout=300.0)
