@@ -235,12 +235,19 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_stages() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(kGStages - 2) : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// kPair: N even and P, Q 16-byte aligned, so that consecutive point pairs
+// are copied with 16-byte cp.async and converted two at a time.
+template <bool kPair>
 __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
                                                    const double* __restrict__ Q, int nb, int tp_log2, int S, int ablk,
                                                    int nblk, double* __restrict__ partial) {
@@ -271,13 +278,29 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
     double* dst = stage0 + (size_t)(tile % kGStages) * stage_elems;
     const long g0 = g_begin + ((long)tile << tp_log2);
     const int cnt = g_end - g0 < tp ? (int)(g_end - g0) : tp;
-    for (int e = tid; e < stage_elems; e += kT) {
-      const int row = e >> tp_log2, p = e & (tp - 1);
-      if (p < cnt) {
-        const double* src = row < na ? P + (long)row * N : Q + (long)(row - na) * N;
-        cp_async8(dst + e, src + g0 + p);
-      } else {
-        dst[e] = 0.0;
+    if (kPair) {
+      for (int e = 2 * tid; e < stage_elems; e += 2 * kT) {  // p even: a pair of points
+        const int row = e >> tp_log2, p = e & (tp - 1);
+        const double* src = (row < na ? P + (long)row * N : Q + (long)(row - na) * N) + g0 + p;
+        if (p + 1 < cnt) {
+          cp_async16(dst + e, src);
+        } else if (p < cnt) {
+          cp_async8(dst + e, src);
+          dst[e + 1] = 0.0;
+        } else {
+          dst[e] = 0.0;
+          dst[e + 1] = 0.0;
+        }
+      }
+    } else {
+      for (int e = tid; e < stage_elems; e += kT) {
+        const int row = e >> tp_log2, p = e & (tp - 1);
+        if (p < cnt) {
+          const double* src = row < na ? P + (long)row * N : Q + (long)(row - na) * N;
+          cp_async8(dst + e, src + g0 + p);
+        } else {
+          dst[e] = 0.0;
+        }
       }
     }
   };
@@ -289,10 +312,20 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
     cp_async_wait_stages();  // this thread's copies of tile `it` have landed
     double* cur = stage0 + (size_t)(it % kGStages) * stage_elems;
     float2* cur2 = reinterpret_cast<float2*>(cur);
-    for (int e = tid; e < stage_elems; e += kT) {  // the elements this thread copied
-      float h, l;
-      df_split(cur[e], h, l);
-      cur2[e] = make_float2(h, l);
+    if (kPair) {
+      for (int e = 2 * tid; e < stage_elems; e += 2 * kT) {  // the pairs this thread copied
+        const double2 d2 = *reinterpret_cast<const double2*>(cur + e);
+        float h0, l0, h1, l1;
+        df_split(d2.x, h0, l0);
+        df_split(d2.y, h1, l1);
+        *reinterpret_cast<float4*>(cur2 + e) = make_float4(h0, l0, h1, l1);
+      }
+    } else {
+      for (int e = tid; e < stage_elems; e += kT) {  // the elements this thread copied
+        float h, l;
+        df_split(cur[e], h, l);
+        cur2[e] = make_float2(h, l);
+      }
     }
     __syncthreads();  // tile `it` converted; everyone is done with tile it-1
     if (it + kGStages - 1 < ntiles) issue(it + kGStages - 1);
@@ -300,16 +333,22 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
     if (active) {
       const long g0 = g_begin + ((long)it << tp_log2);
       const int cnt = g_end - g0 < tp ? (int)(g_end - g0) : tp;
-      for (int p = slice; p < cnt; p += S) {
-        float2 x[kGA], y[kGB];
+      // two consecutive points per step (one 16-byte load per row; a zero
+      // point past the tile's end adds nothing)
+      const float4* cur4 = reinterpret_cast<const float4*>(cur2);
+      for (int p = 2 * slice; p < cnt; p += 2 * S) {
+        float4 y[kGB];
 #pragma unroll
-        for (int i = 0; i < kGA; ++i) x[i] = cur2[ra[i] + p];
+        for (int j = 0; j < kGB; ++j) y[j] = cur4[(rb[j] + p) >> 1];
 #pragma unroll
-        for (int j = 0; j < kGB; ++j) y[j] = cur2[rb[j] + p];
+        for (int i = 0; i < kGA; ++i) {
+          const float4 x = cur4[(ra[i] + p) >> 1];
 #pragma unroll
-        for (int i = 0; i < kGA; ++i)
-#pragma unroll
-          for (int j = 0; j < kGB; ++j) df_fma(sh[i][j], sl[i][j], x[i].x, x[i].y, y[j].x, y[j].y);
+          for (int j = 0; j < kGB; ++j) {
+            df_fma(sh[i][j], sl[i][j], x.x, x.y, y[j].x, y[j].y);
+            df_fma(sh[i][j], sl[i][j], x.z, x.w, y[j].z, y[j].w);
+          }
+        }
       }
     }
   }
@@ -444,6 +483,11 @@ pg_status RedScratch::ensure() {
   return PG_OK;
 }
 
+// 16-byte copies of point pairs: every row start 16-byte aligned
+inline bool pair_ok(long N, const double* P, const double* Q) {
+  return N % 2 == 0 && ((uintptr_t)P % 16) == 0 && ((uintptr_t)Q % 16) == 0;
+}
+
 // Dynamic shared-memory opt-in, once per kernel (the largest size any call
 // needs: 112 + 16 vectors of 33 doubles for the Gram kernels).
 static pg_status opt_in_smem() {
@@ -451,7 +495,9 @@ static pg_status opt_in_smem() {
     const int big = (int)(sizeof(double) * (size_t)(128 + 16) * (kTP + 1));
     cudaError_t e = cudaFuncSetAttribute(k_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
     if (e == cudaSuccess)
-      e = cudaFuncSetAttribute(k_gram_df, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmemMax);
+      e = cudaFuncSetAttribute(k_gram_df<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmemMax);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_gram_df<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGramSmemMax);
     return e;
   }();
   PG_CUDA_TRY(init);
@@ -477,7 +523,10 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
     const int dblocks = (int)((N + dchunk - 1) / dchunk);
     const size_t smem = std::max((size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8,
                                  (size_t)S * nblk * kGA * kGB * 8);
-    k_gram_df<<<dblocks, kT, smem, st>>>(N, dchunk, P, na, Q, nb, tp_log2, S, ablk, nblk, rs.partial.p);
+    if (pair_ok(N, P, Q))
+      k_gram_df<true><<<dblocks, kT, smem, st>>>(N, dchunk, P, na, Q, nb, tp_log2, S, ablk, nblk, rs.partial.p);
+    else
+      k_gram_df<false><<<dblocks, kT, smem, st>>>(N, dchunk, P, na, Q, nb, tp_log2, S, ablk, nblk, rs.partial.p);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(rs.partial.p, dblocks, na * nb, out, false, st);
   } else {
@@ -608,7 +657,10 @@ extern "C" pg_status pg_block_gram_noalloc(long n, const double* P, int np, cons
     const int blocks = (int)((n + chunk - 1) / chunk);
     const size_t smem = std::max((size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8,
                                  (size_t)S * nblk * kGA * kGB * 8);
-    k_gram_df<<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, tp_log2, S, ablk, nblk, partial);
+    if (pair_ok(n, P, Q))
+      k_gram_df<true><<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, tp_log2, S, ablk, nblk, partial);
+    else
+      k_gram_df<false><<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, tp_log2, S, ablk, nblk, partial);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(partial, blocks, no, out, false, st);
   }
