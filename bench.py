@@ -290,8 +290,10 @@ def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
     v = grid.potential(tables, stream=stream.cuda_stream)
     X = torch.randn(nb * N, dtype=torch.float64, device="cuda", generator=g)
     Y = torch.empty_like(X)
+    # queued back to back (pg_hx_async); the status word is checked once after
     ms = _time_launches(torch, stream, lambda: grid.hx(v, X, nvec=nb, precision=precision, out=Y,
-                                                       stream=stream.cuda_stream))
+                                                       stream=stream.cuda_stream, wait=False))
+    grid.check(stream=stream.cuda_stream)
     nx, ny, nz = grid.n
     hbytes = 8.0 * N * (2 * nb + 1)
     flops = N * nb * (2 * (nx + ny + nz) + 2)

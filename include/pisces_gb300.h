@@ -162,6 +162,15 @@ pg_status pg_water_default_tables(int nw, const double* sites, const double* cha
  * src/davdriver.cpp:67-78). */
 pg_status pg_hx(const pg_grid* g, const double* v_dev, const double* x_dev, double* y_dev, int nvec, int precision,
                 void* stream);
+/* pg_hx without the completion check of the mixed form: returns once the
+ * launches are queued (no host wait).  A tensor-core completion wait that
+ * timed out is recorded in the grid's status word and reported by the next
+ * pg_grid_check. */
+pg_status pg_hx_async(const pg_grid* g, const double* v_dev, const double* x_dev, double* y_dev, int nvec,
+                      int precision, void* stream);
+/* Waits for the stream; PG_DEVICE_TIMEOUT if a tensor-core completion wait on
+ * this grid timed out since the last check (the status word is then cleared). */
+pg_status pg_grid_check(const pg_grid* g, void* stream);
 
 /* ---------------------------------------------------------------- Davidson */
 

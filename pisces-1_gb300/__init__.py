@@ -108,6 +108,8 @@ SYMBOLS = {
     "pg_water_sites": (C.c_int, [C.c_int, _dp, _dp, _dp, _ip, _dp, _ip, _ip]),
     "pg_water_default_tables": (C.c_int, [C.c_int, _dp, _dp, _ip, _dp, _ip, _dp, _ip, _dp, _ip, C.POINTER(Sites)]),
     "pg_hx": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "pg_hx_async": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
+    "pg_grid_check": (C.c_int, [_vp, _vp]),
     "pg_davidson_create": (C.c_int, [C.POINTER(_vp)]),
     "pg_davidson_destroy": (C.c_int, [_vp]),
     "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
@@ -319,11 +321,17 @@ class Grid:
         _check(lib().pg_piab_start(self._h, _dev(w), _stream(stream)))
         return w
 
-    def hx(self, v, X, nvec=None, precision=PG_FP64, out=None, stream=None):
+    def hx(self, v, X, nvec=None, precision=PG_FP64, out=None, stream=None, wait=True):
+        """Y = H X.  wait=False: queue only (pg_hx_async); call check() later."""
         nvec = X.numel() // self.N if nvec is None else nvec
         Y = self._new(nvec) if out is None else out
-        _check(lib().pg_hx(self._h, _dev(v), _dev(X), _dev(Y), nvec, precision, _stream(stream)))
+        fn = lib().pg_hx if wait else lib().pg_hx_async
+        _check(fn(self._h, _dev(v), _dev(X), _dev(Y), nvec, precision, _stream(stream)))
         return Y
+
+    def check(self, stream=None):
+        """Waits for the stream and reports a tensor-core wait timeout (pg_grid_check)."""
+        _check(lib().pg_grid_check(self._h, _stream(stream)))
 
     def solve(self, v, nroots=1, maxsub=20, maxiter=100, ptol=5, corrflag=1, precision=PG_FP64, startvec=1,
               refine=1, start=None, stream=None, raise_on_nonconv=True):

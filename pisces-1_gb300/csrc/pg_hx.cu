@@ -149,3 +149,16 @@ extern "C" pg_status pg_hx(const pg_grid* g, const double* v, const double* x, d
   PG_TRY(pg::hx(g, v, x, y, nvec, precision, st));
   return precision == PG_MIXED ? pg::check_tc_error(g, st) : PG_OK;
 }
+
+extern "C" pg_status pg_hx_async(const pg_grid* g, const double* v, const double* x, double* y, int nvec,
+                                 int precision, void* stream) {
+  return pg::hx(g, v, x, y, nvec, precision, pg::as_stream(stream));
+}
+
+extern "C" pg_status pg_grid_check(const pg_grid* g, void* stream) {
+  PG_ARG(g, "pg_grid_check: null grid");
+  cudaStream_t st = pg::as_stream(stream);
+  const pg_status s = pg::check_tc_error(g, st);
+  if (s == PG_DEVICE_TIMEOUT) PG_CUDA_TRY(cudaMemsetAsync(g->tc_err.p, 0, sizeof(int), st));
+  return s;
+}

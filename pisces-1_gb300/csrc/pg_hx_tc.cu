@@ -127,7 +127,7 @@ using pg::TcJob;
 using pg::TcJobs;
 
 template <int AXIS>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
     k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kc, int nch, uint32_t tmem_cols,
             const float* __restrict__ t_hi, const float* __restrict__ t_lo, const __grid_constant__ TcJobs jobs,
             int mode, int* __restrict__ err) {
@@ -284,28 +284,27 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool cvalid = c < ncols;
     const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
     const long gshift = cvalid ? (c / (N / n)) * N : 0;  // vector offset: grid point = address - gshift
-    // two 16-row chunks per round: 32 loads in flight, then the stores
-    for (int c0k = half; c0k * 16 < npad; c0k += 4) {
-      const bool second = (c0k + 2) * 16 < npad;
-      float d[32];
-      tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(c0k * 16), d);
-      if (second) tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)((c0k + 2) * 16), d + 16);
+    // one 16-row chunk per round: 16 loads in flight, then the stores (the
+    // register budget allows two CTAs per SM where shared memory does)
+    for (int ck = half; ck * 16 < npad; ck += 2) {
+      float d[16];
+      tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(ck * 16), d);
       if (cvalid) {
-        double prev[32];
+        double prev[16];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int i = (c0k + 2 * (j >> 4)) * 16 + (j & 15);
+        for (int j = 0; j < 16; ++j) {
+          const int i = ck * 16 + j;
           const long a = base + (long)i * am.stride;
           prev[j] = 0.0;
-          if (i < n && (j < 16 || second)) {
+          if (i < n) {
             if (mode == 2) prev[j] = v[a - gshift] * X[a];
             else if (mode == 1) prev[j] = Y[a];
           }
         }
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int i = (c0k + 2 * (j >> 4)) * 16 + (j & 15);
-          if (i < n && (j < 16 || second)) Y[base + (long)i * am.stride] = prev[j] + (double)d[j];
+        for (int j = 0; j < 16; ++j) {
+          const int i = ck * 16 + j;
+          if (i < n) Y[base + (long)i * am.stride] = prev[j] + (double)d[j];
         }
       }
     }
@@ -385,7 +384,11 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     set_error("tc_axis: %zu bytes of shared memory needed, the device allows %d", smem, g_max_dyn);
     return PG_UNSUPPORTED;
   }
-  const int grid = (int)(tiles < g_num_sms ? tiles : g_num_sms);
+  // two CTAs per SM when both fit the SM's shared memory (one CTA's tiles
+  // then overlap the other's loads and stores)
+  const long per_sm = smem <= (size_t)110 * 1024 ? 2 : 1;
+  const long cap = per_sm * g_num_sms;
+  const int grid = (int)(tiles < cap ? tiles : cap);
   int* err = g->tc_err.p;
   switch (a) {
     case 0:
