@@ -75,6 +75,17 @@ C4 = dict(nreq=512, nbase=16, grids=(48, 64, 80, 96), spacing=0.615, max_roots=4
           base_seed=1000, ptol_fp64=8, corrflag=3)
 
 
+def max_over_ranks(value, ws, device):
+    """The largest of the ranks' values (the replica run's slowest rank); the
+    only collective of the bench (replicas share no data)."""
+    if ws <= 1:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -217,11 +228,7 @@ def run_ours(args, ws, rank, local):
         elif precision == pg.PG_FP64 and args.corrflag == 1:
             refalg = {"solves_per_s": 1000.0 * args.steps / total_ms, "corrflag": 1, "n_matvec": st["n_matvec"],
                       "n_iter": st["n_iter"], "eigenvalues": list(map(float, ev))}
-    max_ms = total_ms
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        max_ms = float(t.item())
+    max_ms = max_over_ranks(total_ms, ws, "cuda")
     de = float(np.max(np.abs(np.asarray(ev) - np.asarray(ev64))))
 
     # end to end through the public host-buffer API: water coordinates in,
@@ -495,7 +502,7 @@ def main():
         n_full = REFERENCE_MATVECS[args.workload]
         steps = []
         for _ in range(args.warmup + args.steps):
-            steps.append(cpu_baseline(args, wl, n_full, budget_s=8.0))
+            steps.append(cpu_baseline(args, wl, n_full, budget_s=4.0))
         timed = steps[args.warmup:]
         val = statistics.median(s["value"] for s in timed)
         line = {"impl": "reference", "metric": "solves/s", "value": val, "unit": "solves/s", "n_gpus": args.gpus,
