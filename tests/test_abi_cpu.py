@@ -100,3 +100,15 @@ def test_subspace_eigensolver_degenerate(pg):
     assert np.max(np.abs(w - lam[:5])) < 1e-12
     assert np.max(np.abs(S @ V - V * w)) < 1e-10
     assert np.max(np.abs(V.T @ V - np.eye(5))) < 1e-10
+
+
+def test_reference_shaped_header_compiles():
+    """include/pisces_gb300_ref.hpp (the reference signatures over the C ABI)
+    and its davdriver-style test driver compile as C++."""
+    import shutil
+    import subprocess
+    cuda = "/usr/local/cuda/include"
+    if not shutil.which("g++") or not os.path.isdir(cuda):
+        pytest.skip("g++ or the CUDA headers are missing")
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), "-I", cuda,
+                    os.path.join(ROOT, "tests", "shim", "check_ref_shim.cpp")], check=True)
