@@ -245,61 +245,82 @@ __device__ __forceinline__ void cp_async_wait_stages() {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
 
+// Tile geometry of k_gram_df: S slices per output block, tiles of tp = 2 S m
+// points so that every slice takes exactly m point pairs of every tile (no
+// lanes idle in the multiply loop), as many pairs as kGStages stages of
+// (na + nb) rows allow in kGramSmemMax.
+struct GramGeom {
+  int ablk, nblk, S, m, tp;
+  size_t smem;
+};
+
+inline GramGeom gram_geometry(int na, int nb) {
+  GramGeom g;
+  g.ablk = (na + kGA - 1) / kGA;
+  g.nblk = g.ablk * ((nb + kGB - 1) / kGB);
+  g.S = g.nblk <= kT ? kT / g.nblk : 1;
+  const size_t per_pair_set = (size_t)kGStages * (na + nb) * 2 * g.S * 8;  // stage bytes per unit of m
+  g.m = (int)std::max<size_t>(1, std::min<size_t>(8, kGramSmemMax / per_pair_set));
+  g.tp = 2 * g.S * g.m;
+  g.smem = std::max((size_t)g.m * per_pair_set, (size_t)g.S * g.nblk * kGA * kGB * 8);
+  return g;
+}
+
 // kPair: N even and P, Q 16-byte aligned, so that consecutive point pairs
 // are copied with 16-byte cp.async and converted two at a time.
 template <bool kPair>
 __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
-                                                   const double* __restrict__ Q, int nb, int tp_log2, int S, int ablk,
-                                                   int nblk, double* __restrict__ partial) {
+                                                   const double* __restrict__ Q, int nb, int tp, int m, int S,
+                                                   int ablk, int nblk, double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char gsm[];
-  const int tp = 1 << tp_log2;
   const int rows = na + nb;
+  const int hp = tp >> 1;  // point pairs per tile row
   const int stage_elems = rows * tp;
   double* stage0 = reinterpret_cast<double*>(gsm);
   const long g_begin = blockIdx.x * chunk;
   const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
-  const int ntiles = g_end > g_begin ? (int)((g_end - g_begin + tp - 1) >> tp_log2) : 0;
+  const int ntiles = g_end > g_begin ? (int)((g_end - g_begin + tp - 1) / tp) : 0;
   const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
   const int blk = tid / S, slice = tid - blk * S;
   const bool active = blk < nblk;
   const int a0 = (blk % ablk) * kGA, b0 = (blk / ablk) * kGB;
   int ra[kGA], rb[kGB];  // stage rows of this thread's outputs (clamped; extra outputs are discarded)
 #pragma unroll
-  for (int i = 0; i < kGA; ++i) ra[i] = (a0 + i < na ? a0 + i : na - 1) * tp;
+  for (int i = 0; i < kGA; ++i) ra[i] = (a0 + i < na ? a0 + i : na - 1) * hp;
 #pragma unroll
-  for (int j = 0; j < kGB; ++j) rb[j] = (na + (b0 + j < nb ? b0 + j : nb - 1)) * tp;
+  for (int j = 0; j < kGB; ++j) rb[j] = (na + (b0 + j < nb ? b0 + j : nb - 1)) * hp;
   float sh[kGA][kGB], sl[kGA][kGB];
 #pragma unroll
   for (int i = 0; i < kGA; ++i)
 #pragma unroll
     for (int j = 0; j < kGB; ++j) sh[i][j] = sl[i][j] = 0.f;
 
+  // staging: warp w copies rows w, w + 8, ...; its lanes stride over the row
   auto issue = [&](int tile) {
     double* dst = stage0 + (size_t)(tile % kGStages) * stage_elems;
-    const long g0 = g_begin + ((long)tile << tp_log2);
+    const long g0 = g_begin + (long)tile * tp;
     const int cnt = g_end - g0 < tp ? (int)(g_end - g0) : tp;
-    if (kPair) {
-      for (int e = 2 * tid; e < stage_elems; e += 2 * kT) {  // p even: a pair of points
-        const int row = e >> tp_log2, p = e & (tp - 1);
-        const double* src = (row < na ? P + (long)row * N : Q + (long)(row - na) * N) + g0 + p;
-        if (p + 1 < cnt) {
-          cp_async16(dst + e, src);
-        } else if (p < cnt) {
-          cp_async8(dst + e, src);
-          dst[e + 1] = 0.0;
-        } else {
-          dst[e] = 0.0;
-          dst[e + 1] = 0.0;
+    for (int row = warp; row < rows; row += kT / 32) {
+      const double* src = (row < na ? P + (long)row * N : Q + (long)(row - na) * N) + g0;
+      double* d = dst + (size_t)row * tp;
+      if (kPair) {
+        for (int q = lane; q < hp; q += 32) {
+          const int p = 2 * q;
+          if (p + 1 < cnt) {
+            cp_async16(d + p, src + p);
+          } else if (p < cnt) {
+            cp_async8(d + p, src + p);
+            d[p + 1] = 0.0;
+          } else {
+            d[p] = 0.0;
+            d[p + 1] = 0.0;
+          }
         }
-      }
-    } else {
-      for (int e = tid; e < stage_elems; e += kT) {
-        const int row = e >> tp_log2, p = e & (tp - 1);
-        if (p < cnt) {
-          const double* src = row < na ? P + (long)row * N : Q + (long)(row - na) * N;
-          cp_async8(dst + e, src + g0 + p);
-        } else {
-          dst[e] = 0.0;
+      } else {
+        for (int p = lane; p < tp; p += 32) {
+          if (p < cnt) cp_async8(d + p, src + p);
+          else d[p] = 0.0;
         }
       }
     }
@@ -311,38 +332,40 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
   for (int it = 0; it < ntiles; ++it) {
     cp_async_wait_stages();  // this thread's copies of tile `it` have landed
     double* cur = stage0 + (size_t)(it % kGStages) * stage_elems;
-    float2* cur2 = reinterpret_cast<float2*>(cur);
-    if (kPair) {
-      for (int e = 2 * tid; e < stage_elems; e += 2 * kT) {  // the pairs this thread copied
-        const double2 d2 = *reinterpret_cast<const double2*>(cur + e);
-        float h0, l0, h1, l1;
-        df_split(d2.x, h0, l0);
-        df_split(d2.y, h1, l1);
-        *reinterpret_cast<float4*>(cur2 + e) = make_float4(h0, l0, h1, l1);
-      }
-    } else {
-      for (int e = tid; e < stage_elems; e += kT) {  // the elements this thread copied
-        float h, l;
-        df_split(cur[e], h, l);
-        cur2[e] = make_float2(h, l);
+    // convert the points this thread copied, in place, to (hi, lo) pairs
+    for (int row = warp; row < rows; row += kT / 32) {
+      double* d = cur + (size_t)row * tp;
+      if (kPair) {
+        for (int q = lane; q < hp; q += 32) {
+          const double2 d2 = *reinterpret_cast<const double2*>(d + 2 * q);
+          float h0, l0, h1, l1;
+          df_split(d2.x, h0, l0);
+          df_split(d2.y, h1, l1);
+          *reinterpret_cast<float4*>(d + 2 * q) = make_float4(h0, l0, h1, l1);
+        }
+      } else {
+        for (int p = lane; p < tp; p += 32) {
+          float h, l;
+          df_split(d[p], h, l);
+          *reinterpret_cast<float2*>(d + p) = make_float2(h, l);
+        }
       }
     }
     __syncthreads();  // tile `it` converted; everyone is done with tile it-1
     if (it + kGStages - 1 < ntiles) issue(it + kGStages - 1);
     cp_async_commit();
     if (active) {
-      const long g0 = g_begin + ((long)it << tp_log2);
-      const int cnt = g_end - g0 < tp ? (int)(g_end - g0) : tp;
-      // two consecutive points per step (one 16-byte load per row; a zero
-      // point past the tile's end adds nothing)
-      const float4* cur4 = reinterpret_cast<const float4*>(cur2);
-      for (int p = 2 * slice; p < cnt; p += 2 * S) {
+      // m point pairs per slice (one 16-byte load per row each; zero points
+      // past the tile's end add nothing)
+      const float4* cur4 = reinterpret_cast<const float4*>(cur);
+      for (int u = 0; u < m; ++u) {
+        const int q = slice + u * S;
         float4 y[kGB];
 #pragma unroll
-        for (int j = 0; j < kGB; ++j) y[j] = cur4[(rb[j] + p) >> 1];
+        for (int j = 0; j < kGB; ++j) y[j] = cur4[rb[j] + q];
 #pragma unroll
         for (int i = 0; i < kGA; ++i) {
-          const float4 x = cur4[(ra[i] + p) >> 1];
+          const float4 x = cur4[ra[i] + q];
 #pragma unroll
           for (int j = 0; j < kGB; ++j) {
             df_fma(sh[i][j], sl[i][j], x.x, x.y, y[j].x, y[j].y);
@@ -513,20 +536,16 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
   const long chunk = chunk_for(N, kRedBlocks, kTP);
   const int blocks = (int)((N + chunk - 1) / chunk);
   if (dfloat) {
-    const int ablk = (na + kGA - 1) / kGA, nblk = ablk * ((nb + kGB - 1) / kGB);
-    PG_ARG(nblk <= kT, "gram: %d output blocks", nblk);  // at most ~160 within the limits above
-    const int S = kT / nblk;
-    const int rows = na + nb;
-    int tp_log2 = 8;          // largest tile with kGStages stages in kGramSmemMax
-    while (tp_log2 > 5 && (size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8 > (size_t)kGramSmemMax) --tp_log2;
-    const long dchunk = chunk_for(N, kRedBlocks, 1 << tp_log2);
+    const GramGeom gg = gram_geometry(na, nb);
+    PG_ARG(gg.nblk <= kT, "gram: %d output blocks", gg.nblk);  // at most ~160 within the limits above
+    const long dchunk = chunk_for(N, kRedBlocks, gg.tp);
     const int dblocks = (int)((N + dchunk - 1) / dchunk);
-    const size_t smem = std::max((size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8,
-                                 (size_t)S * nblk * kGA * kGB * 8);
     if (pair_ok(N, P, Q))
-      k_gram_df<true><<<dblocks, kT, smem, st>>>(N, dchunk, P, na, Q, nb, tp_log2, S, ablk, nblk, rs.partial.p);
+      k_gram_df<true><<<dblocks, kT, gg.smem, st>>>(N, dchunk, P, na, Q, nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
+                                                     rs.partial.p);
     else
-      k_gram_df<false><<<dblocks, kT, smem, st>>>(N, dchunk, P, na, Q, nb, tp_log2, S, ablk, nblk, rs.partial.p);
+      k_gram_df<false><<<dblocks, kT, gg.smem, st>>>(N, dchunk, P, na, Q, nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
+                                                      rs.partial.p);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(rs.partial.p, dblocks, na * nb, out, false, st);
   } else {
@@ -647,20 +666,16 @@ extern "C" pg_status pg_block_gram_noalloc(long n, const double* P, int np, cons
   cudaStream_t st = as_stream(stream);
   const int no = np * nq;
   if (precision == PG_MIXED) {
-    const int ablk = (np + kGA - 1) / kGA, nblk = ablk * ((nq + kGB - 1) / kGB);
-    PG_ARG(nblk <= kT, "pg_block_gram_noalloc: %d output blocks", nblk);
-    const int S = kT / nblk;
-    const int rows = np + nq;
-    int tp_log2 = 8;
-    while (tp_log2 > 5 && (size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8 > (size_t)kGramSmemMax) --tp_log2;
-    const long chunk = chunk_for(n, pg::kRedBlocks, 1 << tp_log2);
+    const GramGeom gg = gram_geometry(np, nq);
+    PG_ARG(gg.nblk <= kT, "pg_block_gram_noalloc: %d output blocks", gg.nblk);
+    const long chunk = chunk_for(n, pg::kRedBlocks, gg.tp);
     const int blocks = (int)((n + chunk - 1) / chunk);
-    const size_t smem = std::max((size_t)kGStages * rows * ((size_t)1 << tp_log2) * 8,
-                                 (size_t)S * nblk * kGA * kGB * 8);
     if (pair_ok(n, P, Q))
-      k_gram_df<true><<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, tp_log2, S, ablk, nblk, partial);
+      k_gram_df<true><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
+                                                    partial);
     else
-      k_gram_df<false><<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, tp_log2, S, ablk, nblk, partial);
+      k_gram_df<false><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
+                                                     partial);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(partial, blocks, no, out, false, st);
   }
