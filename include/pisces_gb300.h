@@ -257,7 +257,8 @@ typedef struct {
   int corrflag;   /* 0 residual, 1 Davidson (default), 2 Jacobi-Davidson, 3 exact-kinetic preconditioner */
   int precision;  /* pg_precision of the H*X products */
   int startvec;   /* 0: start vectors given in evecs_dev; 1: PiaB + random; 2: random */
-  int refine;     /* PG_MIXED only: finish with FP64 H*X Rayleigh-Ritz on the converged vectors */
+  int refine;     /* PG_MIXED only: 1 = finish with an FP64 Rayleigh-Ritz step on the converged vectors;
+                     2 = continue the plain FP64 Davidson from them to residual 10^-max(ptol+2, 8) */
 } pg_solve_params;
 
 typedef struct {

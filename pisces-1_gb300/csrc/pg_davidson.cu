@@ -816,7 +816,7 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
   if (nconv < nr)  // not converged: report the current Ritz values
     for (int r = 0; r < nr && r < (int)d.sse.size(); ++r) evals[r] = d.sse[r];
   if (p->precision == PG_MIXED) PG_TRY(check_tc_error(g, st));
-  if (p->precision == PG_MIXED && p->refine) {
+  if (p->precision == PG_MIXED && p->refine == 1) {
     // FP64 Rayleigh-Ritz on the converged vectors: Z = H B with the FP64
     // operator, S = B^T Z, eigenpairs of S rotate the vectors.
     PG_TRY(hx(g, v, B.p, Z.p, nr, PG_FP64, st));
@@ -846,6 +846,31 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
     stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     stats->host_eig_seconds = d.t_eig;
     stats->device_wait_seconds = d.t_wait;
+  }
+  if (p->precision == PG_MIXED && p->refine == 2 && conv_status == PG_OK) {
+    // FP64 polish: the plain FP64 Davidson continued from the mixed form's
+    // converged vectors to residual 10^-max(ptol+2, 8), so that eigenvectors
+    // (not only eigenvalues) reach FP64 accuracy even for close states
+    pg_solve_params q = *p;
+    q.precision = PG_FP64;
+    q.startvec = 0;
+    q.refine = 0;
+    q.ptol = std::max(p->ptol + 2, 8);
+    pg_solve_stats s2;
+    const pg_status s = solve_with(
+        g, v, &q, evals, evecs, &s2, st,
+        [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, PG_FP64, st); }, &ws);
+    if (stats) {
+      stats->nconv = s2.nconv;
+      stats->n_matvec += s2.n_matvec;
+      stats->n_iter += s2.n_iter;
+      stats->n_restart += s2.n_restart;
+      for (int r = 0; r < 64; ++r) stats->residual[r] = s2.residual[r];
+      stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      stats->host_eig_seconds += s2.host_eig_seconds;
+      stats->device_wait_seconds += s2.device_wait_seconds;
+    }
+    return s;
   }
   return conv_status;
 }

@@ -491,8 +491,13 @@ def test_solve_c5_mixed_against_fp64(pg, torch, clusters):
     grid = pg.Grid((160, 160, 160), (64.0, 64.0, 64.0))
     v = grid.potential(pg.WaterTables(w))
     e64, x64, _ = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=8, corrflag=3)
+    # the FP64 Rayleigh-Ritz step fixes the eigenvalues; with states 2e-4 Eh
+    # apart the vectors need the FP64 polish (refine 2) for overlap 1 - 1e-8
     emx, xmx, _ = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=6, corrflag=3, precision=pg.PG_MIXED,
                              refine=1)
+    assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
+    emx, xmx, st = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=6, corrflag=3, precision=pg.PG_MIXED,
+                              refine=2)
     assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
     ov = torch.abs(torch.sum(x64 * xmx, dim=1)) / (x64.norm(dim=1) * xmx.norm(dim=1))
     assert float(ov.min()) >= 1 - 1e-8, ov
