@@ -27,7 +27,7 @@
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;  // 16 warps: the A fill and the epilogue each take one round of loads at 64^3
 constexpr int kTileM = 128;
 constexpr int kMaxN = 256;  // n_axis limit: the MMA N extent (rows of the axis matrix, padded to 16)
 constexpr int kBatch = 16;  // global loads a thread keeps in flight while filling A
@@ -127,7 +127,7 @@ using pg::TcJob;
 using pg::TcJobs;
 
 template <int AXIS>
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, 1)
     k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kc, int nch, uint32_t tmem_cols,
             const float* __restrict__ t_hi, const float* __restrict__ t_lo, const __grid_constant__ TcJobs jobs,
             int mode, int* __restrict__ err) {
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   const uint32_t lbo = 128, sbo = (uint32_t)(kc >> 2) * 128;
   const int warp = tid >> 5, lane = tid & 31;
   const int quarter = warp & 3;      // TMEM lanes 32*quarter .. +31
-  const int half = warp >> 2;        // which 16-column chunks this warp reads
+  const int group = warp >> 2;       // which 16-column chunks this warp reads (every kThreads/128-th)
   uint32_t phase = 0, b_phase = 0;
   bool ok = true;
   bool b_ready = false;   // single chunk: B resident
@@ -284,9 +284,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     const bool cvalid = c < ncols;
     const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
     const long gshift = cvalid ? (c / (N / n)) * N : 0;  // vector offset: grid point = address - gshift
-    // one 16-row chunk per round: 16 loads in flight, then the stores (the
-    // register budget allows two CTAs per SM where shared memory does)
-    for (int ck = half; ck * 16 < npad; ck += 2) {
+    // one 16-row chunk per warp and round: 16 loads in flight, then the stores
+    for (int ck = group; ck * 16 < npad; ck += kThreads / 128) {
       float d[16];
       tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(ck * 16), d);
       if (cvalid) {
@@ -384,10 +383,8 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     set_error("tc_axis: %zu bytes of shared memory needed, the device allows %d", smem, g_max_dyn);
     return PG_UNSUPPORTED;
   }
-  // two CTAs per SM when both fit the SM's shared memory (one CTA's tiles
-  // then overlap the other's loads and stores)
-  const long per_sm = smem <= (size_t)110 * 1024 ? 2 : 1;
-  const long cap = per_sm * g_num_sms;
+  // one persistent CTA of kThreads per SM
+  const long cap = g_num_sms;
   const int grid = (int)(tiles < cap ? tiles : cap);
   int* err = g->tc_err.p;
   switch (a) {
