@@ -160,26 +160,37 @@ extern "C" pg_status pg_water_sites(int nw, const double* waters, double* sites,
     for (int c = 0; c < 3; ++c) mu[3 * i + c] = 0.5 * alpha[i] * f1[3 * i + c];
   const int maxit = 5 * (ns + 10);
   int iters = -1;
+  // The damped dipole field tensors (FieldOfDipole, src/DPP.cpp:2377-2410)
+  // depend on the geometry only: computed once, then every SCF sweep is a
+  // block matrix-vector product with the same operations in the same order.
+  std::vector<double> tens(6 * (size_t)ns * ns, 0.0);
+  for (int i = 0; i < ns; ++i)
+    for (int j = 0; j < ns; ++j) {
+      if (j == i) continue;
+      const double rx = pos[3 * i] - pos[3 * j], ry = pos[3 * i + 1] - pos[3 * j + 1],
+                   rz = pos[3 * i + 2] - pos[3 * j + 2];
+      const double r2 = rx * rx + ry * ry + rz * rz;
+      const double r5 = pow(r2, -2.5);
+      const double d1 = damp_dd(sqrt(r2), alpha[i], alpha[j], kDampDipole);
+      const double d2 = damp_cd(sqrt(r2), alpha[i], alpha[j], kDampDipole);
+      double* t = &tens[6 * ((size_t)i * ns + j)];
+      t[0] = (d1 * 3. * rx * rx - d2 * r2) * r5;  // xx
+      t[1] = (d1 * 3. * ry * ry - d2 * r2) * r5;  // yy
+      t[2] = (d1 * 3. * rz * rz - d2 * r2) * r5;  // zz
+      t[3] = d1 * 3. * rx * ry * r5;              // xy
+      t[4] = d1 * 3. * rx * rz * r5;              // xz
+      t[5] = d1 * 3. * ry * rz * r5;              // yz
+    }
   for (int it = 0; it < maxit; ++it) {
     std::fill(f2.begin(), f2.end(), 0.0);
     for (int i = 0; i < ns; ++i)
       for (int j = 0; j < ns; ++j) {
         if (j == i) continue;
-        // damped dipole field tensor at site i of the dipole on site j
-        // (FieldOfDipole, src/DPP.cpp:2377-2410)
-        const double rx = pos[3 * i] - pos[3 * j], ry = pos[3 * i + 1] - pos[3 * j + 1],
-                     rz = pos[3 * i + 2] - pos[3 * j + 2];
-        const double r2 = rx * rx + ry * ry + rz * rz;
-        const double r5 = pow(r2, -2.5);
-        const double d1 = damp_dd(sqrt(r2), alpha[i], alpha[j], kDampDipole);
-        const double d2 = damp_cd(sqrt(r2), alpha[i], alpha[j], kDampDipole);
-        const double txx = (d1 * 3. * rx * rx - d2 * r2) * r5, tyy = (d1 * 3. * ry * ry - d2 * r2) * r5,
-                     tzz = (d1 * 3. * rz * rz - d2 * r2) * r5;
-        const double txy = d1 * 3. * rx * ry * r5, txz = d1 * 3. * rx * rz * r5, tyz = d1 * 3. * ry * rz * r5;
+        const double* t = &tens[6 * ((size_t)i * ns + j)];
         const double* m = &mu[3 * j];
-        f2[3 * i] += txx * m[0] + txy * m[1] + txz * m[2];
-        f2[3 * i + 1] += txy * m[0] + tyy * m[1] + tyz * m[2];
-        f2[3 * i + 2] += txz * m[0] + tyz * m[1] + tzz * m[2];
+        f2[3 * i] += t[0] * m[0] + t[3] * m[1] + t[4] * m[2];
+        f2[3 * i + 1] += t[3] * m[0] + t[1] * m[1] + t[5] * m[2];
+        f2[3 * i + 2] += t[4] * m[0] + t[5] * m[1] + t[2] * m[2];
       }
     for (int i = 0; i < ns; ++i)
       for (int c = 0; c < 3; ++c) {
