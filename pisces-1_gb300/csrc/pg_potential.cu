@@ -1,8 +1,9 @@
 // V(r) on the grid: electron-water DPP model, Bloomfield ions, harmonic well.
 //
 // Compiled with -fmad=false: every product and sum is rounded separately, in
-// the reference's evaluation order, so the only differences from the CPU
-// code are the last-place differences of exp/erf.
+// the reference's evaluation order.  The differences from the CPU code are
+// last-place ones: exp/erf, and the undamped inverse powers of R taken from
+// one reciprocal square root per site instead of a square root and divisions.
 //
 // Layout: the reference's per-term lists (charges, dipoles, Slater cores,
 // polarisable sites, each with a site index) are packed on the host into one
@@ -123,13 +124,19 @@ __global__ void __launch_bounds__(kThreads) k_potential_dpp(
         // distance table entry, src/Potential.cpp:136-146
         const double rx = px - R[R_X], ry = py - R[R_Y], rz = pz - R[R_Z];
         const double r2 = rx * rx + ry * ry + rz * rz;
-        const double r = sqrt(r2);
-        if (flags & F_CHARGE) vpc += -R[R_Q] / reff(r, dq);  // :1188-1204
-        if (flags & F_DIPOLE) {                               // :1246-1262
-          double m3 = 1.0 / (r2 * r);
+        // one reciprocal square root per site serves every undamped term
+        // (1/R, 1/R^3, 1/R^4); R = R^2 / R.  The damped branches (R < r0,
+        // including R = 0 on a site) keep the reference's divisions.
+        const double ir = rsqrt(r2);
+        const double r = r2 > 0.0 ? r2 * ir : 0.0;
+        if (flags & F_CHARGE) vpc += r < dq ? -R[R_Q] / reff(r, dq) : -R[R_Q] * ir;  // :1188-1204
+        if (flags & F_DIPOLE) {                                                       // :1246-1262
+          double m3;
           if (r < dd) {
             const double re = reff(r, dd);
             m3 = 1.0 / (re * re * re);
+          } else {
+            m3 = ir * ir * ir;
           }
           vind += -(rx * R[R_MX] + ry * R[R_MY] + rz * R[R_MZ]) * m3;
         }
@@ -142,7 +149,8 @@ __global__ void __launch_bounds__(kThreads) k_potential_dpp(
             const double re2 = re * re;
             spol += R[R_ALPHA] * r2 / (re2 * re2 * re2);
           } else {
-            spol += R[R_ALPHA] / (r2 * r2);
+            const double ir2 = ir * ir;
+            spol += R[R_ALPHA] * (ir2 * ir2);
           }
         }
       }
