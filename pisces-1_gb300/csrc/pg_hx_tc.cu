@@ -314,6 +314,221 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid < 32) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tmem_cols));
 }
 
+
+// Pipelined form of k_hx_tc for CTAs that own several tiles and a single K
+// chunk (n <= 112).  Warps 0-7 (producers) fill the A tile of tile i+1 while
+// warps 8-15 (consumers) drain the accumulator of tile i; thread 0 issues the
+// MMAs.  Two TMEM accumulators alternate between tiles:
+//   mbar_mma[k]  completes when the MMAs into accumulator k are done (A is
+//                then free for the next fill, and the accumulator readable);
+//   mbar_free[k] completes when the eight consumer warps have read
+//                accumulator k (it may then take the tile after next).
+// Every wait is bounded; a timeout raises `abort` in shared memory, every
+// role leaves its loop, and the error word is set.
+constexpr int kPipeThreads = 512;
+constexpr int kProducers = 256;
+
+// OR of f over the kProducers producer threads (named barrier 1): every
+// producer takes the same branch afterwards.
+__device__ __forceinline__ int producers_any(int f) {
+  int r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.s32 p, %1, 0;\n bar.red.or.pred q, 1, %2, p;\n selp.s32 %0, 1, 0, q;\n}"
+      : "=r"(r)
+      : "r"(f), "n"(kProducers)
+      : "memory");
+  return r;
+}
+
+template <int AXIS>
+__global__ void __launch_bounds__(kPipeThreads, 1)
+    k_hx_tc_pipe(int nx, int ny, int nz, AxisMap am, int npad, int kc, uint32_t tmem_cols,
+                 const float* __restrict__ t_hi, const float* __restrict__ t_lo,
+                 const __grid_constant__ TcJobs jobs, int mode, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  const int n = am.n;
+  const uint32_t b_bytes = (uint32_t)npad * kc * 4;
+  const uint32_t a_bytes = (uint32_t)kTileM * kc * 4;
+  unsigned char* sBh = smem;
+  unsigned char* sBl = smem + b_bytes;
+  unsigned char* sAh = smem + 2 * b_bytes;
+  unsigned char* sAl = sAh + a_bytes;
+  __shared__ __align__(8) uint64_t mbar_b, mbar_mma[2], mbar_free[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const long N = (long)nx * ny * nz;
+  const long ntiles = jobs.ntiles;
+  if (tid == 0) {
+    abort_flag = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_b)));
+    for (int k = 0; k < 2; ++k) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_mma[k])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 8;" ::"r"(smem_u32(&mbar_free[k])));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(smem_u32(&mbar_b)), "r"(2 * b_bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sBh)),
+                 "l"(t_hi), "r"(b_bytes), "r"(smem_u32(&mbar_b))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(sBl)),
+                 "l"(t_lo), "r"(b_bytes), "r"(smem_u32(&mbar_b))
+                 : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(2 * tmem_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(npad >> 3) << 17) |
+                         ((uint32_t)(kTileM >> 4) << 24);
+  const uint32_t lbo = 128, sbo = (uint32_t)(kc >> 2) * 128;
+  auto fail = [&]() { atomicExch(&abort_flag, 1); };
+
+  if (tid < kProducers) {
+    // ---------------------------------------------------------------- producers
+    bool b_ready = false;
+    long i = 0;
+    for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int k = (int)(i & 1);
+      // the MMAs of the previous tile have read A (every producer waits, then
+      // all producers agree on whether to go on)
+      int bad = 0;
+      if (i >= 1 && !mbar_wait(smem_u32(&mbar_mma[(i - 1) & 1]), (uint32_t)(((i - 1) >> 1) & 1))) bad = 1;
+      if (producers_any(bad | *(volatile int*)&abort_flag)) {
+        fail();
+        break;
+      }
+      int jb = 0;
+      while (jb + 1 < jobs.n && tile >= jobs.j[jb + 1].tile0) ++jb;
+      const double* __restrict__ X = jobs.j[jb].x;
+      const long ncols = jobs.j[jb].ncols;
+      const long c0 = (tile - jobs.j[jb].tile0) * kTileM;
+      for (int e0 = tid; e0 < kTileM * kc; e0 += kBatch * kProducers) {
+        double xv[kBatch];
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * kProducers;
+          const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
+          const int kk = AXIS == 0 ? e - (e / kc) * kc : (e >> 7);
+          const long c = c0 + m;
+          const bool in = e < kTileM * kc && kk < n && c < ncols;
+          xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)kk * am.stride] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < kBatch; ++u) {
+          const int e = e0 + u * kProducers;
+          if (e < kTileM * kc) {
+            const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
+            const int kk = AXIS == 0 ? e - (e / kc) * kc : (e >> 7);
+            float h, l;
+            split_tf32(xv[u], h, l);
+            *(float*)(sAh + kmajor_off(m, kk, kc)) = h;
+            *(float*)(sAl + kmajor_off(m, kk, kc)) = l;
+          }
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory");  // the A tile is complete
+      if (tid == 0) {
+        bool ok = true;
+        if (!b_ready) ok = b_ready = mbar_wait(smem_u32(&mbar_b), 0);
+        // the consumers have read this accumulator's previous tile (i - 2)
+        if (ok && i >= 2) ok = mbar_wait(smem_u32(&mbar_free[k]), (uint32_t)(((i - 2) >> 1) & 1));
+        if (!ok || *(volatile int*)&abort_flag) {
+          fail();
+        } else {
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t ah = smem_u32(sAh), al = smem_u32(sAl), bh = smem_u32(sBh), bl = smem_u32(sBl);
+          const uint32_t acc = tmem + (uint32_t)k * tmem_cols;
+          for (int kk = 0; kk < kc / 8; ++kk) {
+            const uint32_t off = (uint32_t)kk * 256;
+            const uint64_t dah = smem_desc(ah + off, lbo, sbo), dal = smem_desc(al + off, lbo, sbo);
+            const uint64_t dbh = smem_desc(bh + off, lbo, sbo), dbl = smem_desc(bl + off, lbo, sbo);
+            asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(acc),
+                         "l"(dal), "l"(dbh), "r"(idesc), "r"(kk > 0 ? 1u : 0u));
+            asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(acc),
+                         "l"(dah), "l"(dbl), "r"(idesc), "r"(1u));
+            asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                         " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(acc),
+                         "l"(dah), "l"(dbh), "r"(idesc), "r"(1u));
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_u32(&mbar_mma[k])));
+        }
+      }
+    }
+  } else {
+    // ---------------------------------------------------------------- consumers
+    const int cw = warp - kProducers / 32;  // consumer warp 0..7
+    const int quarter = warp & 3;           // TMEM lanes 32*quarter .. +31
+    const int group = cw >> 2;              // which 16-row chunks this warp reads
+    long i = 0;
+    for (long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int k = (int)(i & 1);
+      if (!mbar_wait(smem_u32(&mbar_mma[k]), (uint32_t)((i >> 1) & 1))) fail();
+      if (*(volatile int*)&abort_flag) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      int jb = 0;
+      while (jb + 1 < jobs.n && tile >= jobs.j[jb + 1].tile0) ++jb;
+      const double* __restrict__ X = jobs.j[jb].x;
+      double* __restrict__ Y = jobs.j[jb].y;
+      const double* __restrict__ v = jobs.j[jb].v;
+      const long ncols = jobs.j[jb].ncols;
+      const long c0 = (tile - jobs.j[jb].tile0) * kTileM;
+      const int m = 32 * quarter + lane;
+      const long c = c0 + m;
+      const bool cvalid = c < ncols;
+      const long base = cvalid ? col_base<AXIS>(c, nx, ny, N) : 0;
+      const long gshift = cvalid ? (c / (N / n)) * N : 0;
+      const uint32_t acc = tmem + (uint32_t)k * tmem_cols;
+      for (int ck = group; ck * 16 < npad; ck += 2) {
+        float d[16];
+        tmem_ld16(acc + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(ck * 16), d);
+        if (cvalid) {
+          double prev[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int r = ck * 16 + j;
+            const long a = base + (long)r * am.stride;
+            prev[j] = 0.0;
+            if (r < n) {
+              if (mode == 2) prev[j] = v[a - gshift] * X[a];
+              else if (mode == 1) prev[j] = Y[a];
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int r = ck * 16 + j;
+            if (r < n) Y[base + (long)r * am.stride] = prev[j] + (double)d[j];
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&mbar_free[k])) : "memory");
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (abort_flag && tid == 0) atomicExch(err, 1);
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * tmem_cols));
+}
+
 }  // namespace
 
 namespace pg {
@@ -341,14 +556,15 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (g_num_sms <= 0) g_num_sms = 148;
-    const void* fns[3] = {(const void*)k_hx_tc<0>, (const void*)k_hx_tc<1>, (const void*)k_hx_tc<2>};
+    const void* fns[6] = {(const void*)k_hx_tc<0>,      (const void*)k_hx_tc<1>,      (const void*)k_hx_tc<2>,
+                          (const void*)k_hx_tc_pipe<0>, (const void*)k_hx_tc_pipe<1>, (const void*)k_hx_tc_pipe<2>};
     int lim = optin;
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k) {
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
       cudaFuncAttributes fa;
       e = cudaFuncGetAttributes(&fa, fns[k]);
       if (e == cudaSuccess) lim = std::min(lim, optin - (int)fa.sharedSizeBytes);
     }
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k)
       e = cudaFuncSetAttribute(fns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     g_max_dyn = lim;
     return e;
@@ -387,6 +603,22 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
   const long cap = g_num_sms;
   const int grid = (int)(tiles < cap ? tiles : cap);
   int* err = g->tc_err.p;
+  if (nch == 1 && tiles > cap) {  // several tiles per CTA: the pipelined form overlaps them
+    switch (a) {
+      case 0:
+        k_hx_tc_pipe<0><<<grid, kPipeThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
+                                                          jobs, mode, err);
+        break;
+      case 1:
+        k_hx_tc_pipe<1><<<grid, kPipeThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
+                                                          jobs, mode, err);
+        break;
+      default:
+        k_hx_tc_pipe<2><<<grid, kPipeThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
+                                                          jobs, mode, err);
+    }
+    return check_launch("k_hx_tc_pipe");
+  }
   switch (a) {
     case 0:
       k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,

@@ -501,3 +501,21 @@ def test_solve_c5_mixed_against_fp64(pg, torch, clusters):
     assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
     ov = torch.abs(torch.sum(x64 * xmx, dim=1)) / (x64.norm(dim=1) * xmx.norm(dim=1))
     assert float(ov.min()) >= 1 - 1e-8, ov
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nvec", [((64, 64, 64), 12), ((96, 80, 48), 6), ((112, 40, 72), 5)])
+def test_hx_mixed_pipelined_many_tiles(pg, torch, n, nvec):
+    """More tiles than SMs: the pipelined tensor-core form (producer warps
+    fill the next tile while consumer warps drain the last accumulator)
+    against FP64 within the mixed form's bound (2e-5 of max |Y|), twice in a
+    row (the second launch reuses nothing of the first)."""
+    rng = np.random.Generator(np.random.PCG64(8))
+    grid = pg.Grid(n, tuple(0.6 * (k + 1) for k in n))
+    N = grid.N
+    x = dev(torch, rng.standard_normal(nvec * N))
+    v = dev(torch, rng.standard_normal(N))
+    y64 = host(grid.hx(v, x, nvec=nvec, precision=0))
+    for _ in range(2):
+        ymx = host(grid.hx(v, x, nvec=nvec, precision=1))
+        assert np.max(np.abs(ymx - y64)) / np.max(np.abs(y64)) <= 2e-5
