@@ -157,9 +157,9 @@ pg_status pg_water_default_tables(int nw, const double* sites, const double* cha
 
 /* Y = H X for nvec vectors: H = V + Tx (+) Ty (+) Tz.  precision PG_FP64:
  * FP64 arithmetic throughout; PG_MIXED: kinetic contractions as split-TF32
- * tensor-core products accumulated in FP32, V*X in FP64.  Replaces
- * DVR::MatrixTimesVector applied vector by vector (src/mtx.cpp:22-109,
- * src/davdriver.cpp:67-78). */
+ * tensor-core products accumulated in FP32, V*X in FP64.  nvec = 0 does
+ * nothing and accepts null X and Y.  Replaces DVR::MatrixTimesVector applied
+ * vector by vector (src/mtx.cpp:22-109, src/davdriver.cpp:67-78). */
 pg_status pg_hx(const pg_grid* g, const double* v_dev, const double* x_dev, double* y_dev, int nvec, int precision,
                 void* stream);
 /* pg_hx without the completion check of the mixed form: returns once the

@@ -129,9 +129,10 @@ pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y
 
 pg_status hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
              cudaStream_t st) {
-  PG_ARG(g && v && x && y && nvec >= 0, "pg_hx: bad arguments");
+  PG_ARG(g && v && nvec >= 0, "pg_hx: bad arguments");
+  if (nvec == 0) return PG_OK;  // an empty block may come with null X and Y
+  PG_ARG(x && y, "pg_hx: null X or Y");
   PG_ARG(x != y, "pg_hx: X and Y must not alias");
-  if (nvec == 0) return PG_OK;
   if (precision == PG_MIXED) return hx_mixed(g, v, x, y, nvec, st, false);
   PG_ARG(precision == PG_FP64, "pg_hx: unknown precision %d", precision);
   constexpr int NV = 4;

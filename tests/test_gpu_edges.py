@@ -1,0 +1,118 @@
+"""Edge cases of the device path against the CPU oracle.
+
+  - the smallest and ragged grids (n = 2 on an axis, odd sizes, one long axis):
+    H*X in FP64 and split-TF32 against the oracle's matvec (Hamiltonian::matvec,
+    src/Hamiltonian.cpp), where the tensor-core tiles are mostly padding;
+  - an empty block (nvec = 0) is a no-op that succeeds;
+  - the largest root count one solve takes (16 roots in a 128-vector subspace)
+    against the dense eigenvalues of the full Hamiltonian built column by column
+    from the oracle;
+  - a cluster with no waters is the particle in a box;
+  - argument limits (roots, subspace, grid sizes) are PG_BAD_ARG before any
+    launch, and the library keeps working after a rejected call.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+MIXED_HX_TOL = 2e-5  # split-TF32 products, FP32 accumulation (same bound as the parity tests)
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available(), "GPU tests need a CUDA device"
+    return t
+
+
+def dev(torch, a):
+    return torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device="cuda")
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("n", [(2, 2, 2), (3, 5, 7), (2, 17, 9), (129, 2, 3), (5, 3, 130)])
+def test_hx_tiny_and_ragged_grids(pg, orc, torch, n):
+    L = tuple(0.6 * (k + 1) for k in n)
+    rng = np.random.default_rng(sum(n))
+    grid = pg.Grid(n, L)
+    og = orc.Grid(n, L)
+    nvec = 3
+    v = rng.normal(size=grid.N)
+    X = rng.normal(size=(nvec, grid.N))
+    ref = np.stack([og.matvec(v, X[r]) for r in range(nvec)])
+    y64 = host(grid.hx(dev(torch, v), dev(torch, X), precision=pg.PG_FP64)).reshape(nvec, -1)
+    assert rel(y64, ref) < 1e-13
+    ymx = host(grid.hx(dev(torch, v), dev(torch, X), precision=pg.PG_MIXED)).reshape(nvec, -1)
+    assert np.max(np.abs(ymx - ref)) / np.max(np.abs(ref)) < MIXED_HX_TOL
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_hx_empty_block(pg, torch, precision):
+    grid = pg.Grid((8, 8, 8), (6.0, 6.0, 6.0))
+    v = torch.zeros(grid.N, dtype=torch.float64, device="cuda")
+    X = torch.zeros(0, dtype=torch.float64, device="cuda")
+    Y = torch.full((4,), 7.0, dtype=torch.float64, device="cuda")
+    grid.hx(v, X, nvec=0, precision=precision, out=Y)
+    assert float(Y.sum()) == 28.0  # nothing written
+
+
+def _dense_h(og, v):
+    N = og.N
+    H = np.empty((N, N))
+    e = np.zeros(N)
+    for j in range(N):
+        e[j] = 1.0
+        H[:, j] = og.matvec(v, e)
+        e[j] = 0.0
+    return H
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_sixteen_roots_in_a_full_subspace(pg, orc, torch, precision):
+    n, L = (8, 7, 9), (7.0, 6.5, 8.0)
+    rng = np.random.default_rng(3)
+    og = orc.Grid(n, L)
+    pts = np.meshgrid(*[np.linspace(-0.5 * L[a], 0.5 * L[a], n[a] + 2)[1:-1] for a in range(3)], indexing="ij")
+    r2 = sum(p * p for p in pts).reshape(-1)
+    v = 0.15 * r2 - 0.4 * np.exp(-r2) + 0.01 * rng.normal(size=og.N)  # lifts the box degeneracies
+    ref = np.linalg.eigvalsh(_dense_h(og, v))[:16]
+    grid = pg.Grid(n, L)
+    ev, vec, st = grid.solve(dev(torch, v), nroots=16, maxsub=128, maxiter=400, ptol=8, corrflag=3,
+                             precision=precision, refine=2 if precision else 1)
+    assert st["nconv"] == 16
+    assert np.max(np.abs(ev - ref)) < 1e-8
+    V = host(vec)
+    assert np.max(np.abs(V @ V.T - np.eye(16))) < 1e-8
+
+
+def test_cluster_without_waters_is_a_box(pg, torch):
+    n, L = (24, 20, 28), (20.0, 18.0, 22.0)
+    ev, _, _ = pg.cluster_solve(n, L, np.zeros((0, 9)), nroots=2, maxsub=30, ptol=8)
+    box = np.array([sum((np.pi * k / (L[a])) ** 2 / 2 for a, k in enumerate(q))
+                    for q in [(1, 1, 1), (1, 1, 2), (1, 2, 1), (2, 1, 1)]])
+    assert np.max(np.abs(np.asarray(ev) - np.sort(box)[:2])) < 1e-6
+
+
+def test_argument_limits(pg, torch):
+    grid = pg.Grid((8, 8, 8), (6.0, 6.0, 6.0))
+    v = torch.zeros(grid.N, dtype=torch.float64, device="cuda")
+    for kw in (dict(nroots=0), dict(nroots=17, maxsub=40), dict(nroots=4, maxsub=4), dict(nroots=2, maxsub=129)):
+        with pytest.raises(pg.PiscesError) as e:
+            grid.solve(v, **kw)
+        assert e.value.status == pg.PG_BAD_ARG
+    for n in ((1, 8, 8), (8, 1025, 8)):
+        with pytest.raises(pg.PiscesError) as e:
+            pg.Grid(n, (6.0, 6.0, 6.0))
+        assert e.value.status == pg.PG_BAD_ARG
+    with pytest.raises(pg.PiscesError) as e:
+        pg.Grid((8, 8, 8), (6.0, -1.0, 6.0))
+    assert e.value.status == pg.PG_BAD_ARG
+    # still serving after the rejected calls
+    ev, _, _ = grid.solve(v, nroots=1, ptol=8)
+    assert abs(ev[0] - 3 * (np.pi / 6.0) ** 2 / 2) < 1e-9
