@@ -453,10 +453,22 @@ void or_potential_spherical(const int n[3], const double* const x[3], double k, 
 
 /* ---------------------------------------------------------- small linalg */
 
+/* Dot product over 64 fixed blocks summed in order: the same bits for any
+ * thread count (an OpenMP reduction combines its partial sums in an
+ * unspecified order). */
+#define OR_DOT_BLOCKS 64
 static double or_dot(long n, const double* a, const double* b) {
+  double part[OR_DOT_BLOCKS];
+  const long chunk = (n + OR_DOT_BLOCKS - 1) / OR_DOT_BLOCKS;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < OR_DOT_BLOCKS; ++k) {
+    const long b0 = (long)k * chunk, b1 = b0 + chunk < n ? b0 + chunk : n;
+    double s = 0;
+    for (long i = b0; i < b1; ++i) s += a[i] * b[i];
+    part[k] = s;
+  }
   double s = 0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-  for (long i = 0; i < n; ++i) s += a[i] * b[i];
+  for (int k = 0; k < OR_DOT_BLOCKS; ++k) s += part[k];
   return s;
 }
 static double or_nrm2(long n, const double* a) { return sqrt(or_dot(n, a, a)); }
@@ -660,6 +672,10 @@ int or_davidson(or_davidson_state* st, int ndim, int maxsub, int nroots, int max
       if (st->conv_w[r] > 0.95) {
         st->ccode[r] = 0;
       } else if (st->residuals[r] < st->thresh) {
+        if (*nconv >= maxsub) { /* the reference's copy would land past B's maxsub columns */
+          st->status = 0;
+          return -2;
+        }
         st->ccode[r] = 1;
         st->bindex[r] = *nconv;
         memcpy(B + (long)(*nconv) * N, ritz + (long)r * N, sizeof(double) * N);
@@ -667,6 +683,24 @@ int or_davidson(or_davidson_state* st, int ndim, int maxsub, int nroots, int max
         newly += 1;
       } else {
         st->ccode[r] = 2;
+      }
+    }
+    /* Inside a near-degenerate set every root's overlap with the locked space
+     * can stay below 0.95, and the same state is locked again, so nconv can
+     * pass nroots.  The reference then keeps nconv + (unconverged roots) >
+     * nroots vectors: its restart writes the extra Z combinations past the
+     * nroots Ritz slots, into the residual (and JD) slots that follow them in
+     * the work array (src/Davidson.cpp:181-187, 303-346), and later locks copy
+     * Ritz vectors to B[nconv] whatever nconv is (:279-284).  The oracle does
+     * the same while those writes stay inside the work array and B; where the
+     * reference's would leave them it stops with -2. */
+    {
+      int kept = *nconv;
+      for (int r = 0; r < nroots; ++r) kept += st->ccode[r] == 2;
+      const int slots = 2 * nroots + (corrflag == 2 ? 1 : 0); /* N-vectors from ritz to the end of work */
+      if (kept > slots || kept > maxsub) {
+        st->status = 0;
+        return -2;
       }
     }
     if (*nconv == nroots) {
@@ -750,6 +784,7 @@ int or_solve(const int n[3], const double* const tp[3], const double* const x[3]
   int stopped = 0;
   while (ido != 0) { /* src/davdriver.cpp:58-86 */
     ido = or_davidson(st, (int)N, maxsub, nstates, maxiter, ptol, corrflag, evals, &nconv, B, Z, diag, work, inout);
+    if (ido < 0) { stopped = ido; break; }
     if (ido == 1) {
       for (int k = 0; k < inout[2]; ++k) {
         or_matvec(n, tp, v, B + (long)(inout[0] + k) * N, Z + (long)(inout[1] + k) * N);
@@ -761,5 +796,5 @@ int or_solve(const int n[3], const double* const tp[3], const double* const x[3]
   or_davidson_destroy(st);
   free(Z); free(diag); free(work);
   if (n_matvec) *n_matvec = nmv;
-  return stopped ? -1 : nconv;
+  return stopped == 1 ? -1 : stopped < 0 ? stopped : nconv;
 }

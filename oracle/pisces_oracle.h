@@ -95,7 +95,9 @@ int or_davidson(or_davidson_state* s, int ndim, int maxsub, int nroots, int maxm
  * seeded with 1, as in a fresh reference process).  B must hold maxsub*N
  * doubles; on return B[0..nstates) are the Ritz vectors.  If n_matvec is
  * given it receives the number of single-vector matvecs; if max_matvec > 0
- * the solve stops after that many (a bounded timing sample) and returns -1. */
+ * the solve stops after that many (a bounded timing sample) and returns -1.
+ * Returns -2 where the reference would lock more than nstates roots and
+ * write past its work array (see or_davidson). */
 int or_solve(const int n[3], const double* const tp[3], const double* const x[3], const double* v, int nstates,
              int maxsub, int maxiter, int ptol, int corrflag, int startvec, double* evals, double* B,
              long* n_matvec, long max_matvec);

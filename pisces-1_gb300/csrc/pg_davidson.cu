@@ -367,20 +367,23 @@ pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* s
 }
 
 // Orthonormalise the k vectors R (contiguous, R[j*N]) against the first nbas
-// columns of B (block classical Gram-Schmidt, two passes), then among
-// themselves (Cholesky-QR, two passes); the result goes to out (k vectors,
-// may equal R).  Same spans as the reference's vector-by-vector
-// orthogonalisation (src/Davidson.cpp:447-514).
+// columns of B and among themselves; the result goes to out (k vectors, may
+// equal R).  Two passes, each a block classical Gram-Schmidt step against B
+// followed by Cholesky-QR of the block.  A correction that lies almost inside
+// span(B) leaves an O(eps) remainder whose components along B the first
+// normalisation scales up to O(1); the second pass projects them out again.
+// Same spans as the reference's vector-by-vector orthogonalisation, which
+// also renormalises between projections (src/Davidson.cpp:447-514).
 pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, const double* B, int nbas, double* out,
                                cudaStream_t st) {
   double* c = d->dcoef.p;
   double* ones = d->dsq.p + kOnes;
-  for (int pass = 0; nbas > 0 && pass < 2; ++pass) {
-    // c[a*k + j] = B_a . R_j ;  R_j <- R_j - sum_a B_a c[a*k + j]
-    PG_TRY(gram(N, B, nbas, R, k, c, d->rs, st, d->dfloat));
-    PG_TRY(combine(N, B, nbas, c, k, 1, -1.0, R, ones, false, R, k, nullptr, d->rs, st, d->dfloat));
-  }
   for (int pass = 0; pass < 2; ++pass) {
+    if (nbas > 0) {
+      // c[a*k + j] = B_a . R_j ;  R_j <- R_j - sum_a B_a c[a*k + j]
+      PG_TRY(gram(N, B, nbas, R, k, c, d->rs, st, d->dfloat));
+      PG_TRY(combine(N, B, nbas, c, k, 1, -1.0, R, ones, false, R, k, nullptr, d->rs, st, d->dfloat));
+    }
     PG_TRY(gram(N, R, k, R, k, d->dgram.p, d->rs, st, d->dfloat));
     k_cholinv<<<1, 32, 0, st>>>(d->dgram.p, k, c);
     PG_TRY(check_launch("k_cholinv"));
@@ -524,8 +527,12 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       PG_TRY(check_launch("k_ritz_residual"));
       PG_TRY(reduce_partials(d->rs.partial.p, nblk, nroots, rsq, true, st));
     }
-    std::vector<double> hr(nroots);
-    PG_CUDA_TRY(cudaMemcpyAsync(hr.data(), rsq, sizeof(double) * nroots, cudaMemcpyDeviceToHost, st));
+    // |r_r|^2 and |U_r|^2 in one read (rsq and usq both live in dsq)
+    static_assert(kUsq == 0 && kRsq > kUsq, "dsq layout");
+    std::vector<double> hsq(kRsq + nroots);
+    PG_CUDA_TRY(cudaMemcpyAsync(hsq.data(), d->dsq.p, sizeof(double) * hsq.size(), cudaMemcpyDeviceToHost, st));
+    const double* hr = hsq.data() + kRsq;
+    const double* hu = hsq.data() + kUsq;
     const auto w1 = std::chrono::steady_clock::now();
     PG_CUDA_TRY(cudaStreamSynchronize(st));
     d->t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - w1).count();
@@ -533,6 +540,14 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       d->residuals[r] = sqrt(hr[r]);
       if (!std::isfinite(d->residuals[r])) {
         set_error("pg_davidson_rci: non-finite residual norm for root %d", r);
+        d->status = 0;
+        return PG_NUMERIC;
+      }
+      // with an orthonormal basis |B v| = 1 for every unit subspace vector v;
+      // a deviation means the basis lost orthonormality and the Ritz pairs
+      // (which the reference would renormalise and accept) are spurious
+      if (!(fabs(hu[r] - 1.0) < 1e-6)) {
+        set_error("pg_davidson_rci: subspace basis lost orthonormality (|Bv|^2 = %.3e for root %d)", hu[r], r);
         d->status = 0;
         return PG_NUMERIC;
       }

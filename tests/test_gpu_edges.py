@@ -6,7 +6,9 @@
   - an empty block (nvec = 0) is a no-op that succeeds;
   - the largest root count one solve takes (16 roots in a 128-vector subspace)
     against the dense eigenvalues of the full Hamiltonian built column by column
-    from the oracle;
+    from the oracle, on well separated and on near-degenerate spectra (the
+    reference algorithm does not finish either: near-degenerate roots get
+    locked twice, and its orthogonalisation lets spurious roots in);
   - a cluster with no waters is the particle in a box;
   - argument limits (roots, subspace, grid sizes) are PG_BAD_ARG before any
     launch, and the library keeps working after a rejected call.
@@ -73,20 +75,44 @@ def _dense_h(og, v):
     return H
 
 
-@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
-def test_sixteen_roots_in_a_full_subspace(pg, orc, torch, precision):
-    n, L = (8, 7, 9), (7.0, 6.5, 8.0)
-    rng = np.random.default_rng(3)
-    og = orc.Grid(n, L)
+def _well(n, L, seed):
+    """A confining well with a little noise: 8x7x9 has well separated
+    levels; on 12x11x13 boxes of near-equal sides its p- and d-like levels are
+    split by 5e-4 Eh only."""
+    rng = np.random.default_rng(seed)
     pts = np.meshgrid(*[np.linspace(-0.5 * L[a], 0.5 * L[a], n[a] + 2)[1:-1] for a in range(3)], indexing="ij")
     r2 = sum(p * p for p in pts).reshape(-1)
-    v = 0.15 * r2 - 0.4 * np.exp(-r2) + 0.01 * rng.normal(size=og.N)  # lifts the box degeneracies
-    ref = np.linalg.eigvalsh(_dense_h(og, v))[:16]
+    return 0.15 * r2 - 0.4 * np.exp(-r2) + 0.01 * rng.normal(size=r2.size)
+
+
+SPECTRA = {"separated": ((8, 7, 9), (7.0, 6.5, 8.0)), "near_degenerate": ((12, 11, 13), (11.05, 10.2, 11.9))}
+
+
+@pytest.fixture(scope="module")
+def spectra(orc):
+    out = {}
+    for name, (n, L) in SPECTRA.items():
+        og = orc.Grid(n, L)
+        v = _well(n, L, 3)
+        out[name] = (n, L, v, np.linalg.eigvalsh(_dense_h(og, v))[:16])
+    return out
+
+
+@pytest.mark.parametrize("precision,ptol", [(0, 6), (0, 8), (1, 5), (1, 6)],
+                         ids=["fp64-6", "fp64-8", "mixed-5", "mixed-6"])
+@pytest.mark.parametrize("spectrum", sorted(SPECTRA))
+def test_sixteen_roots_in_a_full_subspace(pg, torch, spectra, spectrum, precision, ptol):
+    # 16 roots in a 128-vector subspace, checked against the dense spectrum
+    # (the reference algorithm itself does not finish these cases: it locks a
+    # state twice, or corrections inside the subspace wreck its orthonormality).
+    # Eigenvalue error <= |r|^2 / (gap to level 17) <= 1e-10 / 0.0068 for
+    # ptol 5 after the FP64 Rayleigh-Ritz step of the mixed form.
+    n, L, v, ref = spectra[spectrum]
     grid = pg.Grid(n, L)
-    ev, vec, st = grid.solve(dev(torch, v), nroots=16, maxsub=128, maxiter=400, ptol=8, corrflag=3,
-                             precision=precision, refine=2 if precision else 1)
+    ev, vec, st = grid.solve(dev(torch, v), nroots=16, maxsub=128, maxiter=400, ptol=ptol, corrflag=3,
+                             precision=precision, refine=1)
     assert st["nconv"] == 16
-    assert np.max(np.abs(ev - ref)) < 1e-8
+    assert np.max(np.abs(ev - ref)) < (1e-8 if ptol >= 6 else 5e-8)
     V = host(vec)
     assert np.max(np.abs(V @ V.T - np.eye(16))) < 1e-8
 

@@ -175,3 +175,4 @@ def test_fft_apply_is_three_axis_circulants(orc, pg):
     ref = v * x + (np.einsum("ab,kjb->kja", t, X) + np.einsum("ab,kbi->kai", t, X)
                    + np.einsum("ab,bji->aji", t, X)).reshape(-1)
     assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
+
