@@ -616,6 +616,25 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       if (cnt > 0)
         PG_CUDA_TRY(cudaMemcpyAsync(Z + first * N, ritz + first * N, sizeof(double) * N * cnt,
                                     cudaMemcpyDeviceToDevice, st));
+      // The locked vectors are Ritz vectors of an older subspace, so the new
+      // Ritz vectors are orthogonal to them only to O(residual / gap).  The
+      // reference carries that drift on (src/Davidson.cpp:303-346); inside
+      // near-degenerate sets it lets a state be locked twice, and with many
+      // roots it wrecks the basis.  One Cholesky-QR step on the kept block,
+      // applied to B and Z alike (Z = H B stays exact), restores
+      // orthonormality.  With the locked vectors first it only normalises them
+      // and orthogonalises the others against them.  The kept block is
+      // nconv + nnewB = nroots <= 16 vectors.
+      {
+        const int kept = *nconv + d->nnewB;
+        PG_TRY(gram(N, B, kept, B, kept, d->dgram.p, d->rs, st, d->dfloat));
+        k_cholinv<<<1, 32, 0, st>>>(d->dgram.p, kept, d->dcoef.p);
+        PG_TRY(check_launch("k_cholinv"));
+        PG_TRY(combine(N, B, kept, d->dcoef.p, kept, 1, 1.0, nullptr, nullptr, false, B, kept, nullptr, d->rs, st,
+                       d->dfloat));
+        PG_TRY(combine(N, Z, kept, d->dcoef.p, kept, 1, 1.0, nullptr, nullptr, false, Z, kept, nullptr, d->rs, st,
+                       d->dfloat));
+      }
       d->nsub = nroots;
       d->s_valid = 0;
       d->jmacro += 1;
