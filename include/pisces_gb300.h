@@ -198,7 +198,11 @@ pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision);
  * Olsen form -M r + (u.M r / u.M u) M u is used there (detected from diag(H)
  * at the first call).  Not in the reference, whose corrections use diag(H)
  * only (src/Davidson.cpp:530-566); it changes the convergence rate, not the
- * converged eigenpairs.  g must outlive the solve. */
+ * converged eigenpairs.  T - lambda is definite only for Ritz values below
+ * the lowest kinetic level (bound states such as cluster anions); for levels
+ * deep inside the kinetic spectrum (a strong confining well) the corrections
+ * stall and the solve ends in PG_NOT_CONVERGED: use corrflag 1 there.
+ * g must outlive the solve. */
 pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int precision);
 
 /* The subspace eigensolver of the Davidson iteration (host): the k lowest
@@ -244,7 +248,13 @@ long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag);
  * nconv and inout are host.  *ret = 1: compute Z[inout[1]+v] = H B[inout[0]+v]
  * for v < inout[2], then call again; *ret = 0: done (converged eigenpairs in
  * evals_host and B_dev[0..nroots), *nconv converged; PG_NOT_CONVERGED if the
- * macro-iteration limit was reached). */
+ * macro-iteration limit was reached).  Two departures from the reference,
+ * both where its iteration breaks down: locking stops at nroots (inside a
+ * near-degenerate set the reference can lock a state twice and overrun its
+ * arrays), and a restart re-orthonormalises the kept block of B and Z by one
+ * Cholesky-QR step (the reference keeps locked and new Ritz vectors that are
+ * orthogonal only to O(residual / gap)).  PG_NUMERIC if |B v| of a unit
+ * subspace vector still differs from 1 by more than 1e-6. */
 pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int nroots, int maxmacro, int tol, int corrflag,
                           double* evals_host, int* nconv, double* B_dev, double* Z_dev, const double* diag_dev,
                           double* work_dev, int* inout, int* ret, void* stream);
