@@ -86,6 +86,52 @@ struct AxisMap {
   long ncols;     // columns: N * nvec / n
 };
 
+// No staging area: the x-axis epilogue writes straight from the TMEM rows.
+constexpr uint32_t kNoStage = 0xffffffffu;
+constexpr uint32_t kStageWarpBytes = 32 * 16 * 4;  // one warp's 32 x 16 accumulator chunk
+
+// x-axis (AXIS 0) epilogue of one 16-output chunk through shared memory.  Lane
+// L holds the accumulator row of column c0w + L, a grid line along x whose
+// outputs i0 .. i0+15 are consecutive doubles, while neighbouring lanes' lines
+// are nx doubles apart.  The rows go to a 32 x 16 block, XOR-swizzled by row
+// pair so that both the row writes and the column-pair reads hit 32 distinct
+// banks; each global load or store below then covers 16 consecutive outputs of
+// two lines (two 128-byte segments) instead of one output of 32 lines.
+// gshift_own: lane L's vector offset (grid point = address - gshift), passed
+// to the lanes that handle its line.
+__device__ __forceinline__ void epilogue_x16(const float (&d)[16], float* stg, int lane, long c0w, long ncols,
+                                             int i0, int n, int nx, long gshift_own, int mode,
+                                             const double* __restrict__ X, double* __restrict__ Y,
+                                             const double* __restrict__ v) {
+  const int sw = (lane >> 1) & 15;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) stg[lane * 16 + (j ^ sw)] = d[j];
+  __syncwarp();
+  const int j = lane & 15, half = lane >> 4;
+  const int i = i0 + j;
+  double prev[16];
+  float val[16];
+#pragma unroll
+  for (int it = 0; it < 16; ++it) {
+    const int r = 2 * it + half;  // row (line) handled in this round; (r >> 1) & 15 == it
+    val[it] = stg[r * 16 + (j ^ it)];
+    const long gs = (long)__shfl_sync(0xffffffffu, (long long)gshift_own, r);
+    const long c = c0w + r;
+    const long a = (long)nx * c + i;
+    prev[it] = 0.0;
+    if (c < ncols && i < n) {
+      if (mode == 2) prev[it] = v[a - gs] * X[a];
+      else if (mode == 1) prev[it] = Y[a];
+    }
+  }
+#pragma unroll
+  for (int it = 0; it < 16; ++it) {
+    const long c = c0w + 2 * it + half;
+    if (c < ncols && i < n) Y[(long)nx * c + i] = prev[it] + (double)val[it];
+  }
+  __syncwarp();  // the block is rewritten by the warp's next chunk
+}
+
 // base address (element index into X/Y) of column c, and the grid point of
 // its first element, for each axis
 template <int AXIS>
@@ -130,8 +176,11 @@ template <int AXIS>
 __global__ void __launch_bounds__(kThreads, 1)
     k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kc, int nch, uint32_t tmem_cols,
             const float* __restrict__ t_hi, const float* __restrict__ t_lo, const __grid_constant__ TcJobs jobs,
-            int mode, int* __restrict__ err) {
+            int mode, uint32_t stage_off, int* __restrict__ err) {
   // mode 0: Y = D;  1: Y += D;  2: Y = V X + D   (D = the axis contraction)
+  // stage_off (AXIS 0): byte offset of the 16 warps' epilogue blocks in the
+  // dynamic shared memory (it may overlap the A tile, free by then), or
+  // kNoStage
   // K is processed in nch chunks of kc (one chunk for n <= 112): per chunk the
   // A tile and the B chunk are staged, multiplied into the same accumulator,
   // and the shared memory is reused once those MMAs have completed.
@@ -288,7 +337,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int ck = group; ck * 16 < npad; ck += kThreads / 128) {
       float d[16];
       tmem_ld16(tmem + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(ck * 16), d);
-      if (cvalid) {
+      if (AXIS == 0 && stage_off != kNoStage) {
+        float* stg = reinterpret_cast<float*>(smem + stage_off + (uint32_t)warp * kStageWarpBytes);
+        epilogue_x16(d, stg, lane, c0 + 32 * quarter, ncols, ck * 16, n, nx, gshift, mode, X, Y, v);
+      } else if (cvalid) {
         double prev[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -344,7 +396,10 @@ template <int AXIS>
 __global__ void __launch_bounds__(kPipeThreads, 1)
     k_hx_tc_pipe(int nx, int ny, int nz, AxisMap am, int npad, int kc, uint32_t tmem_cols,
                  const float* __restrict__ t_hi, const float* __restrict__ t_lo,
-                 const __grid_constant__ TcJobs jobs, int mode, int* __restrict__ err) {
+                 const __grid_constant__ TcJobs jobs, int mode, uint32_t stage_off, int* __restrict__ err) {
+  // stage_off (AXIS 0): byte offset of the eight consumer warps' epilogue
+  // blocks, after the A tile (which the producers refill meanwhile), or
+  // kNoStage
   extern __shared__ __align__(1024) unsigned char smem[];
   const int n = am.n;
   const uint32_t b_bytes = (uint32_t)npad * kc * 4;
@@ -499,7 +554,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       for (int ck = group; ck * 16 < npad; ck += 2) {
         float d[16];
         tmem_ld16(acc + ((uint32_t)(32 * quarter) << 16) + (uint32_t)(ck * 16), d);
-        if (cvalid) {
+        if (AXIS == 0 && stage_off != kNoStage) {
+          float* stg = reinterpret_cast<float*>(smem + stage_off + (uint32_t)cw * kStageWarpBytes);
+          epilogue_x16(d, stg, lane, c0 + 32 * quarter, ncols, ck * 16, n, nx, gshift, mode, X, Y, v);
+        } else if (cvalid) {
           double prev[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
@@ -603,34 +661,53 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
   const long cap = g_num_sms;
   const int grid = (int)(tiles < cap ? tiles : cap);
   int* err = g->tc_err.p;
+  const size_t a_region = (size_t)2 * kTileM * kc * 4, b_region = (size_t)2 * npad * kc * 4;
   if (nch == 1 && tiles > cap) {  // several tiles per CTA: the pipelined form overlaps them
+    // x-axis epilogue blocks of the eight consumer warps after the A tile
+    const size_t stage = (size_t)(kPipeThreads - kProducers) / 32 * kStageWarpBytes;
+    const bool staged = a == 0 && smem + stage <= (size_t)g_max_dyn;
+    const uint32_t stage_off = staged ? (uint32_t)smem : kNoStage;
+    const size_t smem_p = staged ? smem + stage : smem;
     switch (a) {
       case 0:
-        k_hx_tc_pipe<0><<<grid, kPipeThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
-                                                          jobs, mode, err);
+        k_hx_tc_pipe<0><<<grid, kPipeThreads, smem_p, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
+                                                            jobs, mode, stage_off, err);
         break;
       case 1:
-        k_hx_tc_pipe<1><<<grid, kPipeThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
-                                                          jobs, mode, err);
+        k_hx_tc_pipe<1><<<grid, kPipeThreads, smem_p, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
+                                                            jobs, mode, stage_off, err);
         break;
       default:
-        k_hx_tc_pipe<2><<<grid, kPipeThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
-                                                          jobs, mode, err);
+        k_hx_tc_pipe<2><<<grid, kPipeThreads, smem_p, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
+                                                            jobs, mode, stage_off, err);
     }
     return check_launch("k_hx_tc_pipe");
   }
+  // x-axis epilogue blocks of all 16 warps: in the A tile (free once a tile's
+  // MMAs have completed) when it is large enough, else after it
+  const size_t stage = (size_t)kThreads / 32 * kStageWarpBytes;
+  uint32_t stage_off = kNoStage;
+  size_t smem_t = smem;
+  if (a == 0) {
+    if (a_region >= stage) {
+      stage_off = (uint32_t)b_region;
+    } else if (smem + stage <= (size_t)g_max_dyn) {
+      stage_off = (uint32_t)smem;
+      smem_t = smem + stage;
+    }
+  }
   switch (a) {
     case 0:
-      k_hx_tc<0><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,
-                                               err);
+      k_hx_tc<0><<<grid, kThreads, smem_t, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs,
+                                                 mode, stage_off, err);
       break;
     case 1:
-      k_hx_tc<1><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,
-                                               err);
+      k_hx_tc<1><<<grid, kThreads, smem_t, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs,
+                                                 mode, stage_off, err);
       break;
     default:
-      k_hx_tc<2><<<grid, kThreads, smem, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs, mode,
-                                               err);
+      k_hx_tc<2><<<grid, kThreads, smem_t, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs,
+                                                 mode, stage_off, err);
   }
   return check_launch("k_hx_tc");
 }
