@@ -34,8 +34,6 @@ constexpr int kBatch = 16;  // global loads a thread keeps in flight while filli
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ uint32_t kmajor_off(int r, int k, int kpad) { return pg::tc_kmajor_off(r, k, kpad); }
-
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
   return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
          ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
@@ -144,6 +142,55 @@ __device__ __forceinline__ long col_base(long c, int nx, int ny, long N) {
   const long plane = (long)nx * ny;
   const long vv = c / plane;
   return (c - vv * plane) + N * vv;
+}
+
+// Fill the A operand of one tile: columns c0 .. c0+127 at K values k0 ..
+// k0+kc-1, split into TF32 hi/lo halves in the K-major core-matrix layout.
+// Lane L takes row m = 8 g + (L >> 2) and K index 4 q + (L & 3) of core
+// matrix (g, q), so one warp store fills one 8 x 4 core matrix: 128
+// contiguous bytes, no bank conflicts.  One warp load reads 8 lines x 32 bytes
+// (AXIS 0: four consecutive K of eight grid lines) or 4 rows x 64 bytes (AXIS
+// 1, 2: eight consecutive columns at four K), every sector fully used.  Warp
+// wi of 16 / RG owns the row groups g = wi, wi + 16 / RG, ..., so each lane's
+// column bases are computed once per tile; kBatch loads per thread are in
+// flight before they are split and stored.
+template <int AXIS, int RG>
+__device__ __forceinline__ void fill_a(int wi, int lane, const double* __restrict__ X, long c0, long ncols, int k0,
+                                       int kc, int n, long stride, int nx, int ny, long N, unsigned char* sAh,
+                                       unsigned char* sAl) {
+  static_assert(kBatch % RG == 0, "a load batch covers whole row-group rounds");
+  constexpr int kWarps = (kTileM / 8) / RG;  // warps sharing the fill
+  const int kq = kc >> 2;                    // core matrices along K
+  long base[RG];
+  bool cv[RG];
+#pragma unroll
+  for (int r = 0; r < RG; ++r) {
+    const long c = c0 + 8 * (wi + r * kWarps) + (lane >> 2);
+    cv[r] = c < ncols;
+    base[r] = cv[r] ? (AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) : 0;
+  }
+  const int kl = lane & 3;
+  for (int t0 = 0; t0 < RG * kq; t0 += kBatch) {
+    const int q0 = t0 / RG;
+    double xv[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int q = q0 + u / RG, r = u % RG;
+      const int kk = k0 + 4 * q + kl;
+      xv[u] = (q < kq && kk < n && cv[r]) ? X[base[r] + (long)kk * stride] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int q = q0 + u / RG, r = u % RG;
+      if (q < kq) {
+        float h, l;
+        split_tf32(xv[u], h, l);
+        const uint32_t off = (uint32_t)(((wi + r * kWarps) * kq + q) * 128 + lane * 4);
+        *(float*)(sAh + off) = h;
+        *(float*)(sAl + off) = l;
+      }
+    }
+  }
 }
 
 }  // namespace
@@ -256,34 +303,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int k0 = ch * kc;
       if (nch > 1 && !first && tid == 0) load_b(ch);  // the previous chunk's MMAs have completed
       first = false;
-      // ---- A operand: 128 columns x kc, split into TF32 hi/lo; kBatch loads
-      // per thread in flight, then split and store
-      for (int e0 = tid; e0 < kTileM * kc; e0 += kBatch * kThreads) {
-        double xv[kBatch];
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-          const int e = e0 + u * kThreads;
-          // AXIS 0: a column is a contiguous line, read along K;
-          // AXIS 1, 2: consecutive columns are consecutive addresses, read across columns
-          const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
-          const int k = k0 + (AXIS == 0 ? e - (e / kc) * kc : (e >> 7));
-          const long c = c0 + m;
-          const bool in = e < kTileM * kc && k < n && c < ncols;
-          xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)k * am.stride] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-          const int e = e0 + u * kThreads;
-          if (e < kTileM * kc) {
-            const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
-            const int k = AXIS == 0 ? e - (e / kc) * kc : (e >> 7);
-            float h, l;
-            split_tf32(xv[u], h, l);
-            *(float*)(sAh + kmajor_off(m, k, kc)) = h;
-            *(float*)(sAl + kmajor_off(m, k, kc)) = l;
-          }
-        }
-      }
+      // ---- A operand: 128 columns x kc, split into TF32 hi/lo
+      static_assert(kThreads / 32 == kTileM / 8, "one row group of the A tile per warp");
+      fill_a<AXIS, 1>(warp, lane, X, c0, ncols, k0, kc, n, am.stride, nx, ny, N, sAh, sAl);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       bool bok = true;
@@ -471,30 +493,8 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
       const double* __restrict__ X = jobs.j[jb].x;
       const long ncols = jobs.j[jb].ncols;
       const long c0 = (tile - jobs.j[jb].tile0) * kTileM;
-      for (int e0 = tid; e0 < kTileM * kc; e0 += kBatch * kProducers) {
-        double xv[kBatch];
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-          const int e = e0 + u * kProducers;
-          const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
-          const int kk = AXIS == 0 ? e - (e / kc) * kc : (e >> 7);
-          const long c = c0 + m;
-          const bool in = e < kTileM * kc && kk < n && c < ncols;
-          xv[u] = in ? X[(AXIS == 0 ? (long)nx * c : col_base<AXIS>(c, nx, ny, N)) + (long)kk * am.stride] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < kBatch; ++u) {
-          const int e = e0 + u * kProducers;
-          if (e < kTileM * kc) {
-            const int m = AXIS == 0 ? e / kc : (e & (kTileM - 1));
-            const int kk = AXIS == 0 ? e - (e / kc) * kc : (e >> 7);
-            float h, l;
-            split_tf32(xv[u], h, l);
-            *(float*)(sAh + kmajor_off(m, kk, kc)) = h;
-            *(float*)(sAl + kmajor_off(m, kk, kc)) = l;
-          }
-        }
-      }
+      static_assert(kProducers / 32 == kTileM / 8 / 2, "two row groups of the A tile per producer warp");
+      fill_a<AXIS, 2>(warp, lane, X, c0, ncols, 0, kc, n, am.stride, nx, ny, N, sAh, sAl);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory");  // the A tile is complete
       if (tid == 0) {
