@@ -10,15 +10,19 @@
 //   - S = Z^T B is extended by its new columns only (the reference recomputes
 //     all of it each iteration, src/Davidson.cpp:220, 385-393; the values it
 //     reads -- the upper triangle -- are the same dot products);
-//   - a correction vector is orthogonalised against the basis by block
-//     classical Gram-Schmidt run twice (c = B^T v, v -= B c, twice, then
-//     normalise), where the reference projects and renormalises against one
-//     basis vector at a time, twice each (src/Davidson.cpp:447-474); both
-//     produce the normalised component of v orthogonal to span(B);
+//   - the correction vectors are orthogonalised against the basis and among
+//     themselves as one block, by two passes of block Gram-Schmidt with the
+//     Pythagorean Gram (block_orthonormalise), where the reference projects
+//     and renormalises against one basis vector at a time, twice each
+//     (src/Davidson.cpp:447-514); both produce an orthonormal basis of the
+//     same span;
 //   - the subspace eigenproblem (LAPACK dsyev of all m pairs in the
 //     reference, src/Davidson.cpp:224) computes only the nroots lowest pairs,
 //     the only ones the iteration reads (pg_subspace.cpp), from the same
 //     upper triangle.
+// Two differences do change the subspace, both where the reference's
+// iteration breaks down: locking stops at nroots, and a restart
+// re-orthonormalises the kept block of B and Z (see the restart below).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -259,6 +263,72 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
   return PG_OK;
 }
 
+// Coefficients of one block Gram-Schmidt pass with the Pythagorean Gram (the
+// BCGS-PIP form): the corrections R (k vectors) sit right after the nb basis
+// vectors of B, and G holds the Gram products of [B R] against R,
+// G[a*k + j] = [B R]_a . R_j, so the first nb rows are C = B^T R and the last
+// k rows are R^T R.  With B orthonormal, (R - B C)^T (R - B C) = R^T R - C^T C,
+// whose Cholesky factor L gives U = L^-T; the pass is then one combine over
+// [B R] with coef[a*k + j] = -(C U)[a][j] for a < nb and U[a-nb][j] below.
+// A pivot is floored at 1e-24 of that vector's R^T R diagonal: where the
+// subtraction cancels (R almost inside span(B)) the pass yields scaled
+// rounding noise, mostly orthogonal to B, which the second pass (no
+// cancellation left) projects and normalises.  One block; k <= 16, nb <= 128.
+__global__ void __launch_bounds__(256) k_pip_coef(const double* __restrict__ G, int nb, int k,
+                                                  double* __restrict__ coef) {
+  __shared__ double Cs[128][kMaxCombine];
+  __shared__ double L[kMaxCombine][kMaxCombine + 1];
+  __shared__ double U[kMaxCombine][kMaxCombine + 1];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nb * k; e += blockDim.x) Cs[e / k][e % k] = G[e];
+  __syncthreads();
+  if (tid < k * k) {  // R^T R - C^T C, each entry summed in basis order
+    const int i = tid / k, j = tid % k;
+    double s = G[(long)(nb + i) * k + j];
+    for (int a = 0; a < nb; ++a) s -= Cs[a][i] * Cs[a][j];
+    L[i][j] = s;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    const int lane = tid;
+    for (int j = 0; j < k; ++j) {
+      if (lane == 0) {
+        double s = L[j][j];
+        for (int p = 0; p < j; ++p) s -= L[j][p] * L[j][p];
+        const double floor = 1e-24 * G[(long)(nb + j) * k + j];
+        L[j][j] = sqrt(s > floor ? s : (floor > 1e-300 ? floor : 1e-300));
+      }
+      __syncwarp();
+      if (lane > j && lane < k) {
+        double t = L[lane][j];
+        for (int p = 0; p < j; ++p) t -= L[lane][p] * L[j][p];
+        L[lane][j] = t / L[j][j];
+      }
+      __syncwarp();
+    }
+    if (lane < k) {  // U = L^-T, column c on lane c (upper triangular)
+      const int c = lane;
+      for (int i = k - 1; i >= 0; --i) {
+        double s = i == c ? 1.0 : 0.0;
+        for (int p = i + 1; p < k; ++p) s -= L[p][i] * U[p][c];
+        U[i][c] = i > c ? 0.0 : s / L[i][i];
+      }
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < (nb + k) * k; e += blockDim.x) {
+    const int a = e / k, j = e % k;
+    double s;
+    if (a < nb) {
+      s = 0.0;
+      for (int i = 0; i <= j; ++i) s -= Cs[a][i] * U[i][j];
+    } else {
+      s = U[a - nb][j];
+    }
+    coef[e] = s;
+  }
+}
+
 // C = L^-T for the Cholesky factor of the k x k Gram matrix G (row-major,
 // G[a*k+b] = R_a . R_b), so that R C has orthonormal columns and, C being
 // upper triangular, the same nested spans as Gram-Schmidt.  One warp: lane i
@@ -367,27 +437,24 @@ pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* s
 }
 
 // Orthonormalise the k vectors R (contiguous, R[j*N]) against the first nbas
-// columns of B and among themselves; the result goes to out (k vectors, may
-// equal R).  Two passes, each a block classical Gram-Schmidt step against B
-// followed by Cholesky-QR of the block.  A correction that lies almost inside
-// span(B) leaves an O(eps) remainder whose components along B the first
-// normalisation scales up to O(1); the second pass projects them out again.
-// Same spans as the reference's vector-by-vector orthogonalisation, which
-// also renormalises between projections (src/Davidson.cpp:447-514).
-pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, const double* B, int nbas, double* out,
+// columns of B and among themselves, into B[nbas .. nbas+k) (out must be
+// B + nbas*N; R is copied there first when it lives elsewhere).  Two passes of
+// block Gram-Schmidt with the Pythagorean Gram (k_pip_coef): one Gram over
+// [B R] against R, one coefficient kernel, one combine over [B R] in place.
+// The second pass repairs what the first leaves (rounding, or the cancellation
+// of a correction that lies almost inside span(B)).  Same spans as the
+// reference's vector-by-vector orthogonalisation, which projects and
+// renormalises one vector at a time (src/Davidson.cpp:447-514).
+pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, double* B, int nbas, double* out,
                                cudaStream_t st) {
-  double* c = d->dcoef.p;
-  double* ones = d->dsq.p + kOnes;
+  PG_ARG(out == B + (long)nbas * N && k > 0 && k <= kMaxCombine && nbas + k <= 128,
+         "block_orthonormalise: output must follow the basis (nbas=%d k=%d)", nbas, k);
+  if (R != out) PG_CUDA_TRY(cudaMemcpyAsync(out, R, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
   for (int pass = 0; pass < 2; ++pass) {
-    if (nbas > 0) {
-      // c[a*k + j] = B_a . R_j ;  R_j <- R_j - sum_a B_a c[a*k + j]
-      PG_TRY(gram(N, B, nbas, R, k, c, d->rs, st, d->dfloat));
-      PG_TRY(combine(N, B, nbas, c, k, 1, -1.0, R, ones, false, R, k, nullptr, d->rs, st, d->dfloat));
-    }
-    PG_TRY(gram(N, R, k, R, k, d->dgram.p, d->rs, st, d->dfloat));
-    k_cholinv<<<1, 32, 0, st>>>(d->dgram.p, k, c);
-    PG_TRY(check_launch("k_cholinv"));
-    PG_TRY(combine(N, R, k, c, k, 1, 1.0, nullptr, nullptr, false, pass == 1 ? out : R, k, nullptr, d->rs, st,
+    PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat));
+    k_pip_coef<<<1, 256, 0, st>>>(d->dgram.p, nbas, k, d->dcoef.p);
+    PG_TRY(check_launch("k_pip_coef"));
+    PG_TRY(combine(N, B, nbas + k, d->dcoef.p, k, 1, 1.0, nullptr, nullptr, false, out, k, nullptr, d->rs, st,
                    d->dfloat));
   }
   return PG_OK;
