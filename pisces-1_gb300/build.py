@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               f"-I{INCLUDE}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
 # files whose floating-point evaluation order follows the reference exactly
 NO_FMA = {"pg_potential.cu"}
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
 def _nvcc():

@@ -88,6 +88,36 @@ struct DevBuf {
   }
 };
 
+// Grow-only page-locked host buffer: copies between it and the device are
+// asynchronous (a pageable source or target makes cudaMemcpyAsync stage
+// through a driver buffer, and a device-to-host copy wait for the stream).
+template <typename T>
+struct HostPinned {
+  T* p = nullptr;
+  size_t n = 0;
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+  ~HostPinned() { release(); }
+  pg_status ensure(size_t count) {
+    if (p && n >= count) return PG_OK;
+    release();
+    if (cudaMallocHost(&p, count * sizeof(T)) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      set_error("cudaMallocHost of %zu bytes failed", count * sizeof(T));
+      return PG_OOM;
+    }
+    n = count;
+    return PG_OK;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
 // Byte offset of element (r, k) of a tensor-core operand tile in shared
 // memory: no-swizzle K-major core matrices of 8 rows x 16 bytes (4 FP32/TF32
 // values), K-adjacent core matrices 128 bytes apart, 8-row groups kpad/4 *

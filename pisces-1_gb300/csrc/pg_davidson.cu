@@ -50,6 +50,10 @@ struct pg_davidson {
   pg::DevBuf<double> dcoef;  // maxsub * maxsub coefficients / Gram blocks
   pg::DevBuf<double> dsq;    // device scalars (norms, Ritz values, constants)
   pg::DevBuf<double> dgram;  // small Gram matrices of the Cholesky-QR step
+  // page-locked staging of the per-iteration host<->device copies (offsets
+  // kPin* below); a region is rewritten only after a later stream sync, so
+  // no copy from it is still pending
+  pg::HostPinned<double> hpin;
   // kinetic preconditioner (corrflag 3): grid, arithmetic, work blocks
   const pg_grid* pc_grid = nullptr;
   int pc_precision = PG_FP64;
@@ -246,11 +250,21 @@ constexpr int kDots = 112;  // Jacobi-Davidson dot products (2)
 constexpr int kSigma = 128; // shifts of the kinetic preconditioner (2 x 16)
 constexpr int kScalars = 256;
 
+// Regions of pg_davidson::hpin (doubles)
+constexpr int kPinCols = 0;                    // new S columns, m x nc <= 128 x 128
+constexpr int kPinHsq = kPinCols + 128 * 128;  // |U_r|^2 ... |r_r|^2 (kRsq + 16)
+constexpr int kPinV = kPinHsq + 96;            // Ritz coefficients, maxsub x nroots <= 128 x 16
+constexpr int kPinLam = kPinV + 128 * 16;      // Ritz values (16)
+constexpr int kPinSig = kPinLam + 16;          // preconditioner shifts (2 x 16)
+constexpr int kPinTotal = kPinSig + 32;
+static_assert(kRsq + 16 <= 96, "hsq region");
+
 pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
   // grow-only scratch: a reused handle allocates only while its problems grow
   PG_TRY(d->dcoef.ensure((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
   PG_TRY(d->dgram.ensure((size_t)kMaxGramOut));
   PG_TRY(d->rs.ensure());
+  PG_TRY(d->hpin.ensure(kPinTotal));
   if (!d->dsq.p) {
     PG_TRY(d->dsq.alloc(kScalars));
     std::vector<double> init(kScalars, 0.0);
@@ -541,15 +555,16 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         const int k = std::min(per, nc - cb);
         PG_TRY(gram(N, Z, m, B + (long)(c0 + cb) * N, k, d->dcoef.p + (size_t)cb * m, d->rs, st, d->dfloat));
       }
-      std::vector<double> cols((size_t)m * nc);
-      PG_CUDA_TRY(cudaMemcpyAsync(cols.data(), d->dcoef.p, sizeof(double) * m * nc, cudaMemcpyDeviceToHost, st));
+      const double* cols = d->hpin.p + kPinCols;
       const auto w0 = std::chrono::steady_clock::now();
+      PG_CUDA_TRY(cudaMemcpyAsync(d->hpin.p + kPinCols, d->dcoef.p, sizeof(double) * m * nc, cudaMemcpyDeviceToHost,
+                                  st));
       PG_CUDA_TRY(cudaStreamSynchronize(st));
       d->t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - w0).count();
       // gram output is [a*nb + b] per chunk: a = Z column i, b = new B column
       for (int cb = 0; cb < nc; cb += per) {
         const int k = std::min(per, nc - cb);
-        const double* blk = cols.data() + (size_t)cb * m;
+        const double* blk = cols + (size_t)cb * m;
         for (int i = 0; i < m; ++i)
           for (int b = 0; b < k; ++b) d->S[i + (size_t)(c0 + cb + b) * ms] = blk[(size_t)i * k + b];
       }
@@ -576,8 +591,10 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     double* dlam = d->dsq.p + kLam;
     double* usq = d->dsq.p + kUsq;
     double* rsq = d->dsq.p + kRsq;
-    PG_CUDA_TRY(cudaMemcpyAsync(dV, d->V.data(), sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
-    PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->sse.data(), sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
+    memcpy(d->hpin.p + kPinV, d->V.data(), sizeof(double) * ms * nroots);
+    memcpy(d->hpin.p + kPinLam, d->sse.data(), sizeof(double) * nroots);
+    PG_CUDA_TRY(cudaMemcpyAsync(dV, d->hpin.p + kPinV, sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
+    PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->hpin.p + kPinLam, sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
     PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat));
     PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat));
     {
@@ -596,11 +613,11 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     }
     // |r_r|^2 and |U_r|^2 in one read (rsq and usq both live in dsq)
     static_assert(kUsq == 0 && kRsq > kUsq, "dsq layout");
-    std::vector<double> hsq(kRsq + nroots);
-    PG_CUDA_TRY(cudaMemcpyAsync(hsq.data(), d->dsq.p, sizeof(double) * hsq.size(), cudaMemcpyDeviceToHost, st));
-    const double* hr = hsq.data() + kRsq;
-    const double* hu = hsq.data() + kUsq;
     const auto w1 = std::chrono::steady_clock::now();
+    PG_CUDA_TRY(cudaMemcpyAsync(d->hpin.p + kPinHsq, d->dsq.p, sizeof(double) * (kRsq + nroots),
+                                cudaMemcpyDeviceToHost, st));
+    const double* hr = d->hpin.p + kPinHsq + kRsq;
+    const double* hu = d->hpin.p + kPinHsq + kUsq;
     PG_CUDA_TRY(cudaStreamSynchronize(st));
     d->t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - w1).count();
     for (int r = 0; r < nroots; ++r) {
@@ -747,10 +764,10 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     d->nnewB = (int)sel.size();
     if (corrflag == 3 && d->nnewB > 0 && !d->pc_olsen) {
       // exact-kinetic correction M r_j, M = (T - lambda_j)^-1
-      std::vector<double> sig(d->nnewB);
+      double* sig = d->hpin.p + kPinSig;
       for (int j = 0; j < d->nnewB; ++j) sig[j] = d->sse[sel[j]];
       double* dsig = d->dsq.p + kSigma;
-      PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig.data(), sizeof(double) * d->nnewB, cudaMemcpyHostToDevice, st));
+      PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig, sizeof(double) * d->nnewB, cudaMemcpyHostToDevice, st));
       PG_TRY(kinetic_precondition(d, res, d->nnewB, dsig, st));
     } else if (corrflag == 3 && d->nnewB > 0) {
       // Olsen correction with M = (T - lambda_j)^-1 applied exactly:
@@ -767,10 +784,10 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         PG_CUDA_TRY(cudaMemcpyAsync(RU + (long)(k + j) * N, u, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
       }
       PG_CUDA_TRY(cudaMemcpyAsync(Uc, RU + (long)k * N, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
-      std::vector<double> sig(2 * k);
+      double* sig = d->hpin.p + kPinSig;
       for (int j = 0; j < k; ++j) sig[j] = sig[k + j] = d->sse[sel[j]];
       double* dsig = d->dsq.p + kSigma;
-      PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig.data(), sizeof(double) * 2 * k, cudaMemcpyHostToDevice, st));
+      PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig, sizeof(double) * 2 * k, cudaMemcpyHostToDevice, st));
       PG_TRY(kinetic_precondition(d, RU, 2 * k, dsig, st));  // RU = [M R, M U]
       PG_TRY(gram(N, Uc, k, RU, 2 * k, d->dgram.p, d->rs, st, d->dfloat));
       k_olsen_coef<<<1, 256, 0, st>>>(d->dgram.p, k, d->dcoef.p);

@@ -18,25 +18,21 @@ namespace pg {
 
 namespace {
 
-// Number of eigenvalues of the tridiagonal (d, e) smaller than x (Sturm count).
-int sturm_count(int m, const double* d, const double* e2, double x) {
-  int cnt = 0;
-  double q = d[0] - x;
-  if (q < 0) ++cnt;
-  for (int i = 1; i < m; ++i) {
-    const double prev = q != 0 ? q : 1e-300;
-    q = d[i] - x - e2[i - 1] / prev;
-    if (q < 0) ++cnt;
-  }
-  return cnt;
-}
+// Band storage of the pivoted LU factor of T - lambda I, kept across calls.
+struct TridiagScratch {
+  std::vector<double> u0, u1, u2, l;
+  std::vector<char> swapped;
+  explicit TridiagScratch(int m) : u0(m), u1(m), u2(m), l(m), swapped(m) {}
+};
 
 // Solve (T - lambda I) y = b for tridiagonal T by Gaussian elimination with
 // partial pivoting (in place on b); a tiny pivot is replaced by eps*|T|.
-void tridiag_solve(int m, const double* d, const double* e, double lambda, double tiny, double* b) {
+void tridiag_solve(int m, const double* d, const double* e, double lambda, double tiny, double* b,
+                   TridiagScratch& ts) {
   // bands of the factor: u0 (diagonal), u1, u2 (two super-diagonals after pivoting)
-  std::vector<double> u0(m), u1(m), u2(m), l(m);
-  std::vector<char> swapped(m, 0);
+  double *u0 = ts.u0.data(), *u1 = ts.u1.data(), *u2 = ts.u2.data(), *l = ts.l.data();
+  char* swapped = ts.swapped.data();
+  std::fill(swapped, swapped + m, 0);
   double diag = d[0] - lambda;
   double sup = m > 1 ? e[0] : 0.0;
   for (int i = 0; i < m - 1; ++i) {
@@ -126,12 +122,17 @@ bool lowest_eigenpairs(int m, const double* S, int ld, int k, double* w, double*
     // trailing block A22 <- H A22 H = A22 - v w^T - w v^T,
     // p = beta A22 v, w = p - (beta/2)(p^T v) v
     double* A22 = a.data() + (size_t)(c + 1) * m + (c + 1);
-    for (int i = 0; i < n1; ++i) {
-      double s = 0;
-      const double* row = A22 + (size_t)i * m;
-      for (int j = 0; j < n1; ++j) s += row[j] * v[j];
-      p[i] = beta * s;
+    // p = A22 v as a sum of rows: A22 is exactly symmetric (the rank-2 update
+    // below adds the same two products for (i, j) and (j, i)), so p_i is the
+    // same sum, in the same order of j, as the row-times-vector dot product,
+    // while the inner loop runs over independent i (it vectorises)
+    for (int i = 0; i < n1; ++i) p[i] = 0.0;
+    for (int j = 0; j < n1; ++j) {
+      const double vj = v[j];
+      const double* row = A22 + (size_t)j * m;
+      for (int i = 0; i < n1; ++i) p[i] += row[i] * vj;
     }
+    for (int i = 0; i < n1; ++i) p[i] *= beta;
     double pv = 0;
     for (int i = 0; i < n1; ++i) pv += p[i] * v[i];
     const double half = 0.5 * beta * pv;
@@ -166,27 +167,51 @@ bool lowest_eigenpairs(int m, const double* S, int ld, int k, double* w, double*
   lo -= 4 * eps * tnorm;
   hi += 4 * eps * tnorm;
   const double tol = eps * tnorm;
-  for (int j = 0; j < k; ++j) {
-    double a0 = lo, b0 = hi;
-    for (int it = 0; it < 200 && (b0 - a0) > tol; ++it) {
-      const double mid = 0.5 * (a0 + b0);
-      if (mid == a0 || mid == b0) break;
-      if (sturm_count(m, d.data(), e2.data(), mid) > j) b0 = mid;
-      else a0 = mid;
+  // All k brackets at once: each round evaluates the Sturm counts at the
+  // midpoints of the brackets still open in one pass over the tridiagonal
+  // (their division chains are independent and overlap), and each count c at
+  // x narrows every bracket: eigenvalues 0 .. c-1 lie below x, the rest not.
+  {
+    std::vector<double> blo(k, lo), bhi(k, hi), mids(k), qv(k);
+    std::vector<int> cnt(k);
+    for (int round = 0; round < 200; ++round) {
+      int no = 0;
+      for (int j = 0; j < k; ++j) {
+        const double mid = 0.5 * (blo[j] + bhi[j]);
+        if (bhi[j] - blo[j] > tol && mid != blo[j] && mid != bhi[j]) mids[no++] = mid;
+      }
+      if (no == 0) break;
+      for (int t = 0; t < no; ++t) {
+        qv[t] = d[0] - mids[t];
+        cnt[t] = qv[t] < 0 ? 1 : 0;
+      }
+      for (int i = 1; i < m; ++i) {
+        const double di = d[i], ei2 = e2[i - 1];
+        for (int t = 0; t < no; ++t) {
+          const double prev = qv[t] != 0 ? qv[t] : 1e-300;
+          qv[t] = di - mids[t] - ei2 / prev;
+          cnt[t] += qv[t] < 0 ? 1 : 0;
+        }
+      }
+      for (int t = 0; t < no; ++t)
+        for (int j = 0; j < k; ++j) {
+          if (j < cnt[t]) bhi[j] = std::min(bhi[j], mids[t]);
+          else blo[j] = std::max(blo[j], mids[t]);
+        }
     }
-    w[j] = 0.5 * (a0 + b0);
-    lo = a0;  // the next eigenvalue is not below this one
+    for (int j = 0; j < k; ++j) w[j] = 0.5 * (blo[j] + bhi[j]);
   }
   // --- inverse iteration on the tridiagonal for each wanted vector
   std::vector<double> y((size_t)k * m);
   const double tiny = eps * tnorm;
+  TridiagScratch ts(m);
   for (int j = 0; j < k; ++j) {
     double* yj = y.data() + (size_t)j * m;
     // deterministic, non-degenerate start
     for (int i = 0; i < m; ++i) yj[i] = 1.0 + 0.1 * std::sin(1.0 + 0.7 * i + 1.3 * j);
     const double shift = w[j];
     for (int it = 0; it < 4; ++it) {
-      tridiag_solve(m, d.data(), e.data(), shift, tiny, yj);
+      tridiag_solve(m, d.data(), e.data(), shift, tiny, yj, ts);
       // orthogonalise against the earlier vectors (needed inside clusters of
       // close eigenvalues, harmless elsewhere)
       for (int r = 0; r < j; ++r) {
