@@ -12,9 +12,7 @@
 // TF32 high and low parts, D = Ah*Bh + Ah*Bl + Al*Bh (error ~2^-21 relative per term; Al*Bl dropped),
 // accumulated in FP32 in TMEM.  X is split on the fly from FP64 with integer
 // operations only (the FP64 pipe is two orders of magnitude slower on this
-// part).  Three passes: Y = Tx.X, Y += Ty.X, Y += V X + Tz.X (V X in the
-// z pass, whose epilogue reads V and X along consecutive grid points, not in
-// the x pass, whose columns are grid lines nx doubles apart); X stays L2
+// part).  Three passes: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X; X stays L2
 // resident between passes for the grids of the eigensolve workloads.
 //
 // Operand layout in shared memory: no-swizzle K-major core matrices
@@ -122,7 +120,6 @@ __device__ __forceinline__ void epilogue_x16(const float (&d)[16], float* stg, i
     if (c < ncols && i < n) {
       if (mode == 2) prev[it] = v[a - gs] * X[a];
       else if (mode == 1) prev[it] = Y[a];
-      else if (mode == 3) prev[it] = Y[a] + v[a - gs] * X[a];
     }
   }
 #pragma unroll
@@ -227,7 +224,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_hx_tc(int nx, int ny, int nz, AxisMap am, int npad, int kc, int nch, uint32_t tmem_cols,
             const float* __restrict__ t_hi, const float* __restrict__ t_lo, const __grid_constant__ TcJobs jobs,
             int mode, uint32_t stage_off, int* __restrict__ err) {
-  // mode 0: Y = D;  1: Y += D;  2: Y = V X + D;  3: Y += V X + D   (D = the axis contraction)
+  // mode 0: Y = D;  1: Y += D;  2: Y = V X + D   (D = the axis contraction)
   // stage_off (AXIS 0): byte offset of the 16 warps' epilogue blocks in the
   // dynamic shared memory (it may overlap the A tile, free by then), or
   // kNoStage
@@ -375,7 +372,6 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (i < n) {
             if (mode == 2) prev[j] = v[a - gshift] * X[a];
             else if (mode == 1) prev[j] = Y[a];
-            else if (mode == 3) prev[j] = Y[a] + v[a - gshift] * X[a];
           }
         }
 #pragma unroll
@@ -571,7 +567,6 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
             if (r < n) {
               if (mode == 2) prev[j] = v[a - gshift] * X[a];
               else if (mode == 1) prev[j] = Y[a];
-              else if (mode == 3) prev[j] = Y[a] + v[a - gshift] * X[a];
             }
           }
 #pragma unroll
@@ -726,18 +721,17 @@ pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, c
 pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
                          const int* nvec, int njobs, cudaStream_t st) {
   for (int a = 0; a < 3; ++a)
-    PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 0 : (a == 1 ? 1 : 3), st));
+    PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 2 : 1, st));
   return PG_OK;
 }
 
-// Launches the three axis passes on st: Y = Tx.X, Y += Ty.X, Y += V X + Tz.X.
+// Launches the three axis passes on st: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X.
 // The tensor-core completion waits report a timeout through g->tc_err; with
 // check, the call waits for the stream and returns PG_DEVICE_TIMEOUT if one
 // occurred (the eigensolver checks the word at its own synchronisation points).
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
                    bool check) {
-  for (int a = 0; a < 3; ++a)
-    PG_TRY(tc_axis(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, a == 0 ? 0 : (a == 1 ? 1 : 3), st));
+  for (int a = 0; a < 3; ++a) PG_TRY(tc_axis(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, a == 0 ? 2 : 1, st));
   return check ? check_tc_error(g, st) : PG_OK;
 }
 
