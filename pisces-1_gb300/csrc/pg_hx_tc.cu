@@ -107,25 +107,31 @@ __device__ __forceinline__ void epilogue_x16(const float (&d)[16], float* stg, i
   __syncwarp();
   const int j = lane & 15, half = lane >> 4;
   const int i = i0 + j;
-  double prev[16];
-  float val[16];
+  // 16 rounds in two halves of 8: mode 2 keeps two loads per round in flight,
+  // and 16 rounds of them do not fit the 128 registers of the launch
 #pragma unroll
-  for (int it = 0; it < 16; ++it) {
-    const int r = 2 * it + half;  // row (line) handled in this round; (r >> 1) & 15 == it
-    val[it] = stg[r * 16 + (j ^ it)];
-    const long gs = (long)__shfl_sync(0xffffffffu, (long long)gshift_own, r);
-    const long c = c0w + r;
-    const long a = (long)nx * c + i;
-    prev[it] = 0.0;
-    if (c < ncols && i < n) {
-      if (mode == 2) prev[it] = v[a - gs] * X[a];
-      else if (mode == 1) prev[it] = Y[a];
+  for (int h = 0; h < 16; h += 8) {
+    double prev[8];
+    float val[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int it = h + u;
+      const int r = 2 * it + half;  // row (line) handled in this round; (r >> 1) & 15 == it
+      val[u] = stg[r * 16 + (j ^ it)];
+      const long gs = (long)__shfl_sync(0xffffffffu, (long long)gshift_own, r);
+      const long c = c0w + r;
+      const long a = (long)nx * c + i;
+      prev[u] = 0.0;
+      if (c < ncols && i < n) {
+        if (mode == 2) prev[u] = v[a - gs] * X[a];
+        else if (mode == 1) prev[u] = Y[a];
+      }
     }
-  }
 #pragma unroll
-  for (int it = 0; it < 16; ++it) {
-    const long c = c0w + 2 * it + half;
-    if (c < ncols && i < n) Y[(long)nx * c + i] = prev[it] + (double)val[it];
+    for (int u = 0; u < 8; ++u) {
+      const long c = c0w + 2 * (h + u) + half;
+      if (c < ncols && i < n) Y[(long)nx * c + i] = prev[u] + (double)val[u];
+    }
   }
   __syncwarp();  // the block is rewritten by the warp's next chunk
 }
