@@ -50,6 +50,13 @@ struct pg_davidson {
   pg::DevBuf<double> dcoef;  // maxsub * maxsub coefficients / Gram blocks
   pg::DevBuf<double> dsq;    // device scalars (norms, Ritz values, constants)
   pg::DevBuf<double> dgram;  // small Gram matrices of the Cholesky-QR step
+  // double-float twins of B and Z (a float2 (hi, lo) per point, the form the
+  // double-float kernels compute with), kept next to the FP64 arrays in the
+  // mixed form so that B and Z are not converted again by every kernel that
+  // reads them; Z rows [0, zt_valid) have current twins, B rows always do
+  // where the double-float kernels read them
+  pg::DevBuf<double> bt, zt;
+  int zt_valid = 0;
   // page-locked staging of the per-iteration host<->device copies (offsets
   // kPin* below); a region is rewritten only after a later stream sync, so
   // no copy from it is still pending
@@ -265,6 +272,11 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
   PG_TRY(d->dgram.ensure((size_t)kMaxGramOut));
   PG_TRY(d->rs.ensure());
   PG_TRY(d->hpin.ensure(kPinTotal));
+  if (d->dfloat) {
+    PG_TRY(d->bt.ensure((size_t)maxsub * ndim));
+    PG_TRY(d->zt.ensure((size_t)maxsub * ndim));
+  }
+  d->zt_valid = 0;
   if (!d->dsq.p) {
     PG_TRY(d->dsq.alloc(kScalars));
     std::vector<double> init(kScalars, 0.0);
@@ -464,12 +476,18 @@ pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, double*
   PG_ARG(out == B + (long)nbas * N && k > 0 && k <= kMaxCombine && nbas + k <= 128,
          "block_orthonormalise: output must follow the basis (nbas=%d k=%d)", nbas, k);
   if (R != out) PG_CUDA_TRY(cudaMemcpyAsync(out, R, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
+  // mixed form: both passes read the twins of [B R] and the combines write the
+  // twin of their output, so [B R] is converted once (R here, B as it was
+  // written)
+  double* Bt = d->dfloat ? d->bt.p : nullptr;
+  double* Rt = Bt ? Bt + (long)nbas * N : nullptr;
+  if (Bt) PG_TRY(split_twin(N * k, out, Rt, st));
   for (int pass = 0; pass < 2; ++pass) {
-    PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat));
+    PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat, Bt, Rt));
     k_pip_coef<<<1, 256, 0, st>>>(d->dgram.p, nbas, k, d->dcoef.p);
     PG_TRY(check_launch("k_pip_coef"));
     PG_TRY(combine(N, B, nbas + k, d->dcoef.p, k, 1, 1.0, nullptr, nullptr, false, out, k, nullptr, d->rs, st,
-                   d->dfloat));
+                   d->dfloat, Bt, Rt));
   }
   return PG_OK;
 }
@@ -551,9 +569,14 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       const int c0 = d->s_valid;
       const int nc = m - c0;
       const int per = std::max(1, std::min(kMaxGramOut / m, std::min(16, 144 - m)));
+      if (d->dfloat && d->zt_valid < m) {  // twins of the Z rows the caller has just written
+        PG_TRY(split_twin((long)(m - d->zt_valid) * N, Z + (long)d->zt_valid * N, d->zt.p + (long)d->zt_valid * N, st));
+        d->zt_valid = m;
+      }
       for (int cb = 0; cb < nc; cb += per) {
         const int k = std::min(per, nc - cb);
-        PG_TRY(gram(N, Z, m, B + (long)(c0 + cb) * N, k, d->dcoef.p + (size_t)cb * m, d->rs, st, d->dfloat));
+        PG_TRY(gram(N, Z, m, B + (long)(c0 + cb) * N, k, d->dcoef.p + (size_t)cb * m, d->rs, st, d->dfloat,
+                    d->dfloat ? d->zt.p : nullptr, d->dfloat ? d->bt.p + (long)(c0 + cb) * N : nullptr));
       }
       const double* cols = d->hpin.p + kPinCols;
       const auto w0 = std::chrono::steady_clock::now();
@@ -595,8 +618,10 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     memcpy(d->hpin.p + kPinLam, d->sse.data(), sizeof(double) * nroots);
     PG_CUDA_TRY(cudaMemcpyAsync(dV, d->hpin.p + kPinV, sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
     PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->hpin.p + kPinLam, sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
-    PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat));
-    PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat));
+    PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat,
+                   d->dfloat ? d->bt.p : nullptr));
+    PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat,
+                   d->dfloat ? d->zt.p : nullptr));
     {
       const long chunk = (N + kRedBlocks - 1) / kRedBlocks;
       const int nblk = (int)((N + chunk - 1) / chunk);
@@ -693,7 +718,7 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         if (d->ccode[r] > 0) {
           const int jz = d->bindex[r];
           PG_TRY(combine(N, Z, d->nsub, dV + (size_t)r * ms, 1, ms, 1.0, nullptr, nullptr, false,
-                         ritz + (long)jz * N, 1, nullptr, d->rs, st, d->dfloat));
+                         ritz + (long)jz * N, 1, nullptr, d->rs, st, d->dfloat, d->dfloat ? d->zt.p : nullptr));
         }
       const long first = *nconv - newly;
       const long cnt = (long)(d->nnewB + newly);
@@ -714,10 +739,13 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
         PG_TRY(gram(N, B, kept, B, kept, d->dgram.p, d->rs, st, d->dfloat));
         k_cholinv<<<1, 32, 0, st>>>(d->dgram.p, kept, d->dcoef.p);
         PG_TRY(check_launch("k_cholinv"));
+        // the copies above left these rows' twins stale: read B and Z, write
+        // fresh twins
         PG_TRY(combine(N, B, kept, d->dcoef.p, kept, 1, 1.0, nullptr, nullptr, false, B, kept, nullptr, d->rs, st,
-                       d->dfloat));
+                       d->dfloat, nullptr, d->dfloat ? d->bt.p : nullptr));
         PG_TRY(combine(N, Z, kept, d->dcoef.p, kept, 1, 1.0, nullptr, nullptr, false, Z, kept, nullptr, d->rs, st,
-                       d->dfloat));
+                       d->dfloat, nullptr, d->dfloat ? d->zt.p : nullptr));
+        d->zt_valid = kept;
       }
       d->nsub = nroots;
       d->s_valid = 0;

@@ -268,10 +268,14 @@ inline GramGeom gram_geometry(int na, int nb) {
 
 // kPair: N even and P, Q 16-byte aligned, so that consecutive point pairs
 // are copied with 16-byte cp.async and converted two at a time.
+// split_p / split_q: the rows of P / Q are already double-float "twins" (a
+// float2 (hi, lo) per point, the layout the staging converts to), copied as
+// they are and not converted again.
 template <bool kPair>
 __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
                                                    const double* __restrict__ Q, int nb, int tp, int m, int S,
-                                                   int ablk, int nblk, double* __restrict__ partial) {
+                                                   int ablk, int nblk, int split_p, int split_q,
+                                                   double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char gsm[];
   const int rows = na + nb;
   const int hp = tp >> 1;  // point pairs per tile row
@@ -334,6 +338,7 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
     double* cur = stage0 + (size_t)(it % kGStages) * stage_elems;
     // convert the points this thread copied, in place, to (hi, lo) pairs
     for (int row = warp; row < rows; row += kT / 32) {
+      if (row < na ? split_p : split_q) continue;  // a twin row: already (hi, lo)
       double* d = cur + (size_t)row * tp;
       if (kPair) {
         for (int q = lane; q < hp; q += 32) {
@@ -400,11 +405,15 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
 
 // Combine in double-float: same contract as k_combine (coefficients and
 // alpha are FP64 and split once per block; Y is written as double).
+// split_p: the rows of P are double-float twins (float2 (hi, lo) per point)
+// and are read without converting; Yt (optional): each output is also
+// written as its twin.
 template <int NR>
 __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const double* P, int na,
                                                    const double* __restrict__ C, int ca, int cr, double cscale,
                                                    const double* X, const double* __restrict__ alpha, int inv_sqrt,
-                                                   double* Y, int nr, double* __restrict__ partial) {
+                                                   double* Y, int nr, int split_p, float2* Yt,
+                                                   double* __restrict__ partial) {
   extern __shared__ float smf[];
   float* Ch = smf;              // na x nr
   float* Cl = smf + na * nr;
@@ -451,7 +460,12 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
       for (int u = 0; u < kBatch; ++u) {
         if (a0 + u >= na) break;
         float ph, pl;
-        df_split(pv[u], ph, pl);
+        if (split_p) {  // the 8 bytes are a float2 (hi, lo): hi in the low word
+          ph = __int_as_float(__double2loint(pv[u]));
+          pl = __int_as_float(__double2hiint(pv[u]));
+        } else {
+          df_split(pv[u], ph, pl);
+        }
         const float* ch = Ch + (a0 + u) * nr;
         const float* cl = Cl + (a0 + u) * nr;
 #pragma unroll
@@ -464,6 +478,11 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
       if (r < nr) {
         const double y = (double)sh[r] + (double)sl[r];
         Y[(long)r * N + g] = y;
+        if (Yt) {
+          float h, l;
+          df_split(y, h, l);
+          Yt[(long)r * N + g] = make_float2(h, l);
+        }
         sacc[r] += y * y;
       }
   }
@@ -506,6 +525,15 @@ pg_status RedScratch::ensure() {
   return PG_OK;
 }
 
+// Double-float twins of count doubles: t[i] = (hi, lo) of x[i] (df_split).
+__global__ void __launch_bounds__(kT) k_split_twin(long count, const double* __restrict__ x, float2* __restrict__ t) {
+  for (long i = blockIdx.x * (long)kT + threadIdx.x; i < count; i += (long)gridDim.x * kT) {
+    float h, l;
+    df_split(x[i], h, l);
+    t[i] = make_float2(h, l);
+  }
+}
+
 // 16-byte copies of point pairs: every row start 16-byte aligned
 inline bool pair_ok(long N, const double* P, const double* Q) {
   return N % 2 == 0 && ((uintptr_t)P % 16) == 0 && ((uintptr_t)Q % 16) == 0;
@@ -528,7 +556,7 @@ static pg_status opt_in_smem() {
 }
 
 pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs,
-               cudaStream_t st, bool dfloat) {
+               cudaStream_t st, bool dfloat, const double* Pt, const double* Qt) {
   PG_ARG(na > 0 && nb > 0 && na * nb <= kMaxGramOut && na + nb <= 144, "gram: %d x %d outputs exceed the limits",
          na, nb);
   PG_TRY(rs.ensure());
@@ -540,12 +568,15 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
     PG_ARG(gg.nblk <= kT, "gram: %d output blocks", gg.nblk);  // at most ~160 within the limits above
     const long dchunk = chunk_for(N, kRedBlocks, gg.tp);
     const int dblocks = (int)((N + dchunk - 1) / dchunk);
-    if (pair_ok(N, P, Q))
-      k_gram_df<true><<<dblocks, kT, gg.smem, st>>>(N, dchunk, P, na, Q, nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
-                                                     rs.partial.p);
+    const double* Ps = Pt ? Pt : P;
+    const double* Qs = Qt ? Qt : Q;
+    const int sp = Pt ? 1 : 0, sq = Qt ? 1 : 0;
+    if (pair_ok(N, Ps, Qs))
+      k_gram_df<true><<<dblocks, kT, gg.smem, st>>>(N, dchunk, Ps, na, Qs, nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
+                                                     sp, sq, rs.partial.p);
     else
-      k_gram_df<false><<<dblocks, kT, gg.smem, st>>>(N, dchunk, P, na, Q, nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
-                                                      rs.partial.p);
+      k_gram_df<false><<<dblocks, kT, gg.smem, st>>>(N, dchunk, Ps, na, Qs, nb, gg.tp, gg.m, gg.S, gg.ablk,
+                                                      gg.nblk, sp, sq, rs.partial.p);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(rs.partial.p, dblocks, na * nb, out, false, st);
   } else {
@@ -558,7 +589,7 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
 
 pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
-                  cudaStream_t st, bool dfloat) {
+                  cudaStream_t st, bool dfloat, const double* Pt, double* Yt) {
   PG_ARG(nr > 0 && nr <= kMaxCombine && na >= 0 && na * nr <= 128 * kMaxCombine, "combine: bad sizes na=%d nr=%d",
          na, nr);
   PG_TRY(rs.ensure());
@@ -567,8 +598,9 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
   const int blocks = (int)((N + chunk - 1) / chunk);
   if (dfloat) {
     const size_t smem = sizeof(float) * 2 * (size_t)(na > 0 ? na : 1) * nr;
-#define PG_COMBINE_DF(NRV) \
-  k_combine_df<NRV><<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, \
+#define PG_COMBINE_DF(NRV)                                                                                  \
+  k_combine_df<NRV><<<blocks, kT, smem, st>>>(N, chunk, Pt ? Pt : P, na, C, ca, cr, cscale, X, alpha,             \
+                                              inv_sqrt ? 1 : 0, Y, nr, Pt ? 1 : 0, reinterpret_cast<float2*>(Yt), \
                                               sq ? rs.partial.p : nullptr)
     if (nr <= 1) PG_COMBINE_DF(1);
     else if (nr <= 2) PG_COMBINE_DF(2);
@@ -591,6 +623,13 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
     PG_TRY(check_launch("k_combine"));
   }
   return sq ? reduce(rs.partial.p, blocks, nr, sq, true, st) : PG_OK;
+}
+
+pg_status split_twin(long count, const double* x, double* t, cudaStream_t st) {
+  if (count <= 0) return PG_OK;
+  const long b = (count + kT - 1) / kT;
+  k_split_twin<<<(int)(b < 152L * 8 ? b : 152L * 8), kT, 0, st>>>(count, x, reinterpret_cast<float2*>(t));
+  return check_launch("k_split_twin");
 }
 
 
@@ -671,11 +710,11 @@ extern "C" pg_status pg_block_gram_noalloc(long n, const double* P, int np, cons
     const long chunk = chunk_for(n, pg::kRedBlocks, gg.tp);
     const int blocks = (int)((n + chunk - 1) / chunk);
     if (pair_ok(n, P, Q))
-      k_gram_df<true><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
-                                                    partial);
+      k_gram_df<true><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, 0,
+                                                    0, partial);
     else
-      k_gram_df<false><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
-                                                     partial);
+      k_gram_df<false><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, 0,
+                                                     0, partial);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(partial, blocks, no, out, false, st);
   }

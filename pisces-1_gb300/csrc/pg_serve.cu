@@ -137,8 +137,9 @@ extern "C" double pg_request_footprint(const pg_request* r) {
   const double ms = r->params.maxsub, nr = r->params.nroots;
   const double work = r->params.corrflag == 2 ? 2 * nr + 1 : 2 * nr;  // pg_davidson_work_size
   const double pc = r->params.corrflag == 3 ? 7 * nr : 0;            // preconditioner blocks (2 x 2nr work, 3nr)
+  const double twins = r->params.precision == PG_MIXED ? 2 * ms : 0;  // double-float twins of the basis and products
   // basis + products, work array, diagonal, potential, eigenvectors
-  return 8.0 * (N * (2 * ms + work + 1 + 1 + nr + pc) + 2 * ms * ms + 11 * ms);
+  return 8.0 * (N * (2 * ms + twins + work + 1 + 1 + nr + pc) + 2 * ms * ms + 11 * ms);
 }
 
 pg_status pg_engine::grid_for(const pg_request& r, pg_grid** out) {
