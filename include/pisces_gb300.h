@@ -355,7 +355,8 @@ typedef struct {
 } pg_engine_stats;
 
 /* Footprint of one request in device bytes: the solve buffers (basis and
- * product blocks, work array, diagonal, potential, eigenvectors). */
+ * product blocks, their double-float twins in the mixed form, work array,
+ * diagonal, potential, eigenvectors). */
 double pg_request_footprint(const pg_request* r);
 pg_status pg_engine_create(const pg_engine_config* c, pg_engine** out);
 /* Copies the request's host data; returns at once.  PG_OOM if the request
