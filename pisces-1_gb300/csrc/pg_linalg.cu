@@ -405,15 +405,16 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
 
 // Combine in double-float: same contract as k_combine (coefficients and
 // alpha are FP64 and split once per block; Y is written as double).
-// split_p: the rows of P are double-float twins (float2 (hi, lo) per point)
-// and are read without converting; Yt (optional): each output is also
-// written as its twin.
-template <int NR>
-__global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const double* P, int na,
+// kTwinIn: the rows of P are double-float twins (float2 (hi, lo) per point)
+// and are read without converting; kTwinOut: each output is also written as
+// its twin to Yt.  Compile-time flags: a runtime choice inside the unrolled
+// loop doubles the registers of the kernel and halves its occupancy.  Up to 4
+// outputs the kernel fits 64 registers (4 blocks per SM, no spills).
+template <int NR, bool kTwinIn, bool kTwinOut>
+__global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long chunk, const double* P, int na,
                                                    const double* __restrict__ C, int ca, int cr, double cscale,
                                                    const double* X, const double* __restrict__ alpha, int inv_sqrt,
-                                                   double* Y, int nr, int split_p, float2* Yt,
-                                                   double* __restrict__ partial) {
+                                                   double* Y, int nr, float2* Yt, double* __restrict__ partial) {
   extern __shared__ float smf[];
   float* Ch = smf;              // na x nr
   float* Cl = smf + na * nr;
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
       for (int u = 0; u < kBatch; ++u) {
         if (a0 + u >= na) break;
         float ph, pl;
-        if (split_p) {  // the 8 bytes are a float2 (hi, lo): hi in the low word
+        if (kTwinIn) {  // the 8 bytes are a float2 (hi, lo): hi in the low word
           ph = __int_as_float(__double2loint(pv[u]));
           pl = __int_as_float(__double2hiint(pv[u]));
         } else {
@@ -478,11 +479,9 @@ __global__ void __launch_bounds__(kT) k_combine_df(long N, long chunk, const dou
       if (r < nr) {
         const double y = (double)sh[r] + (double)sl[r];
         Y[(long)r * N + g] = y;
-        if (Yt) {
-          float h, l;
-          df_split(y, h, l);
-          Yt[(long)r * N + g] = make_float2(h, l);
-        }
+        // the accumulator pair is the output in double-float form already
+        // (it and y = sh + sl agree to 2^-53 relative)
+        if (kTwinOut) Yt[(long)r * N + g] = make_float2(sh[r], sl[r]);
         sacc[r] += y * y;
       }
   }
@@ -598,16 +597,24 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
   const int blocks = (int)((N + chunk - 1) / chunk);
   if (dfloat) {
     const size_t smem = sizeof(float) * 2 * (size_t)(na > 0 ? na : 1) * nr;
-#define PG_COMBINE_DF(NRV)                                                                                  \
-  k_combine_df<NRV><<<blocks, kT, smem, st>>>(N, chunk, Pt ? Pt : P, na, C, ca, cr, cscale, X, alpha,             \
-                                              inv_sqrt ? 1 : 0, Y, nr, Pt ? 1 : 0, reinterpret_cast<float2*>(Yt), \
-                                              sq ? rs.partial.p : nullptr)
+#define PG_COMBINE_DF3(NRV, TI, TO)                                                                          \
+  k_combine_df<NRV, TI, TO><<<blocks, kT, smem, st>>>(N, chunk, Pt ? Pt : P, na, C, ca, cr, cscale, X, alpha,      \
+                                                      inv_sqrt ? 1 : 0, Y, nr, reinterpret_cast<float2*>(Yt),     \
+                                                      sq ? rs.partial.p : nullptr)
+#define PG_COMBINE_DF(NRV)                                             \
+  do {                                                                 \
+    if (Pt && Yt) PG_COMBINE_DF3(NRV, true, true);                     \
+    else if (Pt) PG_COMBINE_DF3(NRV, true, false);                     \
+    else if (Yt) PG_COMBINE_DF3(NRV, false, true);                     \
+    else PG_COMBINE_DF3(NRV, false, false);                            \
+  } while (0)
     if (nr <= 1) PG_COMBINE_DF(1);
     else if (nr <= 2) PG_COMBINE_DF(2);
     else if (nr <= 4) PG_COMBINE_DF(4);
     else if (nr <= 8) PG_COMBINE_DF(8);
     else PG_COMBINE_DF(16);
 #undef PG_COMBINE_DF
+#undef PG_COMBINE_DF3
     PG_TRY(check_launch("k_combine_df"));
   } else {
     const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
