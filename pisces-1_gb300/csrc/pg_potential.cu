@@ -3,7 +3,9 @@
 // Compiled with -fmad=false: every product and sum is rounded separately, in
 // the reference's evaluation order.  The differences from the CPU code are
 // last-place ones: exp/erf, and the undamped inverse powers of R taken from
-// one reciprocal square root per site instead of a square root and divisions.
+// one reciprocal square root per site instead of a square root and divisions;
+// and a Slater core term c exp(-z R) with z R > 50 (below 2e-22 c) is not
+// added.
 //
 // Layout: the reference's per-term lists (charges, dipoles, Slater cores,
 // polarisable sites, each with a site index) are packed on the host into one
@@ -60,6 +62,8 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phas
   }
   return false;
 }
+
+constexpr double kStoCut = 50.0;  // z R beyond which a Slater core term is dropped
 
 __device__ __forceinline__ double reff(double r, double r0) {
   // Effective-distance damping (DampType 2), src/Potential.cpp:1192-1196.
@@ -140,9 +144,18 @@ __global__ void __launch_bounds__(kThreads) k_potential_dpp(
           }
           vind += -(rx * R[R_MX] + ry * R[R_MY] + rz * R[R_MZ]) * m3;
         }
-        const int nsto = (flags >> 3) & 3;                    // :1301-1308
-        if (nsto > 0) vrep += R[R_C0] * exp(-R[R_Z0] * r);
-        if (nsto > 1) vrep += R[R_C1] * exp(-R[R_Z1] * r);
+        // repulsive Slater cores c exp(-z R) (:1301-1308); a term with
+        // z R > kStoCut is below c e^-50 (< 1e-20 Eh for the water model's
+        // c <= 43) and is not evaluated
+        const int nsto = (flags >> 3) & 3;
+        if (nsto > 0) {
+          const double zr = R[R_Z0] * r;
+          if (zr < kStoCut) vrep += R[R_C0] * exp(-zr);
+        }
+        if (nsto > 1) {
+          const double zr = R[R_Z1] * r;
+          if (zr < kStoCut) vrep += R[R_C1] * exp(-zr);
+        }
         if (flags & F_POL) {                                  // :1350-1366
           if (r < dp) {
             const double re = reff(r, dp);
