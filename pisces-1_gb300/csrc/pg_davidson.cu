@@ -86,13 +86,6 @@ namespace {
 
 constexpr int kT = 256;
 
-// Hands the launches queued so far on st to the device without waiting (the
-// driver may otherwise hold them until the next synchronisation), so that the
-// device works while the host goes on enqueueing the rest of a phase.
-inline void submit(cudaStream_t st) {
-  if (cudaStreamQuery(st) == cudaErrorNotReady) cudaGetLastError();
-}
-
 int blocks_for(long N) {
   long b = (N + kT - 1) / kT;
   return (int)(b < 152L * 8 ? (b > 0 ? b : 1) : 152L * 8);
@@ -627,7 +620,6 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->hpin.p + kPinLam, sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
     PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat,
                    d->dfloat ? d->bt.p : nullptr));
-    submit(st);
     PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat,
                    d->dfloat ? d->zt.p : nullptr));
     {
@@ -804,7 +796,6 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       for (int j = 0; j < d->nnewB; ++j) sig[j] = d->sse[sel[j]];
       double* dsig = d->dsq.p + kSigma;
       PG_CUDA_TRY(cudaMemcpyAsync(dsig, sig, sizeof(double) * d->nnewB, cudaMemcpyHostToDevice, st));
-      submit(st);
       PG_TRY(kinetic_precondition(d, res, d->nnewB, dsig, st));
     } else if (corrflag == 3 && d->nnewB > 0) {
       // Olsen correction with M = (T - lambda_j)^-1 applied exactly:
@@ -964,7 +955,6 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
     if (ret == 1) {
       // the whole block in one launch (the reference multiplies vector by vector)
       PG_TRY(matvec(B.p + (long)inout[0] * N, Z.p + (long)inout[1] * N, inout[2]));
-      submit(st);
       nmv += inout[2];
     }
   }
