@@ -92,12 +92,14 @@ int blocks_for(long N) {
 }
 
 // ritz_r = U_r / |U_r|;  res_r = W_r - lambda_r ritz_r   (src/Davidson.cpp:240-260),
-// with per-block partial sums of |res_r|^2 (reduced by reduce_partials).
-// uinv[r] = 1/|U_r| (written by the combine that formed U).
+// with per-block partial sums of |res_r|^2, reduced by the last block into
+// rsq (|res_r|^2, then 1/|res_r|).  uinv[r] = 1/|U_r| (written by the
+// combine that formed U).
 template <int NR>
 __global__ void __launch_bounds__(kT) k_ritz_residual(long N, long chunk, int nr, double* __restrict__ U,
                                                       double* __restrict__ W, const double* __restrict__ uinv,
-                                                      const double* __restrict__ lam, double* __restrict__ partial) {
+                                                      const double* __restrict__ lam, double* __restrict__ partial,
+                                                      double* rsq, unsigned* counter) {
   __shared__ double red[kT / 32][NR];
   double inv[NR], nl[NR], acc[NR];
 #pragma unroll
@@ -139,6 +141,7 @@ __global__ void __launch_bounds__(kT) k_ritz_residual(long N, long chunk, int nr
     for (int w = 0; w < kT / 32; ++w) t += red[w][threadIdx.x];
     partial[(long)blockIdx.x * nr + threadIdx.x] = t;
   }
+  reduce_in_last_block(partial, nr, rsq, 1, counter);
 }
 
 // Davidson correction (lambda - diag H)^-1 r with the 1e-12 floor
@@ -626,7 +629,8 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       const long chunk = (N + kRedBlocks - 1) / kRedBlocks;
       const int nblk = (int)((N + chunk - 1) / chunk);
 #define PG_RITZ(NRV) \
-  k_ritz_residual<NRV><<<nblk, kT, 0, st>>>(N, chunk, nroots, ritz, res, usq + nroots, dlam, d->rs.partial.p)
+  k_ritz_residual<NRV><<<nblk, kT, 0, st>>>(N, chunk, nroots, ritz, res, usq + nroots, dlam, d->rs.partial.p, rsq, \
+                                            d->rs.counter.p)
       if (nroots <= 1) PG_RITZ(1);
       else if (nroots <= 2) PG_RITZ(2);
       else if (nroots <= 4) PG_RITZ(4);
@@ -634,7 +638,6 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       else PG_RITZ(16);
 #undef PG_RITZ
       PG_TRY(check_launch("k_ritz_residual"));
-      PG_TRY(reduce_partials(d->rs.partial.p, nblk, nroots, rsq, true, st));
     }
     // |r_r|^2 and |U_r|^2 in one read (rsq and usq both live in dsq)
     static_assert(kUsq == 0 && kRsq > kUsq, "dsq layout");

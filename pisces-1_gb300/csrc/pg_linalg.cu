@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
                                                 const double* __restrict__ C, int ca, int cr, double cscale,
                                                 const double* X,
                                                 const double* __restrict__ alpha, int inv_sqrt, double* Y, int nr,
-                                                double* __restrict__ partial) {
+                                                double* __restrict__ partial, double* sq_out, unsigned* counter) {
   extern __shared__ double sm[];
   double* Cs = sm;                 // na x nr
   __shared__ double al[NR];
@@ -168,6 +168,7 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
     for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
     partial[(long)blockIdx.x * nr + threadIdx.x] = s;
   }
+  reduce_in_last_block(partial, nr, sq_out, 1, counter);
 }
 
 // ------------------------------------------------------------------------
@@ -414,7 +415,8 @@ template <int NR, bool kTwinIn, bool kTwinOut>
 __global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long chunk, const double* P, int na,
                                                    const double* __restrict__ C, int ca, int cr, double cscale,
                                                    const double* X, const double* __restrict__ alpha, int inv_sqrt,
-                                                   double* Y, int nr, float2* Yt, double* __restrict__ partial) {
+                                                   double* Y, int nr, float2* Yt, double* __restrict__ partial,
+                                                   double* sq_out, unsigned* counter) {
   extern __shared__ float smf[];
   float* Ch = smf;              // na x nr
   float* Cl = smf + na * nr;
@@ -499,6 +501,7 @@ __global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long
     for (int w = 0; w < kT / 32; ++w) s += red[w][threadIdx.x];
     partial[(long)blockIdx.x * nr + threadIdx.x] = s;
   }
+  reduce_in_last_block(partial, nr, sq_out, 1, counter);
 }
 
 pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st);
@@ -521,6 +524,10 @@ pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_m
 
 pg_status RedScratch::ensure() {
   if (!partial.p) PG_TRY(partial.alloc((size_t)kRedBlocks * kMaxGramOut));
+  if (!counter.p) {
+    PG_TRY(counter.alloc(1));
+    PG_CUDA_TRY(cudaMemset(counter.p, 0, sizeof(unsigned)));
+  }
   return PG_OK;
 }
 
@@ -600,7 +607,7 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
 #define PG_COMBINE_DF3(NRV, TI, TO)                                                                          \
   k_combine_df<NRV, TI, TO><<<blocks, kT, smem, st>>>(N, chunk, Pt ? Pt : P, na, C, ca, cr, cscale, X, alpha,      \
                                                       inv_sqrt ? 1 : 0, Y, nr, reinterpret_cast<float2*>(Yt),     \
-                                                      sq ? rs.partial.p : nullptr)
+                                                      sq ? rs.partial.p : nullptr, sq, rs.counter.p)
 #define PG_COMBINE_DF(NRV)                                             \
   do {                                                                 \
     if (Pt && Yt) PG_COMBINE_DF3(NRV, true, true);                     \
@@ -620,7 +627,7 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
     const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
 #define PG_COMBINE(NRV) \
   k_combine<NRV><<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, \
-                                           sq ? rs.partial.p : nullptr)
+                                           sq ? rs.partial.p : nullptr, sq, rs.counter.p)
     if (nr <= 1) PG_COMBINE(1);
     else if (nr <= 2) PG_COMBINE(2);
     else if (nr <= 4) PG_COMBINE(4);
@@ -629,7 +636,7 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
 #undef PG_COMBINE
     PG_TRY(check_launch("k_combine"));
   }
-  return sq ? reduce(rs.partial.p, blocks, nr, sq, true, st) : PG_OK;
+  return PG_OK;  // with sq, the kernel's last block has reduced the norms
 }
 
 pg_status split_twin(long count, const double* x, double* t, cudaStream_t st) {

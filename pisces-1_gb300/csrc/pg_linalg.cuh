@@ -1,9 +1,11 @@
 // Skinny FP64 linear algebra of the Davidson subspace on the device.
 //
-// Every reduction is deterministic: blocks write partial sums, and a second
-// launch adds the partials of each output in a fixed order.  Results
-// therefore do not depend on scheduling, which keeps a solve bit-identical
-// whether it runs alone or next to other solves.
+// Every reduction is deterministic: blocks write partial sums, and the
+// partials of each output are added in a fixed order -- by a second launch,
+// or, for the few-output norms, by whichever block of the producing kernel
+// finishes last (reduce_in_last_block), in the same order.  Results therefore
+// do not depend on scheduling, which keeps a solve bit-identical whether it
+// runs alone or next to other solves.
 #pragma once
 
 #include "pg_common.cuh"
@@ -17,8 +19,47 @@ constexpr int kMaxCombine = 16;  // columns produced by one combine launch
 // Scratch for reductions; one per stream of work.
 struct RedScratch {
   DevBuf<double> partial;     // kRedBlocks * kMaxGramOut
+  DevBuf<unsigned> counter;   // arrival count of reduce_in_last_block (zero between launches)
   pg_status ensure();
 };
+
+// Ends a kernel whose block b has written its partial row partial[b*no + o],
+// o < no, and that every thread of every block calls last.  The last block to
+// arrive adds the rows of each output in the order of k_reduce_partials (one
+// warp per output; lanes stride over the rows with eight loads in flight,
+// then a shuffle tree), writes out[o] (and 1/sqrt(out[o]) at out[no + o] with
+// sqrt_mode), and resets the counter for the next launch.
+__device__ __forceinline__ void reduce_in_last_block(const double* partial, int no, double* out, int sqrt_mode,
+                                                     unsigned* counter) {
+  __shared__ int s_last;
+  __threadfence();  // this block's partial row is visible to the last block
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const int nb = (int)gridDim.x;
+  const int lane = threadIdx.x & 31;
+  for (int o = threadIdx.x >> 5; o < no; o += blockDim.x >> 5) {
+    double s = 0;
+    for (int b0 = 0; b0 < nb; b0 += 8 * 32) {
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int b = b0 + u * 32 + lane;
+        v[u] = b < nb ? __ldcg(partial + (long)b * no + o) : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(0xffffffffu, s, d);
+    if (lane == 0) {
+      out[o] = s;
+      if (sqrt_mode) out[no + o] = 1.0 / sqrt(s);
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
 
 // out[o] = sum over b < nb of partial[b*no + o], in a fixed order; with
 // sqrt_mode also out[no + o] = 1/sqrt(out[o]).
