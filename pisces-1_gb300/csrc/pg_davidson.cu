@@ -478,13 +478,13 @@ pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, double*
                                cudaStream_t st) {
   PG_ARG(out == B + (long)nbas * N && k > 0 && k <= kMaxCombine && nbas + k <= 128,
          "block_orthonormalise: output must follow the basis (nbas=%d k=%d)", nbas, k);
-  if (R != out) PG_CUDA_TRY(cudaMemcpyAsync(out, R, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
   // mixed form: both passes read the twins of [B R] and the combines write the
   // twin of their output, so [B R] is converted once (R here, B as it was
-  // written)
+  // written); R is copied into place and split in one pass
   double* Bt = d->dfloat ? d->bt.p : nullptr;
   double* Rt = Bt ? Bt + (long)nbas * N : nullptr;
-  if (Bt) PG_TRY(split_twin(N * k, out, Rt, st));
+  if (Bt) PG_TRY(split_twin(N * k, R, Rt, st, R != out ? out : nullptr));
+  else if (R != out) PG_CUDA_TRY(cudaMemcpyAsync(out, R, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
   for (int pass = 0; pass < 2; ++pass) {
     PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat, Bt, Rt));
     k_pip_coef<<<1, 256, 0, st>>>(d->dgram.p, nbas, k, d->dcoef.p);

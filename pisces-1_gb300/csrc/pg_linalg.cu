@@ -531,12 +531,16 @@ pg_status RedScratch::ensure() {
   return PG_OK;
 }
 
-// Double-float twins of count doubles: t[i] = (hi, lo) of x[i] (df_split).
-__global__ void __launch_bounds__(kT) k_split_twin(long count, const double* __restrict__ x, float2* __restrict__ t) {
+// Double-float twins of count doubles: t[i] = (hi, lo) of x[i] (df_split);
+// with y, also y[i] = x[i] (a copy and its twin in one pass).
+__global__ void __launch_bounds__(kT) k_split_twin(long count, const double* __restrict__ x, float2* __restrict__ t,
+                                                   double* __restrict__ y) {
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < count; i += (long)gridDim.x * kT) {
+    const double v = x[i];
     float h, l;
-    df_split(x[i], h, l);
+    df_split(v, h, l);
     t[i] = make_float2(h, l);
+    if (y) y[i] = v;
   }
 }
 
@@ -639,10 +643,10 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
   return PG_OK;  // with sq, the kernel's last block has reduced the norms
 }
 
-pg_status split_twin(long count, const double* x, double* t, cudaStream_t st) {
+pg_status split_twin(long count, const double* x, double* t, cudaStream_t st, double* copy) {
   if (count <= 0) return PG_OK;
   const long b = (count + kT - 1) / kT;
-  k_split_twin<<<(int)(b < 152L * 8 ? b : 152L * 8), kT, 0, st>>>(count, x, reinterpret_cast<float2*>(t));
+  k_split_twin<<<(int)(b < 152L * 8 ? b : 152L * 8), kT, 0, st>>>(count, x, reinterpret_cast<float2*>(t), copy);
   return check_launch("k_split_twin");
 }
 

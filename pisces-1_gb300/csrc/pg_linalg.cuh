@@ -84,7 +84,8 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
                   cudaStream_t st, bool dfloat = false, const double* Pt = nullptr, double* Yt = nullptr);
 
-// t[i] = double-float twin of x[i] (float2 (hi, lo) in the 8 bytes of t[i]).
-pg_status split_twin(long count, const double* x, double* t, cudaStream_t st);
+// t[i] = double-float twin of x[i] (float2 (hi, lo) in the 8 bytes of t[i]);
+// with copy (not overlapping x), also copy[i] = x[i] in the same pass.
+pg_status split_twin(long count, const double* x, double* t, cudaStream_t st, double* copy = nullptr);
 
 }  // namespace pg
