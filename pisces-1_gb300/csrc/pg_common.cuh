@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "pisces_gb300.h"
@@ -87,6 +88,35 @@ struct DevBuf {
     n = 0;
   }
 };
+
+// Programmatic dependent launch.  A kernel launched by launch_dependent may
+// be scheduled before the kernel ahead of it in the stream has finished; it
+// must call pdl_wait() before it touches global memory (the wait returns once
+// that kernel has completed and its writes are visible; in a kernel launched
+// normally it returns at once).  pdl_release() lets the next dependent launch
+// be scheduled; it is issued right after the wait.  A dependent is scheduled
+// only when every block of the kernel ahead has released or exited, i.e. when
+// all of them are resident, so the early launch cannot take the resources
+// that kernel still needs.  What it saves is the gap between the end of one
+// kernel and the start of the next.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_dependent(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                    Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Grow-only page-locked host buffer: copies between it and the device are
 // asynchronous (a pageable source or target makes cudaMemcpyAsync stage

@@ -100,6 +100,8 @@ __global__ void __launch_bounds__(kT) k_ritz_residual(long N, long chunk, int nr
                                                       double* __restrict__ W, const double* __restrict__ uinv,
                                                       const double* __restrict__ lam, double* __restrict__ partial,
                                                       double* rsq, unsigned* counter) {
+  pdl_wait();
+  pdl_release();
   __shared__ double red[kT / 32][NR];
   double inv[NR], nl[NR], acc[NR];
 #pragma unroll
@@ -305,6 +307,8 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
 // cancellation left) projects and normalises.  One block; k <= 16, nb <= 128.
 __global__ void __launch_bounds__(256) k_pip_coef(const double* __restrict__ G, int nb, int k,
                                                   double* __restrict__ coef) {
+  pdl_wait();
+  pdl_release();
   __shared__ double Cs[128][kMaxCombine];
   __shared__ double L[kMaxCombine][kMaxCombine + 1];
   __shared__ double U[kMaxCombine][kMaxCombine + 1];
@@ -487,7 +491,7 @@ pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, double*
   else if (R != out) PG_CUDA_TRY(cudaMemcpyAsync(out, R, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
   for (int pass = 0; pass < 2; ++pass) {
     PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat, Bt, Rt));
-    k_pip_coef<<<1, 256, 0, st>>>(d->dgram.p, nbas, k, d->dcoef.p);
+    PG_CUDA_TRY(launch_dependent(k_pip_coef, dim3(1), dim3(256), 0, st, d->dgram.p, nbas, k, d->dcoef.p));
     PG_TRY(check_launch("k_pip_coef"));
     PG_TRY(combine(N, B, nbas + k, d->dcoef.p, k, 1, 1.0, nullptr, nullptr, false, out, k, nullptr, d->rs, st,
                    d->dfloat, Bt, Rt));
@@ -629,8 +633,8 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
       const long chunk = (N + kRedBlocks - 1) / kRedBlocks;
       const int nblk = (int)((N + chunk - 1) / chunk);
 #define PG_RITZ(NRV) \
-  k_ritz_residual<NRV><<<nblk, kT, 0, st>>>(N, chunk, nroots, ritz, res, usq + nroots, dlam, d->rs.partial.p, rsq, \
-                                            d->rs.counter.p)
+  PG_CUDA_TRY(launch_dependent(k_ritz_residual<NRV>, dim3(nblk), dim3(kT), 0, st, N, chunk, nroots, ritz, res, \
+                               usq + nroots, dlam, d->rs.partial.p, rsq, d->rs.counter.p))
       if (nroots <= 1) PG_RITZ(1);
       else if (nroots <= 2) PG_RITZ(2);
       else if (nroots <= 4) PG_RITZ(4);

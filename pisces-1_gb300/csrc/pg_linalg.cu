@@ -29,6 +29,8 @@ long chunk_for(long N, int blocks, int align) {
 // store 1/sqrt(out[o]) at out[no + o] (used to normalise vectors on device).
 __global__ void __launch_bounds__(kT) k_reduce_partials(const double* __restrict__ partial, int nb, int no,
                                                         double* __restrict__ out, int sqrt_mode) {
+  pdl_wait();
+  pdl_release();
   const int warp = (blockIdx.x * kT + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= no) return;
@@ -277,6 +279,8 @@ __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const dou
                                                    const double* __restrict__ Q, int nb, int tp, int m, int S,
                                                    int ablk, int nblk, int split_p, int split_q,
                                                    double* __restrict__ partial) {
+  pdl_wait();
+  pdl_release();
   extern __shared__ __align__(16) unsigned char gsm[];
   const int rows = na + nb;
   const int hp = tp >> 1;  // point pairs per tile row
@@ -417,6 +421,8 @@ __global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long
                                                    const double* X, const double* __restrict__ alpha, int inv_sqrt,
                                                    double* Y, int nr, float2* Yt, double* __restrict__ partial,
                                                    double* sq_out, unsigned* counter) {
+  pdl_wait();
+  pdl_release();
   extern __shared__ float smf[];
   float* Ch = smf;              // na x nr
   float* Cl = smf + na * nr;
@@ -516,7 +522,8 @@ namespace {
 
 pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
   const int blocks = (no * 32 + kT - 1) / kT;
-  k_reduce_partials<<<blocks, kT, 0, st>>>(partial, nb, no, out, sqrt_mode ? 1 : 0);
+  PG_CUDA_TRY(launch_dependent(k_reduce_partials, dim3(blocks), dim3(kT), 0, st, partial, nb, no, out,
+                               sqrt_mode ? 1 : 0));
   return check_launch("k_reduce_partials");
 }
 
@@ -535,6 +542,8 @@ pg_status RedScratch::ensure() {
 // with y, also y[i] = x[i] (a copy and its twin in one pass).
 __global__ void __launch_bounds__(kT) k_split_twin(long count, const double* __restrict__ x, float2* __restrict__ t,
                                                    double* __restrict__ y) {
+  pdl_wait();
+  pdl_release();
   for (long i = blockIdx.x * (long)kT + threadIdx.x; i < count; i += (long)gridDim.x * kT) {
     const double v = x[i];
     float h, l;
@@ -582,11 +591,11 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
     const double* Qs = Qt ? Qt : Q;
     const int sp = Pt ? 1 : 0, sq = Qt ? 1 : 0;
     if (pair_ok(N, Ps, Qs))
-      k_gram_df<true><<<dblocks, kT, gg.smem, st>>>(N, dchunk, Ps, na, Qs, nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk,
-                                                     sp, sq, rs.partial.p);
+      PG_CUDA_TRY(launch_dependent(k_gram_df<true>, dim3(dblocks), dim3(kT), gg.smem, st, N, dchunk, Ps, na, Qs, nb,
+                                   gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, sp, sq, rs.partial.p));
     else
-      k_gram_df<false><<<dblocks, kT, gg.smem, st>>>(N, dchunk, Ps, na, Qs, nb, gg.tp, gg.m, gg.S, gg.ablk,
-                                                      gg.nblk, sp, sq, rs.partial.p);
+      PG_CUDA_TRY(launch_dependent(k_gram_df<false>, dim3(dblocks), dim3(kT), gg.smem, st, N, dchunk, Ps, na, Qs,
+                                   nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, sp, sq, rs.partial.p));
     PG_TRY(check_launch("k_gram_df"));
     return reduce(rs.partial.p, dblocks, na * nb, out, false, st);
   } else {
@@ -608,10 +617,10 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
   const int blocks = (int)((N + chunk - 1) / chunk);
   if (dfloat) {
     const size_t smem = sizeof(float) * 2 * (size_t)(na > 0 ? na : 1) * nr;
-#define PG_COMBINE_DF3(NRV, TI, TO)                                                                          \
-  k_combine_df<NRV, TI, TO><<<blocks, kT, smem, st>>>(N, chunk, Pt ? Pt : P, na, C, ca, cr, cscale, X, alpha,      \
-                                                      inv_sqrt ? 1 : 0, Y, nr, reinterpret_cast<float2*>(Yt),     \
-                                                      sq ? rs.partial.p : nullptr, sq, rs.counter.p)
+#define PG_COMBINE_DF3(NRV, TI, TO)                                                                                \
+  PG_CUDA_TRY(launch_dependent(k_combine_df<NRV, TI, TO>, dim3(blocks), dim3(kT), smem, st, N, chunk, Pt ? Pt : P, na, \
+                               C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, reinterpret_cast<float2*>(Yt),  \
+                               sq ? rs.partial.p : nullptr, sq, rs.counter.p))
 #define PG_COMBINE_DF(NRV)                                             \
   do {                                                                 \
     if (Pt && Yt) PG_COMBINE_DF3(NRV, true, true);                     \
@@ -646,7 +655,8 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
 pg_status split_twin(long count, const double* x, double* t, cudaStream_t st, double* copy) {
   if (count <= 0) return PG_OK;
   const long b = (count + kT - 1) / kT;
-  k_split_twin<<<(int)(b < 152L * 8 ? b : 152L * 8), kT, 0, st>>>(count, x, reinterpret_cast<float2*>(t), copy);
+  PG_CUDA_TRY(launch_dependent(k_split_twin, dim3((unsigned)(b < 152L * 8 ? b : 152L * 8)), dim3(kT), 0, st, count, x,
+                               reinterpret_cast<float2*>(t), copy));
   return check_launch("k_split_twin");
 }
 
