@@ -285,6 +285,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // the prologue above reads only the grid's constant operand images; X, Y
+  // and V may still be written by the kernel ahead (programmatic launch)
+  pg::pdl_wait();
+  pg::pdl_release();
   const uint32_t tmem = tmem_base;
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(npad >> 3) << 17) |
                          ((uint32_t)(kTileM >> 4) << 24);
@@ -474,6 +478,10 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // the prologue above reads only the grid's constant operand images; X, Y
+  // and V may still be written by the kernel ahead (programmatic launch)
+  pg::pdl_wait();
+  pg::pdl_release();
   const uint32_t tmem = tmem_base;
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(npad >> 3) << 17) |
                          ((uint32_t)(kTileM >> 4) << 24);
@@ -676,16 +684,16 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     const size_t smem_p = staged ? smem + stage : smem;
     switch (a) {
       case 0:
-        k_hx_tc_pipe<0><<<grid, kPipeThreads, smem_p, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
-                                                            jobs, mode, stage_off, err);
+        PG_CUDA_TRY(launch_dependent(k_hx_tc_pipe<0>, dim3(grid), dim3(kPipeThreads), smem_p, st, g->n[0], g->n[1],
+                                     g->n[2], am, npad, kc, cols, Ahi, Alo, jobs, mode, stage_off, err));
         break;
       case 1:
-        k_hx_tc_pipe<1><<<grid, kPipeThreads, smem_p, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
-                                                            jobs, mode, stage_off, err);
+        PG_CUDA_TRY(launch_dependent(k_hx_tc_pipe<1>, dim3(grid), dim3(kPipeThreads), smem_p, st, g->n[0], g->n[1],
+                                     g->n[2], am, npad, kc, cols, Ahi, Alo, jobs, mode, stage_off, err));
         break;
       default:
-        k_hx_tc_pipe<2><<<grid, kPipeThreads, smem_p, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, cols, Ahi, Alo,
-                                                            jobs, mode, stage_off, err);
+        PG_CUDA_TRY(launch_dependent(k_hx_tc_pipe<2>, dim3(grid), dim3(kPipeThreads), smem_p, st, g->n[0], g->n[1],
+                                     g->n[2], am, npad, kc, cols, Ahi, Alo, jobs, mode, stage_off, err));
     }
     return check_launch("k_hx_tc_pipe");
   }
@@ -704,16 +712,16 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
   }
   switch (a) {
     case 0:
-      k_hx_tc<0><<<grid, kThreads, smem_t, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs,
-                                                 mode, stage_off, err);
+      PG_CUDA_TRY(launch_dependent(k_hx_tc<0>, dim3(grid), dim3(kThreads), smem_t, st, g->n[0], g->n[1], g->n[2], am,
+                                   npad, kc, nch, cols, Ahi, Alo, jobs, mode, stage_off, err));
       break;
     case 1:
-      k_hx_tc<1><<<grid, kThreads, smem_t, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs,
-                                                 mode, stage_off, err);
+      PG_CUDA_TRY(launch_dependent(k_hx_tc<1>, dim3(grid), dim3(kThreads), smem_t, st, g->n[0], g->n[1], g->n[2], am,
+                                   npad, kc, nch, cols, Ahi, Alo, jobs, mode, stage_off, err));
       break;
     default:
-      k_hx_tc<2><<<grid, kThreads, smem_t, st>>>(g->n[0], g->n[1], g->n[2], am, npad, kc, nch, cols, Ahi, Alo, jobs,
-                                                 mode, stage_off, err);
+      PG_CUDA_TRY(launch_dependent(k_hx_tc<2>, dim3(grid), dim3(kThreads), smem_t, st, g->n[0], g->n[1], g->n[2], am,
+                                   npad, kc, nch, cols, Ahi, Alo, jobs, mode, stage_off, err));
   }
   return check_launch("k_hx_tc");
 }
