@@ -176,3 +176,27 @@ def test_fft_apply_is_three_axis_circulants(orc, pg):
                    + np.einsum("ab,bji->aji", t, X)).reshape(-1)
     assert np.max(np.abs(y - ref)) <= 1e-12 * np.max(np.abs(ref))
 
+
+
+def test_oracle_is_deterministic_across_thread_counts(orc):
+    # the oracle's dot products sum fixed blocks in a fixed order, so a solve
+    # gives the same bits whatever OpenMP thread count runs it
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    script = (
+        "import sys, numpy as np\n"
+        f"sys.path.insert(0, {ROOT!r})\n"
+        "import __graft_entry__ as e\n"
+        "orc = e.load_oracle()\n"
+        f"g = dict(np.load({os.path.join(ROOT, 'tests', 'golden', 'small_w6.npz')!r}))\n"
+        "st, ev, vec, nmv = orc.Grid(g['n'], g['L']).solve(g['v'], nstates=2, ptol=8)\n"
+        "print(st, nmv, ev.tobytes().hex(), vec.tobytes()[:4096].hex())\n")
+    outs = []
+    for threads in ("1", "3"):
+        env = dict(os.environ, OMP_NUM_THREADS=threads)
+        r = subprocess.run([sys.executable, "-c", script], env=env, capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr
+        outs.append(r.stdout)
+    assert outs[0] == outs[1]
