@@ -186,7 +186,10 @@ pg_status pg_davidson_destroy(pg_davidson* d);
  * and residual combinations, the block orthogonalisation): PG_FP64 (default,
  * IEEE FP64 throughout) or PG_MIXED, double-float (two FP32 numbers,
  * ~2^-48 relative) on the FP32 pipe.  The subspace eigensolve, the Cholesky
- * factors and the residual norms stay FP64 either way. */
+ * factors and the residual norms stay FP64 either way.  PG_MIXED also keeps
+ * double-float copies of B and Z on the device (2 * maxsub * ndim doubles).
+ * Set it before a solve's first call: PG_BAD_ARG while a solve is in
+ * progress. */
 pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision);
 
 /* Enables corrflag 3 on this handle: the correction vector of a root with

@@ -233,6 +233,10 @@ extern "C" pg_status pg_davidson_destroy(pg_davidson* d) {
 
 extern "C" pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision) {
   PG_ARG(d && (precision == PG_FP64 || precision == PG_MIXED), "pg_davidson_set_arithmetic: bad arguments");
+  // the mixed form's double-float twins of B and Z are set up at a solve's
+  // first call, so the arithmetic is fixed while a solve is in progress
+  PG_ARG(d->status == 0 || (precision == PG_MIXED) == d->dfloat,
+         "pg_davidson_set_arithmetic: the arithmetic cannot change while a solve is in progress");
   d->dfloat = precision == PG_MIXED;
   return PG_OK;
 }
