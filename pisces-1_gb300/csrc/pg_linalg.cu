@@ -213,15 +213,6 @@ __device__ __forceinline__ void df_fma(float& sh, float& sl, float ah, float al,
   sh = t;
 }
 
-// (sh, sl) += (ph, pl)
-__device__ __forceinline__ void df_add(float& sh, float& sl, float ph, float pl) {
-  const float t = sh + ph;
-  const float bp = t - sh;
-  const float err = (sh - (t - bp)) + (ph - bp);
-  sl += err + pl;
-  sh = t;
-}
-
 // Gram partials in double-float, written as double (hi + lo): same contract
 // as k_gram.  A thread owns a kGA x kGB block of outputs (kGA rows of P
 // against kGB rows of Q) for one slice of the points of each tile, so every
@@ -510,16 +501,7 @@ __global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long
   reduce_in_last_block(partial, nr, sq_out, 1, counter);
 }
 
-pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st);
-
-}  // namespace
-
-pg_status reduce_partials(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
-  return reduce(partial, nb, no, out, sqrt_mode, st);
-}
-
-namespace {
-
+// out[o] = sum of partial[b*no + o] over the nb rows, in a fixed order (k_reduce_partials)
 pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
   const int blocks = (no * 32 + kT - 1) / kT;
   PG_CUDA_TRY(launch_dependent(k_reduce_partials, dim3(blocks), dim3(kT), 0, st, partial, nb, no, out,

@@ -61,10 +61,6 @@ __device__ __forceinline__ void reduce_in_last_block(const double* partial, int 
   if (threadIdx.x == 0) *counter = 0u;
 }
 
-// out[o] = sum over b < nb of partial[b*no + o], in a fixed order; with
-// sqrt_mode also out[no + o] = 1/sqrt(out[o]).
-pg_status reduce_partials(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st);
-
 // out[a*nb + b] = sum_g P[a*N + g] * Q[b*N + g]     (a < na, b < nb; na*nb <= kMaxGramOut)
 // dfloat: products and sums in double-float (two-FP32) arithmetic, ~2^-48
 // relative, on the FP32 pipe instead of the FP64 pipe.
