@@ -112,3 +112,21 @@ def test_reference_shaped_header_compiles():
         pytest.skip("g++ or the CUDA headers are missing")
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), "-I", cuda,
                     os.path.join(ROOT, "tests", "shim", "check_ref_shim.cpp")], check=True)
+
+
+def test_request_footprint_counts_the_solve_buffers(pg):
+    # admission footprint (pg_request_footprint), in device bytes: basis and
+    # products (2 maxsub N), the work array (2 nroots N for corrflag 1/3), the
+    # diagonal, the potential, the eigenvectors (nroots N), the kinetic
+    # preconditioner's blocks (7 nroots N, corrflag 3), the mixed form's
+    # double-float twins of basis and products (2 maxsub N), and the small
+    # subspace arrays (2 maxsub^2 + 11 maxsub)
+    n, ms, nr = (48, 40, 56), 30, 3
+    N = 48 * 40 * 56
+    w = np.zeros((1, 9))
+    def fp(**kw):
+        return pg.Engine.footprint(pg.Engine.request(n, 20.0, w, nroots=nr, maxsub=ms, **kw))
+    base = 8.0 * (N * (2 * ms + 2 * nr + 1 + 1 + nr) + 2 * ms * ms + 11 * ms)
+    assert fp(corrflag=1, precision=pg.PG_FP64) == base
+    assert fp(corrflag=3, precision=pg.PG_FP64) == base + 8.0 * N * 7 * nr
+    assert fp(corrflag=3, precision=pg.PG_MIXED) == base + 8.0 * N * (7 * nr + 2 * ms)
