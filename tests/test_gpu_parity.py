@@ -150,6 +150,20 @@ def test_solve_fp64_matches_oracle_iteration_count(pg, orc, torch):
     assert abs(st["n_matvec"] - nmv_o) <= max(8, nmv_o // 20)
 
 
+@pytest.mark.parametrize("corrflag", [0, 2], ids=["residual", "jacobi-davidson"])
+def test_solve_fp64_other_corrections_match_oracle(pg, orc, torch, corrflag):
+    # the reference's other DiagMethods: 4/5 -> corrflag 0 (plain residual),
+    # 3 -> corrflag 2 (zeroth-order Jacobi-Davidson, src/Davidson.cpp:530-549)
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    ev, vec, st = grid.solve(dev(torch, g["v"]), nroots=2, ptol=8, corrflag=corrflag)
+    sto, ev_o, _, nmv_o = orc.Grid(g["n"], g["L"]).solve(g["v"], nstates=2, ptol=8, corrflag=corrflag)
+    assert sto == 2 and st["nconv"] == 2
+    assert np.max(np.abs(ev - ev_o)) < 1e-10
+    assert np.max(np.abs(ev - g["evals"][:2])) < 1e-8
+    assert abs(st["n_matvec"] - nmv_o) <= max(8, nmv_o // 20)
+
+
 def test_solve_analytic(pg, torch):
     g = golden("analytic.npz")
     grid = pg.Grid(g["box_n"], g["box_L"])
