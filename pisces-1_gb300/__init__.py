@@ -374,6 +374,10 @@ class Davidson:
     def work_size(ndim, maxsub, nroots, corrflag):
         return int(lib().pg_davidson_work_size(ndim, maxsub, nroots, corrflag))
 
+    def set_arithmetic(self, precision):
+        """Subspace arithmetic of this handle (pg_davidson_set_arithmetic), set before a solve."""
+        _check(lib().pg_davidson_set_arithmetic(self._h, precision))
+
     def step(self, ndim, maxsub, nroots, maxmacro, tol, corrflag, evals, nconv, B, Z, diag, work, inout,
              stream=None):
         """One call: returns (status, ret) with ret as the reference's return code."""

@@ -215,6 +215,45 @@ def test_reverse_communication_drop_in(pg, torch):
     assert np.max(np.abs(evals - g["evals"])) < 1e-8
 
 
+def test_reverse_communication_mixed_arithmetic(pg, torch):
+    # the same drop-in loop with the mixed form: double-float subspace
+    # arithmetic on the handle (its twins of the caller's B and Z), mixed H*X
+    # in the callback; residual 1e-6, eigenvalues within 1e-6 Eh.  The
+    # arithmetic cannot change while the solve is in progress.
+    import ctypes
+    g = golden("small_w6.npz")
+    grid = pg.Grid(g["n"], g["L"])
+    N, nroots, maxsub = grid.N, 2, 20
+    v = dev(torch, g["v"])
+    B = torch.zeros(maxsub * N, dtype=torch.float64, device="cuda")
+    Z = torch.zeros_like(B)
+    work = torch.zeros(pg.Davidson.work_size(N, maxsub, nroots, 1), dtype=torch.float64, device="cuda")
+    diag = grid.diagonal(v)
+    B[:N] = grid.piab()
+    B[N:2 * N] = dev(torch, np.random.default_rng(3).uniform(-1, 1, N))
+    evals = np.zeros(nroots)
+    nconv = ctypes.c_int(0)
+    inout = np.zeros(3, dtype=np.int32)
+    dav = pg.Davidson()
+    dav.set_arithmetic(pg.PG_MIXED)
+    ret, calls = 1, 0
+    while ret != 0:
+        s, ret = dav.step(N, maxsub, nroots, 100, 6, 1, evals, nconv, B, Z, diag, work, inout)
+        assert s == pg.PG_OK
+        if calls == 1:
+            with pytest.raises(pg.PiscesError) as e:
+                dav.set_arithmetic(pg.PG_FP64)
+            assert e.value.status == pg.PG_BAD_ARG
+        if ret == 1:
+            i0, z0, k = (int(a) for a in inout)
+            grid.hx(v, B[i0 * N:(i0 + k) * N], nvec=k, out=Z[z0 * N:(z0 + k) * N], precision=pg.PG_MIXED)
+            calls += 1
+    assert nconv.value == 2 and calls > 5
+    assert np.max(np.abs(evals - g["evals"])) < 1e-6
+    # the handle is free again once the solve has ended
+    dav.set_arithmetic(pg.PG_FP64)
+
+
 # ---------------------------------------------------------------- mixed form
 # split-TF32 tensor-core kinetic contractions, FP32 accumulation: each output
 # carries an absolute error of about 2^-21 * sum_b |T_ib x_b|, so the bound is
