@@ -25,10 +25,9 @@ struct TridiagScratch {
   explicit TridiagScratch(int m) : u0(m), u1(m), u2(m), l(m), swapped(m) {}
 };
 
-// Solve (T - lambda I) y = b for tridiagonal T by Gaussian elimination with
-// partial pivoting (in place on b); a tiny pivot is replaced by eps*|T|.
-void tridiag_solve(int m, const double* d, const double* e, double lambda, double tiny, double* b,
-                   TridiagScratch& ts) {
+// Factor T - lambda I (tridiagonal T) by Gaussian elimination with partial
+// pivoting into ts; a tiny pivot is replaced by eps*|T|.
+void tridiag_factor(int m, const double* d, const double* e, double lambda, double tiny, TridiagScratch& ts) {
   // bands of the factor: u0 (diagonal), u1, u2 (two super-diagonals after pivoting)
   double *u0 = ts.u0.data(), *u1 = ts.u1.data(), *u2 = ts.u2.data(), *l = ts.l.data();
   char* swapped = ts.swapped.data();
@@ -60,6 +59,12 @@ void tridiag_solve(int m, const double* d, const double* e, double lambda, doubl
     }
   }
   u0[m - 1] = diag != 0 ? diag : tiny;
+}
+
+// Solve (T - lambda I) y = b in place with the factor of tridiag_factor.
+void tridiag_solve(int m, double tiny, double* b, const TridiagScratch& ts) {
+  const double *u0 = ts.u0.data(), *u1 = ts.u1.data(), *u2 = ts.u2.data(), *l = ts.l.data();
+  const char* swapped = ts.swapped.data();
   // forward: apply L^-1 with the row swaps
   for (int i = 0; i < m - 1; ++i) {
     if (swapped[i]) std::swap(b[i], b[i + 1]);
@@ -210,8 +215,9 @@ bool lowest_eigenpairs(int m, const double* S, int ld, int k, double* w, double*
     // deterministic, non-degenerate start
     for (int i = 0; i < m; ++i) yj[i] = 1.0 + 0.1 * std::sin(1.0 + 0.7 * i + 1.3 * j);
     const double shift = w[j];
+    tridiag_factor(m, d.data(), e.data(), shift, tiny, ts);  // one factor for the four solves
     for (int it = 0; it < 4; ++it) {
-      tridiag_solve(m, d.data(), e.data(), shift, tiny, yj, ts);
+      tridiag_solve(m, tiny, yj, ts);
       // orthogonalise against the earlier vectors (needed inside clusters of
       // close eigenvalues, harmless elsewhere)
       for (int r = 0; r < j; ++r) {
