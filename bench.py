@@ -316,8 +316,8 @@ def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
     return gram, hx
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch, from the ncu
-# capture of `python bench.py --roofline-only` (profiles/k_gram_df_c2.md)
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of this shape,
+# from an ncu capture of `python bench.py --roofline-only`
 GRAM_TRAFFIC = {((64, 64, 64), 40, 4, 1): 92320512 + 2397952}
 
 

@@ -48,6 +48,9 @@ const char* pg_last_error(void);
 int pg_version(void);
 /* Number of CUDA kernels this library has launched since it was loaded. */
 long pg_kernel_launches(void);
+/* Number of device allocations (cudaMalloc) this library has made since it
+ * was loaded, successful or not. */
+long pg_device_allocations(void);
 
 /* ------------------------------------------------------------------ kinetic */
 
@@ -234,8 +237,10 @@ pg_status pg_block_combine(long n, const double* P_dev, int np, const double* C_
  * under a latency budget.  The reduction partials go to a fixed file-scope
  * device array of 256 x 296 doubles (592 KiB), so np * nq <= 256
  * (PG_BAD_ARG with a message otherwise).  The first call on a device looks up
- * that array's address and should come before any stream capture.  Nothing in
- * the array has to start at zero.  Calls that overlap in time (other streams
+ * that array's address and should come before any stream capture; the address
+ * is kept for the life of the process, so the entry point must not be called
+ * on a device after cudaDeviceReset of that device.  Nothing in the array has
+ * to start at zero.  Calls that overlap in time (other streams
  * or threads) share the one array and race: serialise them.  Results are
  * bit-identical to pg_block_gram's. */
 pg_status pg_block_gram_noalloc(long n, const double* P_dev, int np, const double* Q_dev, int nq, double* out_dev,

@@ -40,7 +40,8 @@ _lib = None
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        src = os.path.join(HERE, "pisces_oracle.c")
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
             build()
         L = C.CDLL(LIB_PATH)
         L.or_sine_dvr.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp]
@@ -55,8 +56,14 @@ def lib():
                                C.c_int, C.c_int, _dp, _dp, C.POINTER(C.c_long), C.c_long]
         L.or_solve.restype = C.c_int
         L.or_syev.argtypes = [C.c_int, _dp, C.c_int, _dp, _dp, C.c_int]
+        L.or_set_threads.argtypes = [C.c_int]
         _lib = L
     return _lib
+
+
+def set_threads(n: int):
+    """OpenMP thread count of the oracle's loops (the results do not depend on it)."""
+    lib().or_set_threads(int(n))
 
 
 def _d(a):

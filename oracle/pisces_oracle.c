@@ -11,6 +11,18 @@
 #include <stdlib.h>
 #include <string.h>
 #include <stdio.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* Thread count of the OpenMP loops below (results do not depend on it). */
+void or_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
 
 /* The reference's own value of pi, truncated to 15 digits
  * (src/sine_dvr.cpp:24, src/constants.h:4); the kinetic matrix and the

@@ -23,6 +23,9 @@
 extern "C" {
 #endif
 
+/* Thread count of the OpenMP loops (the results are the same for any count). */
+void or_set_threads(int n);
+
 /* 1-D sine DVR: grid points and packed kinetic matrix (src/sine_dvr.cpp:45-131). */
 void or_sine_dvr(int n, double mu, double x0, double xNp1, double* x, double* tpacked);
 

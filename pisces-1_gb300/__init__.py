@@ -92,6 +92,7 @@ SYMBOLS = {
     "pg_last_error": (C.c_char_p, []),
     "pg_version": (C.c_int, []),
     "pg_kernel_launches": (C.c_long, []),
+    "pg_device_allocations": (C.c_long, []),
     "pg_sine_dvr": (C.c_int, [C.c_int, C.c_double, C.c_double, C.c_double, _dp, _dp, C.c_int]),
     "pg_grid_create": (C.c_int, [_ip, _dp, C.POINTER(_vp)]),
     "pg_grid_create_dvr": (C.c_int, [_ip, _dp, C.c_int, C.POINTER(_vp)]),
@@ -406,15 +407,29 @@ def cluster_solve(n, L, waters_angstrom, ions=None, nroots=1, maxsub=20, maxiter
     return ev, (vec.reshape(nroots, N) if want_vectors else None), st.as_dict(nroots)
 
 
+def _check_block_args(P, Q, out, nout):
+    """P and Q are 2-D blocks of equal length on one device; out holds nout values there."""
+    if P.dim() != 2 or Q.dim() != 2 or P.shape[1] != Q.shape[1]:
+        raise ValueError(f"blocks must be 2-D with equal rows, got {tuple(P.shape)} and {tuple(Q.shape)}")
+    if P.device != Q.device:
+        raise ValueError(f"P is on {P.device}, Q on {Q.device}")
+    if out is not None:
+        if out.device != P.device:
+            raise ValueError(f"out is on {out.device}, the blocks on {P.device}")
+        if out.numel() < nout:
+            raise ValueError(f"out holds {out.numel()} values, {nout} needed")
+
+
 def block_gram(P, Q, precision=PG_FP64, out=None, stream=None):
     """out[a, b] = P_a . Q_b for torch CUDA float64 blocks P (np x n), Q (nq x n)."""
     import torch
     np_, n = P.shape
     nq = Q.shape[0]
+    _check_block_args(P, Q, out, np_ * nq)
     if out is None:
         out = torch.empty(np_ * nq, dtype=torch.float64, device=P.device)
     _check(lib().pg_block_gram(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
-    return out.view(np_, nq)
+    return out.view(-1)[:np_ * nq].view(np_, nq)
 
 
 def block_gram_noalloc(P, Q, out, precision=PG_FP64, stream=None):
@@ -422,8 +437,9 @@ def block_gram_noalloc(P, Q, out, precision=PG_FP64, stream=None):
     (out must be given; np * nq <= 256)."""
     np_, n = P.shape
     nq = Q.shape[0]
+    _check_block_args(P, Q, out, np_ * nq)
     _check(lib().pg_block_gram_noalloc(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
-    return out.view(np_, nq)
+    return out.view(-1)[:np_ * nq].view(np_, nq)
 
 
 def block_combine(P, Cm, precision=PG_FP64, out=None, stream=None):

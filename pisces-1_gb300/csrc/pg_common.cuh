@@ -46,6 +46,8 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 
 // Kernel launches issued by this library (every launch site calls check_launch).
 void count_launch();
+// Device allocations made by this library (every cudaMalloc goes through DevBuf).
+void count_device_alloc();
 
 // Launch-status check after a kernel launch.
 inline pg_status check_launch(const char* what) {
@@ -70,6 +72,7 @@ struct DevBuf {
   pg_status alloc(size_t count) {
     release();
     if (count == 0) return PG_OK;
+    count_device_alloc();
     if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;

@@ -927,6 +927,16 @@ struct SolveWorkspace {
 SolveWorkspace* workspace_create() { return new SolveWorkspace(); }
 void workspace_destroy(SolveWorkspace* w) { delete w; }
 
+// Device bytes a workspace keeps between solves (its grow-only buffers and
+// those of its Davidson handle).
+double workspace_bytes(const SolveWorkspace* w) {
+  if (!w) return 0;
+  const pg_davidson& d = w->d;
+  const size_t doubles = w->B.n + w->Z.n + w->diag.n + w->work.n + d.rs.partial.n + d.dcoef.n + d.dsq.n +
+                         d.dgram.n + d.bt.n + d.zt.n + d.pc_w1.n + d.pc_w2.n + d.pc_ru.n;
+  return 8.0 * (double)doubles + 4.0 * (double)(d.rs.counter.n + d.pc_flag.n);
+}
+
 // The device eigensolve of pg_solve with the H*X product supplied by the
 // caller (the serving engine routes it through its cross-solve batcher).
 pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p, double* evals, double* evecs,

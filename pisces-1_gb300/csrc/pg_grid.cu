@@ -23,6 +23,8 @@ const char* last_error() { return g_err; }
 
 static std::atomic<long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+static std::atomic<long> g_device_allocs{0};
+void count_device_alloc() { g_device_allocs.fetch_add(1, std::memory_order_relaxed); }
 
 // The reference defines the sine DVR with a 15-digit value of pi
 // (src/sine_dvr.cpp:24, src/constants.h:4); the kinetic matrix and the
@@ -34,6 +36,7 @@ constexpr double kRefPi = 3.14159265358979;
 extern "C" const char* pg_last_error(void) { return pg::last_error(); }
 extern "C" int pg_version(void) { return 100; }
 extern "C" long pg_kernel_launches(void) { return pg::g_launches.load(); }
+extern "C" long pg_device_allocations(void) { return pg::g_device_allocs.load(); }
 
 extern "C" pg_status pg_sine_dvr(int n, double mu, double x0, double xNp1, double* x, double* ekin, int ldt) {
   PG_ARG(n > 0 && x && ekin && mu > 0 && xNp1 > x0, "pg_sine_dvr: bad arguments");

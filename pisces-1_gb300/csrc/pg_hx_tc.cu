@@ -41,11 +41,20 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
 
 // FP64 -> (hi, lo) TF32 pair with integer operations: truncate to FP32,
 // round the mantissa to 10 bits for hi, lo = the exact FP32 remainder
-// (rounded to TF32 by the tensor core).  Values below 2^-126 flush to zero.
+// (rounded to TF32 by the tensor core).  Values below 2^-126 flush to zero;
+// |x| >= 2^128 and Inf give hi = +-Inf, NaN gives hi = NaN (lo = 0), so a
+// non-finite input reaches the product.
 __device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const uint32_t h = (uint32_t)(b >> 32);
-  const int e = (int)((h >> 20) & 0x7ff) - 1023 + 127;
+  const int ex = (int)((h >> 20) & 0x7ff);
+  const int e = ex - 1023 + 127;
+  if (e >= 255) {
+    const bool nan = ex == 0x7ff && (b & 0xfffffffffffffull) != 0;
+    hi = __uint_as_float(nan ? 0x7fc00000u : ((h & 0x80000000u) | 0x7f800000u));
+    lo = 0.f;
+    return;
+  }
   uint32_t f = 0;
   if (e > 0) f = (h & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
   const uint32_t hb = (f + 0x1000u) & 0xffffe000u;

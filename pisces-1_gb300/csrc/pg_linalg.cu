@@ -179,8 +179,11 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
 // ~1 TFLOP/s for FP64; a double-float multiply-accumulate costs ~11 FP32
 // operations and keeps ~48 significant bits (Dekker 1971, Knuth TwoSum).
 
-// x = hi + lo exactly up to 2^-53 |x|, with integer operations only (the FP64
-// pipe is not touched).  |x| < 2^-126 flushes to zero.
+// x = hi + lo to about 2^-48 |x| (hi takes the top 24 mantissa bits; the
+// remaining 29 are rounded to the 24 of lo), with integer operations only
+// (the FP64 pipe is not touched).  |x| < 2^-126 flushes to zero.  |x| >=
+// 2^128 and Inf give hi = +-Inf, NaN gives hi = NaN (lo = 0), so a
+// non-finite input reaches the products and norms built from the pair.
 __device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const uint32_t h = (uint32_t)(b >> 32);
@@ -192,6 +195,12 @@ __device__ __forceinline__ void df_split(double x, float& hi, float& lo) {
     return;
   }
   const uint32_t sign = h & 0x80000000u;
+  if (ef >= 255) {
+    const bool nan = e == 0x7ff && (b & 0xfffffffffffffull) != 0;
+    hi = __uint_as_float(nan ? 0x7fc00000u : (sign | 0x7f800000u));
+    lo = 0.f;
+    return;
+  }
   hi = __uint_as_float(sign | ((uint32_t)ef << 23) | (uint32_t)((b >> 29) & 0x7fffffu));
   const uint32_t rem = (uint32_t)(b & 0x1fffffffu);  // the 29 mantissa bits below hi
   const int el = e - 1075 + 127;                      // exponent of one unit of rem
@@ -643,22 +652,36 @@ pg_status split_twin(long count, const double* x, double* t, cudaStream_t st, do
 }
 
 
+// The reduction scratch of the public block products: one per calling
+// thread and device (a buffer allocated on one device is not used on another).
+constexpr int kScratchDevices = 64;
+pg_status thread_scratch(RedScratch** out) {
+  static thread_local RedScratch rs[kScratchDevices];
+  int dev = 0;
+  PG_CUDA_TRY(cudaGetDevice(&dev));
+  PG_ARG(dev >= 0 && dev < kScratchDevices, "block products: device %d out of range", dev);
+  *out = &rs[dev];
+  return PG_OK;
+}
+
 }  // namespace pg
 
 extern "C" pg_status pg_block_gram(long n, const double* P, int np, const double* Q, int nq, double* out,
                                    int precision, void* stream) {
   PG_ARG(n > 0 && P && Q && out && np > 0 && nq > 0, "pg_block_gram: bad arguments");
   PG_ARG(precision == PG_FP64 || precision == PG_MIXED, "pg_block_gram: unknown precision");
-  static thread_local pg::RedScratch rs;
-  return pg::gram(n, P, np, Q, nq, out, rs, pg::as_stream(stream), precision == PG_MIXED);
+  pg::RedScratch* rs = nullptr;
+  PG_TRY(pg::thread_scratch(&rs));
+  return pg::gram(n, P, np, Q, nq, out, *rs, pg::as_stream(stream), precision == PG_MIXED);
 }
 
 extern "C" pg_status pg_block_combine(long n, const double* P, int np, const double* C, int ny, double* Y,
                                       int precision, void* stream) {
   PG_ARG(n > 0 && P && C && Y && np > 0 && ny > 0, "pg_block_combine: bad arguments");
   PG_ARG(precision == PG_FP64 || precision == PG_MIXED, "pg_block_combine: unknown precision");
-  static thread_local pg::RedScratch rs;
-  return pg::combine(n, P, np, C, ny, 1, 1.0, nullptr, nullptr, false, Y, ny, nullptr, rs, pg::as_stream(stream),
+  pg::RedScratch* rs = nullptr;
+  PG_TRY(pg::thread_scratch(&rs));
+  return pg::combine(n, P, np, C, ny, 1, 1.0, nullptr, nullptr, false, Y, ny, nullptr, *rs, pg::as_stream(stream),
                      precision == PG_MIXED);
 }
 

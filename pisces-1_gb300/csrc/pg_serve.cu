@@ -102,7 +102,12 @@ struct pg_engine {
   std::deque<long> done_order;
   std::set<long> outstanding;  // submitted, result not yet handed over
   long next_id = 1;
-  double in_use = 0;
+  // device bytes counted against the budget: per worker, the larger of what
+  // it keeps between solves and the footprint of the solve it runs (held),
+  // plus the warm-start cache (cache_bytes, under cm)
+  std::vector<double> held;
+  double in_use = 0;  // sum of held
+  double cache_bytes = 0;
   int in_flight = 0;
   bool stopping = false;
   pg_engine_stats stats{};
@@ -123,6 +128,10 @@ struct pg_engine {
   std::map<std::pair<long, GridKey>, std::unique_ptr<CacheEntry>> cache;
 
   pg_status grid_for(const pg_request& r, pg_grid** out);
+  double cached() {
+    std::lock_guard<std::mutex> l(cm);
+    return cache_bytes;
+  }
   void worker_main(int slot);
   void batcher_main();
   pg_status batched_hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
@@ -340,7 +349,10 @@ void pg_engine::run_job(Job& job, cudaStream_t st, pg::SolveWorkspace* ws, pg::D
           cudaMemcpyAsync(grown.p, e->vecs.p, sizeof(double) * N * e->nroots, cudaMemcpyDeviceToDevice, st) !=
               cudaSuccess)
         cs = PG_CUDA;
-      if (cs == PG_OK) std::swap(grown.p, e->vecs.p), std::swap(grown.n, e->vecs.n);
+      if (cs == PG_OK) {
+        cache_bytes += 8.0 * ((double)grown.n - (double)e->vecs.n);
+        std::swap(grown.p, e->vecs.p), std::swap(grown.n, e->vecs.n);
+      }
       if (cs == PG_OK && cudaStreamSynchronize(st) != cudaSuccess) cs = PG_CUDA;  // before `grown` frees the old one
     }
     if (cs == PG_OK &&
@@ -350,6 +362,7 @@ void pg_engine::run_job(Job& job, cudaStream_t st, pg::SolveWorkspace* ws, pg::D
       cs = PG_CUDA;
     if (cs != PG_OK) {
       if (cs == PG_CUDA) pg::set_error("warm-start store failed: %s", cudaGetErrorString(cudaGetLastError()));
+      cache_bytes -= 8.0 * (double)e->vecs.n;
       cache.erase({r.key, gk});
       return fail(cs);
     }
@@ -366,7 +379,6 @@ void pg_engine::run_job(Job& job, cudaStream_t st, pg::SolveWorkspace* ws, pg::D
 }
 
 void pg_engine::worker_main(int slot) {
-  (void)slot;
   cudaSetDevice(device);
   cudaStream_t st = nullptr;
   cudaEvent_t ready = nullptr, done_ev = nullptr;
@@ -380,16 +392,24 @@ void pg_engine::worker_main(int slot) {
       std::unique_ptr<Job> job;
       {
         std::unique_lock<std::mutex> l(m);
+        // the head runs on this worker's retained buffers (grown to its
+        // footprint): admitted when the budget holds with this worker's share
+        // at max(held, footprint); with nothing in flight it runs regardless
         cv_work.wait(l, [&] {
-          return stopping || (!queue.empty() && (in_flight == 0 || in_use + queue.front()->footprint <= budget));
+          if (stopping) return true;
+          if (queue.empty()) return false;
+          const double f = queue.front()->footprint;
+          return in_flight == 0 || in_use - held[slot] + std::max(held[slot], f) + cached() <= budget;
         });
         if (stopping) break;
         job = std::move(queue.front());
         queue.pop_front();
-        in_use += job->footprint;
+        const double h = std::max(held[slot], job->footprint);
+        in_use += h - held[slot];
+        held[slot] = h;
         in_flight += 1;
         stats.peak_in_flight = std::max(stats.peak_in_flight, in_flight);
-        stats.peak_bytes = std::max(stats.peak_bytes, in_use);
+        stats.peak_bytes = std::max(stats.peak_bytes, in_use + cached());
       }
       const auto t_start = Clock::now();
       pg_result res;
@@ -406,9 +426,21 @@ void pg_engine::worker_main(int slot) {
       const auto t_end = Clock::now();
       res.queue_seconds = seconds_between(job->t_submit, t_start);
       res.latency_seconds = seconds_between(job->t_submit, t_end);
+      // what this worker keeps for its next solve; beyond its share of the
+      // budget the buffers are released, so that idle workers cannot hold
+      // memory an admitted solve needs
+      double keep = pg::workspace_bytes(ws) + 8.0 * (double)(v.n + evecs.n);
+      if (keep > budget / (double)cfg.slots) {
+        pg::workspace_destroy(ws);
+        ws = pg::workspace_create();
+        v.release();
+        evecs.release();
+        keep = 0;
+      }
       {
         std::lock_guard<std::mutex> l(m);
-        in_use -= job->footprint;
+        in_use += keep - held[slot];
+        held[slot] = keep;
         in_flight -= 1;
         stats.completed += 1;
         if (res.status != PG_OK) stats.failed += 1;
@@ -462,6 +494,7 @@ extern "C" pg_status pg_engine_create(const pg_engine_config* c, pg_engine** out
   e->cfg = cfg;
   e->device = dev;
   e->budget = budget;
+  e->held.assign((size_t)cfg.slots, 0.0);
   try {
     e->batcher = std::thread(&pg_engine::batcher_main, e.get());
     for (int i = 0; i < cfg.slots; ++i) e->workers.emplace_back(&pg_engine::worker_main, e.get(), i);

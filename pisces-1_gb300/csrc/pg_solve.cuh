@@ -11,6 +11,7 @@ namespace pg {
 struct SolveWorkspace;
 SolveWorkspace* workspace_create();
 void workspace_destroy(SolveWorkspace* w);
+double workspace_bytes(const SolveWorkspace* w);
 
 // pg_solve with the H*X product supplied by the caller; ws (may be null)
 // holds the solve buffers across calls.

@@ -156,3 +156,48 @@ def test_argument_limits(pg, torch):
     # still serving after the rejected calls
     ev, _, _ = grid.solve(v, nroots=1, ptol=8)
     assert abs(ev[0] - 3 * (np.pi / 6.0) ** 2 / 2) < 1e-9
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+@pytest.mark.parametrize("bad", [float("nan"), float("inf")], ids=["nan", "inf"])
+def test_nonfinite_product_is_a_numeric_status(pg, torch, precision, bad):
+    """A matvec callback that writes one NaN or Inf into Z: the drop-in loop
+    must end in PG_NUMERIC, in the FP64 form and in the mixed form (whose
+    subspace products read double-float copies of Z), and the handle must
+    serve a clean solve afterwards."""
+    import ctypes
+    n, L = (12, 11, 13), (10.0, 9.0, 11.0)
+    grid = pg.Grid(n, L)
+    N, nroots, maxsub = grid.N, 2, 16
+    rng = np.random.default_rng(4)
+    v = dev(torch, -0.5 * np.exp(-0.1 * rng.uniform(0, 30, N)))
+    diag = grid.diagonal(v)
+
+    def run(poison_call):
+        B = torch.zeros(maxsub * N, dtype=torch.float64, device="cuda")
+        Z = torch.zeros_like(B)
+        work = torch.zeros(pg.Davidson.work_size(N, maxsub, nroots, 1), dtype=torch.float64, device="cuda")
+        B[:N] = grid.piab()
+        B[N:2 * N] = dev(torch, np.random.default_rng(3).uniform(-1, 1, N))
+        evals = np.zeros(nroots)
+        nconv = ctypes.c_int(0)
+        inout = np.zeros(3, dtype=np.int32)
+        dav = pg.Davidson()
+        dav.set_arithmetic(precision)
+        ret, calls = 1, 0
+        while ret != 0:
+            s, ret = dav.step(N, maxsub, nroots, 100, 6, 1, evals, nconv, B, Z, diag, work, inout)
+            if s != pg.PG_OK:
+                return s, calls
+            if ret == 1:
+                i0, z0, k = (int(a) for a in inout)
+                grid.hx(v, B[i0 * N:(i0 + k) * N], nvec=k, out=Z[z0 * N:(z0 + k) * N], precision=precision)
+                if calls == poison_call:
+                    Z[z0 * N + N // 3] = bad
+                calls += 1
+        return pg.PG_OK, calls
+
+    s, calls = run(poison_call=2)
+    assert s == pg.PG_NUMERIC and calls == 3, (s, calls)
+    s, calls = run(poison_call=-1)
+    assert s == pg.PG_OK and calls > 3

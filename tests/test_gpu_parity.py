@@ -500,22 +500,61 @@ def test_solve_waters_and_ions_match_reference(pg, torch):
         assert np.max(np.abs(np.asarray(ev) - gd["evals"][:2])) <= 1e-8, (corr, ev, gd["evals"])
 
 
+def check_full_grid_against_oracle(pg, orc, grid, tables, waters, v, ions_bohr=None, ion_q=None):
+    """V(r) on the whole grid against the oracle on the same site tables
+    (<= 1e-13 of max|V|), and the oracle's own site producer against the
+    library's (<= 1e-12); returns the oracle grid and V."""
+    og = orc.Grid(grid.n, grid.L)
+    vo = og.potential_dpp(tables.sites, tables.charges, tables.charge_site, tables.dipoles, tables.dipole_site)
+    if ions_bohr is not None:
+        og.add_ions(vo, ions_bohr.reshape(-1), ion_q)
+    assert rel(host(v), vo) < 1e-13
+    s = orc.dpp_sites(waters)
+    assert rel(tables.sites, s[0]) < 1e-12 and rel(tables.dipoles, s[3]) < 1e-12
+    return og, vo
+
+
+def check_pairs_against_oracle(og, vo, evals, vecs, de_tol, res_tol):
+    """Each returned pair (lambda, v) against the oracle's H (a restatement of
+    src/mtx.cpp:22-109): |v.Hv / v.v - lambda| <= de_tol and
+    |H v - lambda v| / |v| <= res_tol."""
+    V = host(vecs)
+    for r, lam in enumerate(evals):
+        x = V[r]
+        hx = og.matvec(vo, x)
+        nrm2 = float(x @ x)
+        assert abs(float(x @ hx) / nrm2 - lam) <= de_tol, (r, float(x @ hx) / nrm2, lam)
+        res = float(np.linalg.norm(hx - lam * x)) / np.sqrt(nrm2)
+        assert res <= res_tol, (r, res)
+
+
 @pytest.mark.gpu
-def test_solve_c3_mixed_against_fp64(pg, torch, clusters):
-    """c3: (H2O)32 + Na+ + Cl-, 96^3 over 48 bohr, 8 states, block 8.  Mixed
-    form (with FP64 refinement) against the FP64 form: |dE| <= 1e-6 Eh per
-    eigenvalue and eigenvector overlap >= 1 - 1e-8."""
+def test_solve_c3_against_oracle_and_fp64(pg, orc, torch, clusters):
+    """c3: (H2O)32 + Na+ + Cl-, 96^3 over 48 bohr, 8 states, block 8.  V(r)
+    on the full grid against the oracle (DPP + Bloomfield ions); every
+    eigenpair of the FP64 form (ptol 8) and of the mixed form (ptol 6, FP64
+    refinement) against the oracle's H: Rayleigh quotient within 1e-8 /
+    1e-6 Eh of the eigenvalue, residual <= 10^-(ptol-1).  Mixed against FP64:
+    |dE| <= 1e-6 Eh per eigenvalue, eigenvector overlap >= 1 - 1e-8."""
+    import os
+    orc.set_threads(os.cpu_count() or 4)
     w = clusters.water_cluster(32, 10.0, 3)
     ions = clusters.place_ions(w, 10.0, 33)
     grid = pg.Grid((96, 96, 96), (48.0, 48.0, 48.0))
-    v = grid.potential(pg.WaterTables(w))
-    grid.add_ions(v, ions[:, :3] / 0.52917720859, ions[:, 3])
+    tables = pg.WaterTables(w)
+    v = grid.potential(tables)
+    ions_bohr = ions[:, :3] / 0.52917720859
+    grid.add_ions(v, ions_bohr, ions[:, 3])
+    og, vo = check_full_grid_against_oracle(pg, orc, grid, tables, w, v, ions_bohr, ions[:, 3])
     e64, x64, _ = grid.solve(v, nroots=8, maxsub=64, maxiter=400, ptol=8, corrflag=3)
     emx, xmx, _ = grid.solve(v, nroots=8, maxsub=64, maxiter=400, ptol=6, corrflag=3, precision=pg.PG_MIXED,
                              refine=1)
+    check_pairs_against_oracle(og, vo, e64, x64, 1e-8, 1e-7)
+    check_pairs_against_oracle(og, vo, emx, xmx, 1e-6, 1e-5)
     assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
     ov = torch.abs(torch.sum(x64 * xmx, dim=1)) / (x64.norm(dim=1) * xmx.norm(dim=1))
     assert float(ov.min()) >= 1 - 1e-8, ov
+    orc.set_threads(4)
 
 
 @pytest.mark.gpu
@@ -535,15 +574,23 @@ def test_hx_mixed_k_chunked_axes(pg, torch, n):
 
 
 @pytest.mark.gpu
-def test_solve_c5_mixed_against_fp64(pg, torch, clusters):
+def test_solve_c5_against_oracle_and_fp64(pg, orc, torch, clusters):
     """c5: (H2O)128 in a 14 A sphere, 160^3 over 64 bohr (4.1M points), 16
     states, block 16, maxsub 96 -- the K-chunked tensor-core path at full
-    size.  Mixed form (FP64 refinement) against the FP64 form: |dE| <= 1e-6
-    Eh per eigenvalue, eigenvector overlap >= 1 - 1e-8."""
+    size.  V(r) on the full grid against the oracle; every eigenpair of the
+    FP64 form (ptol 8) and of the mixed form (ptol 6, refine 2) against the
+    oracle's H: Rayleigh quotient within 1e-8 / 1e-6 Eh, residual <=
+    10^-(ptol-1).  Mixed form against the FP64 form: |dE| <= 1e-6 Eh per
+    eigenvalue, eigenvector overlap >= 1 - 1e-8."""
+    import os
+    orc.set_threads(os.cpu_count() or 4)
     w = clusters.water_cluster(128, 14.0, 5)
     grid = pg.Grid((160, 160, 160), (64.0, 64.0, 64.0))
-    v = grid.potential(pg.WaterTables(w))
+    tables = pg.WaterTables(w)
+    v = grid.potential(tables)
+    og, vo = check_full_grid_against_oracle(pg, orc, grid, tables, w, v)
     e64, x64, _ = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=8, corrflag=3)
+    check_pairs_against_oracle(og, vo, e64, x64, 1e-8, 1e-7)
     # the FP64 Rayleigh-Ritz step fixes the eigenvalues; with states 2e-4 Eh
     # apart the vectors need the FP64 polish (refine 2) for overlap 1 - 1e-8
     emx, xmx, _ = grid.solve(v, nroots=16, maxsub=96, maxiter=400, ptol=6, corrflag=3, precision=pg.PG_MIXED,
@@ -554,6 +601,8 @@ def test_solve_c5_mixed_against_fp64(pg, torch, clusters):
     assert np.max(np.abs(np.asarray(emx) - np.asarray(e64))) <= 1e-6
     ov = torch.abs(torch.sum(x64 * xmx, dim=1)) / (x64.norm(dim=1) * xmx.norm(dim=1))
     assert float(ov.min()) >= 1 - 1e-8, ov
+    check_pairs_against_oracle(og, vo, emx, xmx, 1e-6, 1e-5)
+    orc.set_threads(4)
 
 
 @pytest.mark.gpu

@@ -1,9 +1,10 @@
 """pg_block_gram_noalloc: the Gram product with its reduction scratch in a
 fixed device array instead of allocated memory.  Compared, bit for bit,
 with pg_block_gram on two calls in a row of different shapes (the second
-call reuses the scratch the first one wrote); sizes beyond the fixed scratch
-are refused.  Collected last, and self-contained, so it passes alone and
-after the other tests."""
+call reuses the scratch the first one wrote); around each call the
+library's device-allocation count and the device's free memory stay the
+same; sizes beyond the fixed scratch are refused.  Collected last, and
+self-contained, so it passes alone and after the other tests."""
 import pytest
 
 pytestmark = pytest.mark.gpu
@@ -26,8 +27,13 @@ def test_noalloc_gram_matches_block_gram_twice(pg, torch, precision):
         Q = torch.randn(nb, n, dtype=torch.float64, device="cuda", generator=g)
         ref = pg.block_gram(P, Q, precision=precision)
         out = torch.full((na * nb,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        allocs0 = pg.lib().pg_device_allocations()
+        free0 = torch.cuda.mem_get_info()[0]
         got = pg.block_gram_noalloc(P, Q, out, precision=precision)
         torch.cuda.synchronize()
+        assert pg.lib().pg_device_allocations() == allocs0, (na, nb)
+        assert torch.cuda.mem_get_info()[0] == free0, (na, nb)
         assert torch.equal(got, ref), (na, nb)
 
 
