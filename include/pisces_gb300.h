@@ -175,6 +175,20 @@ pg_status pg_hx_async(const pg_grid* g, const double* v_dev, const double* x_dev
  * this grid timed out since the last check (the status word is then cleared). */
 pg_status pg_grid_check(const pg_grid* g, void* stream);
 
+/* Kernel of the mixed-form H*X on this grid: 0 = automatic (the fused
+ * kernel where the grid allows it, else three axis passes), 1 = three axis
+ * passes, each a tensor-core contraction over the whole grid, 2 = fused (the
+ * x and y contractions of each grid plane in one tensor-memory tile, the z
+ * contraction of 128-line tiles, one persistent launch; PG_UNSUPPORTED where
+ * the grid does not fit it: more than 128 points along x, an axis above 112
+ * points, or operand images beyond shared memory).  Both give the same
+ * products to the mixed form's accuracy.  No reference counterpart (the
+ * reference multiplies line by line, src/mtx.cpp:61-104). */
+pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind);
+/* One line describing the mixed-form H*X kernel and tile shape this grid
+ * uses (text of at most len bytes including the terminator). */
+pg_status pg_grid_hx_plan(const pg_grid* g, char* text, int len);
+
 /* ---------------------------------------------------------------- Davidson */
 
 typedef struct pg_davidson pg_davidson;

@@ -111,6 +111,8 @@ SYMBOLS = {
     "pg_hx": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pg_hx_async": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_int, _vp]),
     "pg_grid_check": (C.c_int, [_vp, _vp]),
+    "pg_grid_set_hx_kernel": (C.c_int, [_vp, C.c_int]),
+    "pg_grid_hx_plan": (C.c_int, [_vp, C.c_char_p, C.c_int]),
     "pg_davidson_create": (C.c_int, [C.POINTER(_vp)]),
     "pg_davidson_destroy": (C.c_int, [_vp]),
     "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
@@ -329,6 +331,16 @@ class Grid:
         fn = lib().pg_hx if wait else lib().pg_hx_async
         _check(fn(self._h, _dev(v), _dev(X), _dev(Y), nvec, precision, _stream(stream)))
         return Y
+
+    def set_hx_kernel(self, kind):
+        """Mixed H*X kernel of this grid: 0 automatic, 1 three axis passes, 2 fused."""
+        _check(lib().pg_grid_set_hx_kernel(self._h, int(kind)))
+
+    def hx_plan(self):
+        """One-line description of the mixed H*X kernel this grid uses."""
+        buf = C.create_string_buffer(512)
+        _check(lib().pg_grid_hx_plan(self._h, buf, 512))
+        return buf.value.decode()
 
     def check(self, stream=None):
         """Waits for the stream and reports a tensor-core wait timeout (pg_grid_check)."""

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 #include <cstdio>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -205,6 +207,11 @@ struct pg_grid {
   // solve on this grid), generated once and grown on demand
   mutable std::mutex start_m;
   mutable pg::DevBuf<double> start_rand;
+  // mixed H*X kernel choice (0 automatic, 1 three axis passes, 2 fused) and
+  // the fused kernel's work counters, one block per stream id
+  int hx_kernel = 0;
+  mutable std::mutex fused_m;
+  mutable std::map<unsigned long long, std::unique_ptr<pg::DevBuf<unsigned>>> fused_cnt;
 };
 
 namespace pg {

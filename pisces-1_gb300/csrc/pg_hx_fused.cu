@@ -1,0 +1,793 @@
+// Y = H X, mixed form, as one persistent tensor-core kernel with two kinds of
+// work item (the x and y contractions of one grid plane; the z contraction of
+// 128 grid lines), so that each vector's X and the partial sums stay in L2
+// between the two passes and HBM sees X read once and Y written once.
+//
+// H = V + Tx (+) Ty (+) Tz on the x-fastest grid (src/mtx.cpp:22-109).  For
+// one vector u:
+//   xy item (u, k): plane P[i, j] = X[u][i + nx j + nx ny k] (nx x ny);
+//       D[i, j] = sum_i' Tx[i, i'] P[i', j] + sum_j' P[i, j'] Ty[j, j']
+//     both contractions accumulate into ONE TMEM tile D (lanes i, columns j):
+//       x: A = Tx (M = i, K = i'),       B = P as rows j, K = i'  (the plane
+//          in memory order: B[j][i'] = P[i', j])
+//       y: A = P as rows i, K = j' (the plane transposed while it is staged),
+//          B = Ty (N = j, K = j')
+//     epilogue: W = V X + D in FP64, written into Y;
+//   z item (u, t): 128 consecutive plane points p = 128 t .. 128 t + 127,
+//       D[p, k] = sum_k' X[u][p + nx ny k'] Tz[k, k'],  Y += D.
+// The z epilogue of vector u reads W, so it waits (bounded) until all xy
+// items of u have finished; its operand fill and MMAs do not wait.
+//
+// Work order (one global ticket counter): XY(0), XY(1), Z(0), XY(2), Z(1),
+// ..., XY(b-1), Z(b-2), Z(b-1).  A z item's dependencies always hold lower
+// tickets, and every ticket is held by a running CTA, so the waits end
+// whatever the number of resident CTAs.
+//
+// Precision as the three-pass kernels (pg_hx_tc.cu): split-TF32 products
+// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM, V X and the sum into Y
+// in FP64.  The partial W = V X + Kx + Ky is kept in FP64 in Y.
+//
+// Shared memory (no-swizzle K-major core matrices, as pg_hx_tc.cu): the
+// kinetic matrices (resident; one image when the axes share one matrix),
+// the plane in both orientations, and the z tile (over the plane images).
+// An A operand image is read as 128 rows whatever its true row count; the
+// rows past its end fall on the images that follow it and only feed TMEM
+// lanes the epilogue ignores.
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+
+#include "pg_solve.cuh"
+
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kTile = 128;  // MMA M: TMEM lanes
+constexpr int kMaxJobs = 16;
+constexpr int kBatch = 6;   // operand loads a thread keeps in flight per fill round
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+// FP64 -> (hi, lo) TF32 pair with integer operations (as pg_hx_tc.cu):
+// hi = the FP32 truncation rounded to 10 mantissa bits, lo = the FP32
+// remainder; |x| < 2^-126 flushes to zero, Inf/NaN and |x| >= 2^128 give a
+// non-finite hi.
+__device__ __forceinline__ void split_tf32(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t h = (uint32_t)(b >> 32);
+  const int ex = (int)((h >> 20) & 0x7ff);
+  const int e = ex - 1023 + 127;
+  if (e >= 255) {
+    const bool nan = ex == 0x7ff && (b & 0xfffffffffffffull) != 0;
+    hi = __uint_as_float(nan ? 0x7fc00000u : ((h & 0x80000000u) | 0x7f800000u));
+    lo = 0.f;
+    return;
+  }
+  uint32_t f = 0;
+  if (e > 0) f = (h & 0x80000000u) | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+  const uint32_t hb = (f + 0x1000u) & 0xffffe000u;
+  hi = __uint_as_float(hb);
+  lo = __uint_as_float(f) - hi;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  for (long it = 0; it < (1L << 26); ++it) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(phase)
+                 : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* out) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) out[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+               " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+               "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// L2 prefetch of bytes [p, p + n), rounded inward to 16-byte boundaries.
+__device__ __forceinline__ void prefetch_l2(const void* p, long n) {
+  const uintptr_t a = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+  const uintptr_t e = ((uintptr_t)p + (uintptr_t)n) & ~(uintptr_t)15;
+  if (e > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((uint32_t)(e - a)) : "memory");
+}
+
+}  // namespace
+
+namespace pg {
+
+struct FusedJob {
+  const double* x;
+  double* y;
+  const double* v;
+  int nvec;
+  int vec0;  // first vector of this job in the launch's vector list
+};
+struct FusedJobs {
+  FusedJob j[kMaxJobs];
+  int n;
+  int nvec;  // vectors of all jobs
+};
+
+struct FusedGeom {
+  int nx, ny, nz;
+  int kx, ky, kz;    // K extents (padded to 8)
+  int npy, npz;      // MMA N extents (padded to 16)
+  int nzt;           // z items per vector
+  uint32_t tx_hi, tx_lo, ty_hi, ty_lo, tz_hi, tz_lo;  // byte offsets in dynamic shared memory
+  uint32_t pn_hi, pn_lo, pt_hi, pt_lo, z_hi, z_lo;
+  uint32_t acc_cols;  // TMEM columns per accumulator
+};
+
+constexpr int kMaxConst = 6;
+struct FusedConst {  // distinct kinetic operand images, bulk-copied once per CTA
+  const float* src[kMaxConst];
+  uint32_t dst[kMaxConst];
+  uint32_t bytes[kMaxConst];
+  int n;
+  uint32_t total;
+};
+
+constexpr int kFusedMaxVec = 1024;
+struct FusedCounters {
+  unsigned ticket;
+  unsigned finished;
+  unsigned done[kFusedMaxVec];  // finished xy items per vector
+};
+
+}  // namespace pg
+
+namespace {
+
+using pg::FusedConst;
+using pg::FusedCounters;
+using pg::FusedGeom;
+using pg::FusedJobs;
+
+struct Item {
+  int kind;  // 0: xy plane, 1: z tile, -1: none
+  int u;     // vector in the launch's list
+  int idx;   // plane k or z tile t
+};
+
+__device__ __forceinline__ Item decode(unsigned t, int nvec, int nz, int nzt) {
+  Item it{-1, 0, 0};
+  const unsigned ps = (unsigned)(nz + nzt);
+  if (t >= (unsigned)nvec * ps) return it;
+  if (t < (unsigned)nz) return Item{0, 0, (int)t};
+  const unsigned r = t - (unsigned)nz;
+  const unsigned s = r / ps;
+  if (s + 1 < (unsigned)nvec) {
+    const unsigned w = r - s * ps;
+    if (w < (unsigned)nz) return Item{0, (int)s + 1, (int)w};
+    return Item{1, (int)s, (int)(w - nz)};
+  }
+  return Item{1, nvec - 1, (int)(r - (unsigned)(nvec - 1) * ps)};
+}
+
+__device__ __forceinline__ void vec_ptrs(const FusedJobs& J, int u, long N, const double*& x, double*& y,
+                                         const double*& v) {
+  int j = 0;
+  while (j + 1 < J.n && u >= J.j[j + 1].vec0) ++j;
+  const long off = (long)(u - J.j[j].vec0) * N;
+  x = J.j[j].x + off;
+  y = J.j[j].y + off;
+  v = J.j[j].v;
+}
+
+// xy item: the plane of vector u at z index k into both images.  Warp w
+// fills core matrices w, w + 16, ... of the natural image (rows j, K = i):
+// lane L takes row j = 8 gj + L/4 and i = 4 qi + L%4, so a warp load reads 8
+// grid lines x 32 bytes and its store fills one 128-byte core matrix; the
+// same value goes to the transposed image (rows i, K = j).
+__device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __restrict__ P, unsigned char* smem,
+                                           int warp, int lane) {
+  const int kq = G.kx >> 2;
+  const int ncm = (G.npy >> 3) * kq;
+  const int kyq = G.ky >> 2;
+  float* pnh = reinterpret_cast<float*>(smem + G.pn_hi);
+  float* pnl = reinterpret_cast<float*>(smem + G.pn_lo);
+  float* pth = reinterpret_cast<float*>(smem + G.pt_hi);
+  float* ptl = reinterpret_cast<float*>(smem + G.pt_lo);
+  for (int c0 = warp; c0 < ncm; c0 += 16 * kBatch) {
+    double xv[kBatch];
+#pragma unroll
+    for (int b = 0; b < kBatch; ++b) {
+      const int cm = c0 + 16 * b;
+      const int gj = cm / kq, qi = cm - gj * kq;
+      const int j = 8 * gj + (lane >> 2), i = 4 * qi + (lane & 3);
+      xv[b] = (cm < ncm && j < G.ny && i < G.nx) ? P[i + (long)G.nx * j] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < kBatch; ++b) {
+      const int cm = c0 + 16 * b;
+      if (cm < ncm) {
+        const int gj = cm / kq, qi = cm - gj * kq;
+        const int j = 8 * gj + (lane >> 2), i = 4 * qi + (lane & 3);
+        float h, l;
+        split_tf32(xv[b], h, l);
+        pnh[cm * 32 + lane] = h;
+        pnl[cm * 32 + lane] = l;
+        if (j < G.ky) {
+          const int off = (((i >> 3) * kyq + (j >> 2)) << 5) + ((i & 7) << 2) + (j & 3);
+          pth[off] = h;
+          ptl[off] = l;
+        }
+      }
+    }
+  }
+}
+
+// z item: grid points p0 .. p0 + 127 of every plane (rows), K = z index.
+// Lane L takes row 8 g + L/4 and K 4 q + L%4: a warp load reads four runs of
+// eight consecutive points.
+__device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __restrict__ X, long p0, long nxny,
+                                           unsigned char* smem, int warp, int lane) {
+  const int kq = G.kz >> 2;
+  const int ncm = (kTile / 8) * kq;
+  float* zh = reinterpret_cast<float*>(smem + G.z_hi);
+  float* zl = reinterpret_cast<float*>(smem + G.z_lo);
+  for (int c0 = warp; c0 < ncm; c0 += 16 * kBatch) {
+    double xv[kBatch];
+#pragma unroll
+    for (int b = 0; b < kBatch; ++b) {
+      const int cm = c0 + 16 * b;
+      const int g = cm / kq, q = cm - g * kq;
+      const long p = p0 + 8 * g + (lane >> 2);
+      const int k = 4 * q + (lane & 3);
+      xv[b] = (cm < ncm && p < nxny && k < G.nz) ? X[p + nxny * k] : 0.0;
+    }
+#pragma unroll
+    for (int b = 0; b < kBatch; ++b) {
+      const int cm = c0 + 16 * b;
+      if (cm < ncm) {
+        float h, l;
+        split_tf32(xv[b], h, l);
+        zh[cm * 32 + lane] = h;
+        zl[cm * 32 + lane] = l;
+      }
+    }
+  }
+}
+
+// One thread: prefetch the X data of an item into L2 (the fill then reads L2).
+__device__ __forceinline__ void prefetch_item(const FusedGeom& G, const FusedJobs& J, const Item& it, long N,
+                                              long nxny, int lane) {
+  if (it.kind < 0) return;
+  const double *x, *v;
+  double* y;
+  vec_ptrs(J, it.u, N, x, y, v);
+  if (it.kind == 0) {
+    if (lane == 0) prefetch_l2(x + nxny * it.idx, nxny * 8);
+  } else {
+    const long p0 = (long)it.idx * kTile;
+    const long np = std::min((long)kTile, nxny - p0);
+    for (int k = lane; k < G.nz; k += 32) prefetch_l2(x + p0 + nxny * k, np * 8);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_hx_fused(const __grid_constant__ FusedGeom G, const __grid_constant__ FusedConst C,
+               const __grid_constant__ FusedJobs J, FusedCounters* __restrict__ cnt, int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar_t, mbar_mma[2];
+  __shared__ uint32_t tmem_base;
+  __shared__ unsigned s_ticket[2];
+  __shared__ int s_flag;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long nxny = (long)G.nx * G.ny;
+  const long N = nxny * G.nz;
+  const int nvec = J.nvec;
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_t)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_mma[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_mma[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(smem_u32(&mbar_t)), "r"(C.total)
+                 : "memory");
+    for (int c = 0; c < C.n; ++c)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_u32(smem + C.dst[c])),
+                   "l"(C.src[c]), "r"(C.bytes[c]), "r"(smem_u32(&mbar_t))
+                   : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(2 * G.acc_cols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // the prologue read only the grid's constant images; X, Y, V and the
+  // counters may still be in use by the kernel ahead (programmatic launch)
+  pg::pdl_wait();
+  pg::pdl_release();
+  const uint32_t tmem = tmem_base;
+  if (tid == 0) {
+    s_ticket[0] = atomicAdd(&cnt->ticket, 1u);
+    s_ticket[1] = atomicAdd(&cnt->ticket, 1u);
+  }
+  bool ok = __syncthreads_and(mbar_wait(smem_u32(&mbar_t), 0) ? 1 : 0);
+  bool t_landed = ok;
+
+  const uint32_t idesc_xy = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(G.npy >> 3) << 17) |
+                            ((uint32_t)(kTile >> 4) << 24);
+  const uint32_t idesc_z = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(G.npz >> 3) << 17) |
+                           ((uint32_t)(kTile >> 4) << 24);
+  const uint32_t sbo_x = (uint32_t)(G.kx >> 2) * 128, sbo_y = (uint32_t)(G.ky >> 2) * 128,
+                 sbo_z = (uint32_t)(G.kz >> 2) * 128;
+  const uint32_t sb = smem_u32(smem);
+  uint32_t phase = 0;    // bit b: parity of the next completion of mbar_mma[b]
+  uint32_t pending = 0;  // bit b: MMAs committed to mbar_mma[b] and not yet waited for
+  Item prev{-1, 0, 0};
+  int prev_buf = 0, buf = 0;
+  const int quarter = warp & 3, group = warp >> 2;
+
+  while (ok) {
+    const Item cur = decode(s_ticket[0], nvec, G.nz, G.nzt);
+    const Item nxt = decode(s_ticket[1], nvec, G.nz, G.nzt);
+    if (warp == 15) prefetch_item(G, J, nxt, N, nxny, lane);
+    if (cur.kind >= 0) {
+      // the operand images are free once the previous item's MMAs are done
+      if (pending >> prev_buf & 1u) {
+        const bool w = mbar_wait(smem_u32(&mbar_mma[prev_buf]), phase >> prev_buf & 1u);
+        if (!__syncthreads_and(w ? 1 : 0)) {
+          ok = false;
+          break;
+        }
+        phase ^= 1u << prev_buf;
+        pending &= ~(1u << prev_buf);
+      }
+      const double *x, *v;
+      double* y;
+      vec_ptrs(J, cur.u, N, x, y, v);
+      if (cur.kind == 0)
+        fill_plane(G, x + nxny * cur.idx, smem, warp, lane);
+      else
+        fill_ztile(G, x, (long)cur.idx * kTile, nxny, smem, warp, lane);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t acc = tmem + (uint32_t)buf * G.acc_cols;
+        if (cur.kind == 0) {
+          uint32_t first = 0;
+          for (int kk = 0; kk < G.kx / 8; ++kk) {  // x: A = Tx, B = plane (rows j)
+            const uint32_t off = (uint32_t)kk * 256;
+            const uint64_t ah = smem_desc(sb + G.tx_hi + off, 128, sbo_x), al = smem_desc(sb + G.tx_lo + off, 128, sbo_x);
+            const uint64_t bh = smem_desc(sb + G.pn_hi + off, 128, sbo_x), bl = smem_desc(sb + G.pn_lo + off, 128, sbo_x);
+            mma_tf32(acc, al, bh, idesc_xy, first);
+            mma_tf32(acc, ah, bl, idesc_xy, 1u);
+            mma_tf32(acc, ah, bh, idesc_xy, 1u);
+            first = 1u;
+          }
+          for (int kk = 0; kk < G.ky / 8; ++kk) {  // y: A = plane (rows i), B = Ty
+            const uint32_t off = (uint32_t)kk * 256;
+            const uint64_t ah = smem_desc(sb + G.pt_hi + off, 128, sbo_y), al = smem_desc(sb + G.pt_lo + off, 128, sbo_y);
+            const uint64_t bh = smem_desc(sb + G.ty_hi + off, 128, sbo_y), bl = smem_desc(sb + G.ty_lo + off, 128, sbo_y);
+            mma_tf32(acc, al, bh, idesc_xy, 1u);
+            mma_tf32(acc, ah, bl, idesc_xy, 1u);
+            mma_tf32(acc, ah, bh, idesc_xy, 1u);
+          }
+        } else {
+          for (int kk = 0; kk < G.kz / 8; ++kk) {  // z: A = 128 lines, B = Tz
+            const uint32_t off = (uint32_t)kk * 256;
+            const uint64_t ah = smem_desc(sb + G.z_hi + off, 128, sbo_z), al = smem_desc(sb + G.z_lo + off, 128, sbo_z);
+            const uint64_t bh = smem_desc(sb + G.tz_hi + off, 128, sbo_z), bl = smem_desc(sb + G.tz_lo + off, 128, sbo_z);
+            mma_tf32(acc, al, bh, idesc_z, kk > 0 ? 1u : 0u);
+            mma_tf32(acc, ah, bl, idesc_z, 1u);
+            mma_tf32(acc, ah, bh, idesc_z, 1u);
+          }
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(&mbar_mma[buf])));
+      }
+      pending |= 1u << buf;
+    }
+    if (prev.kind >= 0) {
+      // epilogue of the previous item (its MMAs ran during this item's fill)
+      if (pending >> prev_buf & 1u) {
+        const bool w = mbar_wait(smem_u32(&mbar_mma[prev_buf]), phase >> prev_buf & 1u);
+        if (!__syncthreads_and(w ? 1 : 0)) {
+          ok = false;
+          break;
+        }
+        phase ^= 1u << prev_buf;
+        pending &= ~(1u << prev_buf);
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const double *x, *v;
+      double* y;
+      vec_ptrs(J, prev.u, N, x, y, v);
+      const uint32_t acc = tmem + (uint32_t)prev_buf * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
+      if (prev.kind == 0) {
+        const int i = 32 * quarter + lane;
+        const long pl = nxny * prev.idx;
+        for (int c = group; c < (G.npy >> 3); c += 4) {
+          float d[8];
+          tmem_ld8(acc + (uint32_t)(8 * c), d);
+          if (i < G.nx) {
+            double vx[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int j = 8 * c + q;
+              const long a = pl + i + (long)G.nx * j;
+              vx[q] = j < G.ny ? v[a] * x[a] : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int j = 8 * c + q;
+              if (j < G.ny) y[pl + i + (long)G.nx * j] = vx[q] + (double)d[q];
+            }
+          }
+        }
+        // this plane's W is in Y: count it for the z items of vector u
+        __syncthreads();
+        if (tid == 0) {
+          __threadfence();
+          atomicAdd(&cnt->done[prev.u], 1u);
+        }
+      } else {
+        if (tid == 0) {
+          // every plane of the vector has its W in Y (bounded wait, ~2 s)
+          int f = 1;
+          const unsigned long long t0 = globaltimer_ns();
+          while (*(volatile unsigned*)&cnt->done[prev.u] < (unsigned)G.nz) {
+            if (globaltimer_ns() - t0 > 2000000000ull) {
+              f = 0;
+              break;
+            }
+            __nanosleep(256);
+          }
+          __threadfence();
+          s_flag = f;
+        }
+        __syncthreads();
+        if (!s_flag) {
+          ok = false;
+          break;
+        }
+        const long p = (long)prev.idx * kTile + 32 * quarter + lane;
+        for (int c = group; c < (G.npz >> 3); c += 4) {
+          float d[8];
+          tmem_ld8(acc + (uint32_t)(8 * c), d);
+          if (p < nxny) {
+            double w[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int k = 8 * c + q;
+              w[q] = k < G.nz ? __ldcg(y + p + nxny * k) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              const int k = 8 * c + q;
+              if (k < G.nz) y[p + nxny * k] = w[q] + (double)d[q];
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+    if (cur.kind < 0) break;
+    prev = cur;
+    prev_buf = buf;
+    buf ^= 1;
+    __syncthreads();  // every thread has read s_ticket
+    if (tid == 0) {
+      s_ticket[0] = s_ticket[1];
+      s_ticket[1] = atomicAdd(&cnt->ticket, 1u);
+    }
+    __syncthreads();
+  }
+  // drain: MMAs still in flight (after a failed wait) get a bounded wait
+  // before the tensor memory they write is released
+  for (int b = 0; b < 2; ++b)
+    if (pending >> b & 1u) mbar_wait(smem_u32(&mbar_mma[b]), phase >> b & 1u);
+  if (!t_landed) mbar_wait(smem_u32(&mbar_t), 0);
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * G.acc_cols));
+  if (tid == 0) {
+    if (!ok) atomicExch(err, 1);
+    __threadfence();
+    s_flag = atomicAdd(&cnt->finished, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_flag) {
+    // the last CTA to finish: every other CTA has stopped taking tickets and
+    // counting planes, so the counters go back to zero for the next launch
+    for (int u = tid; u < nvec; u += kThreads) cnt->done[u] = 0;
+    if (tid == 0) {
+      cnt->ticket = 0;
+      cnt->finished = 0;
+    }
+    __threadfence();
+  }
+}
+
+}  // namespace
+
+namespace pg {
+
+namespace {
+
+struct FusedPlan {
+  bool ok = false;
+  FusedGeom G{};
+  FusedConst C{};
+  size_t smem = 0;
+  char why[160] = "";
+};
+
+int g_fused_sms = 0;
+int g_fused_max_dyn = 0;
+
+cudaError_t fused_init() {
+  static const cudaError_t init = [] {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_fused_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_hx_fused);
+    if (e == cudaSuccess) {
+      g_fused_max_dyn = optin - (int)fa.sharedSizeBytes;
+      e = cudaFuncSetAttribute(k_hx_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, g_fused_max_dyn);
+    }
+    if (g_fused_sms <= 0) g_fused_sms = 148;
+    return e;
+  }();
+  return init;
+}
+
+bool same_matrix(const pg_grid* g, int a, int b) {
+  return g->n[a] == g->n[b] && g->t[a] == g->t[b];
+}
+
+FusedPlan plan_fused(const pg_grid* g) {
+  FusedPlan P;
+  const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+  auto no = [&](const char* why) {
+    snprintf(P.why, sizeof(P.why), "%s", why);
+    return P;
+  };
+  if (nx > kTile) return no("nx > 128 (TMEM lanes)");
+  for (int a = 0; a < 3; ++a)
+    if (tc_kchunk(g->n[a]) != tc_kpad(g->n[a])) return no("an axis needs K chunks (n > 112)");
+  FusedGeom& G = P.G;
+  G.nx = nx;
+  G.ny = ny;
+  G.nz = nz;
+  G.kx = tc_kpad(nx);
+  G.ky = tc_kpad(ny);
+  G.kz = tc_kpad(nz);
+  G.npy = tc_npad(ny);
+  G.npz = tc_npad(nz);
+  if (G.npy > 256 || G.npz > 256) return no("N > 256");
+  G.nzt = (int)(((long)nx * ny + kTile - 1) / kTile);
+  const int npx = tc_npad(nx);
+  const uint32_t sz_t[3] = {(uint32_t)npx * G.kx * 4, (uint32_t)G.npy * G.ky * 4, (uint32_t)G.npz * G.kz * 4};
+  const uint32_t sz_pt = (uint32_t)G.kx * G.ky * 4;   // rows i (kx), K = j
+  const uint32_t sz_pn = (uint32_t)G.npy * G.kx * 4;  // rows j (npy), K = i
+  const uint32_t sz_z = (uint32_t)kTile * G.kz * 4;
+  uint32_t cur = 0;
+  G.pt_hi = cur;
+  G.pt_lo = cur + sz_pt;
+  cur += 2 * sz_pt;
+  G.tx_hi = cur;
+  G.tx_lo = cur + sz_t[0];
+  cur += 2 * sz_t[0];
+  G.pn_hi = cur;
+  G.pn_lo = cur + sz_pn;
+  cur += 2 * sz_pn;
+  FusedConst& C = P.C;
+  C.n = 0;
+  C.total = 0;
+  auto add_const = [&](const float* src, uint32_t dst, uint32_t bytes) {
+    C.src[C.n] = src;
+    C.dst[C.n] = dst;
+    C.bytes[C.n] = bytes;
+    C.total += bytes;
+    ++C.n;
+  };
+  add_const(g->t_hi[0].p, G.tx_hi, sz_t[0]);
+  add_const(g->t_lo[0].p, G.tx_lo, sz_t[0]);
+  if (same_matrix(g, 1, 0)) {
+    G.ty_hi = G.tx_hi;
+    G.ty_lo = G.tx_lo;
+  } else {
+    G.ty_hi = cur;
+    G.ty_lo = cur + sz_t[1];
+    cur += 2 * sz_t[1];
+    add_const(g->t_hi[1].p, G.ty_hi, sz_t[1]);
+    add_const(g->t_lo[1].p, G.ty_lo, sz_t[1]);
+  }
+  if (same_matrix(g, 2, 0)) {
+    G.tz_hi = G.tx_hi;
+    G.tz_lo = G.tx_lo;
+  } else if (same_matrix(g, 2, 1)) {
+    G.tz_hi = G.ty_hi;
+    G.tz_lo = G.ty_lo;
+  } else {
+    G.tz_hi = cur;
+    G.tz_lo = cur + sz_t[2];
+    cur += 2 * sz_t[2];
+    add_const(g->t_hi[2].p, G.tz_hi, sz_t[2]);
+    add_const(g->t_lo[2].p, G.tz_lo, sz_t[2]);
+  }
+  // the z tile over the plane images where they are large enough
+  if (sz_z <= 2 * sz_pt) {
+    G.z_hi = G.pt_hi;
+  } else {
+    G.z_hi = cur;
+    cur += sz_z;
+  }
+  if (sz_z <= 2 * sz_pn) {
+    G.z_lo = G.pn_hi;
+  } else {
+    G.z_lo = cur;
+    cur += sz_z;
+  }
+  // A operands are read as 128 rows
+  uint32_t total = cur;
+  total = std::max(total, G.tx_hi + (uint32_t)kTile * G.kx * 4);
+  total = std::max(total, G.tx_lo + (uint32_t)kTile * G.kx * 4);
+  total = std::max(total, G.pt_hi + (uint32_t)kTile * G.ky * 4);
+  total = std::max(total, G.pt_lo + (uint32_t)kTile * G.ky * 4);
+  P.smem = total;
+  if ((long)P.smem > (long)g_fused_max_dyn) return no("operand images exceed shared memory");
+  uint32_t cols = 32;
+  while (cols < (uint32_t)std::max(G.npy, G.npz)) cols <<= 1;
+  G.acc_cols = cols;
+  P.ok = true;
+  return P;
+}
+
+}  // namespace
+
+// The counter block of the fused kernel for the calling stream: one per
+// stream (launches on one stream are ordered, and the last CTA of a launch
+// resets its block), keyed by the stream's process-unique id.
+static pg_status fused_counters(const pg_grid* g, cudaStream_t st, FusedCounters** out) {
+  unsigned long long id = 0;
+  PG_CUDA_TRY(cudaStreamGetId(st, &id));
+  std::lock_guard<std::mutex> l(g->fused_m);
+  auto it = g->fused_cnt.find(id);
+  if (it == g->fused_cnt.end()) {
+    if (g->fused_cnt.size() >= 256) {
+      set_error("fused H*X: more than 256 streams used on one grid");
+      return PG_UNSUPPORTED;
+    }
+    std::unique_ptr<DevBuf<unsigned>> b(new DevBuf<unsigned>());
+    PG_TRY(b->alloc(sizeof(FusedCounters) / sizeof(unsigned)));
+    PG_CUDA_TRY(cudaMemset(b->p, 0, sizeof(FusedCounters)));
+    it = g->fused_cnt.emplace(id, std::move(b)).first;
+  }
+  *out = reinterpret_cast<FusedCounters*>(it->second->p);
+  return PG_OK;
+}
+
+bool fused_hx_ok(const pg_grid* g) {
+  if (fused_init() != cudaSuccess) return false;
+  return plan_fused(g).ok;
+}
+
+// Mixed H*X of up to kMaxJobs vector blocks on the same grid in one launch
+// of the fused kernel (the caller has checked fused_hx_ok).
+pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
+                        const int* nvec, int njobs, cudaStream_t st) {
+  PG_ARG(njobs > 0 && njobs <= kMaxJobs, "fused H*X: %d jobs (at most %d)", njobs, kMaxJobs);
+  PG_CUDA_TRY(fused_init());
+  const FusedPlan P = plan_fused(g);
+  if (!P.ok) {
+    set_error("fused H*X not available on this grid: %s", P.why);
+    return PG_UNSUPPORTED;
+  }
+  FusedCounters* cnt = nullptr;
+  PG_TRY(fused_counters(g, st, &cnt));
+  FusedJobs J;
+  memset(&J, 0, sizeof(J));
+  int total = 0;
+  for (int j = 0; j < njobs; ++j) {
+    PG_ARG(nvec[j] >= 0, "fused H*X: negative vector count");
+    J.j[J.n].x = x[j];
+    J.j[J.n].y = y[j];
+    J.j[J.n].v = v[j];
+    J.j[J.n].nvec = nvec[j];
+    J.j[J.n].vec0 = total;
+    total += nvec[j];
+    if (nvec[j] > 0) ++J.n;
+  }
+  if (total == 0) return PG_OK;
+  PG_ARG(total <= kFusedMaxVec, "fused H*X: %d vectors in one launch (at most %d)", total, kFusedMaxVec);
+  J.nvec = total;
+  const long items = (long)total * (P.G.nz + P.G.nzt);
+  const int grid = (int)std::min<long>(items, g_fused_sms);
+  PG_CUDA_TRY(launch_dependent(k_hx_fused, dim3(grid), dim3(kThreads), P.smem, st, P.G, P.C, J, cnt, g->tc_err.p));
+  return check_launch("k_hx_fused");
+}
+
+pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st) {
+  for (int v0 = 0; v0 < nvec; v0 += kFusedMaxVec) {
+    const int nb = std::min(kFusedMaxVec, nvec - v0);
+    const double* xs = x + (long)v0 * g->N;
+    double* ys = y + (long)v0 * g->N;
+    PG_TRY(hx_fused_jobs(g, &v, &xs, &ys, &nb, 1, st));
+  }
+  return PG_OK;
+}
+
+// Text description of the mixed-form H*X plan of a grid.
+void hx_plan_text(const pg_grid* g, char* buf, int len) {
+  if (fused_init() != cudaSuccess) {
+    snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): device query failed");
+    return;
+  }
+  const FusedPlan P = plan_fused(g);
+  if (P.ok)
+    snprintf(buf, (size_t)len,
+             "fused (k_hx_fused): xy planes %dx%d + z tiles of 128 lines (%d per vector), K %d/%d/%d, "
+             "%zu B shared memory, %d constant images, %u TMEM columns x 2",
+             P.G.nx, P.G.ny, P.G.nzt, P.G.kx, P.G.ky, P.G.kz, P.smem, P.C.n / 2, P.G.acc_cols);
+  else
+    snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): %s", P.why);
+}
+
+}  // namespace pg
+
+extern "C" pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind) {
+  PG_ARG(g, "pg_grid_set_hx_kernel: null grid");
+  PG_ARG(kind >= 0 && kind <= 2, "pg_grid_set_hx_kernel: kind must be 0, 1 or 2 (got %d)", kind);
+  if (kind == 2 && !pg::fused_hx_ok(g)) {
+    char why[256];
+    pg::hx_plan_text(g, why, sizeof(why));
+    pg::set_error("pg_grid_set_hx_kernel: %s", why);
+    return PG_UNSUPPORTED;
+  }
+  g->hx_kernel = kind;
+  return PG_OK;
+}
+
+extern "C" pg_status pg_grid_hx_plan(const pg_grid* g, char* text, int len) {
+  PG_ARG(g && text && len > 0, "pg_grid_hx_plan: bad arguments");
+  if (g->hx_kernel == 1)
+    snprintf(text, (size_t)len, "three axis passes (k_hx_tc): chosen for this grid");
+  else
+    pg::hx_plan_text(g, text, len);
+  return PG_OK;
+}

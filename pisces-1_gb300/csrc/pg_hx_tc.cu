@@ -740,9 +740,20 @@ pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, c
   return tc_axis_jobs(g, a, Ahi, Alo, v ? &v : nullptr, &x, &y, &nvec, 1, mode, st);
 }
 
-// Mixed H*X of several solves on the same grid in one launch per axis.
+bool fused_hx_ok(const pg_grid* g);
+pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st);
+pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
+                        const int* nvec, int njobs, cudaStream_t st);
+
+// The fused kernel (pg_hx_fused.cu) where the grid allows it and the grid's
+// choice does not say otherwise; the three axis passes below elsewhere.
+static bool use_fused(const pg_grid* g) { return g->hx_kernel != 1 && fused_hx_ok(g); }
+
+// Mixed H*X of several solves on the same grid in one launch (fused) or one
+// launch per axis.
 pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
                          const int* nvec, int njobs, cudaStream_t st) {
+  if (use_fused(g)) return hx_fused_jobs(g, v, x, y, nvec, njobs, st);
   for (int a = 0; a < 3; ++a)
     PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 2 : 1, st));
   return PG_OK;
@@ -754,6 +765,14 @@ pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double*
 // occurred (the eigensolver checks the word at its own synchronisation points).
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
                    bool check) {
+  if (use_fused(g)) {
+    PG_TRY(hx_fused(g, v, x, y, nvec, st));
+    return check ? check_tc_error(g, st) : PG_OK;
+  }
+  if (g->hx_kernel == 2) {
+    set_error("pg_hx: the fused mixed H*X kernel does not take this grid");
+    return PG_UNSUPPORTED;
+  }
   for (int a = 0; a < 3; ++a) PG_TRY(tc_axis(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, a == 0 ? 2 : 1, st));
   return check ? check_tc_error(g, st) : PG_OK;
 }
