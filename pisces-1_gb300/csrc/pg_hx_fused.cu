@@ -44,10 +44,9 @@
 
 namespace {
 
-constexpr int kThreads = 512;
 constexpr int kTile = 128;  // MMA M: TMEM lanes
 constexpr int kMaxJobs = 16;
-constexpr int kBatch = 6;   // operand loads a thread keeps in flight per fill round
+constexpr int kBatch = 12;  // operand loads a producer thread keeps in flight per fill round
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -88,16 +87,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
     if (ok) return true;
   }
   return false;
-}
-
-__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* out) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 8; ++j) out[j] = __uint_as_float(r[j]);
 }
 
 __device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
@@ -203,13 +192,31 @@ __device__ __forceinline__ void vec_ptrs(const FusedJobs& J, int u, long N, cons
   v = J.j[j].v;
 }
 
-// xy item: the plane of vector u at z index k into both images.  Warp w
-// fills core matrices w, w + 16, ... of the natural image (rows j, K = i):
-// lane L takes row j = 8 gj + L/4 and i = 4 qi + L%4, so a warp load reads 8
-// grid lines x 32 bytes and its store fills one 128-byte core matrix; the
-// same value goes to the transposed image (rows i, K = j).
+// Warp roles of the kernel (one CTA per SM):
+//   warps 0-7   producers: take tickets, fill the operand images of item i
+//               (from L2: the X data of item i+1 is prefetched meanwhile);
+//   warps 8-15  epilogue: drain the accumulator of item i-2 or i-1 (two TMEM
+//               accumulators alternate), two warps per TMEM lane quarter;
+//   warp 16     lane 0 issues the MMAs of item i-1.
+// Hand-over through mbarriers: full (producers -> issuer, images written),
+// empty (MMA completion -> producers, images free), acc_full[b] (MMA
+// completion and the issuer -> epilogue), acc_empty[b] (epilogue -> issuer).
+// Each role decides with one leader thread and broadcasts over a named
+// barrier, so a role's threads always take the same branch; every wait is
+// bounded and also ends when another role has given up (s_abort).
+constexpr int kProdWarps = 8;
+constexpr int kEpiWarps = 8;
+constexpr int kIssueWarp = kProdWarps + kEpiWarps;
+constexpr int kThreadsAll = (kIssueWarp + 1) * 32;
+constexpr int kRing = 4;
+
+// xy item: the plane of vector u at z index k into both images.  Producer
+// warp w fills core matrices w, w + 8, ... of the natural image (rows j, K =
+// i): lane L takes row j = 8 gj + L/4 and i = 4 qi + L%4, so a warp load
+// reads 8 grid lines x 32 bytes and its store fills one 128-byte core
+// matrix; the same value goes to the transposed image (rows i, K = j).
 __device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __restrict__ P, unsigned char* smem,
-                                           int warp, int lane) {
+                                           int pw, int lane) {
   const int kq = G.kx >> 2;
   const int ncm = (G.npy >> 3) * kq;
   const int kyq = G.ky >> 2;
@@ -217,18 +224,18 @@ __device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __r
   float* pnl = reinterpret_cast<float*>(smem + G.pn_lo);
   float* pth = reinterpret_cast<float*>(smem + G.pt_hi);
   float* ptl = reinterpret_cast<float*>(smem + G.pt_lo);
-  for (int c0 = warp; c0 < ncm; c0 += 16 * kBatch) {
+  for (int c0 = pw; c0 < ncm; c0 += kProdWarps * kBatch) {
     double xv[kBatch];
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
-      const int cm = c0 + 16 * b;
+      const int cm = c0 + kProdWarps * b;
       const int gj = cm / kq, qi = cm - gj * kq;
       const int j = 8 * gj + (lane >> 2), i = 4 * qi + (lane & 3);
       xv[b] = (cm < ncm && j < G.ny && i < G.nx) ? P[i + (long)G.nx * j] : 0.0;
     }
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
-      const int cm = c0 + 16 * b;
+      const int cm = c0 + kProdWarps * b;
       if (cm < ncm) {
         const int gj = cm / kq, qi = cm - gj * kq;
         const int j = 8 * gj + (lane >> 2), i = 4 * qi + (lane & 3);
@@ -250,16 +257,16 @@ __device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __r
 // Lane L takes row 8 g + L/4 and K 4 q + L%4: a warp load reads four runs of
 // eight consecutive points.
 __device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __restrict__ X, long p0, long nxny,
-                                           unsigned char* smem, int warp, int lane) {
+                                           unsigned char* smem, int pw, int lane) {
   const int kq = G.kz >> 2;
   const int ncm = (kTile / 8) * kq;
   float* zh = reinterpret_cast<float*>(smem + G.z_hi);
   float* zl = reinterpret_cast<float*>(smem + G.z_lo);
-  for (int c0 = warp; c0 < ncm; c0 += 16 * kBatch) {
+  for (int c0 = pw; c0 < ncm; c0 += kProdWarps * kBatch) {
     double xv[kBatch];
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
-      const int cm = c0 + 16 * b;
+      const int cm = c0 + kProdWarps * b;
       const int g = cm / kq, q = cm - g * kq;
       const long p = p0 + 8 * g + (lane >> 2);
       const int k = 4 * q + (lane & 3);
@@ -267,7 +274,7 @@ __device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __r
     }
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
-      const int cm = c0 + 16 * b;
+      const int cm = c0 + kProdWarps * b;
       if (cm < ncm) {
         float h, l;
         split_tf32(xv[b], h, l);
@@ -280,37 +287,77 @@ __device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __r
 
 // One thread: prefetch the X data of an item into L2 (the fill then reads L2).
 __device__ __forceinline__ void prefetch_item(const FusedGeom& G, const FusedJobs& J, const Item& it, long N,
-                                              long nxny, int lane) {
+                                              long nxny) {
   if (it.kind < 0) return;
   const double *x, *v;
   double* y;
   vec_ptrs(J, it.u, N, x, y, v);
   if (it.kind == 0) {
-    if (lane == 0) prefetch_l2(x + nxny * it.idx, nxny * 8);
+    prefetch_l2(x + nxny * it.idx, nxny * 8);
   } else {
     const long p0 = (long)it.idx * kTile;
     const long np = std::min((long)kTile, nxny - p0);
-    for (int k = lane; k < G.nz; k += 32) prefetch_l2(x + p0 + nxny * k, np * 8);
+    for (int k = 0; k < G.nz; ++k) prefetch_l2(x + p0 + nxny * k, np * 8);
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Bounded wait that also gives up once another role has raised the abort flag.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t phase, volatile int* abort) {
+  for (long it = 0; it < (1L << 26); ++it) {
+    uint32_t ok;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(phase)
+                 : "memory");
+    if (ok) return true;
+    if (*abort) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) out[j] = __uint_as_float(r[j]);
+}
+
+__global__ void __maxnreg__(120)
     k_hx_fused(const __grid_constant__ FusedGeom G, const __grid_constant__ FusedConst C,
                const __grid_constant__ FusedJobs J, FusedCounters* __restrict__ cnt, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t mbar_t, mbar_mma[2];
+  __shared__ __align__(8) uint64_t mbar_t, mbar_full, mbar_empty, mbar_acc_full[2], mbar_acc_empty[2];
   __shared__ uint32_t tmem_base;
-  __shared__ unsigned s_ticket[2];
-  __shared__ int s_flag;
+  __shared__ unsigned ring[kRing], epi_ring[kRing];
+  __shared__ int s_abort, s_prod_ok, s_epi_ok, s_last;
+  volatile int* abort = &s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long nxny = (long)G.nx * G.ny;
   const long N = nxny * G.nz;
   const int nvec = J.nvec;
 
   if (tid == 0) {
+    s_abort = 0;
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_t)));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_mma[0])));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_mma[1])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar_full)), "r"(kProdWarps * 32));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_empty)));
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(smem_u32(&mbar_acc_full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_acc_empty[b])));
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     uint64_t state;
@@ -337,201 +384,215 @@ __global__ void __launch_bounds__(kThreads, 1)
   pg::pdl_wait();
   pg::pdl_release();
   const uint32_t tmem = tmem_base;
-  if (tid == 0) {
-    s_ticket[0] = atomicAdd(&cnt->ticket, 1u);
-    s_ticket[1] = atomicAdd(&cnt->ticket, 1u);
-  }
-  bool ok = __syncthreads_and(mbar_wait(smem_u32(&mbar_t), 0) ? 1 : 0);
-  bool t_landed = ok;
 
-  const uint32_t idesc_xy = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(G.npy >> 3) << 17) |
-                            ((uint32_t)(kTile >> 4) << 24);
-  const uint32_t idesc_z = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(G.npz >> 3) << 17) |
-                           ((uint32_t)(kTile >> 4) << 24);
-  const uint32_t sbo_x = (uint32_t)(G.kx >> 2) * 128, sbo_y = (uint32_t)(G.ky >> 2) * 128,
-                 sbo_z = (uint32_t)(G.kz >> 2) * 128;
-  const uint32_t sb = smem_u32(smem);
-  uint32_t phase = 0;    // bit b: parity of the next completion of mbar_mma[b]
-  uint32_t pending = 0;  // bit b: MMAs committed to mbar_mma[b] and not yet waited for
-  Item prev{-1, 0, 0};
-  int prev_buf = 0, buf = 0;
-  const int quarter = warp & 3, group = warp >> 2;
-
-  while (ok) {
-    const Item cur = decode(s_ticket[0], nvec, G.nz, G.nzt);
-    const Item nxt = decode(s_ticket[1], nvec, G.nz, G.nzt);
-    if (warp == 15) prefetch_item(G, J, nxt, N, nxny, lane);
-    if (cur.kind >= 0) {
-      // the operand images are free once the previous item's MMAs are done
-      if (pending >> prev_buf & 1u) {
-        const bool w = mbar_wait(smem_u32(&mbar_mma[prev_buf]), phase >> prev_buf & 1u);
-        if (!__syncthreads_and(w ? 1 : 0)) {
-          ok = false;
-          break;
-        }
-        phase ^= 1u << prev_buf;
-        pending &= ~(1u << prev_buf);
-      }
-      const double *x, *v;
-      double* y;
-      vec_ptrs(J, cur.u, N, x, y, v);
-      if (cur.kind == 0)
-        fill_plane(G, x + nxny * cur.idx, smem, warp, lane);
-      else
-        fill_ztile(G, x, (long)cur.idx * kTile, nxny, smem, warp, lane);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t acc = tmem + (uint32_t)buf * G.acc_cols;
-        if (cur.kind == 0) {
-          uint32_t first = 0;
-          for (int kk = 0; kk < G.kx / 8; ++kk) {  // x: A = Tx, B = plane (rows j)
-            const uint32_t off = (uint32_t)kk * 256;
-            const uint64_t ah = smem_desc(sb + G.tx_hi + off, 128, sbo_x), al = smem_desc(sb + G.tx_lo + off, 128, sbo_x);
-            const uint64_t bh = smem_desc(sb + G.pn_hi + off, 128, sbo_x), bl = smem_desc(sb + G.pn_lo + off, 128, sbo_x);
-            mma_tf32(acc, al, bh, idesc_xy, first);
-            mma_tf32(acc, ah, bl, idesc_xy, 1u);
-            mma_tf32(acc, ah, bh, idesc_xy, 1u);
-            first = 1u;
-          }
-          for (int kk = 0; kk < G.ky / 8; ++kk) {  // y: A = plane (rows i), B = Ty
-            const uint32_t off = (uint32_t)kk * 256;
-            const uint64_t ah = smem_desc(sb + G.pt_hi + off, 128, sbo_y), al = smem_desc(sb + G.pt_lo + off, 128, sbo_y);
-            const uint64_t bh = smem_desc(sb + G.ty_hi + off, 128, sbo_y), bl = smem_desc(sb + G.ty_lo + off, 128, sbo_y);
-            mma_tf32(acc, al, bh, idesc_xy, 1u);
-            mma_tf32(acc, ah, bl, idesc_xy, 1u);
-            mma_tf32(acc, ah, bh, idesc_xy, 1u);
-          }
+  if (warp < kProdWarps) {
+    // ------------------------------------------------------------ producers
+    const int ptid = tid;  // 0 .. 255
+    if (ptid == 0) ring[0] = atomicAdd(&cnt->ticket, 1u);
+    for (int i = 0;; ++i) {
+      if (ptid == 0) {
+        int ok = 1;
+        // the previous item's MMAs are done with the images
+        if (i >= 1) ok = mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
+        if (ok) {
+          const unsigned t1 = atomicAdd(&cnt->ticket, 1u);
+          ring[(i + 1) % kRing] = t1;
+          prefetch_item(G, J, decode(t1, nvec, G.nz, G.nzt), N, nxny);
         } else {
-          for (int kk = 0; kk < G.kz / 8; ++kk) {  // z: A = 128 lines, B = Tz
-            const uint32_t off = (uint32_t)kk * 256;
-            const uint64_t ah = smem_desc(sb + G.z_hi + off, 128, sbo_z), al = smem_desc(sb + G.z_lo + off, 128, sbo_z);
-            const uint64_t bh = smem_desc(sb + G.tz_hi + off, 128, sbo_z), bl = smem_desc(sb + G.tz_lo + off, 128, sbo_z);
-            mma_tf32(acc, al, bh, idesc_z, kk > 0 ? 1u : 0u);
-            mma_tf32(acc, ah, bl, idesc_z, 1u);
-            mma_tf32(acc, ah, bh, idesc_z, 1u);
-          }
+          *abort = 1;
         }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-            smem_u32(&mbar_mma[buf])));
+        s_prod_ok = ok;
       }
-      pending |= 1u << buf;
+      named_sync(1, kProdWarps * 32);
+      if (!s_prod_ok) break;
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt);
+      if (it.kind >= 0) {
+        const double *x, *v;
+        double* y;
+        vec_ptrs(J, it.u, N, x, y, v);
+        if (it.kind == 0)
+          fill_plane(G, x + nxny * it.idx, smem, warp, lane);
+        else
+          fill_ztile(G, x, (long)it.idx * kTile, nxny, smem, warp, lane);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      }
+      // (ring[i] is rewritten three items later, after the leader has seen
+      // this item's MMAs complete, which needs every producer's arrival)
+      mbar_arrive(smem_u32(&mbar_full));
+      if (it.kind < 0) break;
     }
-    if (prev.kind >= 0) {
-      // epilogue of the previous item (its MMAs ran during this item's fill)
-      if (pending >> prev_buf & 1u) {
-        const bool w = mbar_wait(smem_u32(&mbar_mma[prev_buf]), phase >> prev_buf & 1u);
-        if (!__syncthreads_and(w ? 1 : 0)) {
-          ok = false;
-          break;
-        }
-        phase ^= 1u << prev_buf;
-        pending &= ~(1u << prev_buf);
+  } else if (warp < kIssueWarp) {
+    // ------------------------------------------------------------- epilogue
+    const int quarter = warp & 3, half = (warp - kProdWarps) >> 2;
+    const bool leader = warp == kProdWarps && lane == 0;
+    for (int i = 0;; ++i) {
+      const int b = i & 1;
+      if (leader) s_epi_ok = mbar_wait_or_abort(smem_u32(&mbar_acc_full[b]), (uint32_t)((i >> 1) & 1), abort);
+      named_sync(2, kEpiWarps * 32);
+      if (!s_epi_ok) {
+        if (leader) *abort = 1;
+        break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const Item it = decode(epi_ring[i % kRing], nvec, G.nz, G.nzt);
+      if (it.kind < 0) break;
       const double *x, *v;
       double* y;
-      vec_ptrs(J, prev.u, N, x, y, v);
-      const uint32_t acc = tmem + (uint32_t)prev_buf * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
-      if (prev.kind == 0) {
-        const int i = 32 * quarter + lane;
-        const long pl = nxny * prev.idx;
-        for (int c = group; c < (G.npy >> 3); c += 4) {
-          float d[8];
-          tmem_ld8(acc + (uint32_t)(8 * c), d);
-          if (i < G.nx) {
-            double vx[8];
+      vec_ptrs(J, it.u, N, x, y, v);
+      const uint32_t acc = tmem + (uint32_t)b * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
+      if (it.kind == 0) {
+        const int i0 = 32 * quarter + lane;
+        const long pl = nxny * it.idx;
+        for (int c = half; c < (G.npy >> 4); c += 2) {
+          double vx[16];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const int j = 8 * c + q;
-              const long a = pl + i + (long)G.nx * j;
-              vx[q] = j < G.ny ? v[a] * x[a] : 0.0;
-            }
+          for (int q = 0; q < 16; ++q) {
+            const int j = 16 * c + q;
+            const long a = pl + i0 + (long)G.nx * j;
+            vx[q] = (i0 < G.nx && j < G.ny) ? v[a] * x[a] : 0.0;
+          }
+          float d[16];
+          tmem_ld16(acc + (uint32_t)(16 * c), d);
+          if (i0 < G.nx) {
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const int j = 8 * c + q;
-              if (j < G.ny) y[pl + i + (long)G.nx * j] = vx[q] + (double)d[q];
+            for (int q = 0; q < 16; ++q) {
+              const int j = 16 * c + q;
+              if (j < G.ny) y[pl + i0 + (long)G.nx * j] = vx[q] + (double)d[q];
             }
           }
         }
-        // this plane's W is in Y: count it for the z items of vector u
-        __syncthreads();
-        if (tid == 0) {
-          __threadfence();
-          atomicAdd(&cnt->done[prev.u], 1u);
-        }
       } else {
-        if (tid == 0) {
+        if (leader) {
           // every plane of the vector has its W in Y (bounded wait, ~2 s)
           int f = 1;
           const unsigned long long t0 = globaltimer_ns();
-          while (*(volatile unsigned*)&cnt->done[prev.u] < (unsigned)G.nz) {
-            if (globaltimer_ns() - t0 > 2000000000ull) {
+          while (*(volatile unsigned*)&cnt->done[it.u] < (unsigned)G.nz) {
+            if (*abort || globaltimer_ns() - t0 > 2000000000ull) {
               f = 0;
               break;
             }
-            __nanosleep(256);
+            __nanosleep(128);
           }
           __threadfence();
-          s_flag = f;
+          s_epi_ok = f;
         }
-        __syncthreads();
-        if (!s_flag) {
-          ok = false;
+        named_sync(2, kEpiWarps * 32);
+        if (!s_epi_ok) {
+          if (leader) *abort = 1;
           break;
         }
-        const long p = (long)prev.idx * kTile + 32 * quarter + lane;
-        for (int c = group; c < (G.npz >> 3); c += 4) {
-          float d[8];
-          tmem_ld8(acc + (uint32_t)(8 * c), d);
+        const long p = (long)it.idx * kTile + 32 * quarter + lane;
+        for (int c = half; c < (G.npz >> 4); c += 2) {
+          double w[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int k = 16 * c + q;
+            w[q] = (p < nxny && k < G.nz) ? __ldcg(y + p + nxny * k) : 0.0;
+          }
+          float d[16];
+          tmem_ld16(acc + (uint32_t)(16 * c), d);
           if (p < nxny) {
-            double w[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const int k = 8 * c + q;
-              w[q] = k < G.nz ? __ldcg(y + p + nxny * k) : 0.0;
-            }
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-              const int k = 8 * c + q;
+            for (int q = 0; q < 16; ++q) {
+              const int k = 16 * c + q;
               if (k < G.nz) y[p + nxny * k] = w[q] + (double)d[q];
             }
           }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      named_sync(2, kEpiWarps * 32);
+      if (leader) {
+        if (it.kind == 0) {
+          // this plane's W is in Y: count it for the z items of vector u
+          __threadfence();
+          atomicAdd(&cnt->done[it.u], 1u);
+        }
+        mbar_arrive(smem_u32(&mbar_acc_empty[b]));
+      }
     }
-    if (cur.kind < 0) break;
-    prev = cur;
-    prev_buf = buf;
-    buf ^= 1;
-    __syncthreads();  // every thread has read s_ticket
-    if (tid == 0) {
-      s_ticket[0] = s_ticket[1];
-      s_ticket[1] = atomicAdd(&cnt->ticket, 1u);
+  } else if (lane == 0) {
+    // --------------------------------------------------------------- issuer
+    const uint32_t idesc_xy = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(G.npy >> 3) << 17) |
+                              ((uint32_t)(kTile >> 4) << 24);
+    const uint32_t idesc_z = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(G.npz >> 3) << 17) |
+                             ((uint32_t)(kTile >> 4) << 24);
+    const uint32_t sb = smem_u32(smem);
+    const uint32_t sbo_x = (uint32_t)(G.kx >> 2) * 128, sbo_y = (uint32_t)(G.ky >> 2) * 128,
+                   sbo_z = (uint32_t)(G.kz >> 2) * 128;
+    // descriptors of K step 0; step kk adds kk * 256 bytes to the address field
+    const uint64_t d_txh = smem_desc(sb + G.tx_hi, 128, sbo_x), d_txl = smem_desc(sb + G.tx_lo, 128, sbo_x);
+    const uint64_t d_pnh = smem_desc(sb + G.pn_hi, 128, sbo_x), d_pnl = smem_desc(sb + G.pn_lo, 128, sbo_x);
+    const uint64_t d_pth = smem_desc(sb + G.pt_hi, 128, sbo_y), d_ptl = smem_desc(sb + G.pt_lo, 128, sbo_y);
+    const uint64_t d_tyh = smem_desc(sb + G.ty_hi, 128, sbo_y), d_tyl = smem_desc(sb + G.ty_lo, 128, sbo_y);
+    const uint64_t d_zh = smem_desc(sb + G.z_hi, 128, sbo_z), d_zl = smem_desc(sb + G.z_lo, 128, sbo_z);
+    const uint64_t d_tzh = smem_desc(sb + G.tz_hi, 128, sbo_z), d_tzl = smem_desc(sb + G.tz_lo, 128, sbo_z);
+    bool ok = mbar_wait_or_abort(smem_u32(&mbar_t), 0, abort);
+    int last_commit = -1;
+    for (int i = 0; ok; ++i) {
+      const int b = i & 1;
+      ok = mbar_wait_or_abort(smem_u32(&mbar_full), (uint32_t)(i & 1), abort);
+      if (ok && i >= 2) ok = mbar_wait_or_abort(smem_u32(&mbar_acc_empty[b]), (uint32_t)(((i - 2) >> 1) & 1), abort);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const unsigned t = ring[i % kRing];
+      epi_ring[i % kRing] = t;
+      const Item it = decode(t, nvec, G.nz, G.nzt);
+      if (it.kind < 0) {
+        mbar_arrive(smem_u32(&mbar_acc_full[b]));
+        mbar_arrive(smem_u32(&mbar_acc_full[b]));
+        break;
+      }
+      const uint32_t acc = tmem + (uint32_t)b * G.acc_cols;
+      if (it.kind == 0) {
+        for (int kk = 0; kk < G.kx / 8; ++kk) {  // x: A = Tx, B = plane (rows j)
+          const uint64_t o = (uint64_t)kk * 16;
+          mma_tf32(acc, d_txl + o, d_pnh + o, idesc_xy, kk > 0 ? 1u : 0u);
+          mma_tf32(acc, d_txh + o, d_pnl + o, idesc_xy, 1u);
+          mma_tf32(acc, d_txh + o, d_pnh + o, idesc_xy, 1u);
+        }
+        for (int kk = 0; kk < G.ky / 8; ++kk) {  // y: A = plane (rows i), B = Ty
+          const uint64_t o = (uint64_t)kk * 16;
+          mma_tf32(acc, d_ptl + o, d_tyh + o, idesc_xy, 1u);
+          mma_tf32(acc, d_pth + o, d_tyl + o, idesc_xy, 1u);
+          mma_tf32(acc, d_pth + o, d_tyh + o, idesc_xy, 1u);
+        }
+      } else {
+        for (int kk = 0; kk < G.kz / 8; ++kk) {  // z: A = 128 lines, B = Tz
+          const uint64_t o = (uint64_t)kk * 16;
+          mma_tf32(acc, d_zl + o, d_tzh + o, idesc_z, kk > 0 ? 1u : 0u);
+          mma_tf32(acc, d_zh + o, d_tzl + o, idesc_z, 1u);
+          mma_tf32(acc, d_zh + o, d_tzh + o, idesc_z, 1u);
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar_empty)));
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar_acc_full[b])));
+      mbar_arrive(smem_u32(&mbar_acc_full[b]));  // with it, epi_ring[i] is visible to the epilogue
+      last_commit = i;
     }
-    __syncthreads();
+    if (!ok) {
+      *abort = 1;
+      // MMAs still in flight get a bounded wait before the tensor memory is released
+      if (last_commit >= 0) mbar_wait(smem_u32(&mbar_empty), (uint32_t)(last_commit & 1));
+      mbar_wait(smem_u32(&mbar_t), 0);
+    }
   }
-  // drain: MMAs still in flight (after a failed wait) get a bounded wait
-  // before the tensor memory they write is released
-  for (int b = 0; b < 2; ++b)
-    if (pending >> b & 1u) mbar_wait(smem_u32(&mbar_mma[b]), phase >> b & 1u);
-  if (!t_landed) mbar_wait(smem_u32(&mbar_t), 0);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * G.acc_cols));
   if (tid == 0) {
-    if (!ok) atomicExch(err, 1);
+    if (s_abort) atomicExch(err, 1);
     __threadfence();
-    s_flag = atomicAdd(&cnt->finished, 1u) == gridDim.x - 1;
+    s_last = atomicAdd(&cnt->finished, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (s_flag) {
+  if (s_last) {
     // the last CTA to finish: every other CTA has stopped taking tickets and
     // counting planes, so the counters go back to zero for the next launch
-    for (int u = tid; u < nvec; u += kThreads) cnt->done[u] = 0;
+    for (int u = tid; u < nvec; u += kThreadsAll) cnt->done[u] = 0;
     if (tid == 0) {
       cnt->ticket = 0;
       cnt->finished = 0;
@@ -738,7 +799,7 @@ pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* 
   J.nvec = total;
   const long items = (long)total * (P.G.nz + P.G.nzt);
   const int grid = (int)std::min<long>(items, g_fused_sms);
-  PG_CUDA_TRY(launch_dependent(k_hx_fused, dim3(grid), dim3(kThreads), P.smem, st, P.G, P.C, J, cnt, g->tc_err.p));
+  PG_CUDA_TRY(launch_dependent(k_hx_fused, dim3(grid), dim3(kThreadsAll), P.smem, st, P.G, P.C, J, cnt, g->tc_err.p));
   return check_launch("k_hx_fused");
 }
 
