@@ -192,26 +192,27 @@ __device__ __forceinline__ void vec_ptrs(const FusedJobs& J, int u, long N, cons
   v = J.j[j].v;
 }
 
-// Warp roles of the kernel (one CTA per SM):
-//   warps 0-7   producers: take tickets, fill the operand images of item i
+// Warp roles of the kernel (one CTA per SM, 16 warps: four per SM
+// sub-partition, 128 registers each):
+//   warps 0-6   producers: take tickets, fill the operand images of item i
 //               (from L2: the X data of item i+1 is prefetched meanwhile);
-//   warps 8-15  epilogue: drain the accumulator of item i-2 or i-1 (two TMEM
+//   warps 7-14  epilogue: drain the accumulator of item i-2 or i-1 (two TMEM
 //               accumulators alternate), two warps per TMEM lane quarter;
-//   warp 16     lane 0 issues the MMAs of item i-1.
+//   warp 15     lane 0 issues the MMAs of item i-1.
 // Hand-over through mbarriers: full (producers -> issuer, images written),
 // empty (MMA completion -> producers, images free), acc_full[b] (MMA
 // completion and the issuer -> epilogue), acc_empty[b] (epilogue -> issuer).
 // Each role decides with one leader thread and broadcasts over a named
 // barrier, so a role's threads always take the same branch; every wait is
 // bounded and also ends when another role has given up (s_abort).
-constexpr int kProdWarps = 8;
+constexpr int kProdWarps = 7;
 constexpr int kEpiWarps = 8;
 constexpr int kIssueWarp = kProdWarps + kEpiWarps;
 constexpr int kThreadsAll = (kIssueWarp + 1) * 32;
 constexpr int kRing = 4;
 
 // xy item: the plane of vector u at z index k into both images.  Producer
-// warp w fills core matrices w, w + 8, ... of the natural image (rows j, K =
+// warp w fills core matrices w, w + 7, ... of the natural image (rows j, K =
 // i): lane L takes row j = 8 gj + L/4 and i = 4 qi + L%4, so a warp load
 // reads 8 grid lines x 32 bytes and its store fills one 128-byte core
 // matrix; the same value goes to the transposed image (rows i, K = j).
@@ -335,7 +336,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
   for (int j = 0; j < 16; ++j) out[j] = __uint_as_float(r[j]);
 }
 
-__global__ void __maxnreg__(120)
+__global__ void __launch_bounds__(kThreadsAll, 1)
     k_hx_fused(const __grid_constant__ FusedGeom G, const __grid_constant__ FusedConst C,
                const __grid_constant__ FusedJobs J, FusedCounters* __restrict__ cnt, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -387,7 +388,7 @@ __global__ void __maxnreg__(120)
 
   if (warp < kProdWarps) {
     // ------------------------------------------------------------ producers
-    const int ptid = tid;  // 0 .. 255
+    const int ptid = tid;  // 0 .. 32 kProdWarps - 1
     if (ptid == 0) ring[0] = atomicAdd(&cnt->ticket, 1u);
     for (int i = 0;; ++i) {
       if (ptid == 0) {
