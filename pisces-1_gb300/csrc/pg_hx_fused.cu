@@ -18,14 +18,18 @@
 // The z epilogue of vector u reads W, so it waits (bounded) until all xy
 // items of u have finished; its operand fill and MMAs do not wait.
 //
-// Work order (one global ticket counter): XY(0), XY(1), Z(0), XY(2), Z(1),
-// ..., XY(b-1), Z(b-2), Z(b-1).  A z item's dependencies always hold lower
+// Work order (one global ticket counter), with a lag L of two vectors:
+// XY(0), XY(1), XY(2), Z(0), XY(3), Z(1), ..., XY(b-1), Z(b-3), Z(b-2),
+// Z(b-1).  A z item's dependencies always hold lower
 // tickets, and every ticket is held by a running CTA, so the waits end
 // whatever the number of resident CTAs.
 //
 // Precision as the three-pass kernels (pg_hx_tc.cu): split-TF32 products
-// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM, V X and the sum into Y
-// in FP64.  The partial W = V X + Kx + Ky is kept in FP64 in Y.
+// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM (~2^-21 relative per
+// term); V X and the sums in FP32 (2^-24), converted to and from FP64 with
+// integer operations, because this part's FP64 pipe retires about two FMAs
+// per SM per clock and one FP64 operation per element would bound the
+// epilogue.  The partial W = V X + Kx + Ky is kept in Y (as FP64 storage).
 //
 // Shared memory (no-swizzle K-major core matrices, as pg_hx_tc.cu): the
 // kinetic matrices (resident; one image when the axes share one matrix),
@@ -131,6 +135,7 @@ struct FusedGeom {
   int kx, ky, kz;    // K extents (padded to 8)
   int npy, npz;      // MMA N extents (padded to 16)
   int nzt;           // z items per vector
+  int lag;           // vectors between a vector's xy items and its z items
   uint32_t tx_hi, tx_lo, ty_hi, ty_lo, tz_hi, tz_lo;  // byte offsets in dynamic shared memory
   uint32_t pn_hi, pn_lo, pt_hi, pt_lo, z_hi, z_lo;
   uint32_t acc_cols;  // TMEM columns per accumulator
@@ -167,19 +172,24 @@ struct Item {
   int idx;   // plane k or z tile t
 };
 
-__device__ __forceinline__ Item decode(unsigned t, int nvec, int nz, int nzt) {
-  Item it{-1, 0, 0};
+// Ticket -> work item.  Order: XY(0) .. XY(L-1), then XY(s), Z(s-L) for s =
+// L .. b-1, then the remaining Z blocks (L = lag: the z items of a vector
+// come L vectors after its xy items, so their dependencies are long done).
+__device__ __forceinline__ Item decode(unsigned t, int nvec, int nz, int nzt, int lag) {
   const unsigned ps = (unsigned)(nz + nzt);
-  if (t >= (unsigned)nvec * ps) return it;
-  if (t < (unsigned)nz) return Item{0, 0, (int)t};
-  const unsigned r = t - (unsigned)nz;
-  const unsigned s = r / ps;
-  if (s + 1 < (unsigned)nvec) {
-    const unsigned w = r - s * ps;
-    if (w < (unsigned)nz) return Item{0, (int)s + 1, (int)w};
+  if (t >= (unsigned)nvec * ps) return Item{-1, 0, 0};
+  const int L = lag < nvec ? lag : nvec;
+  const unsigned head = (unsigned)L * nz;
+  if (t < head) return Item{0, (int)(t / nz), (int)(t % nz)};
+  unsigned r = t - head;
+  const unsigned mid = (unsigned)(nvec - L) * ps;
+  if (r < mid) {
+    const unsigned s = r / ps, w = r - s * ps;
+    if (w < (unsigned)nz) return Item{0, L + (int)s, (int)w};
     return Item{1, (int)s, (int)(w - nz)};
   }
-  return Item{1, nvec - 1, (int)(r - (unsigned)(nvec - 1) * ps)};
+  r -= mid;
+  return Item{1, nvec - L + (int)(r / nzt), (int)(r % nzt)};
 }
 
 __device__ __forceinline__ void vec_ptrs(const FusedJobs& J, int u, long N, const double*& x, double*& y,
@@ -209,70 +219,90 @@ constexpr int kProdWarps = 7;
 constexpr int kEpiWarps = 8;
 constexpr int kIssueWarp = kProdWarps + kEpiWarps;
 constexpr int kThreadsAll = (kIssueWarp + 1) * 32;
-constexpr int kRing = 4;
+constexpr int kRing = 8;  // tickets in flight in one CTA: at most five (fill .. epilogue)
 
 // xy item: the plane of vector u at z index k into both images.  Producer
-// warp w fills core matrices w, w + 7, ... of the natural image (rows j, K =
-// i): lane L takes row j = 8 gj + L/4 and i = 4 qi + L%4, so a warp load
-// reads 8 grid lines x 32 bytes and its store fills one 128-byte core
-// matrix; the same value goes to the transposed image (rows i, K = j).
+// warp w fills core matrices cm = w, w + 7, ... of the natural image (rows
+// j, K = i; cm = gj * kx/4 + qi): lane L takes row j = 8 gj + L/4 and i =
+// 4 qi + L%4, so a warp load reads 8 grid lines x 32 bytes and its store
+// fills one 128-byte core matrix; the same value goes to the transposed
+// image (rows i, K = j).  (gj, qi) advance by 7 core matrices per step
+// without a division.  The loads of the first round are issued before
+// ready() returns (ready waits until the images are free), so their latency
+// overlaps that wait.
+template <class Ready>
 __device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __restrict__ P, unsigned char* smem,
-                                           int pw, int lane) {
+                                           int pw, int lane, Ready&& ready) {
   const int kq = G.kx >> 2;
   const int ncm = (G.npy >> 3) * kq;
-  const int kyq = G.ky >> 2;
+  const int kyq32 = (G.ky >> 2) * 32;
+  const int lj = lane >> 2, li = lane & 3;
+  const int pt_lane = (lj >> 2) * 32 + li * 4 + (lj & 3);  // transposed-image offset of the lane in its block
   float* pnh = reinterpret_cast<float*>(smem + G.pn_hi);
   float* pnl = reinterpret_cast<float*>(smem + G.pn_lo);
   float* pth = reinterpret_cast<float*>(smem + G.pt_hi);
   float* ptl = reinterpret_cast<float*>(smem + G.pt_lo);
-  for (int c0 = pw; c0 < ncm; c0 += kProdWarps * kBatch) {
+  const int rounds = (ncm + kProdWarps * kBatch - 1) / (kProdWarps * kBatch);
+  int gj = pw / kq, qi = pw - (pw / kq) * kq;  // of cm = pw
+  for (int r = 0; r < rounds; ++r) {
+    const int c0 = pw + r * kProdWarps * kBatch;
     double xv[kBatch];
+    int sgj = gj, sqi = qi;
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
-      const int cm = c0 + kProdWarps * b;
-      const int gj = cm / kq, qi = cm - gj * kq;
-      const int j = 8 * gj + (lane >> 2), i = 4 * qi + (lane & 3);
-      xv[b] = (cm < ncm && j < G.ny && i < G.nx) ? P[i + (long)G.nx * j] : 0.0;
+      const int j = 8 * gj + lj, i = 4 * qi + li;
+      xv[b] = (c0 + kProdWarps * b < ncm && j < G.ny && i < G.nx) ? P[i + (long)G.nx * j] : 0.0;
+      qi += kProdWarps;
+      while (qi >= kq) qi -= kq, ++gj;
     }
+    if (r == 0) ready();
+    gj = sgj, qi = sqi;
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
       const int cm = c0 + kProdWarps * b;
       if (cm < ncm) {
-        const int gj = cm / kq, qi = cm - gj * kq;
-        const int j = 8 * gj + (lane >> 2), i = 4 * qi + (lane & 3);
         float h, l;
         split_tf32(xv[b], h, l);
         pnh[cm * 32 + lane] = h;
         pnl[cm * 32 + lane] = l;
-        if (j < G.ky) {
-          const int off = (((i >> 3) * kyq + (j >> 2)) << 5) + ((i & 7) << 2) + (j & 3);
+        if (8 * gj + lj < G.ky) {
+          const int off = (qi >> 1) * kyq32 + (qi & 1) * 16 + gj * 64 + pt_lane;
           pth[off] = h;
           ptl[off] = l;
         }
       }
+      qi += kProdWarps;
+      while (qi >= kq) qi -= kq, ++gj;
     }
   }
+  if (rounds == 0) ready();
 }
 
-// z item: grid points p0 .. p0 + 127 of every plane (rows), K = z index.
-// Lane L takes row 8 g + L/4 and K 4 q + L%4: a warp load reads four runs of
-// eight consecutive points.
+// z item: grid points p0 .. p0 + 127 of every plane (rows), K = z index
+// (cm = g * kz/4 + q).  Lane L takes row 8 g + L/4 and K 4 q + L%4: a warp
+// load reads four runs of eight consecutive points.
+template <class Ready>
 __device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __restrict__ X, long p0, long nxny,
-                                           unsigned char* smem, int pw, int lane) {
+                                           unsigned char* smem, int pw, int lane, Ready&& ready) {
   const int kq = G.kz >> 2;
   const int ncm = (kTile / 8) * kq;
+  const int lj = lane >> 2, li = lane & 3;
   float* zh = reinterpret_cast<float*>(smem + G.z_hi);
   float* zl = reinterpret_cast<float*>(smem + G.z_lo);
-  for (int c0 = pw; c0 < ncm; c0 += kProdWarps * kBatch) {
+  const int rounds = (ncm + kProdWarps * kBatch - 1) / (kProdWarps * kBatch);
+  int g = pw / kq, q = pw - (pw / kq) * kq;
+  for (int r = 0; r < rounds; ++r) {
+    const int c0 = pw + r * kProdWarps * kBatch;
     double xv[kBatch];
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
-      const int cm = c0 + kProdWarps * b;
-      const int g = cm / kq, q = cm - g * kq;
-      const long p = p0 + 8 * g + (lane >> 2);
-      const int k = 4 * q + (lane & 3);
-      xv[b] = (cm < ncm && p < nxny && k < G.nz) ? X[p + nxny * k] : 0.0;
+      const long p = p0 + 8 * g + lj;
+      const int k = 4 * q + li;
+      xv[b] = (c0 + kProdWarps * b < ncm && p < nxny && k < G.nz) ? X[p + nxny * k] : 0.0;
+      q += kProdWarps;
+      while (q >= kq) q -= kq, ++g;
     }
+    if (r == 0) ready();
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
       const int cm = c0 + kProdWarps * b;
@@ -284,6 +314,7 @@ __device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __r
       }
     }
   }
+  if (rounds == 0) ready();
 }
 
 // One thread: prefetch the X data of an item into L2 (the fill then reads L2).
@@ -342,7 +373,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t mbar_t, mbar_full, mbar_empty, mbar_acc_full[2], mbar_acc_empty[2];
   __shared__ uint32_t tmem_base;
-  __shared__ unsigned ring[kRing], epi_ring[kRing];
+  __shared__ unsigned ring[kRing];
   __shared__ int s_abort, s_prod_ok, s_epi_ok, s_last;
   volatile int* abort = &s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -385,72 +416,107 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
   pg::pdl_wait();
   pg::pdl_release();
   const uint32_t tmem = tmem_base;
+  if (tid == 0) ring[0] = atomicAdd(&cnt->ticket, 1u);
+  __syncthreads();
 
   if (warp < kProdWarps) {
     // ------------------------------------------------------------ producers
     const int ptid = tid;  // 0 .. 32 kProdWarps - 1
-    if (ptid == 0) ring[0] = atomicAdd(&cnt->ticket, 1u);
     for (int i = 0;; ++i) {
+      // ring[i] was written before the previous item's barrier; the leader
+      // takes the ticket after it now, so its X data is in L2 by its turn
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
       if (ptid == 0) {
-        int ok = 1;
-        // the previous item's MMAs are done with the images
-        if (i >= 1) ok = mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
-        if (ok) {
-          const unsigned t1 = atomicAdd(&cnt->ticket, 1u);
-          ring[(i + 1) % kRing] = t1;
-          prefetch_item(G, J, decode(t1, nvec, G.nz, G.nzt), N, nxny);
-        } else {
-          *abort = 1;
+        const unsigned t1 = atomicAdd(&cnt->ticket, 1u);
+        ring[(i + 1) % kRing] = t1;
+        prefetch_item(G, J, decode(t1, nvec, G.nz, G.nzt, G.lag), N, nxny);
+      }
+      // the images are free once the previous item's MMAs are done
+      auto ready = [&]() {
+        if (ptid == 0) {
+          const int ok = i == 0 || mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
+          if (!ok) *abort = 1;
+          s_prod_ok = ok;
         }
-        s_prod_ok = ok;
-      }
-      named_sync(1, kProdWarps * 32);
+        named_sync(1, kProdWarps * 32);
+      };
+      const double *x, *v;
+      double* y;
+      if (it.kind >= 0) vec_ptrs(J, it.u, N, x, y, v);
+      if (it.kind == 0)
+        fill_plane(G, x + nxny * it.idx, smem, warp, lane, ready);
+      else if (it.kind == 1)
+        fill_ztile(G, x, (long)it.idx * kTile, nxny, smem, warp, lane, ready);
+      else
+        ready();
       if (!s_prod_ok) break;
-      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt);
-      if (it.kind >= 0) {
-        const double *x, *v;
-        double* y;
-        vec_ptrs(J, it.u, N, x, y, v);
-        if (it.kind == 0)
-          fill_plane(G, x + nxny * it.idx, smem, warp, lane);
-        else
-          fill_ztile(G, x, (long)it.idx * kTile, nxny, smem, warp, lane);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      }
-      // (ring[i] is rewritten three items later, after the leader has seen
-      // this item's MMAs complete, which needs every producer's arrival)
+      if (it.kind >= 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(smem_u32(&mbar_full));
       if (it.kind < 0) break;
     }
   } else if (warp < kIssueWarp) {
     // ------------------------------------------------------------- epilogue
+    // No FP64 arithmetic here (see f64_to_f32): V X + D and W + D in FP32,
+    // converted with integer operations; the result is stored as FP64.
     const int quarter = warp & 3, half = (warp - kProdWarps) >> 2;
     const bool leader = warp == kProdWarps && lane == 0;
     for (int i = 0;; ++i) {
       const int b = i & 1;
-      if (leader) s_epi_ok = mbar_wait_or_abort(smem_u32(&mbar_acc_full[b]), (uint32_t)((i >> 1) & 1), abort);
-      named_sync(2, kEpiWarps * 32);
-      if (!s_epi_ok) {
-        if (leader) *abort = 1;
-        break;
+      // ring[i] was written before the producers' arrival for item i - 1,
+      // which the wait for item i - 1 below has seen
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
+      const double *x = nullptr, *v = nullptr;
+      double* y = nullptr;
+      if (it.kind >= 0) vec_ptrs(J, it.u, N, x, y, v);
+      const int i0 = 32 * quarter + lane;
+      const long pl = nxny * (it.kind == 0 ? it.idx : 0);
+      const long p = (long)(it.kind == 1 ? it.idx : 0) * kTile + i0;
+      // the first chunk's V X before the accumulator is ready
+      float pre[16];
+      if (it.kind == 0 && half < (G.npy >> 4)) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int j = 16 * half + q;
+          const long a = pl + i0 + (long)G.nx * j;
+          pre[q] = (i0 < G.nx && j < G.ny) ? pg::f64_to_f32(v[a]) * pg::f64_to_f32(x[a]) : 0.f;
+        }
       }
+      if (leader) {
+        int ok = 1;
+        if (it.kind == 1) {
+          // every plane of the vector has its W in Y (bounded wait, ~2 s)
+          const unsigned long long t0 = globaltimer_ns();
+          while (*(volatile unsigned*)&cnt->done[it.u] < (unsigned)G.nz) {
+            if (*abort || globaltimer_ns() - t0 > 2000000000ull) {
+              ok = 0;
+              break;
+            }
+            __nanosleep(128);
+          }
+          __threadfence();
+        }
+        if (ok) ok = mbar_wait_or_abort(smem_u32(&mbar_acc_full[b]), (uint32_t)((i >> 1) & 1), abort);
+        if (!ok) *abort = 1;
+        s_epi_ok = ok;
+      }
+      named_sync(2, kEpiWarps * 32);
+      if (!s_epi_ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const Item it = decode(epi_ring[i % kRing], nvec, G.nz, G.nzt);
       if (it.kind < 0) break;
-      const double *x, *v;
-      double* y;
-      vec_ptrs(J, it.u, N, x, y, v);
       const uint32_t acc = tmem + (uint32_t)b * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
       if (it.kind == 0) {
-        const int i0 = 32 * quarter + lane;
-        const long pl = nxny * it.idx;
         for (int c = half; c < (G.npy >> 4); c += 2) {
-          double vx[16];
+          float vx[16];
+          if (c == half) {
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int j = 16 * c + q;
-            const long a = pl + i0 + (long)G.nx * j;
-            vx[q] = (i0 < G.nx && j < G.ny) ? v[a] * x[a] : 0.0;
+            for (int q = 0; q < 16; ++q) vx[q] = pre[q];
+          } else {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int j = 16 * c + q;
+              const long a = pl + i0 + (long)G.nx * j;
+              vx[q] = (i0 < G.nx && j < G.ny) ? pg::f64_to_f32(v[a]) * pg::f64_to_f32(x[a]) : 0.f;
+            }
           }
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
@@ -458,37 +524,17 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int j = 16 * c + q;
-              if (j < G.ny) y[pl + i0 + (long)G.nx * j] = vx[q] + (double)d[q];
+              if (j < G.ny) y[pl + i0 + (long)G.nx * j] = pg::f32_to_f64(vx[q] + d[q]);
             }
           }
         }
       } else {
-        if (leader) {
-          // every plane of the vector has its W in Y (bounded wait, ~2 s)
-          int f = 1;
-          const unsigned long long t0 = globaltimer_ns();
-          while (*(volatile unsigned*)&cnt->done[it.u] < (unsigned)G.nz) {
-            if (*abort || globaltimer_ns() - t0 > 2000000000ull) {
-              f = 0;
-              break;
-            }
-            __nanosleep(128);
-          }
-          __threadfence();
-          s_epi_ok = f;
-        }
-        named_sync(2, kEpiWarps * 32);
-        if (!s_epi_ok) {
-          if (leader) *abort = 1;
-          break;
-        }
-        const long p = (long)it.idx * kTile + 32 * quarter + lane;
         for (int c = half; c < (G.npz >> 4); c += 2) {
-          double w[16];
+          float w[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             const int k = 16 * c + q;
-            w[q] = (p < nxny && k < G.nz) ? __ldcg(y + p + nxny * k) : 0.0;
+            w[q] = (p < nxny && k < G.nz) ? pg::f64_to_f32(__ldcg(y + p + nxny * k)) : 0.f;
           }
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
@@ -496,7 +542,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int k = 16 * c + q;
-              if (k < G.nz) y[p + nxny * k] = w[q] + (double)d[q];
+              if (k < G.nz) y[p + nxny * k] = pg::f32_to_f64(w[q] + d[q]);
             }
           }
         }
@@ -536,9 +582,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (ok && i >= 2) ok = mbar_wait_or_abort(smem_u32(&mbar_acc_empty[b]), (uint32_t)(((i - 2) >> 1) & 1), abort);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const unsigned t = ring[i % kRing];
-      epi_ring[i % kRing] = t;
-      const Item it = decode(t, nvec, G.nz, G.nzt);
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
       if (it.kind < 0) {
         mbar_arrive(smem_u32(&mbar_acc_full[b]));
         mbar_arrive(smem_u32(&mbar_acc_full[b]));
@@ -570,7 +614,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
           smem_u32(&mbar_empty)));
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(&mbar_acc_full[b])));
-      mbar_arrive(smem_u32(&mbar_acc_full[b]));  // with it, epi_ring[i] is visible to the epilogue
+      mbar_arrive(smem_u32(&mbar_acc_full[b]));  // orders the issuer's reads before the epilogue's
       last_commit = i;
     }
     if (!ok) {
@@ -662,6 +706,7 @@ FusedPlan plan_fused(const pg_grid* g) {
   G.npz = tc_npad(nz);
   if (G.npy > 256 || G.npz > 256) return no("N > 256");
   G.nzt = (int)(((long)nx * ny + kTile - 1) / kTile);
+  G.lag = 2;
   const int npx = tc_npad(nx);
   const uint32_t sz_t[3] = {(uint32_t)npx * G.kx * 4, (uint32_t)G.npy * G.ky * 4, (uint32_t)G.npz * G.kz * 4};
   const uint32_t sz_pt = (uint32_t)G.kx * G.ky * 4;   // rows i (kx), K = j
@@ -823,9 +868,9 @@ void hx_plan_text(const pg_grid* g, char* buf, int len) {
   const FusedPlan P = plan_fused(g);
   if (P.ok)
     snprintf(buf, (size_t)len,
-             "fused (k_hx_fused): xy planes %dx%d + z tiles of 128 lines (%d per vector), K %d/%d/%d, "
-             "%zu B shared memory, %d constant images, %u TMEM columns x 2",
-             P.G.nx, P.G.ny, P.G.nzt, P.G.kx, P.G.ky, P.G.kz, P.smem, P.C.n / 2, P.G.acc_cols);
+             "fused (k_hx_fused): xy planes %dx%d + z tiles of 128 lines (%d per vector, lag %d vectors), "
+             "K %d/%d/%d, %zu B shared memory, %d constant images, %u TMEM columns x 2",
+             P.G.nx, P.G.ny, P.G.nzt, P.G.lag, P.G.kx, P.G.ky, P.G.kz, P.smem, P.C.n / 2, P.G.acc_cols);
   else
     snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): %s", P.why);
 }
