@@ -161,35 +161,6 @@ struct HostPinned {
 inline __host__ __device__ unsigned tc_kmajor_off(int r, int k, int kpad) {
   return (unsigned)(((r >> 3) * (kpad >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
-// FP64 <-> FP32 conversions with integer operations only, for the mixed
-// form's epilogues: the FP64 pipe of this part retires about two FMAs per SM
-// per clock, so one FP64 instruction per element (a multiply, an add or a
-// float-double conversion) would bound those kernels.  f64_to_f32 rounds to
-// nearest (ties away from zero); |x| below 2^-126 gives a signed zero,
-// |x| >= 2^128 and Inf give +-Inf, NaN gives NaN.  f32_to_f64 is exact for
-// normal numbers and zero, flushes FP32 subnormals to zero, and keeps Inf/NaN.
-__device__ __forceinline__ float f64_to_f32(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-  const int e = (int)((b >> 52) & 0x7ff);
-  const unsigned long long m = (b & 0x7fffffffffffffffull) + (1ull << 28);
-  const int e2 = (int)(m >> 52) - 896;
-  unsigned f = sign | ((unsigned)e2 << 23) | ((unsigned)(m >> 29) & 0x7fffffu);
-  if (e2 <= 0) f = sign;
-  if (e2 >= 255) f = sign | 0x7f800000u;
-  if (e == 0x7ff && (b & 0xfffffffffffffull)) f = 0x7fc00000u;
-  return __uint_as_float(f);
-}
-__device__ __forceinline__ double f32_to_f64(float v) {
-  const unsigned u = __float_as_uint(v);
-  const unsigned sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
-  unsigned hi = sign | ((e + 896u) << 20) | (m >> 3);
-  unsigned lo = m << 29;
-  if (e == 0) hi = sign, lo = 0;
-  if (e == 255) hi = sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u), lo = 0;
-  return __hiloint2double((int)hi, (int)lo);
-}
-
 inline __host__ __device__ int tc_npad(int n) { return (n + 15) / 16 * 16; }
 inline __host__ __device__ int tc_kpad(int n) { return (n + 7) / 8 * 8; }
 // K chunk of the tensor-core contraction: the B chunk (npad x kc) and the A

@@ -25,11 +25,8 @@
 // whatever the number of resident CTAs.
 //
 // Precision as the three-pass kernels (pg_hx_tc.cu): split-TF32 products
-// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM (~2^-21 relative per
-// term); V X and the sums in FP32 (2^-24), converted to and from FP64 with
-// integer operations, because this part's FP64 pipe retires about two FMAs
-// per SM per clock and one FP64 operation per element would bound the
-// epilogue.  The partial W = V X + Kx + Ky is kept in Y (as FP64 storage).
+// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM, V X and the sums into Y
+// in FP64.  The partial W = V X + Kx + Ky is kept in FP64 in Y.
 //
 // Shared memory (no-swizzle K-major core matrices, as pg_hx_tc.cu): the
 // kinetic matrices (resident; one image when the axes share one matrix),
@@ -456,8 +453,6 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     }
   } else if (warp < kIssueWarp) {
     // ------------------------------------------------------------- epilogue
-    // No FP64 arithmetic here (see f64_to_f32): V X + D and W + D in FP32,
-    // converted with integer operations; the result is stored as FP64.
     const int quarter = warp & 3, half = (warp - kProdWarps) >> 2;
     const bool leader = warp == kProdWarps && lane == 0;
     for (int i = 0;; ++i) {
@@ -472,13 +467,13 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       const long pl = nxny * (it.kind == 0 ? it.idx : 0);
       const long p = (long)(it.kind == 1 ? it.idx : 0) * kTile + i0;
       // the first chunk's V X before the accumulator is ready
-      float pre[16];
+      double pre[16];
       if (it.kind == 0 && half < (G.npy >> 4)) {
 #pragma unroll
         for (int q = 0; q < 16; ++q) {
           const int j = 16 * half + q;
           const long a = pl + i0 + (long)G.nx * j;
-          pre[q] = (i0 < G.nx && j < G.ny) ? pg::f64_to_f32(v[a]) * pg::f64_to_f32(x[a]) : 0.f;
+          pre[q] = (i0 < G.nx && j < G.ny) ? v[a] * x[a] : 0.0;
         }
       }
       if (leader) {
@@ -506,7 +501,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       const uint32_t acc = tmem + (uint32_t)b * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
       if (it.kind == 0) {
         for (int c = half; c < (G.npy >> 4); c += 2) {
-          float vx[16];
+          double vx[16];
           if (c == half) {
 #pragma unroll
             for (int q = 0; q < 16; ++q) vx[q] = pre[q];
@@ -515,7 +510,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
             for (int q = 0; q < 16; ++q) {
               const int j = 16 * c + q;
               const long a = pl + i0 + (long)G.nx * j;
-              vx[q] = (i0 < G.nx && j < G.ny) ? pg::f64_to_f32(v[a]) * pg::f64_to_f32(x[a]) : 0.f;
+              vx[q] = (i0 < G.nx && j < G.ny) ? v[a] * x[a] : 0.0;
             }
           }
           float d[16];
@@ -524,17 +519,17 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int j = 16 * c + q;
-              if (j < G.ny) y[pl + i0 + (long)G.nx * j] = pg::f32_to_f64(vx[q] + d[q]);
+              if (j < G.ny) y[pl + i0 + (long)G.nx * j] = vx[q] + (double)d[q];
             }
           }
         }
       } else {
         for (int c = half; c < (G.npz >> 4); c += 2) {
-          float w[16];
+          double w[16];
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             const int k = 16 * c + q;
-            w[q] = (p < nxny && k < G.nz) ? pg::f64_to_f32(__ldcg(y + p + nxny * k)) : 0.f;
+            w[q] = (p < nxny && k < G.nz) ? __ldcg(y + p + nxny * k) : 0.0;
           }
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
@@ -542,7 +537,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int k = 16 * c + q;
-              if (k < G.nz) y[p + nxny * k] = pg::f32_to_f64(w[q] + d[q]);
+              if (k < G.nz) y[p + nxny * k] = w[q] + (double)d[q];
             }
           }
         }

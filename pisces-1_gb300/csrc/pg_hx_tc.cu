@@ -11,11 +11,9 @@
 // runs K in chunks, restaging each chunk of B per tile.  Both are split into
 // TF32 high and low parts, D = Ah*Bh + Ah*Bl + Al*Bh (error ~2^-21 relative per term; Al*Bl dropped),
 // accumulated in FP32 in TMEM.  X is split on the fly from FP64 with integer
-// operations only, and the epilogue adds in FP32 with integer FP64<->FP32
-// conversions (the FP64 pipe is two orders of magnitude slower on this
-// part): Y carries FP32 precision, below the split products' own error.
-// Three passes: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X; X stays L2 resident
-// between passes for the grids of the eigensolve workloads.
+// operations only (the FP64 pipe is two orders of magnitude slower on this
+// part).  Three passes: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X; X stays L2
+// resident between passes for the grids of the eigensolve workloads.
 //
 // Operand layout in shared memory: no-swizzle K-major core matrices
 // (8 rows x 16 bytes); K-adjacent core matrices 128 B apart (leading byte
@@ -122,7 +120,7 @@ __device__ __forceinline__ void epilogue_x16(const float (&d)[16], float* stg, i
   // and 16 rounds of them do not fit the 128 registers of the launch
 #pragma unroll
   for (int h = 0; h < 16; h += 8) {
-    float prev[8];
+    double prev[8];
     float val[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
@@ -132,16 +130,16 @@ __device__ __forceinline__ void epilogue_x16(const float (&d)[16], float* stg, i
       const long gs = (long)__shfl_sync(0xffffffffu, (long long)gshift_own, r);
       const long c = c0w + r;
       const long a = (long)nx * c + i;
-      prev[u] = 0.f;
+      prev[u] = 0.0;
       if (c < ncols && i < n) {
-        if (mode == 2) prev[u] = pg::f64_to_f32(v[a - gs]) * pg::f64_to_f32(X[a]);
-        else if (mode == 1) prev[u] = pg::f64_to_f32(Y[a]);
+        if (mode == 2) prev[u] = v[a - gs] * X[a];
+        else if (mode == 1) prev[u] = Y[a];
       }
     }
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const long c = c0w + 2 * (h + u) + half;
-      if (c < ncols && i < n) Y[(long)nx * c + i] = pg::f32_to_f64(prev[u] + val[u]);
+      if (c < ncols && i < n) Y[(long)nx * c + i] = prev[u] + (double)val[u];
     }
   }
   __syncwarp();  // the block is rewritten by the warp's next chunk
@@ -384,21 +382,21 @@ __global__ void __launch_bounds__(kThreads, 1)
         float* stg = reinterpret_cast<float*>(smem + stage_off + (uint32_t)warp * kStageWarpBytes);
         epilogue_x16(d, stg, lane, c0 + 32 * quarter, ncols, ck * 16, n, nx, gshift, mode, X, Y, v);
       } else if (cvalid) {
-        float prev[16];
+        double prev[16];
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int i = ck * 16 + j;
           const long a = base + (long)i * am.stride;
-          prev[j] = 0.f;
+          prev[j] = 0.0;
           if (i < n) {
-            if (mode == 2) prev[j] = pg::f64_to_f32(v[a - gshift]) * pg::f64_to_f32(X[a]);
-            else if (mode == 1) prev[j] = pg::f64_to_f32(Y[a]);
+            if (mode == 2) prev[j] = v[a - gshift] * X[a];
+            else if (mode == 1) prev[j] = Y[a];
           }
         }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int i = ck * 16 + j;
-          if (i < n) Y[base + (long)i * am.stride] = pg::f32_to_f64(prev[j] + d[j]);
+          if (i < n) Y[base + (long)i * am.stride] = prev[j] + (double)d[j];
         }
       }
     }
@@ -583,21 +581,21 @@ __global__ void __launch_bounds__(kPipeThreads, 1)
           float* stg = reinterpret_cast<float*>(smem + stage_off + (uint32_t)cw * kStageWarpBytes);
           epilogue_x16(d, stg, lane, c0 + 32 * quarter, ncols, ck * 16, n, nx, gshift, mode, X, Y, v);
         } else if (cvalid) {
-          float prev[16];
+          double prev[16];
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int r = ck * 16 + j;
             const long a = base + (long)r * am.stride;
-            prev[j] = 0.f;
+            prev[j] = 0.0;
             if (r < n) {
-              if (mode == 2) prev[j] = pg::f64_to_f32(v[a - gshift]) * pg::f64_to_f32(X[a]);
-              else if (mode == 1) prev[j] = pg::f64_to_f32(Y[a]);
+              if (mode == 2) prev[j] = v[a - gshift] * X[a];
+              else if (mode == 1) prev[j] = Y[a];
             }
           }
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int r = ck * 16 + j;
-            if (r < n) Y[base + (long)r * am.stride] = pg::f32_to_f64(prev[j] + d[j]);
+            if (r < n) Y[base + (long)r * am.stride] = prev[j] + (double)d[j];
           }
         }
       }
