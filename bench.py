@@ -14,11 +14,16 @@ The same run also times the plain FP64 form (residual 1e-8) on the same
 problem -- with the same corrections and with the reference's diagonal
 correction (corrflag 1) -- and reports |dE| of the mixed eigenvalues against
 the FP64 ones.  `value` is mixed solves/s; `e2e` is the same through
-pg_cluster_solve with host buffers.
+pg_cluster_solve with host buffers; `like_for_like` sets the FP64 GPU solve
+with the reference's algorithm against the same algorithm on the host cores;
+`serving_c4` summarises the serving stream (mixed and FP64 solves/s at
+saturation, their ratio, Poisson p50/p99) measured in the same run.
+`config` names the workload only (the same in both arms); `solver` gives
+each arm's arithmetic, correction and residual.
 
   python bench.py [--steps K] [--warmup W] [--precision mixed|fp64] [--corrflag 1|3]
   python bench.py --workload c4         # the serving stream through pg_engine_*
-  python bench.py --impl reference      # the reference algorithm on the host cores
+  python bench.py --impl reference      # the reference algorithm on the host cores, complete solves
   python bench.py --roofline-only       # the dominant kernels alone (for ncu captures)
 
 Multi-GPU (torchrun, one rank per GPU): replicas only -- every rank solves
@@ -250,7 +255,8 @@ def run_ours(args, ws, rank, local):
         e2e_ms = (time.perf_counter() - t0) * 1000 / reps
 
     roof = kernel_rooflines(pg, torch, grid, tables, nroots, precision, stream)
-    return dict(total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
+    hx_plan = grid.hx_plan()
+    return dict(hx_plan=hx_plan, total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
                 de=de, stats=st, fp64=fp64, refalg=refalg, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d,
                 d2h=d2h, roofline=roof, N=N, precision=args.precision, ptol=ptol)
 
@@ -357,6 +363,74 @@ def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
                       f"of a full solve", "seconds_per_matvec": per, "potential_s": t_pot}
 
 
+REFERENCE_BUDGET_S = 170.0  # CPU seconds the reference arm may spend on complete solves
+
+
+def reference_arm(args, wl, cfg):
+    """The reference algorithm on the host cores: the oracle port of the
+    reference's Davidson (src/Davidson.cpp:61-376, diagonal correction, FP64,
+    residual 10^-ptol) and of V(r), with every host thread.  A step is one
+    COMPLETE single point (V(r) on the full grid and the solve to
+    convergence).  Full solves take about a minute each on the GB300 host, so
+    the arm times as many as fit REFERENCE_BUDGET_S (at least one) instead of
+    the requested --steps, and says so; its warm-up steps are bounded samples
+    (the first 20 H*x of the solve)."""
+    orc = entry.load_oracle()
+    import importlib
+    entry.load_package()
+    clusters = importlib.import_module("pisces_gb300.clusters")
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    waters = clusters.water_cluster(wl["nw"], wl["radius"], wl["seed"])
+    ions = workload_ions(clusters, wl, waters)
+    g = orc.Grid(wl["n"], wl["L"])
+    s = orc.dpp_sites(waters)
+
+    def potential():
+        v = g.potential_dpp(*s[:5])
+        if ions is not None:
+            g.add_ions(v, (ions[:, :3] * A2B).reshape(-1), ions[:, 3])
+        return v
+
+    def point(max_matvec=0):
+        v = potential()
+        st, ev, _, nmv = g.solve(v, nstates=wl["nroots"], maxsub=wl["maxsub"], maxiter=2000, ptol=wl["ptol"],
+                                 corrflag=1, max_matvec=max_matvec)
+        return st, ev, nmv
+
+    for _ in range(args.warmup):
+        point(max_matvec=20)
+    # the expected length of a complete solve from a bounded sample
+    t0 = time.perf_counter()
+    _, _, nmv = point(max_matvec=200)
+    per = (time.perf_counter() - t0) / max(nmv, 1)
+    expect = per * REFERENCE_MATVECS.get(args.workload, 4500)
+    nsolves = max(1, min(args.steps, int(REFERENCE_BUDGET_S // max(expect, 1e-9))))
+    times, evals, matvecs = [], None, []
+    for _ in range(nsolves):
+        t0 = time.perf_counter()
+        st, ev, nmv = point()
+        times.append(time.perf_counter() - t0)
+        evals = list(map(float, ev))
+        matvecs.append(int(nmv))
+    ms = 1000.0 * statistics.mean(times)
+    val = 1000.0 / ms
+    return {"impl": "reference", "metric": "solves/s", "value": val, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": nsolves, "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": cfg,
+            "solver": {"precision": "fp64", "corrflag": 1, "residual_tol": 10.0 ** -wl["ptol"],
+                       "algorithm": "the reference's Davidson (diagonal correction) restated in C (oracle port)"},
+            "eigenvalues": evals, "n_matvec": matvecs,
+            "note": f"{nsolves} complete single point(s) timed (of {args.steps} requested: a complete solve "
+                    f"takes ~{expect:.0f} s on these cores); warm-up steps are bounded samples (first 20 H*x)",
+            "cpu_baseline": {"value": val, "unit": "solves/s", "cores": threads, "kind": "port",
+                             "sample": f"{nsolves} complete reference-algorithm single point(s): V(r) on the "
+                                       f"{wl['n'][0]}^3 grid and the Davidson solve to residual "
+                                       f"1e-{wl['ptol']} ({matvecs} H*x)"},
+            "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def c4_stream(clusters, nreq, seed=C4["seed"]):
     rng = np.random.Generator(np.random.PCG64(seed))
     sizes = [int(x) for x in rng.integers(8, 65, size=C4["nbase"])]
@@ -400,18 +474,12 @@ def serve_stream(pg, reqs, precision, rate, slots, batch, window_us):
                 n_matvec=sum(r["stats"]["n_matvec"] for r in res))
 
 
-def run_c4(args):
+def c4_measure(pg, clusters, nreq, warmup, slots, window, unbatched=True):
     """The serving stream through the engine (pg_engine_*): mixed form at
-    saturation and at Poisson arrivals, FP64 at saturation, same requests."""
-    import torch
-    pg = entry.load_package()
-    import importlib
-    clusters = importlib.import_module("pisces_gb300.clusters")
-    torch.cuda.set_device(0)
-    nreq = args.requests
+    saturation and at Poisson arrivals (0.7 of saturation), FP64 at
+    saturation, on the same requests; returns the measurements."""
     sizes, reqs = c4_stream(clusters, nreq)
-    _, warm = c4_stream(clusters, max(3, args.warmup) * 8, seed=C4["seed"] + 1)
-    slots, window = args.slots, args.window_us
+    _, warm = c4_stream(clusters, max(3, warmup) * 8, seed=C4["seed"] + 1)
     for prec in (pg.PG_MIXED, pg.PG_FP64):  # warm-up: kernels, grids, allocator
         serve_stream(pg, warm, prec, None, slots, True, window)
     clocks = ClockSampler(0)
@@ -419,31 +487,63 @@ def run_c4(args):
     mixed = serve_stream(pg, reqs, pg.PG_MIXED, None, slots, True, window)
     clk = clocks.stop()
     fp64 = serve_stream(pg, reqs, pg.PG_FP64, None, slots, True, window)
-    unbatched = serve_stream(pg, reqs, pg.PG_MIXED, None, slots, False, window)
+    unb = serve_stream(pg, reqs, pg.PG_MIXED, None, slots, False, window) if unbatched else None
     rate = 0.7 * mixed["solves_per_s"]
     poisson = serve_stream(pg, reqs, pg.PG_MIXED, rate, slots, True, window)
     de = max(abs(a - b) for rm, rf in zip(mixed["results"], fp64["results"])
              for a, b in zip(rm["evals"], rf["evals"]))
+    return dict(sizes=sizes, reqs=reqs, warm=warm, mixed=mixed, fp64=fp64, unbatched=unb, rate=rate,
+                poisson=poisson, de=de, clocks=clk)
+
+
+def c4_summary(m):
+    """The stream's figures for the default bench line."""
+    return {"requests": len(m["reqs"]), "mixed_solves_per_s": m["mixed"]["solves_per_s"],
+            "fp64_solves_per_s": m["fp64"]["solves_per_s"],
+            "mixed_over_fp64": m["mixed"]["solves_per_s"] / m["fp64"]["solves_per_s"],
+            "poisson": {"rate_per_s": m["rate"], "solves_per_s": m["poisson"]["solves_per_s"],
+                        "p50_ms": m["poisson"]["p50"], "p99_ms": m["poisson"]["p99"]},
+            "saturation_latency_ms": {"p50": m["mixed"]["p50"], "p99": m["mixed"]["p99"]},
+            "max_abs_dE_vs_fp64": m["de"], "failed": m["mixed"]["failed"] + m["fp64"]["failed"],
+            "warm_starts": m["mixed"]["stats"]["warm_starts"], "clocks": m["clocks"],
+            "workload": f"{len(m['reqs'])} single points, grids {list(C4['grids'])}^3, 1-{C4['max_roots']} states, "
+                        f"seed {C4['seed']}; mixed residual 1e-{MIXED_PTOL} + FP64 Rayleigh-Ritz, "
+                        f"FP64 residual 1e-{C4['ptol_fp64']}, corrflag {C4['corrflag']} both"}
+
+
+def run_c4(args):
+    """The serving stream as its own bench line (`--workload c4`)."""
+    import torch
+    pg = entry.load_package()
+    import importlib
+    clusters = importlib.import_module("pisces_gb300.clusters")
+    torch.cuda.set_device(0)
+    nreq = args.requests
+    slots, window = args.slots, args.window_us
+    m = c4_measure(pg, clusters, nreq, args.warmup, slots, window)
+    mixed, fp64, poisson, reqs, sizes = m["mixed"], m["fp64"], m["poisson"], m["reqs"], m["sizes"]
     h2d = sum(q["waters"].size * 8 for q in reqs) / nreq
     d2h = sum(q["nroots"] * 8 for q in reqs) / nreq
     cfg = {"workload": f"c4: {nreq} single points from {C4['nbase']} base (H2O)n clusters (n = {sorted(sizes)}), "
                        f"grids {list(C4['grids'])}^3 at {C4['spacing']} bohr, 1-{C4['max_roots']} states, "
                        f"maxsub {C4['maxsub']}, warm start per base cluster",
-           "seed": C4["seed"], "slots": slots, "batch_window_us": window, "corrflag": C4["corrflag"],
-           "precision": "mixed", "residual_tol": 10.0 ** -MIXED_PTOL, "fp64_residual_tol": 10.0 ** -C4["ptol_fp64"],
+           "seed": C4["seed"], "slots": slots, "batch_window_us": window,
            "l2": "per-solve working sets of 48^3-96^3 grids; no flush (requests differ)"}
     line = {"metric": "solves/s", "value": mixed["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": nreq,
-            "warmup": len(warm), "ms_per_step": 1000.0 * mixed["wall"] / nreq, "higher_is_better": True,
+            "warmup": len(m["warm"]), "ms_per_step": 1000.0 * mixed["wall"] / nreq, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64+tf32x3", "data": "synthetic", "config": cfg,
+            "solver": {"precision": "mixed", "corrflag": C4["corrflag"], "residual_tol": 10.0 ** -MIXED_PTOL,
+                       "fp64_residual_tol": 10.0 ** -C4["ptol_fp64"]},
             "latency_ms": {"p50": mixed["p50"], "p99": mixed["p99"], "at": "saturation (all submitted at once)"},
-            "poisson": {"rate_per_s": rate, "solves_per_s": poisson["solves_per_s"], "p50_ms": poisson["p50"],
+            "poisson": {"rate_per_s": m["rate"], "solves_per_s": poisson["solves_per_s"], "p50_ms": poisson["p50"],
                         "p99_ms": poisson["p99"]},
             "fp64_gpu": {"solves_per_s": fp64["solves_per_s"], "p50_ms": fp64["p50"], "p99_ms": fp64["p99"],
                          "n_matvec": fp64["n_matvec"]},
             "mixed_over_fp64": mixed["solves_per_s"] / fp64["solves_per_s"],
-            "unbatched_mixed_solves_per_s": unbatched["solves_per_s"],
-            "max_abs_dE_vs_fp64": de, "failed": mixed["failed"] + fp64["failed"],
-            "engine": mixed["stats"], "n_matvec": mixed["n_matvec"], "clocks": clk, "gpu_launches": mixed["launches"],
+            "unbatched_mixed_solves_per_s": m["unbatched"]["solves_per_s"],
+            "max_abs_dE_vs_fp64": m["de"], "failed": mixed["failed"] + fp64["failed"],
+            "engine": mixed["stats"], "n_matvec": mixed["n_matvec"], "clocks": m["clocks"],
+            "gpu_launches": mixed["launches"],
             "e2e": {"value": mixed["solves_per_s"], "unit": "solves/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "note": "the engine takes host coordinates and returns host "
                                                       "eigenvalues: value is already end to end"}}
@@ -469,6 +569,7 @@ def main():
     ap.add_argument("--maxsub", type=int, default=0, help="override the workload's subspace size")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c4", action="store_true", help="skip the serving-stream summary of the default line")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload == "c4":
@@ -493,24 +594,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # single-vector H*x products of a full solve of this workload by the
-        # reference algorithm (diagonal correction), counted by the oracle
-        if args.workload not in REFERENCE_MATVECS:
-            print(json.dumps({"impl": "reference", "unavailable": f"no reference H*x count recorded for "
-                                                                  f"{args.workload}; run bench.py (ours) for it"}))
-            return
-        n_full = REFERENCE_MATVECS[args.workload]
-        steps = []
-        for _ in range(args.warmup + args.steps):
-            steps.append(cpu_baseline(args, wl, n_full, budget_s=4.0))
-        timed = steps[args.warmup:]
-        val = statistics.median(s["value"] for s in timed)
-        line = {"impl": "reference", "metric": "solves/s", "value": val, "unit": "solves/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / val, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": cfg, "cpu_baseline": dict(timed[-1], value=val),
-                "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        print(json.dumps(reference_arm(args, wl, cfg)))
         return
 
     import torch
@@ -536,8 +620,10 @@ def main():
     line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+tf32x3",
-            "data": "synthetic", "config": dict(cfg, precision=args.precision, residual_tol=10.0 ** -r["ptol"],
-                                                  corrflag=args.corrflag),
+            "data": "synthetic", "config": cfg,
+            "solver": {"precision": args.precision, "corrflag": args.corrflag, "residual_tol": 10.0 ** -r["ptol"],
+                       "refine": "FP64 Rayleigh-Ritz step" if args.precision == "mixed" else None,
+                       "hx_kernel": r["hx_plan"]},
             "latency_ms": {"p50": p50, "p99": p99},
             "eigenvalues": r["evals"], "max_abs_dE_vs_fp64": r["de"],
             "solve": {k: r["stats"][k] for k in ("n_matvec", "n_iter", "n_restart", "nconv", "seconds",
@@ -556,6 +642,21 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         nfull = r["refalg"]["n_matvec"] if r["refalg"] else REFERENCE_MATVECS.get(args.workload)
         line["cpu_baseline"] = cpu_baseline(args, WORKLOADS[args.workload], nfull)
+        if r["refalg"]:
+            # the same algorithm on both sides: the reference's diagonal
+            # correction in FP64 to the same residual, GPU against host cores
+            a, b = line["fp64_gpu_reference_algorithm"]["solves_per_s"], line["cpu_baseline"]["value"]
+            line["like_for_like"] = {"fp64_gpu_reference_algorithm_solves_per_s": a,
+                                     "cpu_reference_algorithm_solves_per_s": b, "ratio": a / b,
+                                     "note": "reference algorithm (corrflag 1, FP64, residual "
+                                             f"1e-{WORKLOADS[args.workload]['ptol']}) on both; the headline value "
+                                             "also changes the algorithm (corrflag 3, mixed form)"}
+    if rank == 0 and ws == 1 and args.workload == "c2" and not args.no_c4:
+        import importlib
+        pg = entry.load_package()
+        clusters = importlib.import_module("pisces_gb300.clusters")
+        line["serving_c4"] = c4_summary(c4_measure(pg, clusters, args.requests, args.warmup, args.slots,
+                                                   args.window_us, unbatched=False))
     if ws > 1:
         torch.distributed.destroy_process_group()
     if rank == 0:
