@@ -255,7 +255,7 @@ def run_ours(args, ws, rank, local):
         e2e_ms = (time.perf_counter() - t0) * 1000 / reps
 
     roof = kernel_rooflines(pg, torch, grid, tables, nroots, precision, stream)
-    hx_plan = grid.hx_plan()
+    hx_plan = grid.hx_plan(nroots)
     return dict(hx_plan=hx_plan, total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
                 de=de, stats=st, fp64=fp64, refalg=refalg, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d,
                 d2h=d2h, roofline=roof, N=N, precision=args.precision, ptol=ptol)
@@ -310,7 +310,7 @@ def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
     nx, ny, nz = grid.n
     hbytes = 8.0 * N * (2 * nb + 1)
     flops = N * nb * (2 * (nx + ny + nz) + 2)
-    hx = {"kernel": "pg_hx mixed: 3 x k_hx_tc (split-TF32 tcgen05)" if precision == pg.PG_MIXED else "k_hx_fp64",
+    hx = {"kernel": f"pg_hx mixed: {grid.hx_plan(nb)}" if precision == pg.PG_MIXED else "k_hx_fp64",
           "bound": "hbm" if precision == pg.PG_MIXED else "fp64", "ms_per_launch": ms, "algorithmic_bytes": hbytes,
           "vectors_per_launch": nb}
     if precision == pg.PG_MIXED:

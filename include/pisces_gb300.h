@@ -185,9 +185,20 @@ pg_status pg_grid_check(const pg_grid* g, void* stream);
  * products to the mixed form's accuracy.  No reference counterpart (the
  * reference multiplies line by line, src/mtx.cpp:61-104). */
 pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind);
+/* Launch parameters of the mixed-form H*X on this grid, overriding the tuned
+ * table: kind as pg_grid_set_hx_kernel; lag = vectors between a vector's xy
+ * planes and its z tiles in the fused kernel's work order (0: tuned); ctas =
+ * CTAs per launch (0: tuned, at most one per SM); form of the three axis
+ * passes: 0 automatic, 1 serial, 2 pipelined (0 = tuned).  The tuned table
+ * (pisces-1_gb300/hx_tuned.tsv, written by tune_hx.py on a GB300) holds the
+ * fastest measured choice per cubic grid size and block size; other grids
+ * use built-in rules.  No reference counterpart. */
+pg_status pg_grid_set_hx_params(pg_grid* g, int kind, int lag, int ctas, int form);
 /* One line describing the mixed-form H*X kernel and tile shape this grid
- * uses (text of at most len bytes including the terminator). */
+ * uses for blocks of nvec vectors (pg_grid_hx_plan: nvec = 1); text of at
+ * most len bytes including the terminator. */
 pg_status pg_grid_hx_plan(const pg_grid* g, char* text, int len);
+pg_status pg_grid_hx_plan_for(const pg_grid* g, int nvec, char* text, int len);
 
 /* ---------------------------------------------------------------- Davidson */
 

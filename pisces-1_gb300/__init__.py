@@ -113,6 +113,8 @@ SYMBOLS = {
     "pg_grid_check": (C.c_int, [_vp, _vp]),
     "pg_grid_set_hx_kernel": (C.c_int, [_vp, C.c_int]),
     "pg_grid_hx_plan": (C.c_int, [_vp, C.c_char_p, C.c_int]),
+    "pg_grid_hx_plan_for": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),
+    "pg_grid_set_hx_params": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
     "pg_davidson_create": (C.c_int, [C.POINTER(_vp)]),
     "pg_davidson_destroy": (C.c_int, [_vp]),
     "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
@@ -336,10 +338,14 @@ class Grid:
         """Mixed H*X kernel of this grid: 0 automatic, 1 three axis passes, 2 fused."""
         _check(lib().pg_grid_set_hx_kernel(self._h, int(kind)))
 
-    def hx_plan(self):
-        """One-line description of the mixed H*X kernel this grid uses."""
+    def set_hx_params(self, kind=0, lag=0, ctas=0, form=0):
+        """Override the tuned mixed H*X launch parameters (pg_grid_set_hx_params; 0 = tuned)."""
+        _check(lib().pg_grid_set_hx_params(self._h, int(kind), int(lag), int(ctas), int(form)))
+
+    def hx_plan(self, nvec=1):
+        """One-line description of the mixed H*X kernel this grid uses for nvec vectors."""
         buf = C.create_string_buffer(512)
-        _check(lib().pg_grid_hx_plan(self._h, buf, 512))
+        _check(lib().pg_grid_hx_plan_for(self._h, int(nvec), buf, 512))
         return buf.value.decode()
 
     def check(self, stream=None):

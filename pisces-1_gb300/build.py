@@ -22,9 +22,12 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpisces_gb300.so")
 INCLUDE = os.path.join(ROOT, "include")
 
+TUNED = os.path.join(HERE, "hx_tuned.tsv")          # launch parameters measured by tune_hx.py
+TUNED_INC = os.path.join(BUILD, "pg_hx_tuned.inc")  # the same as C initialisers
+
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-              f"-I{INCLUDE}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
+              f"-I{INCLUDE}", f"-I{CSRC}", f"-I{BUILD}", "--expt-relaxed-constexpr"]
 # files whose floating-point evaluation order follows the reference exactly
 NO_FMA = {"pg_potential.cu"}
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
@@ -41,6 +44,23 @@ def _cuda_home(nvcc):
     return os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
 
 
+def write_tuned_include():
+    """hx_tuned.tsv (n, nvec, kind, lag, ctas, form, ...) -> {n, nvec, kind, lag, ctas, form}, lines."""
+    rows = []
+    if os.path.exists(TUNED):
+        with open(TUNED) as f:
+            for line in f:
+                line = line.strip()
+                if not line or line.startswith("#"):
+                    continue
+                v = line.split()
+                rows.append("    {%d, %d, %d, %d, %d, %d}," % tuple(int(x) for x in v[:6]))
+    text = "// generated from hx_tuned.tsv by build.py\n" + "\n".join(rows) + ("\n" if rows else "")
+    if not os.path.exists(TUNED_INC) or open(TUNED_INC).read() != text:
+        with open(TUNED_INC, "w") as f:
+            f.write(text)
+
+
 def sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
@@ -50,6 +70,7 @@ def _compile(src, force, nvcc):
     obj = os.path.join(BUILD, src + ".o")
     deps = [path] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     deps.append(os.path.join(INCLUDE, "pisces_gb300.h"))
+    deps.append(TUNED_INC)
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj, None
     if src.endswith(".cu"):
@@ -67,6 +88,7 @@ def _compile(src, force, nvcc):
 def build(force: bool = False, verbose: bool = False) -> str:
     nvcc = _nvcc()
     os.makedirs(BUILD, exist_ok=True)
+    write_tuned_include()
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         results = list(ex.map(lambda s: _compile(s, force, nvcc), sources()))
     errors = [e for _, e in results if e]

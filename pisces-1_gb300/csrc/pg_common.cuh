@@ -210,11 +210,22 @@ struct pg_grid {
   // mixed H*X kernel choice (0 automatic, 1 three axis passes, 2 fused) and
   // the fused kernel's work counters, one block per stream id
   int hx_kernel = 0;
+  int hx_lag = 0, hx_ctas = 0, hx_form = 0;  // overrides of the tuned launch parameters (0: tuned)
   mutable std::mutex fused_m;
   mutable std::map<unsigned long long, std::unique_ptr<pg::DevBuf<unsigned>>> fused_cnt;
 };
 
 namespace pg {
+// Launch parameters of the mixed-form H*X for one grid shape and block size:
+// from the tuned table (pg_hx_tuned.inc, written by tune_hx.py), else the
+// built-in rules, then the grid's overrides.
+struct HxParams {
+  int kind;  // 1: three axis passes (k_hx_tc), 2: fused (k_hx_fused)
+  int lag;   // fused: vectors between a vector's xy items and its z items
+  int ctas;  // CTAs per launch (0: one per SM)
+  int form;  // three passes: 0 automatic, 1 serial, 2 pipelined (one K chunk only)
+};
+HxParams hx_params(const pg_grid* g, int nvec);
 // Single-axis contraction Y = A x_axis X for nvec vectors, A an n_axis x
 // n_axis matrix given in both FP64 and split-TF32 form; mode 0: Y = A X,
 // mode 1: Y += A X.  FP64 or tensor-core arithmetic per precision.

@@ -36,6 +36,7 @@
 // lanes the epilogue ignores.
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -812,14 +813,15 @@ bool fused_hx_ok(const pg_grid* g) {
 // Mixed H*X of up to kMaxJobs vector blocks on the same grid in one launch
 // of the fused kernel (the caller has checked fused_hx_ok).
 pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
-                        const int* nvec, int njobs, cudaStream_t st) {
+                        const int* nvec, int njobs, const HxParams& hp, cudaStream_t st) {
   PG_ARG(njobs > 0 && njobs <= kMaxJobs, "fused H*X: %d jobs (at most %d)", njobs, kMaxJobs);
   PG_CUDA_TRY(fused_init());
-  const FusedPlan P = plan_fused(g);
+  FusedPlan P = plan_fused(g);
   if (!P.ok) {
     set_error("fused H*X not available on this grid: %s", P.why);
     return PG_UNSUPPORTED;
   }
+  if (hp.lag > 0) P.G.lag = hp.lag;
   FusedCounters* cnt = nullptr;
   PG_TRY(fused_counters(g, st, &cnt));
   FusedJobs J;
@@ -839,35 +841,70 @@ pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* 
   PG_ARG(total <= kFusedMaxVec, "fused H*X: %d vectors in one launch (at most %d)", total, kFusedMaxVec);
   J.nvec = total;
   const long items = (long)total * (P.G.nz + P.G.nzt);
-  const int grid = (int)std::min<long>(items, g_fused_sms);
+  const int cap = hp.ctas > 0 && hp.ctas < g_fused_sms ? hp.ctas : g_fused_sms;
+  const int grid = (int)std::min<long>(items, cap);
   PG_CUDA_TRY(launch_dependent(k_hx_fused, dim3(grid), dim3(kThreadsAll), P.smem, st, P.G, P.C, J, cnt, g->tc_err.p));
   return check_launch("k_hx_fused");
 }
 
-pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st) {
+pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& hp,
+                   cudaStream_t st) {
   for (int v0 = 0; v0 < nvec; v0 += kFusedMaxVec) {
     const int nb = std::min(kFusedMaxVec, nvec - v0);
     const double* xs = x + (long)v0 * g->N;
     double* ys = y + (long)v0 * g->N;
-    PG_TRY(hx_fused_jobs(g, &v, &xs, &ys, &nb, 1, st));
+    PG_TRY(hx_fused_jobs(g, &v, &xs, &ys, &nb, 1, hp, st));
   }
   return PG_OK;
 }
 
-// Text description of the mixed-form H*X plan of a grid.
-void hx_plan_text(const pg_grid* g, char* buf, int len) {
+// The tuned launch parameters (tune_hx.py measures every candidate on a
+// GB300 per cubic grid size and block size and keeps the fastest); the
+// build turns the table into this include.
+struct TunedEntry {
+  int n, nvec, kind, lag, ctas, form;
+};
+static const TunedEntry kTuned[] = {
+#include "pg_hx_tuned.inc"
+    {0, 0, 0, 0, 0, 0}};
+
+HxParams hx_params(const pg_grid* g, int nvec) {
+  const bool fused_ok = fused_hx_ok(g);
+  HxParams p{fused_ok ? 2 : 1, 2, 0, 0};
+  if (g->n[0] == g->n[1] && g->n[1] == g->n[2]) {
+    // the entry of this grid size with the nearest block size
+    const TunedEntry* best = nullptr;
+    for (const TunedEntry* e = kTuned; e->n; ++e)
+      if (e->n == g->n[0] && (!best || std::abs(e->nvec - nvec) < std::abs(best->nvec - nvec))) best = e;
+    if (best) p = HxParams{best->kind, best->lag, best->ctas, best->form};
+  }
+  if (g->hx_kernel) p.kind = g->hx_kernel;
+  if (g->hx_lag) p.lag = g->hx_lag;
+  if (g->hx_ctas) p.ctas = g->hx_ctas;
+  if (g->hx_form) p.form = g->hx_form;
+  if (p.kind == 2 && !fused_ok && g->hx_kernel != 2) p.kind = 1;
+  return p;
+}
+
+// Text description of the mixed-form H*X plan of a grid for blocks of nvec vectors.
+void hx_plan_text(const pg_grid* g, int nvec, char* buf, int len) {
   if (fused_init() != cudaSuccess) {
     snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): device query failed");
     return;
   }
   const FusedPlan P = plan_fused(g);
-  if (P.ok)
+  const HxParams p = hx_params(g, nvec);
+  if (p.kind == 2 && P.ok)
     snprintf(buf, (size_t)len,
              "fused (k_hx_fused): xy planes %dx%d + z tiles of 128 lines (%d per vector, lag %d vectors), "
-             "K %d/%d/%d, %zu B shared memory, %d constant images, %u TMEM columns x 2",
-             P.G.nx, P.G.ny, P.G.nzt, P.G.lag, P.G.kx, P.G.ky, P.G.kz, P.smem, P.C.n / 2, P.G.acc_cols);
+             "K %d/%d/%d, %zu B shared memory, %d constant images, %u TMEM columns x 2, %d CTAs",
+             P.G.nx, P.G.ny, P.G.nzt, p.lag, P.G.kx, P.G.ky, P.G.kz, P.smem, P.C.n / 2, P.G.acc_cols,
+             p.ctas > 0 && p.ctas < g_fused_sms ? p.ctas : g_fused_sms);
   else
-    snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): %s", P.why);
+    snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): %s form, %d CTAs%s%s",
+             p.form == 1 ? "serial" : (p.form == 2 ? "pipelined" : "automatic"),
+             p.ctas > 0 && p.ctas < g_fused_sms ? p.ctas : g_fused_sms, P.ok ? "" : "; fused kernel: ",
+             P.ok ? "" : P.why);
 }
 
 }  // namespace pg
@@ -877,7 +914,7 @@ extern "C" pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind) {
   PG_ARG(kind >= 0 && kind <= 2, "pg_grid_set_hx_kernel: kind must be 0, 1 or 2 (got %d)", kind);
   if (kind == 2 && !pg::fused_hx_ok(g)) {
     char why[256];
-    pg::hx_plan_text(g, why, sizeof(why));
+    pg::hx_plan_text(g, 1, why, sizeof(why));
     pg::set_error("pg_grid_set_hx_kernel: %s", why);
     return PG_UNSUPPORTED;
   }
@@ -885,11 +922,23 @@ extern "C" pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind) {
   return PG_OK;
 }
 
+extern "C" pg_status pg_grid_set_hx_params(pg_grid* g, int kind, int lag, int ctas, int form) {
+  PG_ARG(g, "pg_grid_set_hx_params: null grid");
+  PG_ARG(lag >= 0 && lag <= 64 && ctas >= 0 && ctas <= 4096 && form >= 0 && form <= 2,
+         "pg_grid_set_hx_params: lag %d, ctas %d or form %d out of range", lag, ctas, form);
+  PG_TRY(pg_grid_set_hx_kernel(g, kind));
+  g->hx_lag = lag;
+  g->hx_ctas = ctas;
+  g->hx_form = form;
+  return PG_OK;
+}
+
 extern "C" pg_status pg_grid_hx_plan(const pg_grid* g, char* text, int len) {
-  PG_ARG(g && text && len > 0, "pg_grid_hx_plan: bad arguments");
-  if (g->hx_kernel == 1)
-    snprintf(text, (size_t)len, "three axis passes (k_hx_tc): chosen for this grid");
-  else
-    pg::hx_plan_text(g, text, len);
+  return pg_grid_hx_plan_for(g, 1, text, len);
+}
+
+extern "C" pg_status pg_grid_hx_plan_for(const pg_grid* g, int nvec, char* text, int len) {
+  PG_ARG(g && text && len > 0 && nvec > 0, "pg_grid_hx_plan: bad arguments");
+  pg::hx_plan_text(g, nvec, text, len);
   return PG_OK;
 }

@@ -621,7 +621,7 @@ static int g_num_sms = 0;
 // (n_axis x n_axis, row-major).  Each job covers nvec_j vectors.
 pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* const* v,
                        const double* const* x, double* const* y, const int* nvec, int njobs, int mode,
-                       cudaStream_t st) {
+                       cudaStream_t st, int ctas, int form) {
   PG_ARG(njobs > 0 && njobs <= kMaxTcJobs, "tc_axis: %d jobs (at most %d)", njobs, kMaxTcJobs);
   if (g->n[a] > kMaxN) {
     set_error("mixed form supports n <= %d per axis (got %d)", kMaxN, g->n[a]);
@@ -680,12 +680,14 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
     set_error("tc_axis: %zu bytes of shared memory needed, the device allows %d", smem, g_max_dyn);
     return PG_UNSUPPORTED;
   }
-  // one persistent CTA of kThreads per SM
-  const long cap = g_num_sms;
+  // one persistent CTA of kThreads per SM, or the tuned count
+  const long cap = ctas > 0 && ctas < g_num_sms ? ctas : g_num_sms;
   const int grid = (int)(tiles < cap ? tiles : cap);
   int* err = g->tc_err.p;
   const size_t a_region = (size_t)2 * kTileM * kc * 4, b_region = (size_t)2 * npad * kc * 4;
-  if (nch == 1 && tiles > cap) {  // several tiles per CTA: the pipelined form overlaps them
+  // several tiles per CTA: the pipelined form overlaps them (form 0), or as tuned
+  const bool pipe = nch == 1 && (form == 2 || (form == 0 && tiles > cap));
+  if (pipe) {
     // x-axis epilogue blocks of the eight consumer warps after the A tile
     const size_t stage = (size_t)(kPipeThreads - kProducers) / 32 * kStageWarpBytes;
     const bool staged = a == 0 && smem + stage <= (size_t)g_max_dyn;
@@ -737,43 +739,47 @@ pg_status tc_axis_jobs(const pg_grid* g, int a, const float* Ahi, const float* A
 
 pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, const double* v, const double* x,
                   double* y, int nvec, int mode, cudaStream_t st) {
-  return tc_axis_jobs(g, a, Ahi, Alo, v ? &v : nullptr, &x, &y, &nvec, 1, mode, st);
+  return tc_axis_jobs(g, a, Ahi, Alo, v ? &v : nullptr, &x, &y, &nvec, 1, mode, st, 0, 0);
 }
 
 bool fused_hx_ok(const pg_grid* g);
-pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st);
+pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& p,
+                   cudaStream_t st);
 pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
-                        const int* nvec, int njobs, cudaStream_t st);
-
-// The fused kernel (pg_hx_fused.cu) where the grid allows it and the grid's
-// choice does not say otherwise; the three axis passes below elsewhere.
-static bool use_fused(const pg_grid* g) { return g->hx_kernel != 1 && fused_hx_ok(g); }
+                        const int* nvec, int njobs, const HxParams& p, cudaStream_t st);
 
 // Mixed H*X of several solves on the same grid in one launch (fused) or one
-// launch per axis.
+// launch per axis, with the launch parameters tuned for the whole block.
 pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
                          const int* nvec, int njobs, cudaStream_t st) {
-  if (use_fused(g)) return hx_fused_jobs(g, v, x, y, nvec, njobs, st);
+  int total = 0;
+  for (int j = 0; j < njobs; ++j) total += nvec[j];
+  const HxParams p = hx_params(g, total);
+  if (p.kind == 2) return hx_fused_jobs(g, v, x, y, nvec, njobs, p, st);
   for (int a = 0; a < 3; ++a)
-    PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 2 : 1, st));
+    PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 2 : 1, st, p.ctas, p.form));
   return PG_OK;
 }
 
-// Launches the three axis passes on st: Y = V X + Tx.X, Y += Ty.X, Y += Tz.X.
+// Y = H X: the fused kernel (pg_hx_fused.cu) or the three axis passes
+// Y = V X + Tx.X, Y += Ty.X, Y += Tz.X, as hx_params chooses.
 // The tensor-core completion waits report a timeout through g->tc_err; with
 // check, the call waits for the stream and returns PG_DEVICE_TIMEOUT if one
 // occurred (the eigensolver checks the word at its own synchronisation points).
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
                    bool check) {
-  if (use_fused(g)) {
-    PG_TRY(hx_fused(g, v, x, y, nvec, st));
+  const HxParams p = hx_params(g, nvec);
+  if (p.kind == 2) {
+    PG_TRY(hx_fused(g, v, x, y, nvec, p, st));
     return check ? check_tc_error(g, st) : PG_OK;
   }
   if (g->hx_kernel == 2) {
     set_error("pg_hx: the fused mixed H*X kernel does not take this grid");
     return PG_UNSUPPORTED;
   }
-  for (int a = 0; a < 3; ++a) PG_TRY(tc_axis(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, a == 0 ? 2 : 1, st));
+  for (int a = 0; a < 3; ++a)
+    PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, &v, &x, &y, &nvec, 1, a == 0 ? 2 : 1, st, p.ctas,
+                        p.form));
   return check ? check_tc_error(g, st) : PG_OK;
 }
 
