@@ -333,6 +333,75 @@ pg_status pg_cluster_solve(const int n[3], const double L[3], int nw, const doub
                            const double* ions_angstrom_q, const pg_solve_params* p, double* evals_host,
                            double* evecs_host, pg_solve_stats* stats, void* stream);
 
+/* ---- Observables and wavefunction files ------------------------------------
+ * What the reference reports about converged states and how it stores them
+ * (the hot path's output side): grid reductions of psi^2 on the device, and
+ * the reference's cube file formats, written byte for byte as it writes
+ * them. */
+
+/* Moments of a state psi (a DVR vector: psi^2 at a grid point is the
+ * probability there): norm = sum psi^2, r = (<x>, <y>, <z>) in bohr, r2 =
+ * <r^2>, and for states n >= 1 the transition dipole (<n|x|0>, <n|y|0>,
+ * <n|z|0>) with state 0 (zero for state 0).  |<r>| = |r|, the spread
+ * sqrt(r2 - |r|^2). */
+typedef struct {
+  double norm;
+  double r[3];
+  double r2;
+  double trans_dipole[3];
+} pg_moments;
+
+/* Moments of nstates vectors (vecs_dev[s*N + g]) into out_host[nstates].
+ * Replaces DVR::ExpectationValues (src/DVR.cpp:2329-2449), which prints the
+ * same sums.  Deterministic (fixed summation order). */
+pg_status pg_expectation_values(const pg_grid* g, const double* vecs_dev, int nstates, pg_moments* out_host,
+                                void* stream);
+
+/* Potential-energy partition: out_host[4*s + c] = sum_g psi_s(g)^2 part_c(g)
+ * for the four parts of pg_potential_eval (charges, induced dipoles,
+ * repulsive core, polarisation; hartree).  Replaces
+ * DVR::EnergyPartitioning (src/DVR.cpp:2240-2325). */
+pg_status pg_energy_partition(const pg_grid* g, const double* vecs_dev, int nstates, const double* parts_dev,
+                              double* out_host, void* stream);
+
+/* A state's values on the grid in cube order (x slowest, z fastest) scaled
+ * by 1/sqrt(dV), i.e. in bohr^-3/2 (DVR::GetWaveFnCube, src/DVR.cpp:2025-2074).
+ * wf_host: N doubles; cube_host: N doubles.  dV uses each axis's own extent
+ * (the reference takes all three at index nz-1: the same on cubic grids). */
+pg_status pg_state_cube(const pg_grid* g, const double* wf_host, double* cube_host);
+
+/* Cube file of a state, as DVR::WriteCubeFile (src/DVR.cpp:1887-2023):
+ * cubeflag 1 = gOpenMol text grid, otherwise a Gaussian orbital cube (atom
+ * count written negative, then the line "1 iwf").  Atoms: Z[natoms] and
+ * pos_angstrom[3*natoms].  integral (may be NULL) receives sum rho^2 dV.
+ * Written byte for byte as the reference writes it. */
+pg_status pg_write_state_cube(const pg_grid* g, const double* wf_host, int iwf, const char* path, int natoms,
+                              const int* Z, const double* pos_angstrom, int cubeflag, double* integral);
+
+/* Gaussian cube of any grid function (WriteCubeFile, src/WriteCubeFile.cpp:
+ * 17-78): npts[3] points from x0[3] in steps dx[3] (bohr), values
+ * cube_host[npts0*npts1*npts2] with z fastest. */
+pg_status pg_write_cube(const char* path, int natoms, const int* Z, const double* pos_angstrom, const int npts[3],
+                        const double x0[3], const double dx[3], const double* cube_host);
+
+/* Reads a Gaussian cube (ReadCubeFile, src/ReadCubeFile.cpp:17-104, which
+ * reads the fixed name StartVector.cub): the grid into npts/x0/dx, the atom
+ * count into natoms (may be NULL; negative for an orbital cube, whose
+ * orbital line is skipped), and, if cube_host is not NULL, the values (z
+ * fastest; PG_BAD_ARG if capacity is smaller than the grid).  Only
+ * cartesian grids (PG_BAD_ARG otherwise; the reference exits). */
+pg_status pg_read_cube(const char* path, int npts[3], double x0[3], double dx[3], int* natoms, double* cube_host,
+                       long capacity);
+
+/* Start vector from a wavefunction on a smaller equidistant grid (n[3]
+ * points from xmin in steps dx, values in cube order as pg_read_cube
+ * returns them): trilinear interpolation onto this grid's points, normalised
+ * so that sum psi^2 = 1 (Small2Large, src/Small2Large.cpp:15-220, its
+ * eight-point branch; the large grid is this grid's points x_0 + I L/(n+1)).
+ * wf_dev receives N doubles. */
+pg_status pg_small_to_large(const int n[3], const double xmin[3], const double dx[3], const double* wf_small_host,
+                            const pg_grid* g, double* wf_dev, void* stream);
+
 /* ---- Serving engine ------------------------------------------------------
  * A request loop for streams of single points (geometry-optimisation and
  * MD-snapshot streams): the role of the reference's repeated

@@ -165,6 +165,24 @@ class Grid:
         lib().or_potential_spherical(_i(self.n), self._x_ptrs, float(k), _d(v))
         return v
 
+    def expectation_values(self, wf, nstates):
+        """Sums of psi^2 (1, x, y, z, r^2) and psi_n x psi_0 per state (DVR::ExpectationValues): [nstates, 8]."""
+        out = np.empty(8 * nstates)
+        L = lib()
+        L.or_expectation_values.argtypes = [_ip, C.POINTER(_dp), _dp, C.c_int, _dp]
+        L.or_expectation_values(_i(self.n), self._x_ptrs, _d(np.ascontiguousarray(wf, dtype=np.float64)), nstates,
+                                _d(out))
+        return out.reshape(nstates, 8)
+
+    def energy_partition(self, wf, nstates, parts):
+        """Sums of psi^2 times the four potential parts per state (DVR::EnergyPartitioning): [nstates, 4]."""
+        out = np.empty(4 * nstates)
+        L = lib()
+        L.or_energy_partition.argtypes = [_ip, _dp, C.c_int, _dp, _dp]
+        L.or_energy_partition(_i(self.n), _d(np.ascontiguousarray(wf, dtype=np.float64)), nstates,
+                              _d(np.ascontiguousarray(parts, dtype=np.float64)), _d(out))
+        return out.reshape(nstates, 4)
+
     def solve(self, v, nstates=1, maxsub=20, maxiter=100, ptol=5, corrflag=1, startvec=1, max_matvec=0):
         """Reference-algorithm Davidson; returns (status, evals, vectors, n_matvec)."""
         ev = np.zeros(nstates)
@@ -236,6 +254,17 @@ def dpp_sites(waters_angstrom):
     return sites, q, qs, d, ds, it
 
 
+def small_to_large(n, xmin, dx, wf, N, XMIN, DX):
+    """Small2Large (eight-point interpolation, normalised) onto the grid N, XMIN + I DX."""
+    out = np.empty(int(np.prod(N)))
+    L = lib()
+    L.or_small_to_large.argtypes = [_ip, _dp, _dp, _dp, _ip, _dp, _dp, _dp]
+    a = lambda v, t=np.float64: np.ascontiguousarray(v, dtype=t)
+    L.or_small_to_large(_i(a(n, np.int32)), _d(a(xmin)), _d(a(dx)), _d(a(wf)), _i(a(N, np.int32)), _d(a(XMIN)),
+                        _d(a(DX)), _d(out))
+    return out
+
+
 def syev(a):
     n = a.shape[0]
     A = np.asfortranarray(a, dtype=np.float64).copy()
@@ -273,7 +302,7 @@ def have_reference() -> bool:
 
 def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, maxiter=100, ptol=5, startvec=1,
                   spherical_k=None, matvec_seed=None, fulldiag=False, diagonalize=True, dump_wavefn=True,
-                  threads=None):
+                  threads=None, observables=None):
     """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration."""
     if not have_reference():
         raise FileNotFoundError(REF_BIN)
@@ -295,6 +324,8 @@ def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, 
             lines.append(f"spherical {spherical_k!r}")
         if matvec_seed is not None:
             lines.append(f"matvec_seed {int(matvec_seed)}")
+        if observables is not None:
+            lines.append("observables {} {} {}".format(*[int(v) for v in observables]))
         lines += [f"fulldiag {int(fulldiag)}", f"diagonalize {int(diagonalize)}",
                   f"dump_wavefn {int(dump_wavefn)}", f"out {out}"]
         with open(inp, "w") as f:

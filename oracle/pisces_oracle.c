@@ -810,3 +810,103 @@ int or_solve(const int n[3], const double* const tp[3], const double* const x[3]
   if (n_matvec) *n_matvec = nmv;
   return stopped == 1 ? -1 : stopped < 0 ? stopped : nconv;
 }
+
+/* ---------------------------------------------------------------- observables */
+
+/* DVR::ExpectationValues (src/DVR.cpp:2329-2449): for each state the sums
+ * over the grid of psi^2, psi^2 x, psi^2 y, psi^2 z, psi^2 r^2, and for
+ * states n >= 1 psi_n x psi_0 (and y, z), in the reference's loop order
+ * (x slowest, z fastest).  out[8*s + m]. */
+void or_expectation_values(const int n[3], const double* const xg[3], const double* wf, int nstates, double* out) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const long ngp = (long)nx * ny * nz;
+  for (int m = 0; m < 8 * nstates; ++m) out[m] = 0.0;
+  for (int ix = 0; ix < nx; ++ix)
+    for (int iy = 0; iy < ny; ++iy)
+      for (int iz = 0; iz < nz; ++iz) {
+        const long idx = ix + (long)nx * (iy + (long)ny * iz);
+        const double x = xg[0][ix], y = xg[1][iy], z = xg[2][iz];
+        for (int s = 0; s < nstates; ++s) {
+          const double w = wf[s * ngp + idx], rho = w * w;
+          double* o = out + 8 * s;
+          o[0] += rho;
+          o[1] += rho * x;
+          o[2] += rho * y;
+          o[3] += rho * z;
+          o[4] += rho * (x * x + y * y + z * z);
+          if (s > 0) {
+            const double w0 = wf[idx];
+            o[5] += w * x * w0;
+            o[6] += w * y * w0;
+            o[7] += w * z * w0;
+          }
+        }
+      }
+}
+
+/* DVR::EnergyPartitioning (src/DVR.cpp:2240-2325): sums of psi^2 times the
+ * four potential parts (charges, induced dipoles, repulsion, polarisation),
+ * in the reference's loop order.  parts[c*ngp + g]; out[4*s + c]. */
+void or_energy_partition(const int n[3], const double* wf, int nstates, const double* parts, double* out) {
+  const int nx = n[0], ny = n[1], nz = n[2];
+  const long ngp = (long)nx * ny * nz;
+  for (int m = 0; m < 4 * nstates; ++m) out[m] = 0.0;
+  for (int ix = 0; ix < nx; ++ix)
+    for (int iy = 0; iy < ny; ++iy)
+      for (int iz = 0; iz < nz; ++iz) {
+        const long idx = ix + (long)nx * (iy + (long)ny * iz);
+        for (int s = 0; s < nstates; ++s) {
+          const double w = wf[s * ngp + idx], rho = w * w;
+          for (int c = 0; c < 4; ++c) out[4 * s + c] += rho * parts[c * ngp + idx];
+        }
+      }
+}
+
+/* Small2Large, eight-point branch (src/Small2Large.cpp:135-219): the small
+ * grid in cube order (z fastest), the large grid XMIN + I DX with x fastest,
+ * normalised so that the sum of squares is 1 (summed in the large grid's
+ * order). */
+void or_small_to_large(const int n[3], const double xmin[3], const double dx[3], const double* wf, const int N[3],
+                       const double XMIN[3], const double DX[3], double* WF) {
+  const long xs = (long)n[1] * n[2], ys = n[2];
+  double nrm = 0.0;
+  long c = 0;
+  for (int IZ = 0; IZ < N[2]; ++IZ) {
+    const double Z = XMIN[2] + IZ * DX[2];
+    int iz = (int)((Z - xmin[2]) / dx[2]), izu;
+    if (iz < 0) { iz = 0; izu = 1; }
+    else if (iz > n[2] - 2) { iz = n[2] - 2; izu = n[2] - 1; }
+    else izu = iz + 1;
+    const double wz = (Z - (xmin[2] + iz * dx[2])) / dx[2];
+    for (int IY = 0; IY < N[1]; ++IY) {
+      const double Y = XMIN[1] + IY * DX[1];
+      int iy = (int)((Y - xmin[1]) / dx[1]), iyu;
+      if (iy < 0) { iy = 0; iyu = 1; }
+      else if (iy > n[1] - 2) { iy = n[1] - 2; iyu = n[1] - 1; }
+      else iyu = iy + 1;
+      const double wy = (Y - (xmin[1] + iy * dx[1])) / dx[1];
+      for (int IX = 0; IX < N[0]; ++IX) {
+        const double X = XMIN[0] + IX * DX[0];
+        int ix = (int)((X - xmin[0]) / dx[0]), ixu;
+        if (ix < 0) { ix = 0; ixu = 1; }
+        else if (ix > n[0] - 2) { ix = n[0] - 2; ixu = n[0] - 1; }
+        else ixu = ix + 1;
+        const double wx = (X - (xmin[0] + ix * dx[0])) / dx[0];
+        double sum = 0, w, v;
+        w = (1 - wx) * (1 - wy) * (1 - wz); sum += w; v = wf[ix * xs + iy * ys + iz] * w;
+        w = wx * (1 - wy) * (1 - wz); sum += w; v += wf[ixu * xs + iy * ys + iz] * w;
+        w = (1 - wx) * wy * (1 - wz); sum += w; v += wf[ix * xs + iyu * ys + iz] * w;
+        w = (1 - wx) * (1 - wy) * wz; sum += w; v += wf[ix * xs + iy * ys + izu] * w;
+        w = wx * wy * (1 - wz); sum += w; v += wf[ixu * xs + iyu * ys + iz] * w;
+        w = wx * (1 - wy) * wz; sum += w; v += wf[ixu * xs + iy * ys + izu] * w;
+        w = (1 - wx) * wy * wz; sum += w; v += wf[ix * xs + iyu * ys + izu] * w;
+        w = wx * wy * wz; sum += w; v += wf[ixu * xs + iyu * ys + izu] * w;
+        v /= sum;
+        WF[c++] = v;
+        nrm += v * v;
+      }
+    }
+  }
+  nrm = 1.0 / sqrt(nrm);
+  for (long k = 0; k < c; ++k) WF[k] *= nrm;
+}

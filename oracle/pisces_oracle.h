@@ -110,6 +110,13 @@ int or_solve(const int n[3], const double* const tp[3], const double* const x[3]
  * with leading dimension lda (overwritten); w ascending, v column-major (ldv). */
 int or_syev(int n, double* a, int lda, double* w, double* v, int ldv);
 
+/* Observables and the coarse-grid start vector (src/DVR.cpp:2240-2449,
+ * src/Small2Large.cpp:15-220). */
+void or_expectation_values(const int n[3], const double* const xg[3], const double* wf, int nstates, double* out);
+void or_energy_partition(const int n[3], const double* wf, int nstates, const double* parts, double* out);
+void or_small_to_large(const int n[3], const double xmin[3], const double dx[3], const double* wf, const int N[3],
+                       const double XMIN[3], const double DX[3], double* WF);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,8 @@
 #include <sstream>
 #include <chrono>
 #include <mpi.h>
+#include <fcntl.h>
+#include <unistd.h>
 #include "vecdefs.h"
 #include "constants.h"
 #include "GTO.h"
@@ -43,6 +45,9 @@
 #include "DVR.h"
 #undef private
 #include "lapackblas.h"
+#include "WriteCubeFile.h"
+#include "ReadCubeFile.h"
+#include "Small2Large.h"
 
 namespace {
 
@@ -101,6 +106,7 @@ struct Input {
   int fulldiag = 0;
   int diagonalize = 1;
   int dump_wavefn = 1;
+  int s2l[3] = {0, 0, 0};  // > 0: the observables and cube-file records, Small2Large onto this grid
   std::string out = "out.rec";
 };
 
@@ -119,10 +125,44 @@ Input read_input(const char* path) {
     else if (key == "fulldiag") { f >> in.fulldiag; }
     else if (key == "diagonalize") { f >> in.diagonalize; }
     else if (key == "dump_wavefn") { f >> in.dump_wavefn; }
+    else if (key == "observables") { f >> in.s2l[0] >> in.s2l[1] >> in.s2l[2]; }
     else if (key == "out") { f >> in.out; }
     else { fprintf(stderr, "unknown key %s\n", key.c_str()); exit(2); }
   }
   return in;
+}
+
+// Everything the process writes to standard output (printf and cout) while
+// fn runs, as text.
+template <class F>
+std::string capture_stdout(const std::string& tmp, F&& fn) {
+  fflush(stdout);
+  std::cout.flush();
+  const int saved = dup(1);
+  const int fd = open(tmp.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
+  dup2(fd, 1);
+  close(fd);
+  fn();
+  fflush(stdout);
+  std::cout.flush();
+  dup2(saved, 1);
+  close(saved);
+  std::ifstream f(tmp);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  return ss.str();
+}
+
+void put_text(const std::string& name, const std::string& text) {
+  std::vector<int> b(text.begin(), text.end());
+  put(name, b.data(), b.size());
+}
+
+std::string read_file(const std::string& path) {
+  std::ifstream f(path);
+  std::stringstream ss;
+  ss << f.rdbuf();
+  return ss.str();
 }
 
 }  // namespace
@@ -288,6 +328,66 @@ int main(int argc, char** argv) {
     if (in.dump_wavefn) put("wavefn", Hel.wavefn.data(), (size_t)ngp * in.nstates);
     fprintf(stderr, "nconv %d t_diag %.3f s\n", nconv, t_diag);
     for (int k = 0; k < in.nstates; ++k) fprintf(stderr, "E[%d] = %.17g\n", k, ev[k]);
+
+    if (in.s2l[0] > 0 && nconv > 0) {
+      // The output side of a single point (src/ClusterAnion.cpp:96-120):
+      // expectation values and the energy partition as the reference prints
+      // them, the state cube, the cube files it writes, its cube reader on a
+      // file of its own writer, and Small2Large onto a second grid.
+      const std::string dir = in.out.substr(0, in.out.find_last_of('/') + 1);
+      put_text("expect_text", capture_stdout(dir + "expect.txt", [&] { Hel.ExpectationValues(2); }));
+      if (nW > 0) put_text("energy_text", capture_stdout(dir + "energy.txt", [&] { Hel.EnergyPartitioning(Vel); }));
+      std::vector<int> Z(3 * nW);
+      for (int w = 0; w < nW; ++w) Z[3 * w] = 8, Z[3 * w + 1] = 1, Z[3 * w + 2] = 1;
+      Hel.SetVerbose(0);
+      const int last = nconv < in.nstates ? nconv : in.nstates;
+      Hel.WriteCubeFile(1, (dir + "state_gauss.cub").c_str(), 3 * nW, Z.data(), in.waters.data(), 0);
+      Hel.WriteCubeFile(last, (dir + "state_gomol.cub").c_str(), 3 * nW, Z.data(), in.waters.data(), 1);
+      put_text("cube_gauss", read_file(dir + "state_gauss.cub"));
+      put_text("cube_gomol", read_file(dir + "state_gomol.cub"));
+      put1i("cube_gomol_state", last);
+      dVec cube(ngp);
+      Hel.GetWaveFnCube(1, cube.data());
+      put("state_cube", cube.data(), ngp);
+      int npts[3] = {in.n[0], in.n[1], in.n[2]};
+      double x0[3], dx[3];
+      for (int a = 0; a < 3; ++a) {
+        const double* xa = Hel.x_dvr + (a == 0 ? 0 : (a == 1 ? Hel.max1db[0] : Hel.max1db[0] + Hel.max1db[1]));
+        x0[a] = xa[0];
+        dx[a] = xa[1] - xa[0];
+      }
+      put("cube_x0", x0, 3);
+      put("cube_dx", dx, 3);
+      WriteCubeFile((dir + "StartVector.cub").c_str(), 3 * nW, Z.data(), in.waters.data(), npts, x0, dx, cube.data(),
+                    nullptr);
+      put_text("cube_free", read_file(dir + "StartVector.cub"));
+      // ReadCubeFile reads StartVector.cub from the working directory
+      char cwd[4096];
+      if (!getcwd(cwd, sizeof(cwd)) || chdir(dir.c_str()) != 0) { fprintf(stderr, "chdir failed\n"); return 2; }
+      int rn[3];
+      double rx0[3], rdx[3];
+      double* rcube = nullptr;
+      capture_stdout("read.txt", [&] { ReadCubeFile(rn, rx0, rdx, &rcube); });
+      if (chdir(cwd) != 0) { fprintf(stderr, "chdir failed\n"); return 2; }
+      put("read_npts", rn, 3);
+      put("read_x0", rx0, 3);
+      put("read_dx", rdx, 3);
+      put("read_cube", rcube, (size_t)rn[0] * rn[1] * rn[2]);
+      // Small2Large onto N points over the same box (sine-DVR points)
+      int N[3] = {in.s2l[0], in.s2l[1], in.s2l[2]};
+      double XMIN[3], DX[3];
+      for (int a = 0; a < 3; ++a) {
+        DX[a] = in.L[a] / (double)(N[a] + 1);
+        XMIN[a] = -0.5 * in.L[a] + DX[a];
+      }
+      dVec WF((size_t)N[0] * N[1] * N[2]);
+      capture_stdout(dir + "s2l.txt", [&] { Small2Large(rn, rx0, rdx, rcube, N, XMIN, DX, WF.data()); });
+      put("s2l_N", N, 3);
+      put("s2l_xmin", XMIN, 3);
+      put("s2l_dx", DX, 3);
+      put("s2l", WF.data(), WF.size());
+      delete[] rcube;
+    }
   }
   write_records(in.out);
   return 0;

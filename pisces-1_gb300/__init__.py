@@ -62,6 +62,11 @@ class SolveStats(C.Structure):
                 "host_eig_seconds": self.host_eig_seconds, "device_wait_seconds": self.device_wait_seconds}
 
 
+class Moments(C.Structure):
+    """pg_moments: sum psi^2, <x,y,z>, <r^2> and the transition dipole with state 0."""
+    _fields_ = [("norm", C.c_double), ("r", C.c_double * 3), ("r2", C.c_double), ("trans_dipole", C.c_double * 3)]
+
+
 class EngineConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("slots", C.c_int), ("memory_budget", C.c_double),
                 ("batch_matvecs", C.c_int), ("batch_window_us", C.c_int), ("warm_start", C.c_int)]
@@ -130,6 +135,13 @@ SYMBOLS = {
     "pg_block_gram": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_block_combine": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_block_gram_noalloc": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
+    "pg_expectation_values": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(Moments), _vp]),
+    "pg_energy_partition": (C.c_int, [_vp, _vp, C.c_int, _vp, _dp, _vp]),
+    "pg_state_cube": (C.c_int, [_vp, _dp, _dp]),
+    "pg_write_state_cube": (C.c_int, [_vp, _dp, C.c_int, C.c_char_p, C.c_int, _ip, _dp, C.c_int, _dp]),
+    "pg_write_cube": (C.c_int, [C.c_char_p, C.c_int, _ip, _dp, _ip, _dp, _dp, _dp]),
+    "pg_read_cube": (C.c_int, [C.c_char_p, _ip, _dp, _dp, _ip, _dp, C.c_long]),
+    "pg_small_to_large": (C.c_int, [_ip, _dp, _dp, _dp, _vp, _vp, _vp]),
     "pg_request_footprint": (C.c_double, [C.POINTER(Request)]),
     "pg_engine_create": (C.c_int, [C.POINTER(EngineConfig), C.POINTER(_vp)]),
     "pg_engine_submit": (C.c_int, [_vp, C.POINTER(Request), C.POINTER(C.c_long)]),
@@ -367,6 +379,74 @@ class Grid:
         if s != PG_OK and (s != PG_NOT_CONVERGED or raise_on_nonconv):
             _check(s)
         return ev, vec.view(nroots, self.N), st.as_dict(nroots)
+
+
+    # ------------------------------------------------ observables and cube files
+
+    def expectation_values(self, vecs, nstates=None, stream=None):
+        """pg_expectation_values: list of dicts (norm, r, r2, trans_dipole) per state."""
+        nstates = vecs.numel() // self.N if nstates is None else nstates
+        out = (Moments * nstates)()
+        _check(lib().pg_expectation_values(self._h, _dev(vecs), nstates, out, _stream(stream)))
+        return [{"norm": m.norm, "r": list(m.r), "r2": m.r2, "trans_dipole": list(m.trans_dipole)} for m in out]
+
+    def energy_partition(self, vecs, parts, nstates=None, stream=None):
+        """pg_energy_partition: [nstates, 4] sums of psi^2 times the potential parts (hartree)."""
+        nstates = vecs.numel() // self.N if nstates is None else nstates
+        out = np.empty(4 * nstates)
+        _check(lib().pg_energy_partition(self._h, _dev(vecs), nstates, _dev(parts), _d(out), _stream(stream)))
+        return out.reshape(nstates, 4)
+
+    def state_cube(self, wf_host):
+        """pg_state_cube: a state's values in cube order, in bohr^-3/2."""
+        wf = np.ascontiguousarray(wf_host, dtype=np.float64)
+        out = np.empty(self.N)
+        _check(lib().pg_state_cube(self._h, _d(wf), _d(out)))
+        return out
+
+    def write_state_cube(self, path, wf_host, iwf=1, Z=(), pos_angstrom=(), cubeflag=0):
+        """pg_write_state_cube; returns sum rho^2 dV."""
+        wf = np.ascontiguousarray(wf_host, dtype=np.float64)
+        Zs = np.ascontiguousarray(Z, dtype=np.int32)
+        pos = np.ascontiguousarray(pos_angstrom, dtype=np.float64).reshape(-1)
+        integral = C.c_double(0)
+        _check(lib().pg_write_state_cube(self._h, _d(wf), int(iwf), os.fsencode(path), len(Zs),
+                                         _i(Zs) if len(Zs) else None, _d(pos) if len(Zs) else None, int(cubeflag),
+                                         C.byref(integral)))
+        return integral.value
+
+    def small_to_large(self, n, xmin, dx, wf_small, stream=None):
+        """pg_small_to_large: a start vector on this grid from a smaller grid's values (cube order)."""
+        out = self._new()
+        n = np.ascontiguousarray(n, dtype=np.int32)
+        xmin = np.ascontiguousarray(xmin, dtype=np.float64)
+        dx = np.ascontiguousarray(dx, dtype=np.float64)
+        wf = np.ascontiguousarray(wf_small, dtype=np.float64)
+        _check(lib().pg_small_to_large(_i(n), _d(xmin), _d(dx), _d(wf), self._h, _dev(out), _stream(stream)))
+        return out
+
+
+def write_cube(path, npts, x0, dx, cube, Z=(), pos_angstrom=()):
+    """pg_write_cube: a Gaussian cube of any grid function (values with z fastest)."""
+    npts = np.ascontiguousarray(npts, dtype=np.int32)
+    x0 = np.ascontiguousarray(x0, dtype=np.float64)
+    dx = np.ascontiguousarray(dx, dtype=np.float64)
+    cube = np.ascontiguousarray(cube, dtype=np.float64)
+    Zs = np.ascontiguousarray(Z, dtype=np.int32)
+    pos = np.ascontiguousarray(pos_angstrom, dtype=np.float64).reshape(-1)
+    _check(lib().pg_write_cube(os.fsencode(path), len(Zs), _i(Zs) if len(Zs) else None,
+                               _d(pos) if len(Zs) else None, _i(npts), _d(x0), _d(dx), _d(cube)))
+
+
+def read_cube(path):
+    """pg_read_cube: (npts, x0, dx, natoms, values with z fastest)."""
+    npts = np.zeros(3, dtype=np.int32)
+    x0, dx = np.zeros(3), np.zeros(3)
+    nat = C.c_int(0)
+    _check(lib().pg_read_cube(os.fsencode(path), _i(npts), _d(x0), _d(dx), C.byref(nat), None, 0))
+    cube = np.empty(int(np.prod(npts)))
+    _check(lib().pg_read_cube(os.fsencode(path), _i(npts), _d(x0), _d(dx), C.byref(nat), _d(cube), len(cube)))
+    return npts, x0, dx, nat.value, cube
 
 
 class Davidson:

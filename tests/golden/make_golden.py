@@ -107,6 +107,24 @@ def analytic():
          full_evals=rf["full_evals"], full_dav_evals=rf["evals"], full_v=rf["v"])
 
 
+def observables():
+    """(H2O)6 on 14^3 over 20 bohr, three states: what the reference prints
+    (expectation values, energy partition), the cube files it writes (state
+    cubes in Gaussian and gOpenMol form, the general writer), its cube reader
+    on its own file, and Small2Large onto 17^3 over the same box."""
+    w = clusters.water_cluster(6, 6.0, SEED_C1)
+    n, L = (14, 14, 14), (20.0, 20.0, 20.0)
+    r = oracle.run_reference(n, L, waters=w, nstates=3, ptol=7, maxsub=40, maxiter=400, observables=(17, 17, 17))
+    text = lambda k: np.array(bytes(r[k].astype(np.uint8)).decode())
+    save("observables.npz", waters=w, seed=SEED_C1, n=np.array(n), L=np.array(L), nconv=r["nconv"],
+         evals=r["evals"], wavefn=r["wavefn"], v=r["v"], v_pc=r["v_pc"], v_ind=r["v_ind"], v_rep=r["v_rep"],
+         v_pol=r["v_pol"], expect_text=text("expect_text"), energy_text=text("energy_text"),
+         cube_gauss=text("cube_gauss"), cube_gomol=text("cube_gomol"), cube_gomol_state=r["cube_gomol_state"],
+         cube_free=text("cube_free"), state_cube=r["state_cube"], cube_x0=r["cube_x0"], cube_dx=r["cube_dx"],
+         read_npts=r["read_npts"], read_x0=r["read_x0"], read_dx=r["read_dx"], read_cube=r["read_cube"],
+         s2l_N=r["s2l_N"], s2l_xmin=r["s2l_xmin"], s2l_dx=r["s2l_dx"], s2l=r["s2l"])
+
+
 def c2():
     # (H2O)24, 9 A sphere, 64^3 over 40 bohr, 4 states, residual 1e-8.  With
     # the default 20-vector subspace the reference stalls on four roots (its
@@ -131,7 +149,8 @@ if __name__ == "__main__":
     a = ap.parse_args()
     if not oracle.have_reference():
         sys.exit("build the reference first: make -C oracle/ref")
-    jobs = {"kinetic": kinetic, "dpp": dpp_and_small, "c1": c1, "ions": ions_small, "analytic": analytic}
+    jobs = {"kinetic": kinetic, "dpp": dpp_and_small, "c1": c1, "ions": ions_small, "analytic": analytic,
+            "observables": observables}
     if a.c2:
         jobs["c2"] = c2
     for name, fn in jobs.items():
