@@ -12,9 +12,10 @@
 //          in memory order: B[j][i'] = P[i', j])
 //       y: A = P as rows i, K = j' (the plane transposed while it is staged),
 //          B = Ty (N = j, K = j')
-//     epilogue: W = V X + D in FP64, written into Y;
+//     epilogue: W = D in FP32, into the low word of each point's Y slot;
 //   z item (u, t): 128 consecutive plane points p = 128 t .. 128 t + 127,
-//       D[p, k] = sum_k' X[u][p + nx ny k'] Tz[k, k'],  Y += D.
+//       D[p, k] = sum_k' X[u][p + nx ny k'] Tz[k, k'],
+//     epilogue: Y = V X + (W + D), one FP64 multiply-add per point.
 // The z epilogue of vector u reads W, so it waits (bounded) until all xy
 // items of u have finished; its operand fill and MMAs do not wait.
 //
@@ -25,8 +26,10 @@
 // whatever the number of resident CTAs.
 //
 // Precision as the three-pass kernels (pg_hx_tc.cu): split-TF32 products
-// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM, V X and the sums into Y
-// in FP64.  The partial W = V X + Kx + Ky is kept in FP64 in Y.
+// Ah Bh + Ah Bl + Al Bh accumulated in FP32 in TMEM; the x + y and z sums
+// add in FP32 (their own precision) and V X in FP64.  The FP64 pipe of this
+// part retires about two FMAs per SM per clock, so the epilogues use two
+// FP64 instructions per point (one conversion, one multiply-add), not five.
 //
 // Shared memory (no-swizzle K-major core matrices, as pg_hx_tc.cu): the
 // kinetic matrices (resident; one image when the axes share one matrix),
@@ -353,6 +356,16 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t phase,
   return false;
 }
 
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* out) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) out[j] = __uint_as_float(r[j]);
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
   uint32_t r[16];
   asm volatile(
@@ -467,16 +480,6 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       const int i0 = 32 * quarter + lane;
       const long pl = nxny * (it.kind == 0 ? it.idx : 0);
       const long p = (long)(it.kind == 1 ? it.idx : 0) * kTile + i0;
-      // the first chunk's V X before the accumulator is ready
-      double pre[16];
-      if (it.kind == 0 && half < (G.npy >> 4)) {
-#pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int j = 16 * half + q;
-          const long a = pl + i0 + (long)G.nx * j;
-          pre[q] = (i0 < G.nx && j < G.ny) ? v[a] * x[a] : 0.0;
-        }
-      }
       if (leader) {
         int ok = 1;
         if (it.kind == 1) {
@@ -501,44 +504,44 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (it.kind < 0) break;
       const uint32_t acc = tmem + (uint32_t)b * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
       if (it.kind == 0) {
+        // the x + y sums of the plane, FP32, into the low word of each point's
+        // Y slot (the z item of the same points reads them, then overwrites
+        // the slot with the result)
+        float* yw = reinterpret_cast<float*>(y);
         for (int c = half; c < (G.npy >> 4); c += 2) {
-          double vx[16];
-          if (c == half) {
-#pragma unroll
-            for (int q = 0; q < 16; ++q) vx[q] = pre[q];
-          } else {
-#pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int j = 16 * c + q;
-              const long a = pl + i0 + (long)G.nx * j;
-              vx[q] = (i0 < G.nx && j < G.ny) ? v[a] * x[a] : 0.0;
-            }
-          }
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
           if (i0 < G.nx) {
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int j = 16 * c + q;
-              if (j < G.ny) y[pl + i0 + (long)G.nx * j] = vx[q] + (double)d[q];
+              if (j < G.ny) yw[2 * (pl + i0 + (long)G.nx * j)] = d[q];
             }
           }
         }
       } else {
-        for (int c = half; c < (G.npz >> 4); c += 2) {
-          double w[16];
+        // Y = V X + (Kxy + Kz): the partial sums add in FP32 (the accumulators'
+        // own precision) and V X joins in one FP64 multiply-add
+        const float* yw = reinterpret_cast<const float*>(y);
+        for (int c = half; c < (G.npz >> 3); c += 2) {
+          double vv[8], xx[8];
+          float w[8];
 #pragma unroll
-          for (int q = 0; q < 16; ++q) {
-            const int k = 16 * c + q;
-            w[q] = (p < nxny && k < G.nz) ? __ldcg(y + p + nxny * k) : 0.0;
+          for (int q = 0; q < 8; ++q) {
+            const int k = 8 * c + q;
+            const bool in = p < nxny && k < G.nz;
+            const long a = p + nxny * k;
+            vv[q] = in ? v[a] : 0.0;
+            xx[q] = in ? x[a] : 0.0;
+            w[q] = in ? __ldcg(yw + 2 * a) : 0.f;
           }
-          float d[16];
-          tmem_ld16(acc + (uint32_t)(16 * c), d);
+          float d[8];
+          tmem_ld8(acc + (uint32_t)(8 * c), d);
           if (p < nxny) {
 #pragma unroll
-            for (int q = 0; q < 16; ++q) {
-              const int k = 16 * c + q;
-              if (k < G.nz) y[p + nxny * k] = w[q] + (double)d[q];
+            for (int q = 0; q < 8; ++q) {
+              const int k = 8 * c + q;
+              if (k < G.nz) y[p + nxny * k] = fma(vv[q], xx[q], (double)(w[q] + d[q]));
             }
           }
         }
