@@ -1,0 +1,78 @@
+// DVR::ComputePotential on the GB300 library: a drop-in for the member of
+// the same name (DVR.h:63, src/DVR.cpp:661-1059), built into the reference
+// in place of that function.  The reference asks Potential::Evaluate for
+// every grid point (src/DVR.cpp:751-859); here the site tables the
+// Potential was set up with go to pg_potential_eval, which evaluates the
+// whole grid on the device, and v_diag and its four parts come back.
+//
+// Potential keeps its tables private and has no accessors, so this file
+// reads them by compiling Potential.h with its members public; the class
+// layout is unchanged.  Supported: the default electron-water model
+// (DPPGTOP with STO repulsive cores, effective-radius damping, first-order
+// polarisation: src/GetInput.cpp:43-63) and single sampling; other models
+// print and exit, as the reference does for what it cannot evaluate.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <iostream>
+#include <vector>
+
+#define private public
+#include "Potential.h"
+#undef private
+#include "DVR.h"
+#include "pisces_gb300.h"
+
+namespace {
+
+void stop(const char* what) {
+  std::cout << "ComputePotential (GB300): " << what << "\n";
+  exit(1);
+}
+
+}  // namespace
+
+void DVR::ComputePotential(class Potential& V) {
+  if (V.PotFlags.empty() || V.PotFlags[0] != 3 || V.DampType != 2 || V.PolType != 1 || V.AdiabaticPolPot != 0 ||
+      V.RepCoreType != 2 || V.nMolPol != 0)
+    stop("only the default electron-water model (DPPGTOP, STO cores, DampType 2, PolType 1) is supported");
+  if (sampling != 1) stop("only single sampling is supported");
+  std::vector<int> stosite(V.nGauss), polsite(V.nPPS);
+  std::vector<double> alpha(V.nPPS);
+  for (int i = 0; i < V.nGauss; ++i) stosite[i] = V.GaussSite[i];
+  for (int i = 0; i < V.nPPS; ++i) alpha[i] = V.PPS[2 * i], polsite[i] = V.PPSSite[i];
+  pg_sites t;
+  t.nsites = V.nSites;
+  t.sites = V.Site.data();
+  t.ncharges = V.nCharges;
+  t.charges = V.Charge.data();
+  t.charge_site = V.ChargeSite.data();
+  t.ndipoles = V.nDipoles;
+  t.dipoles = V.Dipole.data();
+  t.dipole_site = V.DipoleSite.data();
+  t.nsto = V.nGauss;
+  t.sto = V.Gauss.data();
+  t.sto_site = stosite.data();
+  t.npol = V.nPPS;
+  t.pol_alpha = alpha.data();
+  t.pol_site = polsite.data();
+  t.charge_damp = V.ChargeDamping;
+  t.dipole_damp = V.DipoleDamping;
+  t.pol_damp = V.PolDamping;
+  double L[3] = {gridpara[0], gridpara[1], gridpara[2]};
+  pg_grid* g = nullptr;
+  if (pg_grid_create_dvr(n_1dbas, L, dvrtype == 3 ? 3 : 2, &g) != PG_OK) stop(pg_last_error());
+  double *v = nullptr, *parts = nullptr;
+  if (cudaMalloc(&v, sizeof(double) * ngp) != cudaSuccess || cudaMalloc(&parts, 4 * sizeof(double) * ngp) != cudaSuccess)
+    stop("cudaMalloc failed");
+  if (pg_potential_eval(g, &t, v, parts, nullptr) != PG_OK) stop(pg_last_error());
+  double* out[5] = {v_diag, v_diag_pc, v_diag_ind, v_diag_rep, v_diag_pol};
+  if (cudaMemcpy(out[0], v, sizeof(double) * ngp, cudaMemcpyDeviceToHost) != cudaSuccess) stop("copy of V failed");
+  for (int c = 0; c < 4; ++c)
+    if (cudaMemcpy(out[c + 1], parts + (size_t)c * ngp, sizeof(double) * ngp, cudaMemcpyDeviceToHost) != cudaSuccess)
+      stop("copy of the parts failed");
+  cudaFree(v);
+  cudaFree(parts);
+  pg_grid_destroy(g);
+}
