@@ -265,66 +265,112 @@ GRAM_SHAPE = (40, 4)  # P rows x Q rows of the timed Gram launch: mid-solve basi
 
 
 def _time_launches(torch, stream, fn, reps=20, warm=3):
+    """Mean CUDA-event time of fn(i), i = 0 .. reps-1, queued back to back on
+    stream after warm untimed calls."""
     with torch.cuda.stream(stream):
-        for _ in range(warm):
-            fn()
+        for i in range(warm):
+            fn(i)
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        for _ in range(reps):
-            fn()
+        for i in range(reps):
+            fn(i)
         b.record(stream)
         torch.cuda.synchronize()
     return a.elapsed_time(b) / reps
 
 
+def _rotation(torch, set_bytes):
+    """Copies of a launch's operands to cycle through so that consecutive
+    launches touch more than twice the L2 between reuses of one copy: each
+    launch then streams its operands from HBM, as in the solve."""
+    l2 = torch.cuda.get_device_properties(0).L2_cache_size or (129 << 20)
+    return max(2, -(-2 * l2 // int(set_bytes)) + 1)
+
+
 def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
-    """The dominant kernel of the solve (the subspace Gram, k_gram_df in the
-    mixed form) and the H*X product, each timed alone with CUDA events on its
-    stream.  Algorithmic bytes: every input vector read once (Gram); X read,
-    Y written, V read once (H*X)."""
+    """The dominant kernels of the solve, each timed alone with CUDA events on
+    its stream, in the form the solve launches them.  Mixed form: the subspace
+    Gram (k_gram_df on double-float twins of both operands, the largest
+    single share of a point) and the subspace combine (k_combine_df reading
+    twins and writing the twin of its output, the Gram-Schmidt form);
+    FP64 form: k_gram and k_combine.  Then the H*X product.  Algorithmic
+    bytes: every input vector read once and every output written once
+    (Gram, combine); X read, Y written, V read once (H*X)."""
     peaks, which = measured_peaks()
     N = grid.N
     g = torch.Generator(device="cuda").manual_seed(5)
     na, nq = GRAM_SHAPE
-    P = torch.randn(na, N, dtype=torch.float64, device="cuda", generator=g)
-    Q = torch.randn(nq, N, dtype=torch.float64, device="cuda", generator=g)
+    mixed = precision == pg.PG_MIXED
+    s = stream.cuda_stream
+    k = _rotation(torch, 8.0 * N * (na + 2 * nq))
+    sets = []
+    for _ in range(k):
+        P = torch.randn(na, N, dtype=torch.float64, device="cuda", generator=g)
+        Q = torch.randn(nq, N, dtype=torch.float64, device="cuda", generator=g)
+        Y = torch.empty(nq, N, dtype=torch.float64, device="cuda")
+        if mixed:  # the solve keeps these operands as twins only
+            P, Q = pg.split_twin(P, stream=s), pg.split_twin(Q, stream=s)
+        sets.append((P, Q, Y, torch.empty_like(Y) if mixed else None))
     out = torch.empty(na * nq, dtype=torch.float64, device="cuda")
-    ms = _time_launches(torch, stream, lambda: pg.block_gram(P, Q, precision=precision, out=out,
-                                                             stream=stream.cuda_stream))
-    gbytes = 8.0 * N * (na + nq)
-    # one k_gram_df launch plus its partial-sum reduction; traffic from the ncu
-    # capture of this shape (dram read + write of k_gram_df, one launch)
-    gram = {"kernel": "k_gram_df" if precision == pg.PG_MIXED else "k_gram", "bound": "hbm",
-            "achieved": gbytes / (ms * 1e-3) / 1e9, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": gbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], "peak_source": which,
-            "traffic": GRAM_TRAFFIC.get((tuple(grid.n), na, nq, precision)), "ms_per_launch": ms,
-            "algorithmic_bytes": gbytes, "shape": f"{na} x {nq} vectors of {N} points"}
-    v = grid.potential(tables, stream=stream.cuda_stream)
-    X = torch.randn(nb * N, dtype=torch.float64, device="cuda", generator=g)
-    Y = torch.empty_like(X)
+    Cm = torch.randn(na, nq, dtype=torch.float64, device="cuda", generator=g)
+    if mixed:
+        gram_call = lambda i: pg.block_gram_twin(sets[i % k][0], sets[i % k][1], out=out, stream=s)
+        comb_call = lambda i: pg.block_combine_twin(sets[i % k][0], Cm, out=sets[i % k][2], out_twin=sets[i % k][3],
+                                                    stream=s)
+    else:
+        gram_call = lambda i: pg.block_gram(sets[i % k][0], sets[i % k][1], precision=precision, out=out, stream=s)
+        comb_call = lambda i: pg.block_combine(sets[i % k][0], Cm, precision=precision, out=sets[i % k][2], stream=s)
+    rot = f"operands rotated over {k} copies (more than twice the L2 between reuses)"
+
+    def hbm_line(kernel, ms, nbytes, traffic, shape):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        return {"kernel": kernel, "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": gbs / peaks["hbm_gbs"], "peak_source": which, "traffic": traffic, "ms_per_launch": ms,
+                "algorithmic_bytes": nbytes, "shape": shape, "l2": rot}
+
+    # Gram: one k_gram_df launch plus its partial-sum reduction per call
+    ms = _time_launches(torch, stream, gram_call)
+    gram = hbm_line("k_gram_df (twin inputs)" if mixed else "k_gram", ms, 8.0 * N * (na + nq),
+                    KERNEL_TRAFFIC.get(("gram", tuple(grid.n), na, nq, precision)),
+                    f"{na} x {nq} vectors of {N} points")
+    # combine: Y (nq rows) = P^T C, one launch per call; the twin output is
+    # written beside Y in the mixed form
+    ms = _time_launches(torch, stream, comb_call)
+    comb = hbm_line("k_combine_df (twin in, twin out)" if mixed else "k_combine", ms,
+                    8.0 * N * (na + (2 if mixed else 1) * nq),
+                    KERNEL_TRAFFIC.get(("combine", tuple(grid.n), na, nq, precision)),
+                    f"{na} vectors of {N} points combined into {nq}")
+    del sets
+    v0 = grid.potential(tables, stream=s)
+    kh = _rotation(torch, 8.0 * N * (2 * nb + 1))
+    hsets = [(v0 if j == 0 else v0.clone(), torch.randn(nb * N, dtype=torch.float64, device="cuda", generator=g),
+              torch.empty(nb * N, dtype=torch.float64, device="cuda")) for j in range(kh)]
     # queued back to back (pg_hx_async); the status word is checked once after
-    ms = _time_launches(torch, stream, lambda: grid.hx(v, X, nvec=nb, precision=precision, out=Y,
-                                                       stream=stream.cuda_stream, wait=False))
-    grid.check(stream=stream.cuda_stream)
+    ms = _time_launches(torch, stream, lambda i: grid.hx(hsets[i % kh][0], hsets[i % kh][1], nvec=nb,
+                                                         precision=precision, out=hsets[i % kh][2], stream=s,
+                                                         wait=False))
+    grid.check(stream=s)
+    del hsets
     nx, ny, nz = grid.n
     hbytes = 8.0 * N * (2 * nb + 1)
     flops = N * nb * (2 * (nx + ny + nz) + 2)
-    hx = {"kernel": f"pg_hx mixed: {grid.hx_plan(nb)}" if precision == pg.PG_MIXED else "k_hx_fp64",
-          "bound": "hbm" if precision == pg.PG_MIXED else "fp64", "ms_per_launch": ms, "algorithmic_bytes": hbytes,
-          "vectors_per_launch": nb}
-    if precision == pg.PG_MIXED:
+    hx = {"kernel": f"pg_hx mixed: {grid.hx_plan(nb)}" if mixed else "k_hx_fp64",
+          "bound": "hbm" if mixed else "fp64", "ms_per_launch": ms, "algorithmic_bytes": hbytes,
+          "vectors_per_launch": nb, "l2": f"operands rotated over {kh} copies (more than twice the L2 between reuses)"}
+    if mixed:
         hx.update(achieved=hbytes / (ms * 1e-3) / 1e9, peak=peaks["hbm_gbs"], unit="GB/s",
                   frac=hbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], peak_source=which)
     else:
         hx.update(achieved=flops / (ms * 1e-3) / 1e12, peak=1.0, unit="TFLOP/s", frac=flops / (ms * 1e-3) / 1e12,
                   peak_source="FP64 FMA pipe of this GB300, measured with a DFMA loop (not in MEASURED_PEAKS.json)")
-    return gram, hx
+    return gram, hx, comb
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch of this shape,
-# from an ncu capture of `python bench.py --roofline-only`
-GRAM_TRAFFIC = {((64, 64, 64), 40, 4, 1): 92320512 + 2397952}
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of these shapes
+# (kernel, grid, vectors in, vectors out, precision), from an ncu capture of
+# `python bench.py --roofline-only`; shapes not captured report null
+KERNEL_TRAFFIC = {}
 
 
 def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
@@ -606,8 +652,8 @@ def main():
         grid = pg.Grid(wl["n"], wl["L"])
         tables = pg.WaterTables(clusters.water_cluster(wl["nw"], wl["radius"], wl["seed"]))
         prec = pg.PG_MIXED if args.precision == "mixed" else pg.PG_FP64
-        gram, hx = kernel_rooflines(pg, torch, grid, tables, wl["nroots"], prec, torch.cuda.Stream())
-        print(json.dumps({"roofline": gram, "roofline_hx": hx, "config": cfg}))
+        gram, hx, comb = kernel_rooflines(pg, torch, grid, tables, wl["nroots"], prec, torch.cuda.Stream())
+        print(json.dumps({"roofline": gram, "roofline_combine": comb, "roofline_hx": hx, "config": cfg}))
         return
     if ws > 1:
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
@@ -628,7 +674,8 @@ def main():
             "eigenvalues": r["evals"], "max_abs_dE_vs_fp64": r["de"],
             "solve": {k: r["stats"][k] for k in ("n_matvec", "n_iter", "n_restart", "nconv", "seconds",
                                                  "host_eig_seconds", "device_wait_seconds")},
-            "roofline": r["roofline"][0], "roofline_hx": r["roofline"][1], "clocks": r["clocks"],
+            "roofline": r["roofline"][0], "roofline_combine": r["roofline"][2],
+            "roofline_hx": r["roofline"][1], "clocks": r["clocks"],
             "gpu_launches": r["launches"]}
     if r["fp64"]:
         line["fp64_gpu"] = dict(r["fp64"], solves_per_s=ws * r["fp64"]["solves_per_s"])

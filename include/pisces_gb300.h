@@ -255,6 +255,21 @@ pg_status pg_block_gram(long n, const double* P_dev, int np, const double* Q_dev
 pg_status pg_block_combine(long n, const double* P_dev, int np, const double* C_dev, int ny, double* Y_dev,
                            int precision, void* stream);
 
+/* The same products on double-float twins, the form the mixed Davidson
+ * keeps its basis and products in: a twin holds, in the 8 bytes of each
+ * value, the float2 (hi, lo) with hi + lo = x to about 2^-48 relative.
+ *   pg_split_twin:         twin_dev[i] = twin of x_dev[i]
+ *   pg_block_gram_twin:    out[a*nq + b] = P_a . Q_b, P and Q given as twins
+ *   pg_block_combine_twin: Y_r = sum_a P_a C[a*ny + r], P given as twins; Yt_dev
+ *                          (may be NULL) receives the twins of Y.
+ * Limits as pg_block_gram / pg_block_combine.  No reference counterpart
+ * (the reference's products are FP64 dgemm, src/Davidson.cpp:220, 240-260). */
+pg_status pg_split_twin(long n, const double* x_dev, double* twin_dev, void* stream);
+pg_status pg_block_gram_twin(long n, const double* Ptwin_dev, int np, const double* Qtwin_dev, int nq,
+                             double* out_dev, void* stream);
+pg_status pg_block_combine_twin(long n, const double* Ptwin_dev, int np, const double* C_dev, int ny, double* Y_dev,
+                                double* Yt_dev, void* stream);
+
 /* pg_block_gram without any device allocation; no counterpart in the
  * reference.  For callers that must not allocate device memory: a framework
  * may already hold the free memory in its own caching allocator, so a

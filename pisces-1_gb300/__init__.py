@@ -135,6 +135,9 @@ SYMBOLS = {
     "pg_block_gram": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_block_combine": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_block_gram_noalloc": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
+    "pg_split_twin": (C.c_int, [C.c_long, _vp, _vp, _vp]),
+    "pg_block_gram_twin": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, _vp]),
+    "pg_block_combine_twin": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, _vp, _vp]),
     "pg_expectation_values": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(Moments), _vp]),
     "pg_energy_partition": (C.c_int, [_vp, _vp, C.c_int, _vp, _dp, _vp]),
     "pg_state_cube": (C.c_int, [_vp, _dp, _dp]),
@@ -538,6 +541,39 @@ def block_gram_noalloc(P, Q, out, precision=PG_FP64, stream=None):
     _check_block_args(P, Q, out, np_ * nq)
     _check(lib().pg_block_gram_noalloc(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
     return out.view(-1)[:np_ * nq].view(np_, nq)
+
+
+def split_twin(X, out=None, stream=None):
+    """Double-float twins of a float64 CUDA tensor (pg_split_twin; same shape, float2 (hi, lo) per value)."""
+    import torch
+    out = torch.empty_like(X) if out is None else out
+    _check(lib().pg_split_twin(X.numel(), _dev(X), _dev(out), _stream(stream)))
+    return out
+
+
+def block_gram_twin(Pt, Qt, out=None, stream=None):
+    """out[a, b] = P_a . Q_b from twins (pg_block_gram_twin)."""
+    import torch
+    np_, n = Pt.shape
+    nq = Qt.shape[0]
+    _check_block_args(Pt, Qt, out, np_ * nq)
+    if out is None:
+        out = torch.empty(np_ * nq, dtype=torch.float64, device=Pt.device)
+    _check(lib().pg_block_gram_twin(n, _dev(Pt), np_, _dev(Qt), nq, _dev(out), _stream(stream)))
+    return out.view(-1)[:np_ * nq].view(np_, nq)
+
+
+def block_combine_twin(Pt, Cm, out=None, out_twin=None, stream=None):
+    """Y_r = sum_a P_a C[a, r] from twins of P (pg_block_combine_twin); out_twin receives Y's twins."""
+    import torch
+    np_, n = Pt.shape
+    ny = Cm.shape[1]
+    if out is None:
+        out = torch.empty(ny, n, dtype=torch.float64, device=Pt.device)
+    Cc = Cm.contiguous()
+    _check(lib().pg_block_combine_twin(n, _dev(Pt), np_, _dev(Cc), ny, _dev(out),
+                                       _dev(out_twin) if out_twin is not None else None, _stream(stream)))
+    return out
 
 
 def block_combine(P, Cm, precision=PG_FP64, out=None, stream=None):

@@ -685,6 +685,28 @@ extern "C" pg_status pg_block_combine(long n, const double* P, int np, const dou
                      precision == PG_MIXED);
 }
 
+extern "C" pg_status pg_split_twin(long n, const double* x, double* twin, void* stream) {
+  PG_ARG(n > 0 && x && twin && x != twin, "pg_split_twin: bad arguments");
+  return pg::split_twin(n, x, twin, pg::as_stream(stream));
+}
+
+extern "C" pg_status pg_block_gram_twin(long n, const double* Pt, int np, const double* Qt, int nq, double* out,
+                                        void* stream) {
+  PG_ARG(n > 0 && Pt && Qt && out && np > 0 && nq > 0, "pg_block_gram_twin: bad arguments");
+  pg::RedScratch* rs = nullptr;
+  PG_TRY(pg::thread_scratch(&rs));
+  return pg::gram(n, Pt, np, Qt, nq, out, *rs, pg::as_stream(stream), true, Pt, Qt);
+}
+
+extern "C" pg_status pg_block_combine_twin(long n, const double* Pt, int np, const double* C, int ny, double* Y,
+                                           double* Yt, void* stream) {
+  PG_ARG(n > 0 && Pt && C && Y && np > 0 && ny > 0, "pg_block_combine_twin: bad arguments");
+  pg::RedScratch* rs = nullptr;
+  PG_TRY(pg::thread_scratch(&rs));
+  return pg::combine(n, Pt, np, C, ny, 1, 1.0, nullptr, nullptr, false, Y, ny, nullptr, *rs, pg::as_stream(stream),
+                     true, Pt, Yt);
+}
+
 // ---------------------------------------------------------------------------
 // pg_block_gram_noalloc: pg_block_gram for callers that may not allocate
 // device memory.  The per-block partial sums live in a fixed file-scope

@@ -363,6 +363,34 @@ def test_block_combine(pg, torch, precision, n, na, ny):
     assert err <= (1e-14 if precision == 0 else 1e-12), err
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,na,nq", [(262144, 40, 4), (1000, 7, 3), (4097, 16, 16)])
+def test_block_products_on_twins(pg, torch, n, na, nq):
+    # the twin-input forms the mixed Davidson launches: the same products as
+    # the FP64-input mixed entry points (which split their inputs on the fly)
+    g = torch.Generator(device="cuda").manual_seed(n + na)
+    P = torch.randn(na, n, dtype=torch.float64, device="cuda", generator=g)
+    Q = torch.randn(nq, n, dtype=torch.float64, device="cuda", generator=g)
+    Cm = torch.randn(na, nq, dtype=torch.float64, device="cuda", generator=g)
+    Pt, Qt = pg.split_twin(P), pg.split_twin(Q)
+    hi_lo = Pt.view(torch.float32).view(na, n, 2).double()
+    assert float((hi_lo.sum(-1) - P).abs().max()) <= 2.0 ** -46 * float(P.abs().max())
+    S = pg.block_gram_twin(Pt, Qt)
+    torch.cuda.synchronize()
+    ref = P @ Q.T
+    scale = float(P.abs().max()) * float(Q.abs().max()) * n
+    assert float((S - ref).abs().max()) / scale <= 1e-14
+    assert float((S - pg.block_gram(P, Q, precision=pg.PG_MIXED)).abs().max()) / scale <= 1e-15
+    Yt = torch.empty(nq, n, dtype=torch.float64, device="cuda")
+    Y = pg.block_combine_twin(Pt, Cm, out_twin=Yt)
+    torch.cuda.synchronize()
+    cscale = float(Cm.abs().sum(dim=0).max()) * float(P.abs().max())
+    assert float((Y - Cm.T @ P).abs().max()) / cscale <= 1e-12
+    # the twin written beside Y is the accumulator pair: hi + lo = Y to 2^-46
+    yhl = Yt.view(torch.float32).view(nq, n, 2).double().sum(-1)
+    assert float((yhl - Y).abs().max()) <= 2.0 ** -46 * float(Y.abs().max())
+
+
 # ---------------------------------------------------------------- c2 workload
 
 def _c2(pg, torch):
