@@ -370,7 +370,8 @@ def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of these shapes
 # (kernel, grid, vectors in, vectors out, precision), from an ncu capture of
 # `python bench.py --roofline-only`; shapes not captured report null
-KERNEL_TRAFFIC = {}
+KERNEL_TRAFFIC = {("gram", (64, 64, 64), 40, 4, 1): 92536832 + 2773248,
+                  ("combine", (64, 64, 64), 40, 4, 1): 83933696 + 2898176}
 
 
 def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
