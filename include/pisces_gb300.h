@@ -136,6 +136,74 @@ pg_status pg_potential_ions_add(const pg_grid* g, int nions, const double* pos_h
  * src/Model_pot.cpp:144-156). */
 pg_status pg_potential_spherical(const pg_grid* g, double k, double* v_dev, void* stream);
 
+/* --------------------------------------- self-consistent polarisation */
+
+/* The self-consistent polarisation model of the electron-water potential
+ * (PolType 3, 5, 6; Potential::SetupDPPGTOP, src/Potential.cpp:383-460,
+ * MolPol[0]).  Host pointers.  pol_site: the site (index into the site list
+ * of the pg_sites tables it is used with) of each polarisable atom
+ * (SiteList); inva: A = (alpha^-1 - T)^-1, (3 npp)^2 doubles (InvA); epc:
+ * the water charges' field at those atoms, 3 npp (Epc); damp_type 1:
+ * g(R) = (1 - exp(-damp R^3)) / R^3, 2: effective radius r0 = damp
+ * (PolDamping); vpol_ww: the water-water polarisation energy subtracted
+ * from the term (Potential::VpolWaterWater). */
+typedef struct {
+  int npp;
+  const int* pol_site;
+  const double* inva;
+  const double* epc;
+  int damp_type;
+  double damp;
+  double vpol_ww;
+} pg_scpol_model;
+
+/* A = (alpha^-1 - T)^-1 for npp point-polarisable atoms with Thole-damped
+ * dipole tensors (ComputeInvA = BuildPolarizationMatrix + InvertMatrix,
+ * src/MolPolAux.cpp:39-136, 264-336).  Host; pos: 3*npp bohr; inva: (3 npp)^2
+ * row-major, symmetric.  PG_NUMERIC if the matrix is singular. */
+pg_status pg_scpol_inva(int npp, const double* pos_bohr, const double* alpha, double a_thole, double* inva);
+
+/* v_dev[g] += -1/2 E(r_g)^T A E(r_g) - vpol_ww, the self-consistent
+ * polarisation term (Potential::SelfConsistentPolarizability,
+ * src/Potential.cpp:1495-1628), FP64.  E(r) holds the electron's damped
+ * field at every polarisable atom plus epc.  With parts_dev (the four parts
+ * of pg_potential_eval, 4*N) the term is also added to its polarisation
+ * part.  For the reference's PolType 3 and 6 potentials, evaluate the
+ * charges and repulsive core with pg_potential_eval (no dipoles, no
+ * non-interacting polarisable sites) and add this term. */
+pg_status pg_potential_scpol_add(const pg_grid* g, const pg_sites* tables, const pg_scpol_model* m, double* v_dev,
+                                 double* parts_dev, void* stream);
+
+/* ----------------------------------------------- Hellmann-Feynman gradient */
+
+/* The grid part of the electron's gradient with respect to the site
+ * positions (DVR::ComputeGradient's loop, src/DVR.cpp:1099-1150, with
+ * Potential::EvaluateDPPGTOPGradient, DerivElecField and MuCrossMu,
+ * src/Gradients.cpp:80-241), FP64, for the density psi_dev[g]^2 of a state
+ * (N doubles on the device):
+ *   grad[3 nsites]  = sum_g psi_g^2 dV(r_g)/dR  over the charges, Slater
+ *                     cores and the field derivative at each polarisable atom
+ *   tmu[3 npp]      = sum_g psi_g^2 mu(r_g),  mu = A E(r)
+ *   mcm[(3 npp)^2]  = sum_g psi_g^2 mu(r_g) mu(r_g)^T
+ * Host outputs.  The model's damp_type must be 2 (the reference's gradient
+ * damps by the effective radius only) and pol_site increasing. */
+pg_status pg_hf_gradient_grid(const pg_grid* g, const pg_sites* tables, const pg_scpol_model* m,
+                              const double* psi_dev, double* grad, double* tmu, double* mcm, void* stream);
+
+/* The terms after the grid loop (Potential::FinalGradient and
+ * SubtractWWGradient, src/Gradients.cpp:252-289), host:
+ *   gradient[3j+d] += -dEfield[3npp (3j+d) + k] tmu[k]
+ *                     - dT_d[9 npp a_j + k] mcm[9 npp a_j + k]  (a_j: atom of
+ *                       site j, O/H sites only),
+ *   gradient -= pol_grad (if not NULL).
+ * Rigid-water layout: nsites = 4 nw (O,H,H,M), npp = 3 nw (O,H,H).
+ * dT_x/y/z: 9 npp^2 each (BuildSuperdT); dEfield: 3 nsites * 3 npp
+ * (WaterCluster::Calc_dInducedDipoles).  Together with
+ * pg_hf_gradient_grid this is DVR::ComputeGradient. */
+pg_status pg_hf_gradient_final(int nsites, int npp, const double* tmu, const double* mcm, const double* dT_x,
+                               const double* dT_y, const double* dT_z, const double* dEfield, const double* pol_grad,
+                               double* gradient);
+
 /* Rigid-water DPP site producer (host): projects each O,H,H triple onto the
  * rigid model (Water::Reposition, src/Water.cpp:695-824), solves the damped
  * self-consistent induced dipoles (WaterCluster::CalcInducedDipoles,
@@ -146,6 +214,16 @@ pg_status pg_potential_spherical(const pg_grid* g, double k, double* v_dev, void
  * *scf_iters receives the SCF iteration count (-1: not converged). */
 pg_status pg_water_sites(int nw, const double* waters_angstrom, double* sites, double* charges, int* charge_site,
                          double* dipoles, int* dipole_site, int* scf_iters);
+
+/* The polarisable atoms of the same cluster for the self-consistent model
+ * (WaterCluster::ReportPolSitesAndField, src/DPP.cpp:540-640): O, H1, H2 of
+ * every water, pol_site[3*nw] = their site indices (4j, 4j+1, 4j+2),
+ * alpha[3*nw], epc[9*nw] = the damped field of the other waters' charges at
+ * them; *vpol_ww = the water-water polarisation energy with the converged
+ * dipoles (WaterCluster::ReportPolarization, src/DPP.cpp:1648-1691,
+ * 1935-2010), the offset the reference subtracts from the term. */
+pg_status pg_water_scpol(int nw, const double* waters_angstrom, int* pol_site, double* alpha, double* epc,
+                         double* vpol_ww);
 
 /* Default electron-water model tables for those lists: 4-STO repulsive core
  * scaled by 1/4.4837, one polarisable site (alpha 9.745) per water on M,

@@ -183,6 +183,34 @@ class Grid:
                               _d(np.ascontiguousarray(parts, dtype=np.float64)), _d(out))
         return out.reshape(nstates, 4)
 
+    def potential_scpol_add(self, v, pos, inva, epc, damp_type=2, damp=2.536, vww=0.0):
+        """v += -1/2 E.(A E) - vww point by point (or_potential_scpol_add)."""
+        L = lib()
+        L.or_potential_scpol_add.argtypes = [_ip, C.POINTER(_dp), C.c_int, _dp, _dp, _dp, C.c_int, C.c_double,
+                                             C.c_double, _dp]
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        inva = np.ascontiguousarray(inva, dtype=np.float64)
+        epc = np.ascontiguousarray(epc, dtype=np.float64).reshape(-1)
+        L.or_potential_scpol_add(_i(self.n), self._x_ptrs, len(pos) // 3, _d(pos), _d(inva), _d(epc), int(damp_type),
+                                 float(damp), float(vww), _d(v))
+        return v
+
+    def hf_gradient_grid(self, sites, charges, charge_site, sto, sto_site, pol_site, inva, epc, psi,
+                         charge_damp=1.7724, pol_damp=2.536):
+        """(grad, tmu, mcm): the density-weighted grid sums (or_hf_gradient_grid)."""
+        L = lib()
+        L.or_hf_gradient_grid.argtypes = [_ip, C.POINTER(_dp), C.c_int, _dp, C.c_int, _dp, _ip, C.c_double, C.c_int,
+                                          _dp, _ip, C.c_int, _ip, _dp, _dp, C.c_double, _dp, _dp, _dp, _dp]
+        a = lambda x, t=np.float64: np.ascontiguousarray(x, dtype=t).reshape(-1)
+        sites, charges, sto, inva, epc, psi = a(sites), a(charges), a(sto), a(inva), a(epc), a(psi)
+        charge_site, sto_site, pol_site = a(charge_site, np.int32), a(sto_site, np.int32), a(pol_site, np.int32)
+        ns, npp = len(sites) // 3, len(pol_site)
+        grad, tmu, mcm = np.empty(3 * ns), np.empty(3 * npp), np.empty((3 * npp, 3 * npp))
+        L.or_hf_gradient_grid(_i(self.n), self._x_ptrs, ns, _d(sites), len(charges), _d(charges), _i(charge_site),
+                              float(charge_damp), len(sto) // 2, _d(sto), _i(sto_site), npp, _i(pol_site), _d(inva),
+                              _d(epc), float(pol_damp), _d(psi), _d(grad), _d(tmu), _d(mcm))
+        return grad, tmu, mcm
+
     def solve(self, v, nstates=1, maxsub=20, maxiter=100, ptol=5, corrflag=1, startvec=1, max_matvec=0):
         """Reference-algorithm Davidson; returns (status, evals, vectors, n_matvec)."""
         ev = np.zeros(nstates)
@@ -254,6 +282,29 @@ def dpp_sites(waters_angstrom):
     return sites, q, qs, d, ds, it
 
 
+def scpol_inva(pos, alpha, a_thole=0.3):
+    """A = (alpha^-1 - T)^-1 (or_scpol_inva), (3 npp, 3 npp)."""
+    L = lib()
+    L.or_scpol_inva.argtypes = [C.c_int, _dp, _dp, C.c_double, _dp]
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+    alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+    a = np.empty((3 * len(alpha), 3 * len(alpha)))
+    if L.or_scpol_inva(len(alpha), _d(pos), _d(alpha), float(a_thole), _d(a)) != 0:
+        raise ValueError("singular polarisation matrix")
+    return a
+
+
+def hf_gradient_final(nsites, tmu, mcm, dT_x, dT_y, dT_z, dEfield, pol_grad, gradient):
+    """gradient += FinalGradient terms - pol_grad (or_hf_gradient_final), in place."""
+    L = lib()
+    L.or_hf_gradient_final.argtypes = [C.c_int, C.c_int] + [_dp] * 8
+    arr = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (tmu, mcm, dT_x, dT_y, dT_z, dEfield)]
+    pgd = None if pol_grad is None else np.ascontiguousarray(pol_grad, dtype=np.float64)
+    L.or_hf_gradient_final(int(nsites), len(arr[0]) // 3, *[_d(a) for a in arr], _d(pgd) if pgd is not None else None,
+                           _d(gradient))
+    return gradient
+
+
 def small_to_large(n, xmin, dx, wf, N, XMIN, DX):
     """Small2Large (eight-point interpolation, normalised) onto the grid N, XMIN + I DX."""
     out = np.empty(int(np.prod(N)))
@@ -302,7 +353,7 @@ def have_reference() -> bool:
 
 def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, maxiter=100, ptol=5, startvec=1,
                   spherical_k=None, matvec_seed=None, fulldiag=False, diagonalize=True, dump_wavefn=True,
-                  threads=None, observables=None):
+                  threads=None, observables=None, poltype=None, gradient=False):
     """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration."""
     if not have_reference():
         raise FileNotFoundError(REF_BIN)
@@ -326,6 +377,10 @@ def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, 
             lines.append(f"matvec_seed {int(matvec_seed)}")
         if observables is not None:
             lines.append("observables {} {} {}".format(*[int(v) for v in observables]))
+        if poltype is not None:
+            lines.append(f"poltype {int(poltype)}")
+        if gradient:
+            lines.append("gradient 1")
         lines += [f"fulldiag {int(fulldiag)}", f"diagonalize {int(diagonalize)}",
                   f"dump_wavefn {int(dump_wavefn)}", f"out {out}"]
         with open(inp, "w") as f:

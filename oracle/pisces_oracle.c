@@ -910,3 +910,231 @@ void or_small_to_large(const int n[3], const double xmin[3], const double dx[3],
   nrm = 1.0 / sqrt(nrm);
   for (long k = 0; k < c; ++k) WF[k] *= nrm;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Self-consistent polarisation and the Hellmann-Feynman gradient.          */
+
+/* BuildPolarizationMatrix + CalcDDTensor (src/MolPolAux.cpp:100-136,
+ * 311-336), then the inverse column by column from an LU factorisation with
+ * partial pivoting (the reference inverts with LAPACK dsytrf/dsytri,
+ * src/MolPolAux.cpp:264-293; any exact inverse agrees to round-off). */
+int or_scpol_inva(int npp, const double* pos, const double* alpha, double a_thole, double* inva) {
+  const int n = 3 * npp;
+  double* a = calloc((size_t)n * n, sizeof(double));
+  int* piv = malloc(sizeof(int) * n);
+  for (int i = 0; i < npp; ++i)
+    for (int c = 0; c < 3; ++c) a[(size_t)(3 * i + c) * n + 3 * i + c] = 1.0 / alpha[i];
+  for (int i = 0; i < npp; ++i)
+    for (int j = i + 1; j < npp; ++j) {
+      const double r[3] = {pos[3 * i] - pos[3 * j], pos[3 * i + 1] - pos[3 * j + 1], pos[3 * i + 2] - pos[3 * j + 2]};
+      const double r2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2], rr = sqrt(r2);
+      const double r3 = rr * r2, r5 = r2 * r3;
+      const double te = a_thole * r3 / sqrt(alpha[i] * alpha[j]);
+      const double tf = exp(-te);
+      const double f3 = 1 - tf, f5 = 1 - (1 + te) * tf;
+      const double c1 = f5 * 3.0 / r5, c2 = f3 / r3;
+      for (int p = 0; p < 3; ++p)
+        for (int q = 0; q < 3; ++q) {
+          const double t = c1 * r[p] * r[q] - (p == q ? c2 : 0.0);
+          a[(size_t)(3 * j + p) * n + 3 * i + q] = a[(size_t)(3 * i + p) * n + 3 * j + q] = -t;
+        }
+    }
+  /* LU = P A (Doolittle, row pivoting) */
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(a[(size_t)i * n + k]) > fabs(a[(size_t)p * n + k])) p = i;
+    piv[k] = p;
+    if (a[(size_t)p * n + k] == 0) { free(a); free(piv); return -1; }
+    if (p != k)
+      for (int j = 0; j < n; ++j) { double t = a[(size_t)k * n + j]; a[(size_t)k * n + j] = a[(size_t)p * n + j]; a[(size_t)p * n + j] = t; }
+    for (int i = k + 1; i < n; ++i) {
+      const double l = a[(size_t)i * n + k] / a[(size_t)k * n + k];
+      a[(size_t)i * n + k] = l;
+      for (int j = k + 1; j < n; ++j) a[(size_t)i * n + j] -= l * a[(size_t)k * n + j];
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int col = 0; col < n; ++col) {
+    double* y = malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) y[i] = 0.0;
+    /* e_col permuted */
+    int src = col;
+    double* e = calloc(n, sizeof(double));
+    e[src] = 1.0;
+    for (int k = 0; k < n; ++k) { const double t = e[k]; e[k] = e[piv[k]]; e[piv[k]] = t; }
+    for (int i = 0; i < n; ++i) {
+      double s = e[i];
+      for (int j = 0; j < i; ++j) s -= a[(size_t)i * n + j] * y[j];
+      y[i] = s;
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double s = y[i];
+      for (int j = i + 1; j < n; ++j) s -= a[(size_t)i * n + j] * y[j];
+      y[i] = s / a[(size_t)i * n + i];
+    }
+    for (int i = 0; i < n; ++i) inva[(size_t)i * n + col] = y[i];
+    free(y); free(e);
+  }
+  free(a); free(piv);
+  return 0;
+}
+
+/* Damped field of the electron at r on every polarisable atom plus Epc
+ * (src/Potential.cpp:1518-1552). */
+static void scpol_field(const double r[3], int npp, const double* pos, const double* epc, int damp_type, double damp,
+                        double* E) {
+  for (int i = 0; i < npp; ++i) {
+    const double rx = r[0] - pos[3 * i], ry = r[1] - pos[3 * i + 1], rz = r[2] - pos[3 * i + 2];
+    const double r2 = rx * rx + ry * ry + rz * rz, R = sqrt(r2);
+    double g = 1.0 / (r2 * R);
+    if (damp_type == 1) {
+      g *= 1.0 - exp(-damp * R * r2);
+    } else if (R < damp) {
+      const double q = R / damp;
+      const double reff = damp * (0.5 + q * q * q * (1.0 - 0.5 * q));
+      g = 1.0 / (reff * reff * reff);
+    }
+    E[3 * i] = g * rx + epc[3 * i];
+    E[3 * i + 1] = g * ry + epc[3 * i + 1];
+    E[3 * i + 2] = g * rz + epc[3 * i + 2];
+  }
+}
+
+void or_potential_scpol_add(const int n[3], const double* const x[3], int npp, const double* pos, const double* inva,
+                            const double* epc, int damp_type, double damp, double vww, double* v) {
+  const int m = 3 * npp;
+  const long N = (long)n[0] * n[1] * n[2];
+#pragma omp parallel
+  {
+    double* E = malloc(sizeof(double) * m);
+#pragma omp for schedule(static)
+    for (long g = 0; g < N; ++g) {
+      const int ix = (int)(g % n[0]), iy = (int)((g / n[0]) % n[1]), iz = (int)(g / ((long)n[0] * n[1]));
+      const double r[3] = {x[0][ix], x[1][iy], x[2][iz]};
+      scpol_field(r, npp, pos, epc, damp_type, damp, E);
+      double e = 0.0;
+      for (int i = 0; i < m; ++i) {
+        double mu = 0.0;
+        for (int j = 0; j < m; ++j) mu += inva[(size_t)i * m + j] * E[j];
+        e += E[i] * mu;
+      }
+      v[g] += -0.5 * e - vww;
+    }
+    free(E);
+  }
+}
+
+void or_hf_gradient_grid(const int n[3], const double* const x[3], int nsites, const double* sites, int ncharges,
+                         const double* charges, const int* charge_site, double charge_damp, int nsto,
+                         const double* sto, const int* sto_site, int npp, const int* pol_site, const double* inva,
+                         const double* epc, double pol_damp, const double* psi, double* grad, double* tmu,
+                         double* mcm) {
+  const int m = 3 * npp;
+  const long N = (long)n[0] * n[1] * n[2];
+  double* pos = malloc(sizeof(double) * m);
+  for (int i = 0; i < npp; ++i)
+    for (int c = 0; c < 3; ++c) pos[3 * i + c] = sites[3 * pol_site[i] + c];
+  for (int k = 0; k < 3 * nsites; ++k) grad[k] = 0.0;
+  for (int k = 0; k < m; ++k) tmu[k] = 0.0;
+  for (long k = 0; k < (long)m * m; ++k) mcm[k] = 0.0;
+  /* serial over points: the sums are the checker's, in grid order */
+  double *E = malloc(sizeof(double) * m), *mu = malloc(sizeof(double) * m);
+  double *Rx = malloc(sizeof(double) * nsites), *Ry = malloc(sizeof(double) * nsites),
+         *Rz = malloc(sizeof(double) * nsites), *R = malloc(sizeof(double) * nsites),
+         *tg = malloc(sizeof(double) * 3 * nsites);
+  for (long g = 0; g < N; ++g) {
+    const double w = psi[g] * psi[g];
+    if (w == 0.0) continue; /* contributes nothing; lets tests use sparse densities on large grids */
+    const int ix = (int)(g % n[0]), iy = (int)((g / n[0]) % n[1]), iz = (int)(g / ((long)n[0] * n[1]));
+    const double r[3] = {x[0][ix], x[1][iy], x[2][iz]};
+    for (int s = 0; s < nsites; ++s) {
+      Rx[s] = r[0] - sites[3 * s];
+      Ry[s] = r[1] - sites[3 * s + 1];
+      Rz[s] = r[2] - sites[3 * s + 2];
+      R[s] = sqrt(Rx[s] * Rx[s] + Ry[s] * Ry[s] + Rz[s] * Rz[s]);
+    }
+    for (int k = 0; k < 3 * nsites; ++k) tg[k] = 0.0;
+    /* charges (src/Gradients.cpp:88-107) */
+    for (int e = 0; e < ncharges; ++e) {
+      const int s = charge_site[e];
+      double vg;
+      if (R[s] < charge_damp) {
+        const double q = R[s] / charge_damp;
+        const double reff = charge_damp * (0.5 + q * q * q * (1.0 - 0.5 * q));
+        vg = charges[e] * (3.0 * q * q - 2.0 * q * q * q) / (reff * reff);
+      } else {
+        vg = charges[e] / (R[s] * R[s]);
+      }
+      tg[3 * s] += -vg * Rx[s] / R[s];
+      tg[3 * s + 1] += -vg * Ry[s] / R[s];
+      tg[3 * s + 2] += -vg * Rz[s] / R[s];
+    }
+    /* Slater repulsive cores (src/Gradients.cpp:110-116) */
+    for (int e = 0; e < nsto; ++e) {
+      const int s = sto_site[e];
+      const double d = sto[2 * e + 1] * (-sto[2 * e]) * exp(-sto[2 * e] * R[s]);
+      tg[3 * s] += -d * Rx[s] / R[s];
+      tg[3 * s + 1] += -d * Ry[s] / R[s];
+      tg[3 * s + 2] += -d * Rz[s] / R[s];
+    }
+    /* dipoles mu = A E (src/Gradients.cpp:125-152) */
+    scpol_field(r, npp, pos, epc, 2, pol_damp, E);
+    for (int i = 0; i < m; ++i) {
+      double t = 0.0;
+      for (int j = 0; j < m; ++j) t += inva[(size_t)i * m + j] * E[j];
+      mu[i] = t;
+    }
+    /* DerivElecField (src/Gradients.cpp:164-228) */
+    for (int i = 0; i < npp; ++i) {
+      const int s = pol_site[i];
+      const double Rs = R[s];
+      double gij = 1.0 / (Rs * Rs * Rs);
+      double reff = Rs, dg = -3.0 / (reff * reff * reff * reff);
+      if (reff < pol_damp) {
+        const double q = reff / pol_damp;
+        reff = pol_damp * (0.5 + q * q * q * (1.0 - 0.5 * q));
+        dg = (3.0 * q * q - 2.0 * q * q * q) * (-3.0 / (reff * reff * reff * reff));
+        gij = 1.0 / (reff * reff * reff);
+      }
+      const double rv[3] = {Rx[s], Ry[s], Rz[s]};
+      for (int a = 0; a < 3; ++a) {
+        double d = 0.0;
+        for (int b = 0; b < 3; ++b) d += (-dg * rv[a] / Rs * rv[b] - (a == b ? gij : 0.0)) * mu[3 * i + b];
+        tg[3 * s + a] += -d;
+      }
+    }
+    for (int k = 0; k < 3 * nsites; ++k) grad[k] += w * tg[k];
+    /* MuCrossMu (src/Gradients.cpp:231-241) */
+    for (int i = 0; i < m; ++i) {
+      const double t0 = w * mu[i];
+      tmu[i] += t0;
+      for (int j = 0; j < m; ++j) mcm[(size_t)i * m + j] += t0 * mu[j];
+    }
+  }
+  free(E); free(mu); free(Rx); free(Ry); free(Rz); free(R); free(tg); free(pos);
+}
+
+void or_hf_gradient_final(int nsites, int npp, const double* tmu, const double* mcm, const double* dT_x,
+                          const double* dT_y, const double* dT_z, const double* dEfield, const double* pol_grad,
+                          double* gradient) {
+  const int n3 = 3 * npp, n9 = 9 * npp;
+  const double* dT[3] = {dT_x, dT_y, dT_z};
+  for (int j = 0; j < nsites; ++j) {
+    for (int d = 0; d < 3; ++d) {
+      double s = 0.0;
+      for (int k = 0; k < n3; ++k) s += dEfield[(size_t)n3 * (3 * j + d) + k] * tmu[k];
+      gradient[3 * j + d] -= s;
+    }
+    if ((j + 1) % 4 != 0) {
+      const int aj = 3 * (j / 4) + j % 4;
+      for (int d = 0; d < 3; ++d) {
+        double s = 0.0;
+        for (int k = 0; k < n9; ++k) s += dT[d][(size_t)aj * n9 + k] * mcm[(size_t)aj * n9 + k];
+        gradient[3 * j + d] -= s;
+      }
+    }
+  }
+  if (pol_grad)
+    for (int k = 0; k < 3 * nsites; ++k) gradient[k] -= pol_grad[k];
+}

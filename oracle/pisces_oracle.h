@@ -117,6 +117,29 @@ void or_energy_partition(const int n[3], const double* wf, int nstates, const do
 void or_small_to_large(const int n[3], const double xmin[3], const double dx[3], const double* wf, const int N[3],
                        const double XMIN[3], const double DX[3], double* WF);
 
+/* Self-consistent polarisation (PolType 3/5/6) and the electron's
+ * Hellmann-Feynman gradient on the grid.
+ * or_scpol_inva: A = (alpha^-1 - T)^-1, row-major (3 npp)^2
+ *   (src/MolPolAux.cpp:39-136, 311-336), inverted by LU with partial pivoting.
+ * or_potential_scpol_add: v[g] += -1/2 E(r_g).(A E(r_g)) - vww point by point
+ *   (src/Potential.cpp:1495-1591).
+ * or_hf_gradient_grid: the density-weighted grid sums of DVR::ComputeGradient
+ *   (src/DVR.cpp:1099-1150, src/Gradients.cpp:80-241): grad[3 nsites],
+ *   tmu[3 npp], mcm[(3 npp)^2].
+ * or_hf_gradient_final: FinalGradient and SubtractWWGradient
+ *   (src/Gradients.cpp:252-289). */
+int or_scpol_inva(int npp, const double* pos, const double* alpha, double a_thole, double* inva);
+void or_potential_scpol_add(const int n[3], const double* const x[3], int npp, const double* pos, const double* inva,
+                            const double* epc, int damp_type, double damp, double vww, double* v);
+void or_hf_gradient_grid(const int n[3], const double* const x[3], int nsites, const double* sites, int ncharges,
+                         const double* charges, const int* charge_site, double charge_damp, int nsto,
+                         const double* sto, const int* sto_site, int npp, const int* pol_site, const double* inva,
+                         const double* epc, double pol_damp, const double* psi, double* grad, double* tmu,
+                         double* mcm);
+void or_hf_gradient_final(int nsites, int npp, const double* tmu, const double* mcm, const double* dT_x,
+                          const double* dT_y, const double* dT_z, const double* dEfield, const double* pol_grad,
+                          double* gradient);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,8 @@ struct Input {
   int diagonalize = 1;
   int dump_wavefn = 1;
   int s2l[3] = {0, 0, 0};  // > 0: the observables and cube-file records, Small2Large onto this grid
+  int poltype = 1;         // 3: self-consistent polarisation (PotFlag[3])
+  int gradient = 0;        // 1: the Hellmann-Feynman gradient records (needs poltype 3)
   std::string out = "out.rec";
 };
 
@@ -126,6 +128,8 @@ Input read_input(const char* path) {
     else if (key == "diagonalize") { f >> in.diagonalize; }
     else if (key == "dump_wavefn") { f >> in.dump_wavefn; }
     else if (key == "observables") { f >> in.s2l[0] >> in.s2l[1] >> in.s2l[2]; }
+    else if (key == "poltype") { f >> in.poltype; }
+    else if (key == "gradient") { f >> in.gradient; }
     else if (key == "out") { f >> in.out; }
     else { fprintf(stderr, "unknown key %s\n", key.c_str()); exit(2); }
   }
@@ -174,7 +178,7 @@ int main(int argc, char** argv) {
 
   // Default electron-water model parameters (src/GetInput.cpp:43-63).
   iVec potflag(6);
-  potflag[0] = 3; potflag[1] = 2; potflag[2] = 0; potflag[3] = 1; potflag[4] = 0; potflag[5] = 0;
+  potflag[0] = 3; potflag[1] = 2; potflag[2] = 0; potflag[3] = in.poltype; potflag[4] = 0; potflag[5] = 0;
   double potpara[100] = {0};
   potpara[0] = 9.745; potpara[1] = 2.536; potpara[2] = 4.4837; potpara[3] = 1.7724;
   potpara[4] = 1.7724; potpara[5] = 4.4837; potpara[6] = 0.5 / sqrt(potpara[0]); potpara[10] = 20.0;
@@ -248,8 +252,16 @@ int main(int argc, char** argv) {
     put("alpha_site", ips.data(), ips.size());
     put("epc", Epc.data(), Epc.size());
 
+    // src/ClusterAnion.cpp:173: the water-water polarisation energy is the
+    // offset of the self-consistent term
+    Vel.VpolWaterWater = WaterN.ReportPolarization();
+    put1("vpol_ww", Vel.VpolWaterWater);
     Vel.Setup(potflag, nSites, Sites.data(), nCharges, Charges.data(), iqs.data(), nDipoles, Dipoles.data(),
               ids.data(), nPntPol, Alphas.data(), ips.data(), Epc.data(), DmuByDR.data(), potpara);
+    if (in.poltype == 3) {
+      put("inva", Vel.MolPol[0].InvA.data(), Vel.MolPol[0].InvA.size());
+      put("pol_site_list", Vel.MolPol[0].SiteList.data(), Vel.MolPol[0].nAtoms);
+    }
     auto t0 = std::chrono::steady_clock::now();
     Hel.ComputePotential(Vel);
     t_pot = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -327,6 +339,51 @@ int main(int argc, char** argv) {
     put1("t_diagonalize", t_diag);
     if (in.dump_wavefn) put("wavefn", Hel.wavefn.data(), (size_t)ngp * in.nstates);
     fprintf(stderr, "nconv %d t_diag %.3f s\n", nconv, t_diag);
+
+    if (in.gradient && in.poltype == 3 && nW > 0 && nconv > 0) {
+      // ClusterAnion::GetAnalGrad (src/ClusterAnion.cpp:322-416) on the
+      // converged ground state: water-side inputs, then DVR::ComputeGradient
+      // twice, once with every water-side input zero (the grid sums alone)
+      // and once as the reference calls it.
+      int nSites = 0, nCharges = 0, nDip = 0;
+      WaterN.ReportNoOfSites(nSites, nCharges, nDip);
+      const int nPntPol = WaterN.ReportNoOfPolSites();
+      dVec Sites(3 * nSites), Charges(nCharges), Dipoles(3 * nDip), DmuByDR(3 * nSites * 3 * nDip);
+      iVec iqs(nCharges), ids(nDip);
+      WaterN.GetLists(nSites, Sites.data(), nCharges, Charges.data(), iqs.data(), nDip, Dipoles.data(), ids.data(),
+                      DmuByDR.data(), 0);
+      dVec dEfield(3 * nSites * nCharges * 3), dTensor(3 * nSites * 3 * nDip * 3);
+      WaterN.Calc_dInducedDipoles(0, DmuByDR.data(), dEfield.data(), dTensor.data());
+      dVec Gradient(3 * nSites, 0.0), PolGrad(3 * nSites, 0.0);
+      const double E0g = WaterN.CalcGradient(nSites * 3, Gradient.data(), PolGrad.data(), 0);
+      put1("grad_E0", E0g);
+      put("grad_ww", Gradient.data(), Gradient.size());
+      put("pol_grad", PolGrad.data(), PolGrad.size());
+      put("dEfield", dEfield.data(), dEfield.size());
+      dVec Alphas(nPntPol), Epc(3 * nPntPol);
+      iVec ips(nPntPol);
+      WaterN.ReportPolSitesAndField(nPntPol, Alphas.data(), ips.data(), Epc.data(), 0);
+      dVec Rpps(3 * nPntPol);
+      for (int i = 0; i < nPntPol; ++i)
+        for (int c = 0; c < 3; ++c) Rpps[3 * i + c] = Sites[3 * ips[i] + c];
+      void BuildSuperdT(int, const double*, const double*, double, double*, double*, double*);
+      dVec dT_x(9 * nPntPol * nPntPol), dT_y(dT_x.size()), dT_z(dT_x.size());
+      BuildSuperdT(nPntPol, Rpps.data(), Alphas.data(), 0.3, dT_x.data(), dT_y.data(), dT_z.data());
+      put("dT_x", dT_x.data(), dT_x.size());
+      put("dT_y", dT_y.data(), dT_y.size());
+      put("dT_z", dT_z.data(), dT_z.size());
+      dVec G0(3 * nSites, 0.0), zT(dT_x.size(), 0.0), zP(3 * nSites, 0.0), zE(dEfield.size(), 0.0);
+      Hel.ComputeGradient(Vel, nSites, G0.data(), zT.data(), zT.data(), zT.data(), zP.data(), WaterN, zE.data());
+      put("grad_grid", G0.data(), G0.size());
+      auto tg0 = std::chrono::steady_clock::now();
+      Hel.ComputeGradient(Vel, nSites, Gradient.data(), dT_x.data(), dT_y.data(), dT_z.data(), PolGrad.data(), WaterN,
+                          dEfield.data());
+      put1("t_gradient", std::chrono::duration<double>(std::chrono::steady_clock::now() - tg0).count());
+      put("grad_total", Gradient.data(), Gradient.size());
+      dVec analgrad(6 * nW);
+      WaterN.ConvertF(Gradient.data(), analgrad.data());
+      put("grad_rigid", analgrad.data(), analgrad.size());
+    }
     for (int k = 0; k < in.nstates; ++k) fprintf(stderr, "E[%d] = %.17g\n", k, ev[k]);
 
     if (in.s2l[0] > 0 && nconv > 0) {

@@ -46,6 +46,12 @@ class Sites(C.Structure):
                 ("charge_damp", C.c_double), ("dipole_damp", C.c_double), ("pol_damp", C.c_double)]
 
 
+class ScPolModel(C.Structure):
+    """pg_scpol_model: the self-consistent polarisation model (host pointers)."""
+    _fields_ = [("npp", C.c_int), ("pol_site", _ip), ("inva", _dp), ("epc", _dp), ("damp_type", C.c_int),
+                ("damp", C.c_double), ("vpol_ww", C.c_double)]
+
+
 class SolveParams(C.Structure):
     _fields_ = [("nroots", C.c_int), ("maxsub", C.c_int), ("maxiter", C.c_int), ("ptol", C.c_int),
                 ("corrflag", C.c_int), ("precision", C.c_int), ("startvec", C.c_int), ("refine", C.c_int)]
@@ -136,6 +142,11 @@ SYMBOLS = {
     "pg_block_combine": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_block_gram_noalloc": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, C.c_int, _vp]),
     "pg_split_twin": (C.c_int, [C.c_long, _vp, _vp, _vp]),
+    "pg_water_scpol": (C.c_int, [C.c_int, _dp, _ip, _dp, _dp, _dp]),
+    "pg_scpol_inva": (C.c_int, [C.c_int, _dp, _dp, C.c_double, _dp]),
+    "pg_potential_scpol_add": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "pg_hf_gradient_grid": (C.c_int, [_vp, _vp, _vp, _vp, _dp, _dp, _dp, _vp]),
+    "pg_hf_gradient_final": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "pg_block_gram_twin": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, _vp]),
     "pg_block_combine_twin": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, _vp, _vp]),
     "pg_expectation_values": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(Moments), _vp]),
@@ -268,6 +279,58 @@ class WaterTables:
         return self
 
 
+def scpol_inva(pos_bohr, alpha, a_thole=0.3):
+    """A = (alpha^-1 - T)^-1 of point-polarisable atoms (pg_scpol_inva), (3 npp, 3 npp)."""
+    pos = np.ascontiguousarray(pos_bohr, dtype=np.float64).reshape(-1)
+    alpha = np.ascontiguousarray(alpha, dtype=np.float64)
+    npp = len(alpha)
+    if len(pos) != 3 * npp:
+        raise ValueError("pos must hold 3 coordinates per polarisable atom")
+    a = np.empty((3 * npp, 3 * npp))
+    _check(lib().pg_scpol_inva(npp, _d(pos), _d(alpha), float(a_thole), _d(a)))
+    return a
+
+
+class ScPol:
+    """The self-consistent polarisation model of a water cluster (PolType 3/5/6
+    of the reference): polarisable atoms O, H1, H2 of every water, A, Epc and
+    the water-water offset; `tables` are the electron's charge and
+    repulsive-core lists of the same cluster, without induced dipoles or the
+    one-site polarisation term."""
+
+    def __init__(self, waters_angstrom=None, damp=2.536, damp_type=2, a_thole=0.3, tables=None, pol_site=None,
+                 inva=None, epc=None, vpol_ww=None):
+        if waters_angstrom is not None:
+            w = WaterTables(waters_angstrom)
+            nw = w.nw
+            ps = np.empty(3 * nw, dtype=np.int32)
+            alpha = np.empty(3 * nw)
+            epc_ = np.empty(9 * nw)
+            vww = C.c_double(0)
+            _check(lib().pg_water_scpol(nw, _d(w.waters), _i(ps), _d(alpha), _d(epc_), C.byref(vww)))
+            pos = w.sites.reshape(-1, 3)[ps]
+            self.base = w
+            self.alpha = alpha
+            pol_site, epc, vpol_ww = ps, epc_, vww.value
+            inva = scpol_inva(pos, alpha, a_thole) if inva is None else inva
+            tables = w
+        self.base = tables
+        self.pol_site = np.ascontiguousarray(pol_site, dtype=np.int32)
+        self.inva = np.ascontiguousarray(inva, dtype=np.float64)
+        self.epc = np.ascontiguousarray(epc, dtype=np.float64).reshape(-1)
+        self.vpol_ww = float(vpol_ww)
+        npp = len(self.pol_site)
+        if self.inva.size != 9 * npp * npp or self.epc.size != 3 * npp:
+            raise ValueError("inva must be (3 npp)^2 and epc 3 npp values")
+        self.model = ScPolModel(npp, _i(self.pol_site), _d(self.inva), _d(self.epc), int(damp_type), float(damp),
+                                self.vpol_ww)
+        # the charges and Slater cores of the cluster, no dipoles, no
+        # one-site polarisation
+        t = tables.table
+        self.table = Sites(t.nsites, t.sites, t.ncharges, t.charges, t.charge_site, 0, None, None, t.nsto, t.sto,
+                           t.sto_site, 0, None, None, t.charge_damp, t.dipole_damp, t.pol_damp)
+
+
 class Grid:
     """3-D grid on the current CUDA device (pg_grid): dvrtype 2 = sine DVR,
     3 = periodic FFT kinetic term (the reference's DVRType values)."""
@@ -318,6 +381,35 @@ class Grid:
         _check(lib().pg_potential_eval(self._h, C.byref(tables.table), _dev(v), _dev(p) if parts else None,
                                        _stream(stream)))
         return (v, p.view(4, self.N)) if parts else v
+
+    def potential_scpol(self, model: ScPol, parts=False, stream=None):
+        """V(r) of the self-consistent polarisation model: charges and
+        repulsive core (pg_potential_eval) plus the polarisation term
+        (pg_potential_scpol_add)."""
+        v = self._new()
+        p = self._new(4) if parts else None
+        _check(lib().pg_potential_eval(self._h, C.byref(model.table), _dev(v), _dev(p) if parts else None,
+                                       _stream(stream)))
+        _check(lib().pg_potential_scpol_add(self._h, C.byref(model.table), C.byref(model.model), _dev(v),
+                                            _dev(p) if parts else None, _stream(stream)))
+        return (v, p.view(4, self.N)) if parts else v
+
+    def scpol_add(self, model: ScPol, v, parts=None, stream=None):
+        """v += the self-consistent polarisation term (pg_potential_scpol_add)."""
+        _check(lib().pg_potential_scpol_add(self._h, C.byref(model.table), C.byref(model.model), _dev(v),
+                                            _dev(parts) if parts is not None else None, _stream(stream)))
+        return v
+
+    def hf_gradient_grid(self, model: ScPol, psi, stream=None):
+        """(grad[3 nsites], tmu[3 npp], mcm[3 npp, 3 npp]): the grid sums of the
+        electron's Hellmann-Feynman gradient for the density psi^2
+        (pg_hf_gradient_grid)."""
+        ns = model.table.nsites
+        n = 3 * len(model.pol_site)
+        grad, tmu, mcm = np.empty(3 * ns), np.empty(n), np.empty((n, n))
+        _check(lib().pg_hf_gradient_grid(self._h, C.byref(model.table), C.byref(model.model), _dev(psi),
+                                         _d(grad), _d(tmu), _d(mcm), _stream(stream)))
+        return grad, tmu, mcm
 
     def add_ions(self, v, pos_bohr, q, r_cation=2.9, r_anion=1.0, stream=None):
         pos = np.ascontiguousarray(pos_bohr, dtype=np.float64).reshape(-1)
@@ -541,6 +633,19 @@ def block_gram_noalloc(P, Q, out, precision=PG_FP64, stream=None):
     _check_block_args(P, Q, out, np_ * nq)
     _check(lib().pg_block_gram_noalloc(n, _dev(P), np_, _dev(Q), nq, _dev(out), precision, _stream(stream)))
     return out.view(-1)[:np_ * nq].view(np_, nq)
+
+
+def hf_gradient_final(nsites, tmu, mcm, dT_x, dT_y, dT_z, dEfield, pol_grad, gradient):
+    """gradient += the FinalGradient terms - pol_grad (pg_hf_gradient_final), in place."""
+    tmu = np.ascontiguousarray(tmu, dtype=np.float64)
+    npp = len(tmu) // 3
+    args = [np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (mcm, dT_x, dT_y, dT_z, dEfield)]
+    pg_ = None if pol_grad is None else np.ascontiguousarray(pol_grad, dtype=np.float64)
+    if gradient.dtype != np.float64 or not gradient.flags.c_contiguous:
+        raise TypeError("gradient must be a contiguous float64 array")
+    _check(lib().pg_hf_gradient_final(int(nsites), npp, _d(tmu), *[_d(a) for a in args],
+                                      _d(pg_) if pg_ is not None else None, _d(gradient)))
+    return gradient
 
 
 def split_twin(X, out=None, stream=None):

@@ -109,20 +109,24 @@ inline double damp_dd(double r, double ai, double aj, double a) {
   return 1.0 - (1 + x) * exp(-x);
 }
 
-}  // namespace
+// The rigid monomers of a cluster and their damped self-consistent induced
+// dipoles (WaterCluster::CalcInducedDipoles, src/DPP.cpp:760-1060): the
+// polarisable atoms O, H1, H2 of every water, their polarisabilities, the
+// field f1 of the other waters' charges at them and the dipoles mu.
+struct Scf {
+  std::vector<Monomer> w;
+  std::vector<double> alpha, f1, mu;
+  int iters = -1;
+};
 
-extern "C" pg_status pg_water_sites(int nw, const double* waters, double* sites, double* charges, int* charge_site,
-                                    double* dipoles, int* dipole_site, int* scf_iters) {
-  if (nw <= 0 || !waters || !sites || !charges || !charge_site || !dipoles || !dipole_site) {
-    pg::set_error("pg_water_sites: bad arguments");
-    return PG_BAD_ARG;
-  }
-  std::vector<Monomer> w(nw);
+pg_status water_scf(const char* who, int nw, const double* waters, Scf& out) {
+  std::vector<Monomer>& w = out.w;
+  w.resize(nw);
   for (int i = 0; i < nw; ++i) {
     double b[9];
     for (int c = 0; c < 9; ++c) b[c] = waters[9 * i + c] * kAngs2Bohr;
     if (!std::isfinite(b[0] + b[1] + b[2] + b[3] + b[4] + b[5] + b[6] + b[7] + b[8])) {
-      pg::set_error("pg_water_sites: water %d has a non-finite coordinate", i);
+      pg::set_error("%s: water %d has a non-finite coordinate", who, i);
       return PG_BAD_ARG;
     }
     w[i].from_atoms(b);
@@ -131,8 +135,13 @@ extern "C" pg_status pg_water_sites(int nw, const double* waters, double* sites,
   // and M carry a damping polarisability of their own (H: alpha_H, M:
   // alpha_O; src/Water.cpp:229-232).
   const int ns = 3 * nw;
-  std::vector<double> pos(3 * (size_t)ns), alpha(ns), f1(3 * (size_t)ns, 0.0), f2(3 * (size_t)ns), mu(3 * (size_t)ns),
-      old(3 * (size_t)ns);
+  std::vector<double> pos(3 * (size_t)ns), f2(3 * (size_t)ns), old(3 * (size_t)ns);
+  std::vector<double>& alpha = out.alpha;
+  std::vector<double>& f1 = out.f1;
+  std::vector<double>& mu = out.mu;
+  alpha.assign(ns, 0.0);
+  f1.assign(3 * (size_t)ns, 0.0);
+  mu.assign(3 * (size_t)ns, 0.0);
   for (int j = 0; j < nw; ++j)
     for (int k = 0; k < 3; ++k) {
       for (int c = 0; c < 3; ++c) pos[3 * (3 * j + k) + c] = w[j].site[k][c];
@@ -159,7 +168,6 @@ extern "C" pg_status pg_water_sites(int nw, const double* waters, double* sites,
   for (int i = 0; i < ns; ++i)
     for (int c = 0; c < 3; ++c) mu[3 * i + c] = 0.5 * alpha[i] * f1[3 * i + c];
   const int maxit = 5 * (ns + 10);
-  int iters = -1;
   // The damped dipole field tensors (FieldOfDipole, src/DPP.cpp:2377-2410)
   // depend on the geometry only: computed once, then every SCF sweep is a
   // block matrix-vector product with the same operations in the same order.
@@ -204,22 +212,84 @@ extern "C" pg_status pg_water_sites(int nw, const double* waters, double* sites,
     }
     change = sqrt(change) / 3 / ns;
     if (change < 1e-12) {
-      iters = it + 1;
+      out.iters = it + 1;
       break;
     }
   }
+  return PG_OK;
+}
+
+}  // namespace
+
+extern "C" pg_status pg_water_sites(int nw, const double* waters, double* sites, double* charges, int* charge_site,
+                                    double* dipoles, int* dipole_site, int* scf_iters) {
+  if (nw <= 0 || !waters || !sites || !charges || !charge_site || !dipoles || !dipole_site) {
+    pg::set_error("pg_water_sites: bad arguments");
+    return PG_BAD_ARG;
+  }
+  Scf scf;
+  const pg_status st = water_scf("pg_water_sites", nw, waters, scf);
+  if (st != PG_OK) return st;
   // Lists for the electron (GetLists / ReportInducedDipoles, src/DPP.cpp:402-529).
   for (int j = 0; j < nw; ++j) {
     for (int s = 0; s < 4; ++s)
-      for (int c = 0; c < 3; ++c) sites[12 * j + 3 * s + c] = w[j].site[s][c];
+      for (int c = 0; c < 3; ++c) sites[12 * j + 3 * s + c] = scf.w[j].site[s][c];
     for (int k = 0; k < 3; ++k) {
       charges[3 * j + k] = k == 2 ? kQM : kQH;
       charge_site[3 * j + k] = 4 * j + 1 + k;
       dipole_site[3 * j + k] = 4 * j + k;
-      for (int c = 0; c < 3; ++c) dipoles[9 * j + 3 * k + c] = mu[3 * (3 * j + k) + c];
+      for (int c = 0; c < 3; ++c) dipoles[9 * j + 3 * k + c] = scf.mu[3 * (3 * j + k) + c];
     }
   }
-  if (scf_iters) *scf_iters = iters;
+  if (scf_iters) *scf_iters = scf.iters;
+  return PG_OK;
+}
+
+extern "C" pg_status pg_water_scpol(int nw, const double* waters, int* pol_site, double* alpha, double* epc,
+                                    double* vpol_ww) {
+  if (nw <= 0 || !waters || !pol_site || !alpha || !epc || !vpol_ww) {
+    pg::set_error("pg_water_scpol: bad arguments");
+    return PG_BAD_ARG;
+  }
+  Scf scf;
+  const pg_status st = water_scf("pg_water_scpol", nw, waters, scf);
+  if (st != PG_OK) return st;
+  // WaterCluster::ReportPolSitesAndField (src/DPP.cpp:540-640): the field
+  // there is the same sum as the SCF's f1.
+  for (int j = 0; j < nw; ++j)
+    for (int k = 0; k < 3; ++k) {
+      pol_site[3 * j + k] = 4 * j + k;
+      alpha[3 * j + k] = scf.alpha[3 * j + k];
+      for (int c = 0; c < 3; ++c) epc[3 * (3 * j + k) + c] = scf.f1[3 * (3 * j + k) + c];
+    }
+  // Water-water polarisation energy, summed pair by pair as
+  // CalcIntermolecularPotential / WaterWaterPolarizationEnergy
+  // (src/DPP.cpp:1648-1691, 1935-2010): each polarisable atom of one water
+  // in the damped field of the other water's charges, halved.
+  double pol = 0.0;
+  for (int a = 0; a < nw - 1; ++a)
+    for (int b = a + 1; b < nw; ++b) {
+      double e = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        for (int side = 0; side < 2; ++side) {
+          const int w1 = side == 0 ? a : b, w2 = side == 0 ? b : a;
+          const double* x1 = scf.w[w1].site[k].data();
+          const double* m1 = &scf.mu[3 * (3 * w1 + k)];
+          const double al = scf.alpha[3 * w1 + k];
+          for (int q = 1; q < 4; ++q) {
+            const double qq = q == 3 ? kQM : kQH;
+            const double aq = q == 3 ? kPolO : kPolH;
+            const double rx = x1[0] - scf.w[w2].site[q][0], ry = x1[1] - scf.w[w2].site[q][1],
+                         rz = x1[2] - scf.w[w2].site[q][2];
+            const double d = sqrt(rx * rx + ry * ry + rz * rz);
+            const double damp = damp_cd(d, al, aq, kDampCharge);
+            e -= qq * (m1[0] * rx + m1[1] * ry + m1[2] * rz) * damp * pow(rx * rx + ry * ry + rz * rz, -1.5) / 2.0;
+          }
+        }
+      }
+      pol += e;
+    }
+  *vpol_ww = pol;
   return PG_OK;
 }
 

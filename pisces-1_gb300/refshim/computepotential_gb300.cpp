@@ -7,10 +7,12 @@
 //
 // Potential keeps its tables private and has no accessors, so this file
 // reads them by compiling Potential.h with its members public; the class
-// layout is unchanged.  Supported: the default electron-water model
-// (DPPGTOP with STO repulsive cores, effective-radius damping, first-order
-// polarisation: src/GetInput.cpp:43-63) and single sampling; other models
-// print and exit, as the reference does for what it cannot evaluate.
+// layout is unchanged.  Supported: the electron-water model with STO
+// repulsive cores and effective-radius damping (src/GetInput.cpp:43-63),
+// with first-order polarisation (PolType 1, the default) or self-consistent
+// polarisation (PolType 3: the MolPol[0] tables go to
+// pg_potential_scpol_add), and single sampling; other models print and
+// exit, as the reference does for what it cannot evaluate.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -34,9 +36,10 @@ void stop(const char* what) {
 }  // namespace
 
 void DVR::ComputePotential(class Potential& V) {
-  if (V.PotFlags.empty() || V.PotFlags[0] != 3 || V.DampType != 2 || V.PolType != 1 || V.AdiabaticPolPot != 0 ||
-      V.RepCoreType != 2 || V.nMolPol != 0)
-    stop("only the default electron-water model (DPPGTOP, STO cores, DampType 2, PolType 1) is supported");
+  const bool sc = V.PolType == 3;
+  if (V.PotFlags.empty() || V.PotFlags[0] != 3 || V.DampType != 2 || (V.PolType != 1 && !sc) ||
+      V.AdiabaticPolPot != 0 || V.RepCoreType != 2 || V.nMolPol != (sc ? 1 : 0))
+    stop("only the electron-water model with STO cores, DampType 2 and PolType 1 or 3 is supported");
   if (sampling != 1) stop("only single sampling is supported");
   std::vector<int> stosite(V.nGauss), polsite(V.nPPS);
   std::vector<double> alpha(V.nPPS);
@@ -67,6 +70,20 @@ void DVR::ComputePotential(class Potential& V) {
   if (cudaMalloc(&v, sizeof(double) * ngp) != cudaSuccess || cudaMalloc(&parts, 4 * sizeof(double) * ngp) != cudaSuccess)
     stop("cudaMalloc failed");
   if (pg_potential_eval(g, &t, v, parts, nullptr) != PG_OK) stop(pg_last_error());
+  if (sc) {
+    // SelfConsistentPolarizability (src/Potential.cpp:1495-1591); PolType 3
+    // sets no dipoles (src/Potential.cpp:325-335), so the second part is zero
+    const DistributedPolarizabilities& mp = V.MolPol[0];
+    pg_scpol_model m;
+    m.npp = mp.nAtoms;
+    m.pol_site = mp.SiteList.data();
+    m.inva = mp.InvA.data();
+    m.epc = mp.Epc.data();
+    m.damp_type = V.DampType;
+    m.damp = V.PolDamping;
+    m.vpol_ww = V.VpolWaterWater;
+    if (pg_potential_scpol_add(g, &t, &m, v, parts, nullptr) != PG_OK) stop(pg_last_error());
+  }
   double* out[5] = {v_diag, v_diag_pc, v_diag_ind, v_diag_rep, v_diag_pol};
   if (cudaMemcpy(out[0], v, sizeof(double) * ngp, cudaMemcpyDeviceToHost) != cudaSuccess) stop("copy of V failed");
   for (int c = 0; c < 4; ++c)

@@ -125,6 +125,28 @@ def observables():
          s2l_N=r["s2l_N"], s2l_xmin=r["s2l_xmin"], s2l_dx=r["s2l_dx"], s2l=r["s2l"])
 
 
+def scpol():
+    """(H2O)6 with self-consistent polarisation (PolType 3) on 16^3 points
+    over a 20 x 22 x 24 bohr box: the model's inputs (polarisable atoms, Epc,
+    A, the water-water offset), V with its parts, the ground state, and the
+    Hellmann-Feynman gradient: the grid sums alone (every water-side input
+    zero), the water-side inputs and the gradient as ClusterAnion::GetAnalGrad
+    forms it.  The point count is the same on every axis: the reference's
+    gradient loop takes the y and z coordinates at offsets max1db[1] and
+    2 max1db[2] of its coordinate array (src/DVR.cpp:1127-1133), which are
+    the right ones only then."""
+    w = clusters.water_cluster(6, 6.0, SEED_C1)
+    n, L = (16, 16, 16), (20.0, 22.0, 24.0)
+    r = oracle.run_reference(n, L, waters=w, nstates=1, ptol=7, maxsub=20, maxiter=300, poltype=3, gradient=True)
+    save("scpol.npz", waters=w, seed=SEED_C1, n=np.array(n), L=np.array(L), sites=r["sites"], charges=r["charges"],
+         charge_site=r["charge_site"], alphas=r["alphas"], alpha_site=r["alpha_site"], epc=r["epc"],
+         vpol_ww=r["vpol_ww"], inva=r["inva"], pol_site_list=r["pol_site_list"], v=r["v"], v_pc=r["v_pc"],
+         v_ind=r["v_ind"], v_rep=r["v_rep"], v_pol=r["v_pol"], evals=r["evals"], nconv=r["nconv"],
+         wavefn=r["wavefn"], grad_grid=r["grad_grid"], grad_ww=r["grad_ww"], pol_grad=r["pol_grad"],
+         dEfield=r["dEfield"], dT_x=r["dT_x"], dT_y=r["dT_y"], dT_z=r["dT_z"], grad_total=r["grad_total"],
+         grad_rigid=r["grad_rigid"])
+
+
 def c2():
     # (H2O)24, 9 A sphere, 64^3 over 40 bohr, 4 states, residual 1e-8.  With
     # the default 20-vector subspace the reference stalls on four roots (its
@@ -150,7 +172,7 @@ if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("build the reference first: make -C oracle/ref")
     jobs = {"kinetic": kinetic, "dpp": dpp_and_small, "c1": c1, "ions": ions_small, "analytic": analytic,
-            "observables": observables}
+            "observables": observables, "scpol": scpol}
     if a.c2:
         jobs["c2"] = c2
     for name, fn in jobs.items():
