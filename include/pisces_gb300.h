@@ -174,6 +174,37 @@ pg_status pg_scpol_inva(int npp, const double* pos_bohr, const double* alpha, do
 pg_status pg_potential_scpol_add(const pg_grid* g, const pg_sites* tables, const pg_scpol_model* m, double* v_dev,
                                  double* parts_dev, void* stream);
 
+/* ------------------------------------------------------------- dual grid */
+
+/* The coarse grid of the dual-grid single point (PotFlag[3] = 6;
+ * ClusterAnion::EnergyFromConfiguration, src/ClusterAnion.cpp:211-236):
+ * for n x n x n points over a cubic box of side L, with h = L / (n + 1):
+ * odd n: nc = (n + 1) / 2 points over nc*2h + 2h (double spacing);
+ * even n: nc = 2 ((n/2 + 1) / 3) points over nc*3h + 3h (triple spacing).
+ * *spacing (may be NULL) receives 2 or 3.  PG_BAD_ARG unless the grid is
+ * cubic (the reference's dual grid is). */
+pg_status pg_dual_grid_coarse(const int n[3], const double L[3], int nc[3], double Lc[3], int* spacing);
+
+/* V of PolType 6 on the fine grid g (DVR::ComputePotential's dual branch,
+ * src/DVR.cpp:751-832): the charges and Slater cores of `tables` (no
+ * dipoles, no one-site polarisation) everywhere; at points where every
+ * site is farther than rtol (PotPara[10]), or that lie on the coarse
+ * lattice, V is interpolated from v_coarse_dev (the coarse grid's full V,
+ * nc^3 values) by the reference's inverse-distance weights
+ * (DVR::InterpolVtriple / InterpolVdouble, src/DVR.cpp:1240-1444); the
+ * other points add the self-consistent polarisation term of m.  With
+ * triple spacing the reference zeroes V on the outer layers its coarse
+ * lattice does not reach; so does this.  *n_exact (may be NULL) receives
+ * the number of points evaluated exactly.  Waits for the stream. */
+pg_status pg_dual_grid_potential(const pg_grid* g, const int nc[3], const double* v_coarse_dev,
+                                 const pg_sites* tables, const pg_scpol_model* m, double rtol, double* v_dev,
+                                 long* n_exact, void* stream);
+
+/* Start vector on the fine grid from a coarse state, interpolated the same
+ * way (DVR::ExtendWfThree / ExtendWfDouble, src/DVR.cpp:1446-1723). */
+pg_status pg_dual_grid_extend(const pg_grid* g, const int nc[3], const double* wf_coarse_dev, double* wf_dev,
+                              void* stream);
+
 /* ----------------------------------------------- Hellmann-Feynman gradient */
 
 /* The grid part of the electron's gradient with respect to the site
@@ -392,7 +423,8 @@ typedef struct {
   int ptol;       /* residual threshold 10^-ptol (pTol) */
   int corrflag;   /* 0 residual, 1 Davidson (default), 2 Jacobi-Davidson, 3 exact-kinetic preconditioner */
   int precision;  /* pg_precision of the H*X products */
-  int startvec;   /* 0: start vectors given in evecs_dev; 1: PiaB + random; 2: random */
+  int startvec;   /* 0: start vectors given in evecs_dev; 1: PiaB + random; 2: random;
+                     3: column 0 given in evecs_dev (pg_dual_grid_extend), the others random */
   int refine;     /* PG_MIXED only: 1 = finish with an FP64 Rayleigh-Ritz step on the converged vectors;
                      2 = continue the plain FP64 Davidson from them to residual 10^-max(ptol+2, 8) */
 } pg_solve_params;

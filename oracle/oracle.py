@@ -211,6 +211,18 @@ class Grid:
                               _d(epc), float(pol_damp), _d(psi), _d(grad), _d(tmu), _d(mcm))
         return grad, tmu, mcm
 
+    def dual_potential(self, nc, sites, rtol, v_coarse, v_exact):
+        """PolType 6 V from the exact fine V and the coarse V (or_dual_potential)."""
+        L = lib()
+        L.or_dual_potential.argtypes = [C.c_int, C.c_int, C.POINTER(_dp), C.c_int, _dp, C.c_double, _dp, _dp, _dp]
+        sites = np.ascontiguousarray(sites, dtype=np.float64).reshape(-1)
+        vc = np.ascontiguousarray(v_coarse, dtype=np.float64)
+        ve = np.ascontiguousarray(v_exact, dtype=np.float64)
+        v = np.empty(self.N)
+        L.or_dual_potential(int(self.n[0]), int(nc), self._x_ptrs, len(sites) // 3, _d(sites), float(rtol), _d(vc),
+                            _d(ve), _d(v))
+        return v
+
     def solve(self, v, nstates=1, maxsub=20, maxiter=100, ptol=5, corrflag=1, startvec=1, max_matvec=0):
         """Reference-algorithm Davidson; returns (status, evals, vectors, n_matvec)."""
         ev = np.zeros(nstates)
@@ -305,6 +317,16 @@ def hf_gradient_final(nsites, tmu, mcm, dT_x, dT_y, dT_z, dEfield, pol_grad, gra
     return gradient
 
 
+def dual_extend(n, nc, wf_coarse):
+    """Fine start vector from a coarse state (or_dual_extend); n, nc: points per axis."""
+    L = lib()
+    L.or_dual_extend.argtypes = [C.c_int, C.c_int, _dp, _dp]
+    wc = np.ascontiguousarray(wf_coarse, dtype=np.float64)
+    out = np.empty(n ** 3)
+    L.or_dual_extend(int(n), int(nc), _d(wc), _d(out))
+    return out
+
+
 def small_to_large(n, xmin, dx, wf, N, XMIN, DX):
     """Small2Large (eight-point interpolation, normalised) onto the grid N, XMIN + I DX."""
     out = np.empty(int(np.prod(N)))
@@ -353,7 +375,7 @@ def have_reference() -> bool:
 
 def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, maxiter=100, ptol=5, startvec=1,
                   spherical_k=None, matvec_seed=None, fulldiag=False, diagonalize=True, dump_wavefn=True,
-                  threads=None, observables=None, poltype=None, gradient=False):
+                  threads=None, observables=None, poltype=None, gradient=False, dual=False, rtol=None):
     """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration."""
     if not have_reference():
         raise FileNotFoundError(REF_BIN)
@@ -381,6 +403,10 @@ def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, 
             lines.append(f"poltype {int(poltype)}")
         if gradient:
             lines.append("gradient 1")
+        if dual:
+            lines.append("dual 1")
+        if rtol is not None:
+            lines.append(f"rtol {float(rtol)!r}")
         lines += [f"fulldiag {int(fulldiag)}", f"diagonalize {int(diagonalize)}",
                   f"dump_wavefn {int(dump_wavefn)}", f"out {out}"]
         with open(inp, "w") as f:

@@ -1138,3 +1138,104 @@ void or_hf_gradient_final(int nsites, int npp, const double* tmu, const double* 
   if (pol_grad)
     for (int k = 0; k < 3 * nsites; ++k) gradient[k] -= pol_grad[k];
 }
+
+/* ------------------------------------------------------------------------ */
+/* Dual grid.                                                               */
+
+/* Interpolated value at coarse position (px, py, pz) (fine steps from the
+ * first coarse point), spacing sp, nc coarse points per axis, following
+ * DVR::InterpolVtriple / InterpolVdouble (src/DVR.cpp:1240-1444): corners
+ * in the reference's order (0,0,0), x, y, z, xy, yz, xz, xyz, products
+ * rounded before they are added.  extend: the start-vector form
+ * (DVR::ExtendWfThree, src/DVR.cpp:1446-1642), whose table differs in two
+ * cases: remainders (2, 0, 1) weigh the corner (x, z + 1) by 1/sqrt(2)
+ * instead of 1/sqrt(8) (:1563-1566 against :1329-1332), and remainders
+ * (2, 1, 2) weigh the corner x + 1 by 1/sqrt(9) and (x + 1, y + 1) by
+ * 1/sqrt(6) (:1610-1615 against :1374-1379). */
+static double dual_interp_w(const double* F, int nc, int sp, int px, int py, int pz, int extend) {
+  static const int order[8][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1},
+                                  {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, {1, 1, 1}};
+  const int P[3] = {px, py, pz};
+  int c[3], r[3], nz = 0;
+  for (int a = 0; a < 3; ++a) {
+    c[a] = P[a] / sp;
+    r[a] = P[a] % sp;
+    if (r[a]) ++nz;
+  }
+  const long s1 = nc, s2 = (long)nc * nc;
+  if (nz == 0) return F[c[0] + c[1] * s1 + c[2] * s2];
+  double sum = 0.0;
+  for (int q = 0; q < 8; ++q) {
+    const int* o = order[q];
+    int used = 1, d2 = 0;
+    for (int a = 0; a < 3; ++a) {
+      if (o[a] && !r[a]) used = 0;
+      if (r[a]) {
+        const int dd = o[a] ? sp - r[a] : r[a];
+        d2 += dd * dd;
+      }
+    }
+    if (!used) continue;
+    const double f = F[(c[0] + o[0]) + (c[1] + o[1]) * s1 + (c[2] + o[2]) * s2];
+    if (sp == 2) {
+      sum += f;
+      continue;
+    }
+    if (extend && r[0] == 2 && r[1] == 0 && r[2] == 1 && !o[0] && o[2]) d2 = 2;
+    if (extend && r[0] == 2 && r[1] == 1 && r[2] == 2 && o[0] && !o[1] && !o[2]) d2 = 9;
+    if (extend && r[0] == 2 && r[1] == 1 && r[2] == 2 && o[0] && o[1] && !o[2]) d2 = 6;
+    double w;
+    if (nz == 1) w = d2 == 1 ? 2.0 / 3.0 : 1.0 / 3.0;
+    else if (nz == 2) w = (d2 == 2 ? 0.707107 : d2 == 5 ? 0.447214 : 0.353553) / 1.955087;
+    else w = (d2 == 3 ? 0.57735 : d2 == 6 ? 0.408248 : d2 == 9 ? 0.33333 : 0.288675) / 3.09077;
+    sum += f * w;
+  }
+  return sp == 2 ? sum / (double)(1 << nz) : sum;
+}
+
+static double dual_interp(const double* F, int nc, int sp, int px, int py, int pz) {
+  return dual_interp_w(F, nc, sp, px, py, pz, 0);
+}
+
+void or_dual_potential(int n, int nc, const double* const x[3], int nsites, const double* sites, double rtol,
+                       const double* v_coarse, const double* v_exact, double* v) {
+  const int sp = n % 2 == 1 ? 2 : 3;
+  const int checkM = sp == 3 ? n - (nc * 3 / 2 - 1) * 2 : 0;
+  long g = 0;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i, ++g) {
+        const int px = i - checkM / 2, py = j - checkM / 2, pz = k - checkM / 2;
+        double md = 50.0;
+        for (int s = 0; s < nsites; ++s) {
+          const double rx = x[0][i] - sites[3 * s], ry = x[1][j] - sites[3 * s + 1], rz = x[2][k] - sites[3 * s + 2];
+          const double r = sqrt(rx * rx + ry * ry + rz * rz);
+          if (md > r) md = r;
+        }
+        if (sp == 3 && (px < 0 || py < 0 || pz < 0 || px >= n - checkM || py >= n - checkM || pz >= n - checkM)) {
+          v[g] = 0.0;
+        } else if (md > rtol || (px % sp == 0 && py % sp == 0 && pz % sp == 0)) {
+          v[g] = dual_interp(v_coarse, nc, sp, px, py, pz);
+        } else {
+          v[g] = v_exact[g];
+        }
+      }
+}
+
+void or_dual_extend(int n, int nc, const double* wf_coarse, double* wf) {
+  const int sp = n % 2 == 1 ? 2 : 3;
+  const int checkM = sp == 3 ? n - (nc * 3 / 2 - 1) * 2 : 0;
+  long g = 0, coarse = 0;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i, ++g) {
+        const int px = i - checkM / 2, py = j - checkM / 2, pz = k - checkM / 2;
+        if (sp == 3 && (px < 0 || py < 0 || pz < 0 || px >= n - checkM || py >= n - checkM || pz >= n - checkM)) {
+          wf[g] = 0.0;
+        } else if (px % sp == 0 && py % sp == 0 && pz % sp == 0) {
+          wf[g] = wf_coarse[coarse++]; /* the coarse points in their own order, as the reference counts them */
+        } else {
+          wf[g] = dual_interp_w(wf_coarse, nc, sp, px, py, pz, 1);
+        }
+      }
+}

@@ -140,6 +140,15 @@ void or_hf_gradient_final(int nsites, int npp, const double* tmu, const double* 
                           const double* dT_y, const double* dT_z, const double* dEfield, const double* pol_grad,
                           double* gradient);
 
+/* Dual grid (PolType 6): or_dual_potential combines the fine grid's exact V
+ * (v_exact) with the interpolated coarse V as DVR::ComputePotential's dual
+ * branch does (src/DVR.cpp:751-832, InterpolVtriple/InterpolVdouble
+ * :1240-1444); or_dual_extend is DVR::ExtendWfThree / ExtendWfDouble
+ * (:1446-1723).  n, nc: points per axis (cubic grids). */
+void or_dual_potential(int n, int nc, const double* const x[3], int nsites, const double* sites, double rtol,
+                       const double* v_coarse, const double* v_exact, double* v);
+void or_dual_extend(int n, int nc, const double* wf_coarse, double* wf);
+
 #ifdef __cplusplus
 }
 #endif

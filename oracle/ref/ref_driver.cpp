@@ -109,6 +109,8 @@ struct Input {
   int s2l[3] = {0, 0, 0};  // > 0: the observables and cube-file records, Small2Large onto this grid
   int poltype = 1;         // 3: self-consistent polarisation (PotFlag[3])
   int gradient = 0;        // 1: the Hellmann-Feynman gradient records (needs poltype 3)
+  int dual = 0;            // 1: the dual-grid single point of PotFlag[3] = 6 (coarse solve, then this grid)
+  double rtol = 20.0;      // PotPara[10]: distance from every site beyond which V is interpolated
   std::string out = "out.rec";
 };
 
@@ -130,6 +132,8 @@ Input read_input(const char* path) {
     else if (key == "observables") { f >> in.s2l[0] >> in.s2l[1] >> in.s2l[2]; }
     else if (key == "poltype") { f >> in.poltype; }
     else if (key == "gradient") { f >> in.gradient; }
+    else if (key == "dual") { f >> in.dual; }
+    else if (key == "rtol") { f >> in.rtol; }
     else if (key == "out") { f >> in.out; }
     else { fprintf(stderr, "unknown key %s\n", key.c_str()); exit(2); }
   }
@@ -181,7 +185,7 @@ int main(int argc, char** argv) {
   potflag[0] = 3; potflag[1] = 2; potflag[2] = 0; potflag[3] = in.poltype; potflag[4] = 0; potflag[5] = 0;
   double potpara[100] = {0};
   potpara[0] = 9.745; potpara[1] = 2.536; potpara[2] = 4.4837; potpara[3] = 1.7724;
-  potpara[4] = 1.7724; potpara[5] = 4.4837; potpara[6] = 0.5 / sqrt(potpara[0]); potpara[10] = 20.0;
+  potpara[4] = 1.7724; potpara[5] = 4.4837; potpara[6] = 0.5 / sqrt(potpara[0]); potpara[10] = in.rtol;
 
   DVR Hel;
   Hel.SetupDVR(in.n, 0, 1, in.L, 0);
@@ -256,6 +260,58 @@ int main(int argc, char** argv) {
     // offset of the self-consistent term
     Vel.VpolWaterWater = WaterN.ReportPolarization();
     put1("vpol_ww", Vel.VpolWaterWater);
+    if (in.dual) {
+      // ClusterAnion::EnergyFromConfiguration with PotFlag[3] = 6
+      // (src/ClusterAnion.cpp:211-236, 274-290): a coarse grid of double
+      // (odd point count) or triple (even) spacing over a slightly larger
+      // box, the self-consistent model (PolType 3) solved on it, then this
+      // grid with PolType 6 and the coarse ground state as start vector.
+      int Tn[3];
+      double TL[3];
+      const double spacing = in.L[0] / (in.n[0] + 1);
+      for (int a = 0; a < 3; ++a) {
+        if (in.n[0] % 2 == 1) {
+          Tn[a] = (in.n[a] + 1) / 2;
+          TL[a] = Tn[a] * 2 * spacing + 2 * spacing;
+        } else {
+          Tn[a] = (in.n[a] / 2 + 1) / 3 * 2;
+          TL[a] = Tn[a] * 3 * spacing + 3 * spacing;
+        }
+      }
+      Hel.SetupDVR2(Tn, 0, 1, TL, 0);
+      Hel.DiagonalizeSetup(in.nstates, in.method, in.maxsub, in.maxiter, in.ptol);
+      potflag[3] = 3;
+      Vel.Setup(potflag, nSites, Sites.data(), nCharges, Charges.data(), iqs.data(), nDipoles, Dipoles.data(),
+                ids.data(), nPntPol, Alphas.data(), ips.data(), Epc.data(), DmuByDR.data(), potpara);
+      Hel.ComputePotential(Vel);
+      const int cngp = Hel.ngp;
+      put("coarse_n", Tn, 3);
+      put("coarse_L", TL, 3);
+      for (int a = 0; a < 3; ++a) {
+        int off = a == 0 ? 0 : (a == 1 ? Hel.max1db[0] : Hel.max1db[0] + Hel.max1db[1]);
+        put(std::string("coarse_x") + char('0' + a), Hel.x_dvr + off, Tn[a]);
+      }
+      put("coarse_v", Hel.v_diag, cngp);
+      dVec cev(in.nstates);
+      const int cconv = Hel.Diagonalize(in.startvec, cev.data());
+      put1i("coarse_nconv", cconv);
+      put("coarse_evals", cev.data(), in.nstates);
+      put("coarse_wavefn", Hel.wavefn.data(), (size_t)cngp * in.nstates);
+      Hel.SetupDVR2(in.n, 0, 1, in.L, 0);
+      Hel.DiagonalizeSetup(in.nstates, in.method, in.maxsub, in.maxiter, in.ptol);
+      put1i("idual", Hel.Idual);
+      {
+        // the start vector DVR::Diagonalize builds from the coarse ground
+        // state (src/DVR.cpp:422-434)
+        dVec ext(Hel.ngp, 0.0);
+        for (int g = 0; g < cngp; ++g) ext[g] = Hel.wavefn[g];
+        if (Hel.Idual == 0) Hel.ExtendWfThree(ext.data());
+        else Hel.ExtendWfDouble(ext.data());
+        put("extended_wf", ext.data(), ext.size());
+      }
+      potflag[3] = 6;
+      in.startvec = 3;
+    }
     Vel.Setup(potflag, nSites, Sites.data(), nCharges, Charges.data(), iqs.data(), nDipoles, Dipoles.data(),
               ids.data(), nPntPol, Alphas.data(), ips.data(), Epc.data(), DmuByDR.data(), potpara);
     if (in.poltype == 3) {

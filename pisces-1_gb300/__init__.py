@@ -147,6 +147,9 @@ SYMBOLS = {
     "pg_potential_scpol_add": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "pg_hf_gradient_grid": (C.c_int, [_vp, _vp, _vp, _vp, _dp, _dp, _dp, _vp]),
     "pg_hf_gradient_final": (C.c_int, [C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "pg_dual_grid_coarse": (C.c_int, [_ip, _dp, _ip, _dp, _ip]),
+    "pg_dual_grid_potential": (C.c_int, [_vp, _ip, _vp, _vp, _vp, C.c_double, _vp, C.POINTER(C.c_long), _vp]),
+    "pg_dual_grid_extend": (C.c_int, [_vp, _ip, _vp, _vp, _vp]),
     "pg_block_gram_twin": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, _vp]),
     "pg_block_combine_twin": (C.c_int, [C.c_long, _vp, C.c_int, _vp, C.c_int, _vp, _vp, _vp]),
     "pg_expectation_values": (C.c_int, [_vp, _vp, C.c_int, C.POINTER(Moments), _vp]),
@@ -279,6 +282,15 @@ class WaterTables:
         return self
 
 
+def dual_grid_coarse(n, L):
+    """(nc, Lc, spacing) of the dual grid's coarse grid (pg_dual_grid_coarse)."""
+    n = np.ascontiguousarray(np.broadcast_to(n, 3), dtype=np.int32)
+    L = np.ascontiguousarray(np.broadcast_to(L, 3), dtype=np.float64)
+    nc, Lc, sp = np.empty(3, dtype=np.int32), np.empty(3), C.c_int(0)
+    _check(lib().pg_dual_grid_coarse(_i(n), _d(L), _i(nc), _d(Lc), C.byref(sp)))
+    return tuple(int(v) for v in nc), tuple(float(v) for v in Lc), sp.value
+
+
 def scpol_inva(pos_bohr, alpha, a_thole=0.3):
     """A = (alpha^-1 - T)^-1 of point-polarisable atoms (pg_scpol_inva), (3 npp, 3 npp)."""
     pos = np.ascontiguousarray(pos_bohr, dtype=np.float64).reshape(-1)
@@ -400,6 +412,22 @@ class Grid:
                                             _dev(parts) if parts is not None else None, _stream(stream)))
         return v
 
+    def dual_potential(self, nc, v_coarse, model: ScPol, rtol, stream=None):
+        """(V, exact point count) of PolType 6 from the coarse grid's V (pg_dual_grid_potential)."""
+        nc = np.ascontiguousarray(np.broadcast_to(nc, 3), dtype=np.int32)
+        v = self._new()
+        ne = C.c_long(0)
+        _check(lib().pg_dual_grid_potential(self._h, _i(nc), _dev(v_coarse), C.byref(model.table),
+                                            C.byref(model.model), float(rtol), _dev(v), C.byref(ne), _stream(stream)))
+        return v, ne.value
+
+    def dual_extend(self, nc, wf_coarse, stream=None):
+        """Fine-grid start vector from a coarse state (pg_dual_grid_extend)."""
+        nc = np.ascontiguousarray(np.broadcast_to(nc, 3), dtype=np.int32)
+        w = self._new()
+        _check(lib().pg_dual_grid_extend(self._h, _i(nc), _dev(wf_coarse), _dev(w), _stream(stream)))
+        return w
+
     def hf_gradient_grid(self, model: ScPol, psi, stream=None):
         """(grad[3 nsites], tmu[3 npp], mcm[3 npp, 3 npp]): the grid sums of the
         electron's Hellmann-Feynman gradient for the density psi^2
@@ -463,12 +491,14 @@ class Grid:
               refine=1, start=None, stream=None, raise_on_nonconv=True):
         """Device Davidson eigensolve; returns (evals, evecs[nroots, N] on the device, stats dict)."""
         import torch
-        p = SolveParams(nroots, maxsub, maxiter, ptol, corrflag, precision, 0 if start is not None else startvec,
-                        refine)
+        if start is not None and startvec != 3:
+            startvec = 0
+        p = SolveParams(nroots, maxsub, maxiter, ptol, corrflag, precision, startvec, refine)
         ev = np.zeros(nroots)
         vec = torch.empty(nroots * self.N, dtype=torch.float64, device="cuda")
         if start is not None:
-            vec.copy_(start.reshape(-1))
+            # startvec 3: only the first column is given
+            vec[:start.numel()].copy_(start.reshape(-1))
         st = SolveStats()
         s = lib().pg_solve(self._h, _dev(v), C.byref(p), _d(ev), _dev(vec), C.byref(st), _stream(stream))
         if s != PG_OK and (s != PG_NOT_CONVERGED or raise_on_nonconv):
@@ -598,6 +628,30 @@ def cluster_solve(n, L, waters_angstrom, ions=None, nroots=1, maxsub=20, maxiter
                                _stream(stream) if stream is not None else None)
     _check(s)
     return ev, (vec.reshape(nroots, N) if want_vectors else None), st.as_dict(nroots)
+
+
+def dual_single_point(n, L, model: ScPol, rtol=20.0, nroots=1, maxsub=20, maxiter=100, ptol=5, corrflag=1,
+                      precision=PG_FP64, refine=1, stream=None):
+    """The dual-grid single point (PotFlag[3] = 6 of
+    ClusterAnion::EnergyFromConfiguration, src/ClusterAnion.cpp:211-290):
+    the self-consistent model (PolType 3) solved on the coarse grid of
+    pg_dual_grid_coarse, V of PolType 6 on the n^3 grid from the coarse V
+    (pg_dual_grid_potential), then the fine solve from the coarse ground
+    state interpolated onto it (pg_dual_grid_extend; startvec 3).
+    Returns a dict: evals, evecs (device), v (device), n_exact, stats, and
+    the coarse grid's nc, Lc, evals."""
+    nc, Lc, _ = dual_grid_coarse(n, L)
+    coarse = Grid(nc, Lc)
+    vc = coarse.potential_scpol(model, stream=stream)
+    kw = dict(maxsub=maxsub, maxiter=maxiter, ptol=ptol, corrflag=corrflag, precision=precision, refine=refine,
+              stream=stream)
+    ec, wc, _ = coarse.solve(vc, nroots=nroots, startvec=1, **kw)
+    fine = Grid(np.broadcast_to(n, 3), np.broadcast_to(L, 3))
+    v, n_exact = fine.dual_potential(nc, vc, model, rtol, stream=stream)
+    start = fine.dual_extend(nc, wc[0], stream=stream)
+    ev, vec, st = fine.solve(v, nroots=nroots, startvec=3, start=start, **kw)
+    return {"evals": ev, "evecs": vec, "v": v, "n_exact": n_exact, "stats": st, "grid": fine, "coarse_n": nc,
+            "coarse_L": Lc, "coarse_evals": ec}
 
 
 def _check_block_args(P, Q, out, nout):

@@ -29,7 +29,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               f"-I{INCLUDE}", f"-I{CSRC}", f"-I{BUILD}", "--expt-relaxed-constexpr"]
 # files whose floating-point evaluation order follows the reference exactly
-NO_FMA = {"pg_potential.cu", "pg_observables.cu"}
+NO_FMA = {"pg_potential.cu", "pg_observables.cu", "pg_dual.cu"}
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 

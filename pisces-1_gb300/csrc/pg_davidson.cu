@@ -945,6 +945,7 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
   PG_ARG(g && v && p && evals && evecs, "pg_solve: null argument");
   PG_ARG(p->nroots > 0 && p->maxsub > p->nroots && p->maxiter > 0 && p->ptol > 0, "pg_solve: bad parameters");
   PG_ARG(p->precision == PG_FP64 || p->precision == PG_MIXED, "pg_solve: unknown precision");
+  PG_ARG(p->startvec >= 0 && p->startvec <= 3, "pg_solve: startvec %d is not 0, 1, 2 or 3", p->startvec);
   PG_ARG(g->N < (1L << 31), "pg_solve: grid too large for the reverse-communication interface");
   auto t0 = std::chrono::steady_clock::now();
   const long N = g->N;
@@ -956,10 +957,16 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
   PG_TRY(Z.ensure((size_t)ms * N));
   PG_TRY(diag.ensure(N));
   PG_TRY(work.ensure((size_t)pg_davidson_work_size((int)N, ms, nr, p->corrflag)));
-  if (p->startvec == 0)
+  if (p->startvec == 0) {
     PG_CUDA_TRY(cudaMemcpyAsync(B.p, evecs, sizeof(double) * N * nr, cudaMemcpyDeviceToDevice, st));
-  else
+  } else if (p->startvec == 3) {
+    // SVFlag 3 (src/DVR.cpp:422-434): column 0 given (the coarse state
+    // interpolated onto this grid), the others random
+    PG_CUDA_TRY(cudaMemcpyAsync(B.p, evecs, sizeof(double) * N, cudaMemcpyDeviceToDevice, st));
+    if (nr > 1) PG_TRY(start_vectors(g, nr - 1, 2, B.p + N, st));
+  } else {
     PG_TRY(start_vectors(g, nr, p->startvec, B.p, st));
+  }
   PG_TRY(pg_diagonal(g, v, diag.p, st));
   pg_davidson& d = ws.d;
   d.status = 0;  // a fresh solve, whatever the last one left behind
@@ -1134,7 +1141,7 @@ extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw,
   PG_ARG(n && L && p && evals && nw >= 0 && nions >= 0, "pg_cluster_solve: bad arguments");
   PG_ARG(nw == 0 || waters, "pg_cluster_solve: null water coordinates");
   PG_ARG(nions == 0 || ions, "pg_cluster_solve: null ion list");
-  PG_ARG(p->startvec != 0, "pg_cluster_solve: start vectors 0 need pg_solve");
+  PG_ARG(p->startvec == 1 || p->startvec == 2, "pg_cluster_solve: start vectors 0 and 3 need pg_solve");
   PG_ARG(p->nroots > 0, "pg_cluster_solve: bad parameters");
   cudaStream_t st = as_stream(stream);
   std::shared_ptr<pg_grid> gs;

@@ -31,7 +31,7 @@
 #include <cstring>
 #include <vector>
 
-#include "pg_common.cuh"
+#include "pg_solve.cuh"
 
 namespace {
 
@@ -134,19 +134,19 @@ long chunk_points(long N, int n) {
 // ---------------------------------------------------------------- device side
 
 // Field of the electron at every polarisable site plus Epc, for points
-// [p0, p0 + np) of the grid (x fastest):  E[p*n + 3i + c]
-// (src/Potential.cpp:1518-1552; distances as Potential::Evaluate,
-// src/Potential.cpp:136-146).
-__global__ void k_scpol_field(long p0, long np, int nx, int ny, const double* __restrict__ gx,
-                              const double* __restrict__ gy, const double* __restrict__ gz, int npp,
-                              const double* __restrict__ pos, const double* __restrict__ epc, int damp_type,
-                              double damp, double* __restrict__ E) {
+// [p0, p0 + np) of the grid (x fastest), or of a point list (list[p0 + p]):
+// E[p*n + 3i + c] (src/Potential.cpp:1518-1552; distances as
+// Potential::Evaluate, src/Potential.cpp:136-146).
+__global__ void k_scpol_field(long p0, long np, const int* __restrict__ list, int nx, int ny,
+                              const double* __restrict__ gx, const double* __restrict__ gy,
+                              const double* __restrict__ gz, int npp, const double* __restrict__ pos,
+                              const double* __restrict__ epc, int damp_type, double damp, double* __restrict__ E) {
   const long total = np * npp;
   const int n = 3 * npp;
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
     const long p = t / npp;
     const int i = (int)(t - p * npp);
-    const long gi = p0 + p;
+    const long gi = list ? (long)list[p0 + p] : p0 + p;
     const int ix = (int)(gi % nx);
     const long r = gi / nx;
     const int iy = (int)(r % ny), iz = (int)(r / ny);
@@ -241,15 +241,17 @@ __global__ void __launch_bounds__(kGT) k_scpol_gemm(long np, int n, const double
   }
 }
 
-// v[p0+p] += -1/2 sum_ct part[ct*np + p] - vww  (and the polarisation part)
-__global__ void k_scpol_finish(long p0, long np, int nct, const double* __restrict__ part, double vww,
-                               double* __restrict__ v, double* __restrict__ vpol) {
+// v[g] += -1/2 sum_ct part[ct*np + p] - vww (and the polarisation part),
+// g = p0 + p or list[p0 + p]
+__global__ void k_scpol_finish(long p0, long np, const int* __restrict__ list, int nct, const double* __restrict__ part,
+                               double vww, double* __restrict__ v, double* __restrict__ vpol) {
   for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np; p += (long)gridDim.x * blockDim.x) {
     double s = 0.0;
     for (int ct = 0; ct < nct; ++ct) s += part[(long)ct * np + p];
     const double val = -0.5 * s - vww;
-    v[p0 + p] += val;
-    if (vpol) vpol[p0 + p] += val;
+    const long g = list ? (long)list[p0 + p] : p0 + p;
+    v[g] += val;
+    if (vpol) vpol[g] += val;
   }
 }
 
@@ -477,34 +479,41 @@ extern "C" pg_status pg_scpol_inva(int npp, const double* pos, const double* alp
   return PG_OK;
 }
 
-extern "C" pg_status pg_potential_scpol_add(const pg_grid* g, const pg_sites* t, const pg_scpol_model* m, double* v,
-                                            double* parts, void* stream) {
-  PG_ARG(g && v, "pg_potential_scpol_add: null argument");
+namespace pg {
+
+pg_status scpol_add_points(const pg_grid* g, const pg_sites* t, const pg_scpol_model* m, const int* list, long count,
+                           double* v, double* vpol, cudaStream_t st) {
   PG_TRY(check_model("pg_potential_scpol_add", t, m));
-  cudaStream_t st = pg::as_stream(stream);
+  if (count == 0) return PG_OK;
   ModelDev md;
   PG_TRY(md.upload(t, m, st));
   const int n = 3 * m->npp;
-  const long N = g->N;
-  const long chunk = chunk_points(N, n);
+  const long chunk = chunk_points(count, n);
   const int nct = (n + kBN - 1) / kBN;
   pg::DevBuf<double> E, part;
   PG_TRY(E.alloc((size_t)chunk * n));
   PG_TRY(part.alloc((size_t)chunk * nct));
-  double* vpol = parts ? parts + 3 * N : nullptr;
-  for (long p0 = 0; p0 < N; p0 += chunk) {
-    const long np = chunk < N - p0 ? chunk : N - p0;
-    k_scpol_field<<<stride_blocks(np * m->npp), 256, 0, st>>>(p0, np, g->n[0], g->n[1], g->x_dev[0].p, g->x_dev[1].p,
-                                                             g->x_dev[2].p, m->npp, md.pos.p, md.epc.p, m->damp_type,
-                                                             m->damp, E.p);
+  for (long p0 = 0; p0 < count; p0 += chunk) {
+    const long np = chunk < count - p0 ? chunk : count - p0;
+    k_scpol_field<<<stride_blocks(np * m->npp), 256, 0, st>>>(p0, np, list, g->n[0], g->n[1], g->x_dev[0].p,
+                                                             g->x_dev[1].p, g->x_dev[2].p, m->npp, md.pos.p, md.epc.p,
+                                                             m->damp_type, m->damp, E.p);
     PG_TRY(pg::check_launch("k_scpol_field"));
     k_scpol_gemm<false><<<dim3((unsigned)((np + kBM - 1) / kBM), nct), kGT, 0, st>>>(np, n, E.p, md.inva.p, part.p);
     PG_TRY(pg::check_launch("k_scpol_gemm"));
-    k_scpol_finish<<<stride_blocks(np), 256, 0, st>>>(p0, np, nct, part.p, m->vpol_ww, v, vpol);
+    k_scpol_finish<<<stride_blocks(np), 256, 0, st>>>(p0, np, list, nct, part.p, m->vpol_ww, v, vpol);
     PG_TRY(pg::check_launch("k_scpol_finish"));
   }
   PG_CUDA_TRY(cudaStreamSynchronize(st));
   return PG_OK;
+}
+
+}  // namespace pg
+
+extern "C" pg_status pg_potential_scpol_add(const pg_grid* g, const pg_sites* t, const pg_scpol_model* m, double* v,
+                                            double* parts, void* stream) {
+  PG_ARG(g && v, "pg_potential_scpol_add: null argument");
+  return pg::scpol_add_points(g, t, m, nullptr, g->N, v, parts ? parts + 3 * g->N : nullptr, pg::as_stream(stream));
 }
 
 extern "C" pg_status pg_hf_gradient_grid(const pg_grid* g, const pg_sites* t, const pg_scpol_model* m,
@@ -579,9 +588,9 @@ extern "C" pg_status pg_hf_gradient_grid(const pg_grid* g, const pg_sites* t, co
   const int nct = (n + kBN - 1) / kBN;
   for (long p0 = 0; p0 < N; p0 += chunk) {
     const long np = chunk < N - p0 ? chunk : N - p0;
-    k_scpol_field<<<stride_blocks(np * m->npp), 256, 0, st>>>(p0, np, g->n[0], g->n[1], g->x_dev[0].p, g->x_dev[1].p,
-                                                             g->x_dev[2].p, m->npp, md.pos.p, md.epc.p, 2, m->damp,
-                                                             E.p);
+    k_scpol_field<<<stride_blocks(np * m->npp), 256, 0, st>>>(p0, np, nullptr, g->n[0], g->n[1], g->x_dev[0].p,
+                                                             g->x_dev[1].p, g->x_dev[2].p, m->npp, md.pos.p, md.epc.p,
+                                                             2, m->damp, E.p);
     PG_TRY(pg::check_launch("k_scpol_field"));
     k_scpol_gemm<true><<<dim3((unsigned)((np + kBM - 1) / kBM), nct), kGT, 0, st>>>(np, n, E.p, md.inva.p, MU.p);
     PG_TRY(pg::check_launch("k_scpol_gemm"));

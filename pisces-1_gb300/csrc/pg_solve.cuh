@@ -1,5 +1,7 @@
 // Internal interfaces between the eigensolver (pg_davidson.cu), the
-// tensor-core H*X (pg_hx_tc.cu) and the serving engine (pg_serve.cu).
+// tensor-core H*X (pg_hx_tc.cu), the serving engine (pg_serve.cu) and the
+// self-consistent polarisation term with the dual grid built on it
+// (pg_scpol.cu, pg_dual.cu).
 #pragma once
 
 #include <functional>
@@ -26,6 +28,12 @@ pg_status start_vectors(const pg_grid* g, int nroots, int startvec, double* B, c
 // V(r) of a water cluster (default model) plus Bloomfield ions on the device.
 pg_status cluster_potential(const pg_grid* g, int nw, const double* waters, int nions, const double* ions, double* v,
                             cudaStream_t st);
+
+// v[g] += the self-consistent polarisation term for the grid points
+// list[0 .. count) (all points, in order, if list is null; list on the
+// device); the same term also added to vpol if not null.  Waits for st.
+pg_status scpol_add_points(const pg_grid* g, const pg_sites* t, const pg_scpol_model* m, const int* list, long count,
+                           double* v, double* vpol, cudaStream_t st);
 
 constexpr int kMaxBatchJobs = 16;  // job-table entries of one tensor-core launch
 

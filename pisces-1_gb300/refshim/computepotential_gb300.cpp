@@ -11,8 +11,11 @@
 // repulsive cores and effective-radius damping (src/GetInput.cpp:43-63),
 // with first-order polarisation (PolType 1, the default) or self-consistent
 // polarisation (PolType 3: the MolPol[0] tables go to
-// pg_potential_scpol_add), and single sampling; other models print and
-// exit, as the reference does for what it cannot evaluate.
+// pg_potential_scpol_add), or the dual grid's PolType 6 (the coarse V that
+// v_diag still holds from the previous call, on the Pre1db grid, goes to
+// pg_dual_grid_potential with Rtol; src/DVR.cpp:735-832), and single
+// sampling; other models print and exit, as the reference does for what it
+// cannot evaluate.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -36,10 +39,11 @@ void stop(const char* what) {
 }  // namespace
 
 void DVR::ComputePotential(class Potential& V) {
-  const bool sc = V.PolType == 3;
+  const bool dual = V.PolType == 6;
+  const bool sc = V.PolType == 3 || dual;
   if (V.PotFlags.empty() || V.PotFlags[0] != 3 || V.DampType != 2 || (V.PolType != 1 && !sc) ||
       V.AdiabaticPolPot != 0 || V.RepCoreType != 2 || V.nMolPol != (sc ? 1 : 0))
-    stop("only the electron-water model with STO cores, DampType 2 and PolType 1 or 3 is supported");
+    stop("only the electron-water model with STO cores, DampType 2 and PolType 1, 3 or 6 is supported");
   if (sampling != 1) stop("only single sampling is supported");
   std::vector<int> stosite(V.nGauss), polsite(V.nPPS);
   std::vector<double> alpha(V.nPPS);
@@ -69,6 +73,33 @@ void DVR::ComputePotential(class Potential& V) {
   double *v = nullptr, *parts = nullptr;
   if (cudaMalloc(&v, sizeof(double) * ngp) != cudaSuccess || cudaMalloc(&parts, 4 * sizeof(double) * ngp) != cudaSuccess)
     stop("cudaMalloc failed");
+  if (dual) {
+    // PolType 6 has no induced-dipole part (src/Potential.cpp:904-907) and
+    // no one-site term; the four parts are not written, as the reference
+    // does not write them for this model
+    t.ndipoles = 0, t.npol = 0;
+    const DistributedPolarizabilities& mp = V.MolPol[0];
+    pg_scpol_model m;
+    m.npp = mp.nAtoms;
+    m.pol_site = mp.SiteList.data();
+    m.inva = mp.InvA.data();
+    m.epc = mp.Epc.data();
+    m.damp_type = V.DampType;
+    m.damp = V.PolDamping;
+    m.vpol_ww = V.VpolWaterWater;
+    const size_t ncg = (size_t)Pre1db[0] * Pre1db[1] * Pre1db[2];
+    double* vc = nullptr;
+    if (cudaMalloc(&vc, sizeof(double) * ncg) != cudaSuccess) stop("cudaMalloc failed");
+    if (cudaMemcpy(vc, v_diag, sizeof(double) * ncg, cudaMemcpyHostToDevice) != cudaSuccess)
+      stop("copy of the coarse V failed");
+    if (pg_dual_grid_potential(g, Pre1db, vc, &t, &m, V.Rtol, v, nullptr, nullptr) != PG_OK) stop(pg_last_error());
+    if (cudaMemcpy(v_diag, v, sizeof(double) * ngp, cudaMemcpyDeviceToHost) != cudaSuccess) stop("copy of V failed");
+    cudaFree(vc);
+    cudaFree(v);
+    cudaFree(parts);
+    pg_grid_destroy(g);
+    return;
+  }
   if (pg_potential_eval(g, &t, v, parts, nullptr) != PG_OK) stop(pg_last_error());
   if (sc) {
     // SelfConsistentPolarizability (src/Potential.cpp:1495-1591); PolType 3

@@ -147,6 +147,28 @@ def scpol():
          grad_rigid=r["grad_rigid"])
 
 
+def dual():
+    """(H2O)6, the dual-grid single point (PotFlag[3] = 6) on four cubic
+    grids over a 20 bohr box: 16^3 (triple spacing, no zeroed layer), 18^3
+    (one zeroed layer on each side), 20^3 (two) and 17^3 (double spacing),
+    with Rtol = 6 bohr so that both interpolated and exact points occur.
+    Per grid: the coarse grid, its V (PolType 3) and ground state, the
+    interpolated start vector, the fine V (PolType 6) and the fine ground
+    state.  The model's inputs (PolType 3) once."""
+    w = clusters.water_cluster(6, 6.0, SEED_C1)
+    out = {"waters": w, "seed": SEED_C1, "L": np.array([20.0] * 3), "rtol": 6.0, "grids": np.array([16, 17, 18, 20])}
+    for n in (16, 17, 18, 20):
+        r = oracle.run_reference((n,) * 3, (20.0,) * 3, waters=w, nstates=1, ptol=7, maxsub=20, maxiter=300,
+                                 poltype=3, dual=True, rtol=6.0)
+        for k in ("coarse_n", "coarse_L", "coarse_v", "coarse_evals", "coarse_nconv", "extended_wf", "v", "evals",
+                  "nconv", "idual"):
+            out[f"{k}_{n}"] = r[k]
+        out[f"coarse_wavefn_{n}"] = r["coarse_wavefn"][:int(np.prod(r["coarse_n"]))]
+        for k in ("sites", "charges", "charge_site", "pol_site_list", "alphas", "epc", "vpol_ww", "inva"):
+            out[k] = r[k]
+    save("dual.npz", **out)
+
+
 def c2():
     # (H2O)24, 9 A sphere, 64^3 over 40 bohr, 4 states, residual 1e-8.  With
     # the default 20-vector subspace the reference stalls on four roots (its
@@ -172,7 +194,7 @@ if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("build the reference first: make -C oracle/ref")
     jobs = {"kinetic": kinetic, "dpp": dpp_and_small, "c1": c1, "ions": ions_small, "analytic": analytic,
-            "observables": observables, "scpol": scpol}
+            "observables": observables, "scpol": scpol, "dual": dual}
     if a.c2:
         jobs["c2"] = c2
     for name, fn in jobs.items():

@@ -45,7 +45,7 @@ def test_shims_link_into_the_reference(pg):
     undef = subprocess.run(["nm", "-D", "--undefined-only", EXE], capture_output=True, text=True,
                            check=True).stdout
     calls = ("pg_solve", "pg_grid_create_dvr", "pg_potential_eval", "pg_hx", "pg_potential_scpol_add",
-             "pg_hf_gradient_grid", "pg_hf_gradient_final")
+             "pg_hf_gradient_grid", "pg_hf_gradient_final", "pg_dual_grid_potential")
     for call in calls:
         assert f" {call}" in undef, call
     needed = subprocess.run(["readelf", "-d", EXE], capture_output=True, text=True, check=True).stdout
