@@ -72,6 +72,9 @@ struct pg_davidson {
   // M r is the Ritz vector itself there, so the Olsen form is used instead
   bool pc_olsen = false;
   pg::DevBuf<int> pc_flag;
+  // set by the first block Gram-Schmidt pass when its Cholesky pivots show
+  // that no correction lost enough of its norm for the second pass to matter
+  pg::DevBuf<int> pip_skip;
   // counters for the solve statistics
   long n_iter = 0, n_restart = 0;
   double t_eig = 0, t_wait = 0;  // host seconds in the subspace eigensolver / waiting for the device
@@ -280,6 +283,7 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
   PG_TRY(d->dcoef.ensure((size_t)std::max(maxsub * maxsub, 2 * kMaxGramOut)));
   PG_TRY(d->dgram.ensure((size_t)kMaxGramOut));
   PG_TRY(d->rs.ensure());
+  PG_TRY(d->pip_skip.ensure(1));
   PG_TRY(d->hpin.ensure(kPinTotal));
   if (d->dfloat) {
     PG_TRY(d->bt.ensure((size_t)maxsub * ndim));
@@ -309,13 +313,26 @@ pg_status ensure_scratch(pg_davidson* d, int ndim, int maxsub, int nroots) {
 // subtraction cancels (R almost inside span(B)) the pass yields scaled
 // rounding noise, mostly orthogonal to B, which the second pass (no
 // cancellation left) projects and normalises.  One block; k <= 16, nb <= 128.
+//
+// skip_out (first pass): 1 when every squared pivot L_jj^2 keeps at least
+// kPipKeep of that correction's squared norm R_j^T R_j, else 0.  Pivot j is
+// what remains of R_j after removing span(B) and the corrections before it;
+// with ratios that large the pass's rounding leaves the block orthonormal to
+// about u / kPipKeep (u: the unit roundoff of the products, 2^-53 in FP64,
+// about 2^-48 in double-float), and the second pass, which would change the
+// vectors only by that much, is skipped.  skip_in (second pass): return at
+// once when set.
+constexpr double kPipKeep = 1e-3;
 __global__ void __launch_bounds__(256) k_pip_coef(const double* __restrict__ G, int nb, int k,
-                                                  double* __restrict__ coef) {
+                                                  double* __restrict__ coef, int* __restrict__ skip_out,
+                                                  const int* __restrict__ skip_in) {
   pdl_wait();
   pdl_release();
+  if (skip_in && *skip_in) return;
   __shared__ double Cs[128][kMaxCombine];
   __shared__ double L[kMaxCombine][kMaxCombine + 1];
   __shared__ double U[kMaxCombine][kMaxCombine + 1];
+  __shared__ int Keep[kMaxCombine];
   const int tid = threadIdx.x;
   for (int e = tid; e < nb * k; e += blockDim.x) Cs[e / k][e % k] = G[e];
   __syncthreads();
@@ -333,7 +350,9 @@ __global__ void __launch_bounds__(256) k_pip_coef(const double* __restrict__ G, 
         double s = L[j][j];
         for (int p = 0; p < j; ++p) s -= L[j][p] * L[j][p];
         const double floor = 1e-24 * G[(long)(nb + j) * k + j];
-        L[j][j] = sqrt(s > floor ? s : (floor > 1e-300 ? floor : 1e-300));
+        const double piv = s > floor ? s : (floor > 1e-300 ? floor : 1e-300);
+        L[j][j] = sqrt(piv);
+        Keep[j] = piv >= kPipKeep * G[(long)(nb + j) * k + j];
       }
       __syncwarp();
       if (lane > j && lane < k) {
@@ -342,6 +361,11 @@ __global__ void __launch_bounds__(256) k_pip_coef(const double* __restrict__ G, 
         L[lane][j] = t / L[j][j];
       }
       __syncwarp();
+    }
+    if (skip_out && lane == 0) {
+      int all = 1;
+      for (int j = 0; j < k; ++j) all &= Keep[j];
+      *skip_out = all;
     }
     if (lane < k) {  // U = L^-T, column c on lane c (upper triangular)
       const int c = lane;
@@ -493,12 +517,16 @@ pg_status block_orthonormalise(pg_davidson* d, long N, double* R, int k, double*
   double* Rt = Bt ? Bt + (long)nbas * N : nullptr;
   if (Bt) PG_TRY(split_twin(N * k, R, Rt, st, R != out ? out : nullptr));
   else if (R != out) PG_CUDA_TRY(cudaMemcpyAsync(out, R, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, st));
+  // the second pass runs only where the first one's pivots ask for it
+  // (k_pip_coef); the decision stays on the device
   for (int pass = 0; pass < 2; ++pass) {
-    PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat, Bt, Rt));
-    PG_CUDA_TRY(launch_dependent(k_pip_coef, dim3(1), dim3(256), 0, st, d->dgram.p, nbas, k, d->dcoef.p));
+    const int* skip = pass == 1 ? d->pip_skip.p : nullptr;
+    PG_TRY(gram(N, B, nbas + k, out, k, d->dgram.p, d->rs, st, d->dfloat, Bt, Rt, skip));
+    PG_CUDA_TRY(launch_dependent(k_pip_coef, dim3(1), dim3(256), 0, st, d->dgram.p, nbas, k, d->dcoef.p,
+                                 pass == 0 ? d->pip_skip.p : nullptr, skip));
     PG_TRY(check_launch("k_pip_coef"));
     PG_TRY(combine(N, B, nbas + k, d->dcoef.p, k, 1, 1.0, nullptr, nullptr, false, out, k, nullptr, d->rs, st,
-                   d->dfloat, Bt, Rt));
+                   d->dfloat, Bt, Rt, skip));
   }
   return PG_OK;
 }
@@ -934,7 +962,7 @@ double workspace_bytes(const SolveWorkspace* w) {
   const pg_davidson& d = w->d;
   const size_t doubles = w->B.n + w->Z.n + w->diag.n + w->work.n + d.rs.partial.n + d.dcoef.n + d.dsq.n +
                          d.dgram.n + d.bt.n + d.zt.n + d.pc_w1.n + d.pc_w2.n + d.pc_ru.n;
-  return 8.0 * (double)doubles + 4.0 * (double)(d.rs.counter.n + d.pc_flag.n);
+  return 8.0 * (double)doubles + 4.0 * (double)(d.rs.counter.n + d.pc_flag.n + d.pip_skip.n);
 }
 
 // The device eigensolve of pg_solve with the H*X product supplied by the

@@ -28,9 +28,11 @@ long chunk_for(long N, int blocks, int align) {
 // lanes stride over the rows, then a fixed shuffle tree.  inv_sqrt_out: also
 // store 1/sqrt(out[o]) at out[no + o] (used to normalise vectors on device).
 __global__ void __launch_bounds__(kT) k_reduce_partials(const double* __restrict__ partial, int nb, int no,
-                                                        double* __restrict__ out, int sqrt_mode) {
+                                                        double* __restrict__ out, int sqrt_mode,
+                                                        const int* __restrict__ skip) {
   pdl_wait();
   pdl_release();
+  if (skip && *skip) return;
   const int warp = (blockIdx.x * kT + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= no) return;
@@ -53,7 +55,9 @@ __global__ void __launch_bounds__(kT) k_reduce_partials(const double* __restrict
 }
 
 __global__ void __launch_bounds__(kT) k_gram(long N, long chunk, const double* __restrict__ P, int na,
-                                             const double* __restrict__ Q, int nb, double* __restrict__ partial) {
+                                             const double* __restrict__ Q, int nb, double* __restrict__ partial,
+                                             const int* __restrict__ skip) {
+  if (skip && *skip) return;
   extern __shared__ double sm[];
   double* Ps = sm;                       // na x (kTP+1)
   double* Qs = sm + na * (kTP + 1);      // nb x (kTP+1)
@@ -114,7 +118,9 @@ __global__ void __launch_bounds__(kT) k_combine(long N, long chunk, const double
                                                 const double* __restrict__ C, int ca, int cr, double cscale,
                                                 const double* X,
                                                 const double* __restrict__ alpha, int inv_sqrt, double* Y, int nr,
-                                                double* __restrict__ partial, double* sq_out, unsigned* counter) {
+                                                double* __restrict__ partial, double* sq_out, unsigned* counter,
+                                                const int* __restrict__ skip) {
+  if (skip && *skip) return;
   extern __shared__ double sm[];
   double* Cs = sm;                 // na x nr
   __shared__ double al[NR];
@@ -278,9 +284,10 @@ template <bool kPair>
 __global__ void __launch_bounds__(kT, 2) k_gram_df(long N, long chunk, const double* __restrict__ P, int na,
                                                    const double* __restrict__ Q, int nb, int tp, int m, int S,
                                                    int ablk, int nblk, int split_p, int split_q,
-                                                   double* __restrict__ partial) {
+                                                   double* __restrict__ partial, const int* __restrict__ skip) {
   pdl_wait();
   pdl_release();
+  if (skip && *skip) return;
   extern __shared__ __align__(16) unsigned char gsm[];
   const int rows = na + nb;
   const int hp = tp >> 1;  // point pairs per tile row
@@ -420,9 +427,10 @@ __global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long
                                                    const double* __restrict__ C, int ca, int cr, double cscale,
                                                    const double* X, const double* __restrict__ alpha, int inv_sqrt,
                                                    double* Y, int nr, float2* Yt, double* __restrict__ partial,
-                                                   double* sq_out, unsigned* counter) {
+                                                   double* sq_out, unsigned* counter, const int* __restrict__ skip) {
   pdl_wait();
   pdl_release();
+  if (skip && *skip) return;
   extern __shared__ float smf[];
   float* Ch = smf;              // na x nr
   float* Cl = smf + na * nr;
@@ -511,10 +519,11 @@ __global__ void __launch_bounds__(kT, NR <= 4 ? 4 : 2) k_combine_df(long N, long
 }
 
 // out[o] = sum of partial[b*no + o] over the nb rows, in a fixed order (k_reduce_partials)
-pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st) {
+pg_status reduce(const double* partial, int nb, int no, double* out, bool sqrt_mode, cudaStream_t st,
+                 const int* skip = nullptr) {
   const int blocks = (no * 32 + kT - 1) / kT;
   PG_CUDA_TRY(launch_dependent(k_reduce_partials, dim3(blocks), dim3(kT), 0, st, partial, nb, no, out,
-                               sqrt_mode ? 1 : 0));
+                               sqrt_mode ? 1 : 0, skip));
   return check_launch("k_reduce_partials");
 }
 
@@ -566,7 +575,7 @@ static pg_status opt_in_smem() {
 }
 
 pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs,
-               cudaStream_t st, bool dfloat, const double* Pt, const double* Qt) {
+               cudaStream_t st, bool dfloat, const double* Pt, const double* Qt, const int* skip) {
   PG_ARG(na > 0 && nb > 0 && na * nb <= kMaxGramOut && na + nb <= 144, "gram: %d x %d outputs exceed the limits",
          na, nb);
   PG_TRY(rs.ensure());
@@ -583,23 +592,23 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
     const int sp = Pt ? 1 : 0, sq = Qt ? 1 : 0;
     if (pair_ok(N, Ps, Qs))
       PG_CUDA_TRY(launch_dependent(k_gram_df<true>, dim3(dblocks), dim3(kT), gg.smem, st, N, dchunk, Ps, na, Qs, nb,
-                                   gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, sp, sq, rs.partial.p));
+                                   gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, sp, sq, rs.partial.p, skip));
     else
       PG_CUDA_TRY(launch_dependent(k_gram_df<false>, dim3(dblocks), dim3(kT), gg.smem, st, N, dchunk, Ps, na, Qs,
-                                   nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, sp, sq, rs.partial.p));
+                                   nb, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, sp, sq, rs.partial.p, skip));
     PG_TRY(check_launch("k_gram_df"));
-    return reduce(rs.partial.p, dblocks, na * nb, out, false, st);
+    return reduce(rs.partial.p, dblocks, na * nb, out, false, st, skip);
   } else {
     const size_t smem = sizeof(double) * (size_t)(na + nb) * (kTP + 1);
-    k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p);
+    k_gram<<<blocks, kT, smem, st>>>(N, chunk, P, na, Q, nb, rs.partial.p, skip);
     PG_TRY(check_launch("k_gram"));
   }
-  return reduce(rs.partial.p, blocks, na * nb, out, false, st);
+  return reduce(rs.partial.p, blocks, na * nb, out, false, st, skip);
 }
 
 pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
-                  cudaStream_t st, bool dfloat, const double* Pt, double* Yt) {
+                  cudaStream_t st, bool dfloat, const double* Pt, double* Yt, const int* skip) {
   PG_ARG(nr > 0 && nr <= kMaxCombine && na >= 0 && na * nr <= 128 * kMaxCombine, "combine: bad sizes na=%d nr=%d",
          na, nr);
   PG_TRY(rs.ensure());
@@ -611,7 +620,7 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
 #define PG_COMBINE_DF3(NRV, TI, TO)                                                                                \
   PG_CUDA_TRY(launch_dependent(k_combine_df<NRV, TI, TO>, dim3(blocks), dim3(kT), smem, st, N, chunk, Pt ? Pt : P, na, \
                                C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, reinterpret_cast<float2*>(Yt),  \
-                               sq ? rs.partial.p : nullptr, sq, rs.counter.p))
+                               sq ? rs.partial.p : nullptr, sq, rs.counter.p, skip))
 #define PG_COMBINE_DF(NRV)                                             \
   do {                                                                 \
     if (Pt && Yt) PG_COMBINE_DF3(NRV, true, true);                     \
@@ -631,7 +640,7 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
     const size_t smem = sizeof(double) * (size_t)(na > 0 ? na : 1) * nr;
 #define PG_COMBINE(NRV) \
   k_combine<NRV><<<blocks, kT, smem, st>>>(N, chunk, P, na, C, ca, cr, cscale, X, alpha, inv_sqrt ? 1 : 0, Y, nr, \
-                                           sq ? rs.partial.p : nullptr, sq, rs.counter.p)
+                                           sq ? rs.partial.p : nullptr, sq, rs.counter.p, skip)
     if (nr <= 1) PG_COMBINE(1);
     else if (nr <= 2) PG_COMBINE(2);
     else if (nr <= 4) PG_COMBINE(4);
@@ -766,17 +775,17 @@ extern "C" pg_status pg_block_gram_noalloc(long n, const double* P, int np, cons
     const int blocks = (int)((n + chunk - 1) / chunk);
     if (pair_ok(n, P, Q))
       k_gram_df<true><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, 0,
-                                                    0, partial);
+                                                    0, partial, nullptr);
     else
       k_gram_df<false><<<blocks, kT, gg.smem, st>>>(n, chunk, P, np, Q, nq, gg.tp, gg.m, gg.S, gg.ablk, gg.nblk, 0,
-                                                     0, partial);
+                                                     0, partial, nullptr);
     PG_TRY(check_launch("k_gram_df"));
     return reduce(partial, blocks, no, out, false, st);
   }
   const long chunk = chunk_for(n, pg::kRedBlocks, kTP);
   const int blocks = (int)((n + chunk - 1) / chunk);
   const size_t smem = sizeof(double) * (size_t)(np + nq) * (kTP + 1);
-  k_gram<<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, partial);
+  k_gram<<<blocks, kT, smem, st>>>(n, chunk, P, np, Q, nq, partial, nullptr);
   PG_TRY(check_launch("k_gram"));
   return reduce(partial, blocks, no, out, false, st);
 }

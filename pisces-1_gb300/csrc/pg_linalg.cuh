@@ -67,8 +67,12 @@ __device__ __forceinline__ void reduce_in_last_block(const double* partial, int 
 // Pt / Qt (dfloat only, optional): double-float twins of P / Q, one float2
 // (hi, lo) per point as written by split_twin or a combine's Yt, read instead
 // of converting P / Q again.
+// skip (optional, device): when *skip is nonzero at the time the launches
+// run, they return at once and out is left as it was (a decision taken by an
+// earlier kernel on the same stream, without a device-to-host read).
 pg_status gram(long N, const double* P, int na, const double* Q, int nb, double* out, RedScratch& rs, cudaStream_t st,
-               bool dfloat = false, const double* Pt = nullptr, const double* Qt = nullptr);
+               bool dfloat = false, const double* Pt = nullptr, const double* Qt = nullptr,
+               const int* skip = nullptr);
 
 // Y[r*N + g] = alpha_r * X[r*N + g] + cscale * sum_a P[a*N + g] * C[a*ca + r*cr]   (r < nr <= kMaxCombine)
 // alpha_r: 0 if alpha is null; alpha[r] if inv_sqrt is false; 1/sqrt(alpha[r]) if true.
@@ -76,9 +80,11 @@ pg_status gram(long N, const double* P, int na, const double* Q, int nb, double*
 // not null, sq[r] = |Y_r|^2 and sq[nr + r] = 1/|Y_r|.
 // Pt (dfloat only, optional): twin of P, read instead of P; Yt (dfloat only,
 // optional): receives the twin of Y.  Pt and Yt may overlap as P and Y may.
+// skip: as for gram (Y, Yt and sq are left as they were).
 pg_status combine(long N, const double* P, int na, const double* C, int ca, int cr, double cscale, const double* X,
                   const double* alpha, bool inv_sqrt, double* Y, int nr, double* sq, RedScratch& rs,
-                  cudaStream_t st, bool dfloat = false, const double* Pt = nullptr, double* Yt = nullptr);
+                  cudaStream_t st, bool dfloat = false, const double* Pt = nullptr, double* Yt = nullptr,
+                  const int* skip = nullptr);
 
 // t[i] = double-float twin of x[i] (float2 (hi, lo) in the 8 bytes of t[i]);
 // with copy (not overlapping x), also copy[i] = x[i] in the same pass.
