@@ -31,6 +31,13 @@
 // part retires about two FMAs per SM per clock, so the epilogues use two
 // FP64 instructions per point (one conversion, one multiply-add), not five.
 //
+// Staged fill (where shared memory has room, n <= 64 per axis): the raw
+// FP64 rows of the next work item are bulk-copied (cp.async.bulk, one row per
+// copy, rows padded so that the producers' shared-memory reads are free of
+// bank conflicts) into a staging buffer while the current item is converted
+// and multiplied; the producers then convert from shared memory instead of
+// waiting on global loads in register batches.
+//
 // Shared memory (no-swizzle K-major core matrices, as pg_hx_tc.cu): the
 // kinetic matrices (resident; one image when the axes share one matrix),
 // the plane in both orientations, and the z tile (over the plane images).
@@ -140,6 +147,10 @@ struct FusedGeom {
   uint32_t tx_hi, tx_lo, ty_hi, ty_lo, tz_hi, tz_lo;  // byte offsets in dynamic shared memory
   uint32_t pn_hi, pn_lo, pt_hi, pt_lo, z_hi, z_lo;
   uint32_t acc_cols;  // TMEM columns per accumulator
+  int staged;         // 1: raw rows of the next item are bulk-copied into the staging buffer
+  uint32_t stg;       // byte offset of the staging buffer
+  uint32_t stg_pxy;   // its row pitch for a plane (bytes; row j holds X[0..nx) of grid line j)
+  uint32_t stg_pz;    // its row pitch for a z tile (bytes; row k holds the tile's points of plane k)
 };
 
 constexpr int kMaxConst = 6;
@@ -231,9 +242,9 @@ constexpr int kRing = 8;  // tickets in flight in one CTA: at most five (fill ..
 // without a division.  The loads of the first round are issued before
 // ready() returns (ready waits until the images are free), so their latency
 // overlaps that wait.
-template <class Ready>
-__device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __restrict__ P, unsigned char* smem,
-                                           int pw, int lane, Ready&& ready) {
+template <class Src, class Ready>
+__device__ __forceinline__ void fill_plane(const FusedGeom& G, Src&& P, unsigned char* smem, int pw, int lane,
+                                           Ready&& ready) {
   const int kq = G.kx >> 2;
   const int ncm = (G.npy >> 3) * kq;
   const int kyq32 = (G.ky >> 2) * 32;
@@ -252,7 +263,7 @@ __device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __r
 #pragma unroll
     for (int b = 0; b < kBatch; ++b) {
       const int j = 8 * gj + lj, i = 4 * qi + li;
-      xv[b] = (c0 + kProdWarps * b < ncm && j < G.ny && i < G.nx) ? P[i + (long)G.nx * j] : 0.0;
+      xv[b] = (c0 + kProdWarps * b < ncm && j < G.ny && i < G.nx) ? P(i, j) : 0.0;
       qi += kProdWarps;
       while (qi >= kq) qi -= kq, ++gj;
     }
@@ -282,9 +293,9 @@ __device__ __forceinline__ void fill_plane(const FusedGeom& G, const double* __r
 // z item: grid points p0 .. p0 + 127 of every plane (rows), K = z index
 // (cm = g * kz/4 + q).  Lane L takes row 8 g + L/4 and K 4 q + L%4: a warp
 // load reads four runs of eight consecutive points.
-template <class Ready>
-__device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __restrict__ X, long p0, long nxny,
-                                           unsigned char* smem, int pw, int lane, Ready&& ready) {
+template <class Src, class Ready>
+__device__ __forceinline__ void fill_ztile(const FusedGeom& G, Src&& X, long p0, long nxny, unsigned char* smem,
+                                           int pw, int lane, Ready&& ready) {
   const int kq = G.kz >> 2;
   const int ncm = (kTile / 8) * kq;
   const int lj = lane >> 2, li = lane & 3;
@@ -299,7 +310,7 @@ __device__ __forceinline__ void fill_ztile(const FusedGeom& G, const double* __r
     for (int b = 0; b < kBatch; ++b) {
       const long p = p0 + 8 * g + lj;
       const int k = 4 * q + li;
-      xv[b] = (c0 + kProdWarps * b < ncm && p < nxny && k < G.nz) ? X[p + nxny * k] : 0.0;
+      xv[b] = (c0 + kProdWarps * b < ncm && p < nxny && k < G.nz) ? X(p - p0, k) : 0.0;
       q += kProdWarps;
       while (q >= kq) q -= kq, ++g;
     }
@@ -332,6 +343,51 @@ __device__ __forceinline__ void prefetch_item(const FusedGeom& G, const FusedJob
     const long np = std::min((long)kTile, nxny - p0);
     for (int k = 0; k < G.nz; ++k) prefetch_l2(x + p0 + nxny * k, np * 8);
   }
+}
+
+// The lanes of one warp: bulk-copy the raw rows of an item into the staging
+// buffer, completing on mbarrier bar (lane 0 sets the byte count first).
+// Rows: a plane's ny grid lines (nx doubles each), or a z tile's nz planes
+// (up to 128 points each).  Every address and size is a multiple of 16
+// bytes (the launch checks nx even and X 16-byte aligned).
+__device__ __forceinline__ void stage_item(const FusedGeom& G, const FusedJobs& J, const Item& it, long N, long nxny,
+                                           unsigned char* smem, uint32_t bar, int lane) {
+  if (it.kind < 0) return;
+  const double *x, *v;
+  double* y;
+  vec_ptrs(J, it.u, N, x, y, v);
+  int rows;
+  uint32_t row_bytes, pitch;
+  const double* src;
+  long src_stride;
+  if (it.kind == 0) {
+    rows = G.ny;
+    row_bytes = (uint32_t)G.nx * 8u;
+    pitch = G.stg_pxy;
+    src = x + nxny * it.idx;
+    src_stride = G.nx;
+  } else {
+    const long p0 = (long)it.idx * kTile;
+    rows = G.nz;
+    row_bytes = (uint32_t)std::min((long)kTile, nxny - p0) * 8u;
+    pitch = G.stg_pz;
+    src = x + p0;
+    src_stride = nxny;
+  }
+  if (lane == 0) {
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(bar), "r"((uint32_t)rows * row_bytes)
+                 : "memory");
+  }
+  __syncwarp();
+  const uint32_t dst0 = smem_u32(smem + G.stg);
+  for (int r = lane; r < rows; r += 32)
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     dst0 + (uint32_t)r * pitch),
+                 "l"(src + src_stride * r), "r"(row_bytes), "r"(bar)
+                 : "memory");
 }
 
 __device__ __forceinline__ void named_sync(int id, int nthreads) {
@@ -382,10 +438,10 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     k_hx_fused(const __grid_constant__ FusedGeom G, const __grid_constant__ FusedConst C,
                const __grid_constant__ FusedJobs J, FusedCounters* __restrict__ cnt, int* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  __shared__ __align__(8) uint64_t mbar_t, mbar_full, mbar_empty, mbar_acc_full[2], mbar_acc_empty[2];
+  __shared__ __align__(8) uint64_t mbar_t, mbar_full, mbar_empty, mbar_acc_full[2], mbar_acc_empty[2], mbar_stg;
   __shared__ uint32_t tmem_base;
   __shared__ unsigned ring[kRing];
-  __shared__ int s_abort, s_prod_ok, s_epi_ok, s_last;
+  __shared__ int s_abort, s_prod_ok, s_epi_ok, s_last, s_stg_issued;
   volatile int* abort = &s_abort;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long nxny = (long)G.nx * G.ny;
@@ -397,6 +453,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_t)));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar_full)), "r"(kProdWarps * 32));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_empty)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_stg)));
+    s_stg_issued = 0;
     for (int b = 0; b < 2; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(smem_u32(&mbar_acc_full[b])));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_acc_empty[b])));
@@ -433,6 +491,12 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
   if (warp < kProdWarps) {
     // ------------------------------------------------------------ producers
     const int ptid = tid;  // 0 .. 32 kProdWarps - 1
+    const uint32_t bar_stg = smem_u32(&mbar_stg);
+    if (G.staged && warp == 0) {
+      const Item it0 = decode(ring[0], nvec, G.nz, G.nzt, G.lag);
+      stage_item(G, J, it0, N, nxny, smem, bar_stg, lane);
+      if (lane == 0 && it0.kind >= 0) s_stg_issued = 1;
+    }
     for (int i = 0;; ++i) {
       // ring[i] was written before the previous item's barrier; the leader
       // takes the ticket after it now, so its X data is in L2 by its turn
@@ -440,7 +504,17 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (ptid == 0) {
         const unsigned t1 = atomicAdd(&cnt->ticket, 1u);
         ring[(i + 1) % kRing] = t1;
-        prefetch_item(G, J, decode(t1, nvec, G.nz, G.nzt, G.lag), N, nxny);
+        if (!G.staged) prefetch_item(G, J, decode(t1, nvec, G.nz, G.nzt, G.lag), N, nxny);
+      }
+      if (G.staged && it.kind >= 0) {
+        // this item's rows are in the staging buffer once its copies land
+        if (ptid == 0) {
+          const int ok = mbar_wait_or_abort(bar_stg, (uint32_t)(i & 1), abort);
+          if (!ok) *abort = 1;
+          s_prod_ok = ok;
+        }
+        named_sync(1, kProdWarps * 32);
+        if (!s_prod_ok) break;
       }
       // the images are free once the previous item's MMAs are done
       auto ready = [&]() {
@@ -454,14 +528,36 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       const double *x, *v;
       double* y;
       if (it.kind >= 0) vec_ptrs(J, it.u, N, x, y, v);
-      if (it.kind == 0)
-        fill_plane(G, x + nxny * it.idx, smem, warp, lane, ready);
-      else if (it.kind == 1)
-        fill_ztile(G, x, (long)it.idx * kTile, nxny, smem, warp, lane, ready);
-      else
+      const unsigned char* stg = smem + G.stg;
+      if (it.kind == 0) {
+        const double* P = x + nxny * it.idx;
+        if (G.staged)
+          fill_plane(G, [&](int i, int j) { return *reinterpret_cast<const double*>(stg + j * G.stg_pxy + i * 8); },
+                     smem, warp, lane, ready);
+        else
+          fill_plane(G, [&](int i, int j) { return P[i + (long)G.nx * j]; }, smem, warp, lane, ready);
+      } else if (it.kind == 1) {
+        const long p0 = (long)it.idx * kTile;
+        if (G.staged)
+          fill_ztile(G, [&](long q, int k) { return *reinterpret_cast<const double*>(stg + k * G.stg_pz + q * 8); },
+                     p0, nxny, smem, warp, lane, ready);
+        else
+          fill_ztile(G, [&](long q, int k) { return x[p0 + q + nxny * k]; }, p0, nxny, smem, warp, lane, ready);
+      } else {
         ready();
+      }
       if (!s_prod_ok) break;
       if (it.kind >= 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (G.staged && it.kind >= 0) {
+        // every producer has read the staging buffer (and fenced those reads
+        // against the async proxy): the next item's copies may overwrite it
+        named_sync(1, kProdWarps * 32);
+        if (warp == 0) {
+          const Item nx_it = decode(ring[(i + 1) % kRing], nvec, G.nz, G.nzt, G.lag);
+          stage_item(G, J, nx_it, N, nxny, smem, bar_stg, lane);
+          if (lane == 0 && nx_it.kind >= 0) s_stg_issued = i + 2;
+        }
+      }
       mbar_arrive(smem_u32(&mbar_full));
       if (it.kind < 0) break;
     }
@@ -626,6 +722,10 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // a staging copy issued for an item that an aborted loop never consumed
+  // lands before the CTA leaves (bounded wait; s_stg_issued = last item + 1)
+  if (tid == 0 && G.staged && s_abort && s_stg_issued > 0)
+    mbar_wait(smem_u32(&mbar_stg), (uint32_t)((s_stg_issued - 1) & 1));
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * G.acc_cols));
   if (tid == 0) {
     if (s_abort) atomicExch(err, 1);
@@ -777,6 +877,21 @@ FusedPlan plan_fused(const pg_grid* g) {
   total = std::max(total, G.pt_lo + (uint32_t)kTile * G.ky * 4);
   P.smem = total;
   if ((long)P.smem > (long)g_fused_max_dyn) return no("operand images exceed shared memory");
+  // staging buffer for the next item's raw rows, where it fits (row pitches:
+  // a multiple of 16 bytes, 32 resp. 64 bytes past a multiple of 128, so
+  // that the producers' reads of eight rows resp. four rows take the minimum
+  // number of shared-memory wavefronts)
+  G.staged = 0;
+  if (nx % 2 == 0) {
+    G.stg_pxy = (uint32_t)((nx * 8 + 127) / 128 * 128 + 32);
+    G.stg_pz = (uint32_t)(kTile * 8 + 64);
+    G.stg = (total + 127u) / 128u * 128u;
+    const size_t with = (size_t)G.stg + std::max((size_t)ny * G.stg_pxy, (size_t)nz * G.stg_pz);
+    if ((long)with <= (long)g_fused_max_dyn) {
+      G.staged = 1;
+      P.smem = with;
+    }
+  }
   uint32_t cols = 32;
   while (cols < (uint32_t)std::max(G.npy, G.npz)) cols <<= 1;
   G.acc_cols = cols;
@@ -825,6 +940,11 @@ pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* 
     return PG_UNSUPPORTED;
   }
   if (hp.lag > 0) P.G.lag = hp.lag;
+  // bulk copies need 16-byte aligned rows: every block of X must start on a
+  // 16-byte boundary (nx even makes every row and tile offset a multiple)
+  for (int j = 0; j < njobs; ++j)
+    if (nvec[j] > 0 && ((uintptr_t)x[j] & 15u) != 0) P.G.staged = 0;
+  if (g->N % 2 != 0) P.G.staged = 0;
   FusedCounters* cnt = nullptr;
   PG_TRY(fused_counters(g, st, &cnt));
   FusedJobs J;
@@ -900,8 +1020,10 @@ void hx_plan_text(const pg_grid* g, int nvec, char* buf, int len) {
   if (p.kind == 2 && P.ok)
     snprintf(buf, (size_t)len,
              "fused (k_hx_fused): xy planes %dx%d + z tiles of 128 lines (%d per vector, lag %d vectors), "
-             "K %d/%d/%d, %zu B shared memory, %d constant images, %u TMEM columns x 2, %d CTAs",
-             P.G.nx, P.G.ny, P.G.nzt, p.lag, P.G.kx, P.G.ky, P.G.kz, P.smem, P.C.n / 2, P.G.acc_cols,
+             "K %d/%d/%d, %s, %zu B shared memory, %d constant images, %u TMEM columns x 2, %d CTAs",
+             P.G.nx, P.G.ny, P.G.nzt, p.lag, P.G.kx, P.G.ky, P.G.kz,
+             P.G.staged ? "rows bulk-copied to a staging buffer" : "rows loaded from L2", P.smem, P.C.n / 2,
+             P.G.acc_cols,
              p.ctas > 0 && p.ctas < g_fused_sms ? p.ctas : g_fused_sms);
   else
     snprintf(buf, (size_t)len, "three axis passes (k_hx_tc): %s form, %d CTAs%s%s",
