@@ -290,8 +290,14 @@ pg_status pg_grid_check(const pg_grid* g, void* stream);
  * x and y contractions of each grid plane in one tensor-memory tile, the z
  * contraction of 128-line tiles, one persistent launch; PG_UNSUPPORTED where
  * the grid does not fit it: more than 128 points along x, an axis above 112
- * points, or operand images beyond shared memory).  Both give the same
- * products to the mixed form's accuracy.  No reference counterpart (the
+ * points, or operand images beyond shared memory), 3 = the same work items
+ * with an FP16 split of the operands scaled by a power of two per item (one
+ * plane image read K-major by the x contraction and MN-major by the y
+ * contraction, the next item's rows bulk-copied into shared memory; grids of
+ * at most 96 points per axis whose axes share one kinetic matrix, nx even;
+ * an X block not 16-byte aligned falls back to kind 2).  Automatic selection
+ * prefers 3, then 2.  All give the same products to the mixed form's
+ * accuracy.  No reference counterpart (the
  * reference multiplies line by line, src/mtx.cpp:61-104). */
 pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind);
 /* Launch parameters of the mixed-form H*X on this grid, overriding the tuned

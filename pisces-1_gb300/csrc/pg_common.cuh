@@ -161,6 +161,12 @@ struct HostPinned {
 inline __host__ __device__ unsigned tc_kmajor_off(int r, int k, int kpad) {
   return (unsigned)(((r >> 3) * (kpad >> 2) + (k >> 2)) * 128 + (r & 7) * 16 + (k & 3) * 4);
 }
+// The same for FP16 operands: core matrices of 8 rows x 8 values (16
+// bytes), K padded to 16 (one MMA K step).
+inline __host__ __device__ unsigned tc16_kmajor_off(int r, int k, int kpad16) {
+  return (unsigned)(((r >> 3) * (kpad16 >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+inline __host__ __device__ int tc16_kpad(int n) { return (n + 15) / 16 * 16; }
 inline __host__ __device__ int tc_npad(int n) { return (n + 15) / 16 * 16; }
 inline __host__ __device__ int tc_kpad(int n) { return (n + 7) / 8 * 8; }
 // K chunk of the tensor-core contraction: the B chunk (npad x kc) and the A
@@ -191,6 +197,12 @@ struct pg_grid {
   // image per K chunk)
   pg::DevBuf<float> t_hi[3];
   pg::DevBuf<float> t_lo[3];
+  // FP16 high part and remainder of T * 2^t16_scale (one power of two for
+  // all axes, chosen so that the largest entry lies in [2^14, 2^15)), as
+  // tc16_kmajor_off images (rows padded to 16, K to 16); built for n <= 128
+  pg::DevBuf<unsigned short> t16_hi[3];
+  pg::DevBuf<unsigned short> t16_lo[3];
+  int t16_scale = 0;
   pg::DevBuf<double> x_dev[3];     // grid points on the device
   pg::DevBuf<int> tc_err;          // set by the tensor-core H*X kernels if a completion wait times out
   // eigenbasis of the kinetic matrices (the orthonormal DST-I, symmetric),

@@ -1,5 +1,6 @@
 // Grid handle, kinetic builders (sine DVR; periodic FFT kinetic), diag(H)
 // and the particle-in-a-box start vector.
+#include <cuda_fp16.h>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -116,6 +117,40 @@ std::vector<float> tc_image(const std::vector<float>& M, int n) {
   return img;
 }
 
+// FP16 hi/lo images of the kinetic matrices of a grid (all axes <= 128
+// points), T scaled by one power of two 2^tau so that max |T| * 2^tau lies in
+// [2^14, 2^15): hi = fp16(T 2^tau), lo = fp16(T 2^tau - hi), each rounded to
+// nearest, about 22 significant bits together.
+pg_status build_t16(pg_grid* g) {
+  for (int a = 0; a < 3; ++a)
+    if (g->n[a] > 128) return PG_OK;
+  double tmax = 0.0;
+  for (int a = 0; a < 3; ++a)
+    for (double v : g->t[a]) tmax = std::max(tmax, std::fabs(v));
+  int e = 0;
+  if (tmax > 0.0) std::frexp(tmax, &e);  // tmax = m 2^e, m in [0.5, 1)
+  const int tau = tmax > 0.0 ? 15 - e : 0;
+  g->t16_scale = tau;
+  for (int a = 0; a < 3; ++a) {
+    const int m = g->n[a], npad = pg::tc_npad(m), kpad = pg::tc16_kpad(m);
+    std::vector<unsigned short> hi((size_t)npad * kpad, 0), lo((size_t)npad * kpad, 0);
+    for (int r = 0; r < m; ++r)
+      for (int k = 0; k < m; ++k) {
+        const double v = std::ldexp(g->t[a][(size_t)r * m + k], tau);
+        const __half h = __float2half_rn((float)v);
+        const __half l = __float2half_rn((float)(v - (double)__half2float(h)));
+        const size_t o = pg::tc16_kmajor_off(r, k, kpad) / 2;
+        hi[o] = __half_as_ushort(h);
+        lo[o] = __half_as_ushort(l);
+      }
+    PG_TRY(g->t16_hi[a].alloc(hi.size()));
+    PG_TRY(g->t16_lo[a].alloc(lo.size()));
+    PG_CUDA_TRY(cudaMemcpy(g->t16_hi[a].p, hi.data(), sizeof(unsigned short) * hi.size(), cudaMemcpyHostToDevice));
+    PG_CUDA_TRY(cudaMemcpy(g->t16_lo[a].p, lo.data(), sizeof(unsigned short) * lo.size(), cudaMemcpyHostToDevice));
+  }
+  return PG_OK;
+}
+
 float to_tf32(float f) {
   unsigned u;
   memcpy(&u, &f, 4);
@@ -225,6 +260,13 @@ extern "C" pg_status pg_grid_create_dvr(const int n[3], const double L[3], int d
       pg::set_error("pg_grid_create: upload failed: %s", cudaGetErrorString(cudaGetLastError()));
       delete g;
       return PG_CUDA;
+    }
+  }
+  {
+    const pg_status s16 = build_t16(g);
+    if (s16 != PG_OK) {
+      delete g;
+      return s16;
     }
   }
   // Eigenbasis of the kinetic matrix of each axis, T = Q diag(d) Q^T, for the

@@ -1,0 +1,979 @@
+// Y = H X, mixed form with an FP16 split: one persistent tensor-core kernel
+// with the work items of the fused kernel (pg_hx_fused.cu: the x and y
+// contractions of one grid plane into one TMEM tile; the z contraction of 128
+// grid lines; a ticket queue that keeps each vector's X and partial sums in
+// L2 between the two), for grids of at most 96 points per axis whose axes
+// share one kinetic matrix.
+//
+// H = V + Tx (+) Ty (+) Tz on the x-fastest grid (src/mtx.cpp:22-109).
+//
+// Operands.  Each item's raw FP64 values are copied by the tensor memory
+// accelerator into a staging buffer while the item before it is converted
+// and multiplied: boxes 16 values (128 bytes) wide with the 128-byte swizzle
+// (16-byte chunk c of box row r lands at chunk c ^ (r mod 8)), six to eight
+// copies per item; the producers read eight consecutive rows at a time, so
+// the swizzle puts their reads in distinct banks.  The
+// producer warps convert them to an FP16 high part and remainder scaled by a
+// power of two 2^s per item (the largest |x| of the item lands in
+// [2^14, 2^15): s from the largest FP64 exponent), so that hi + lo holds
+// about 22 significant bits, the precision of the TF32 split of the other
+// kernels.  The kinetic matrices are kept as FP16 images of T 2^tau
+// (pg_grid.t16_*).  D = Ah Bh + Ah Bl + Al Bh accumulates in FP32 in TMEM and
+// the epilogue multiplies by 2^-(s + tau), exactly.
+//
+// One plane image serves both contractions of an xy item: stored with rows
+// j and K = i (8 x 8 FP16 core matrices, no swizzle), it is the K-major B
+// operand of the x contraction (A = Tx, K = i) and the MN-major A operand of
+// the y contraction (M = i, K = j; B = Ty).  The z tile's image holds 8
+// planes x 8 points per core matrix: the MN-major A operand of the z
+// contraction (M = point, K = plane; B = Tz).  So each value is converted
+// once and stored as one 16-byte row of a core matrix, from 64 contiguous
+// staging bytes.
+//
+// Epilogues as the fused kernel: the x + y sums go, as FP32, to the low word
+// of each point's Y slot; the z epilogue writes Y = fma(V, X, W + Kz), with
+// V X in FP64 (one FP64 operation per point: W + Kz is converted with
+// integer operations).
+//
+// Every wait is bounded; a timeout sets the grid's error word (pg_hx reports
+// PG_DEVICE_TIMEOUT) and the kernel drains its copies and MMAs and returns.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <mutex>
+
+#include "pg_solve.cuh"
+
+namespace {
+
+constexpr int kTile = 128;  // MMA M: TMEM lanes, z-tile points
+constexpr int kMaxJobs = 8;  // jobs of one launch (each carries two tensor maps); more go to further launches
+constexpr int kProdWarps = 7;
+constexpr int kEpiWarps = 8;
+constexpr int kIssueWarp = kProdWarps + kEpiWarps;
+constexpr int kThreadsAll = (kIssueWarp + 1) * 32;
+constexpr int kRing = 8;  // tickets in flight in one CTA
+constexpr int kF16MaxVec = 1024;
+constexpr uint32_t kOverread = 2048;
+constexpr int kMaxAcc = 4;  // bytes past a plane image the y contraction's 128-row A read may touch
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t phase) {
+  uint32_t ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok)
+               : "r"(bar), "r"(phase)
+               : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  for (long it = 0; it < (1L << 26); ++it)
+    if (mbar_try(bar, phase)) return true;
+  return false;
+}
+
+// Bounded wait that also gives up once another role has raised the abort flag.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t phase, volatile int* abort) {
+  for (long it = 0; it < (1L << 26); ++it) {
+    if (mbar_try(bar, phase)) return true;
+    if (*abort) return false;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+__device__ __forceinline__ void mma_f16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+               " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d),
+               "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float* out) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; ++j) out[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* out) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) out[j] = __uint_as_float(r[j]);
+}
+
+// 2^e as FP32 for -126 <= e <= 127.
+__device__ __forceinline__ float exp2i(int e) {
+  e = e < -126 ? -126 : (e > 127 ? 127 : e);
+  return __uint_as_float((uint32_t)(e + 127) << 23);
+}
+
+// FP64 x 2^s -> FP32 with 32-bit integer operations (the mantissa
+// truncated to 23 bits, 2^-24 relative); sb = s - 896 (the exponent rebias).
+// Below 2^-126 gives a signed zero; Inf and NaN stay non-finite (the scale
+// keeps finite values below 2^15).
+__device__ __forceinline__ float f64_scaled_to_f32(double x, int sb) {
+  const uint32_t h = (uint32_t)__double2hiint(x), l = (uint32_t)__double2loint(x);
+  const uint32_t e = (h >> 20) & 0x7ffu;
+  const uint32_t man = __funnelshift_l(l, h, 3) & 0x7fffffu;
+  const int ef = (int)e + sb;
+  uint32_t f = (h & 0x80000000u) | ((uint32_t)ef << 23) | man;
+  f = ef > 0 ? f : (h & 0x80000000u);
+  f = e == 0x7ffu ? ((h & 0x80000000u) | 0x7f800000u | (man | l ? 0x400000u : 0u)) : f;
+  return __uint_as_float(f);
+}
+
+// FP32 -> FP64 with integer operations: exact for normal numbers and zero;
+// FP32 subnormals flush to a signed zero; Inf and NaN are kept.  (The FP64
+// pipe of this part retires about two operations per SM per clock, so the z
+// epilogue keeps one FP64 operation per point, the multiply-add.)
+__device__ __forceinline__ double f32_to_f64(float v) {
+  const uint32_t u = __float_as_uint(v);
+  const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  uint32_t hi = sign | ((e + 896u) << 20) | (m >> 3);
+  uint32_t lo = m << 29;
+  hi = e == 0 ? sign : hi;
+  lo = e == 0 ? 0u : lo;
+  hi = e == 255 ? (sign | 0x7ff00000u | (m >> 3) | (m ? 0x80000u : 0u)) : hi;
+  lo = e == 255 ? 0u : lo;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// Eight FP64 values (scaled by 2^s, sb = s - 896) -> eight FP16 high parts
+// and eight FP16 remainders, as two 16-byte rows.
+__device__ __forceinline__ void split8(const double* v, int sb, uint4& hi, uint4& lo) {
+  uint32_t h[4], l[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const float a = f64_scaled_to_f32(v[2 * q], sb), b = f64_scaled_to_f32(v[2 * q + 1], sb);
+    const __half2 hh = __floats2half2_rn(a, b);
+    const float2 hf = __half22float2(hh);
+    const __half2 ll = __floats2half2_rn(a - hf.x, b - hf.y);
+    h[q] = *reinterpret_cast<const uint32_t*>(&hh);
+    l[q] = *reinterpret_cast<const uint32_t*>(&ll);
+  }
+  hi = make_uint4(h[0], h[1], h[2], h[3]);
+  lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+}  // namespace
+
+namespace pg {
+
+struct F16Job {
+  CUtensorMap txy;  // X of the job as (x, y, plane of all its vectors), boxes 16 x ny x 1
+  CUtensorMap tz;   // X of the job as (plane point, plane of all its vectors), boxes 16 x nz
+  const double* x;
+  double* y;
+  const double* v;
+  int nvec;
+  int vec0;
+};
+struct F16Jobs {
+  F16Job j[kMaxJobs];
+  int n;
+  int nvec;
+};
+
+struct F16Geom {
+  int nx, ny, nz;
+  int kx, ky, kz;     // K extents padded to 16
+  int npy, npz;       // MMA N extents padded to 16
+  int nzt;            // z items per vector
+  int lag;            // vectors between a vector's xy items and its z items
+  int tau;            // the kinetic images hold T 2^tau
+  uint32_t t_hi, t_lo;            // the kinetic image (shared by the three axes)
+  uint32_t t_bytes;               // bytes of one kinetic image as copied
+  uint32_t op_hi, op_lo;          // operand images of the current item
+  uint32_t stg;                   // staging buffer (1024-byte aligned)
+  uint32_t reg_xy, reg_z;         // bytes of one 16-value-wide box region: 128 ny, 128 nz (rounded to 1024)
+  uint32_t acc_cols;              // TMEM columns per accumulator
+  int acc_shift;                  // log2 of the accumulators (2 or 4) the epilogue may lag behind by
+};
+
+struct F16Counters {
+  unsigned ticket;
+  unsigned finished;
+  unsigned done[kF16MaxVec];  // finished xy items per vector
+};
+
+}  // namespace pg
+
+namespace {
+
+using pg::F16Counters;
+using pg::F16Geom;
+using pg::F16Jobs;
+
+struct Item {
+  int kind;  // 0: xy plane, 1: z tile, -1: none
+  int u;     // vector in the launch's list
+  int idx;   // plane k or z tile t
+};
+
+// Ticket -> work item, as the fused kernel: XY(0) .. XY(L-1), then XY(s),
+// Z(s-L) for s = L .. b-1, then the remaining Z blocks.
+__device__ __forceinline__ Item decode(unsigned t, int nvec, int nz, int nzt, int lag) {
+  const unsigned ps = (unsigned)(nz + nzt);
+  if (t >= (unsigned)nvec * ps) return Item{-1, 0, 0};
+  const int L = lag < nvec ? lag : nvec;
+  const unsigned head = (unsigned)L * nz;
+  if (t < head) return Item{0, (int)(t / nz), (int)(t % nz)};
+  unsigned r = t - head;
+  const unsigned mid = (unsigned)(nvec - L) * ps;
+  if (r < mid) {
+    const unsigned s = r / ps, w = r - s * ps;
+    if (w < (unsigned)nz) return Item{0, L + (int)s, (int)w};
+    return Item{1, (int)s, (int)(w - nz)};
+  }
+  r -= mid;
+  return Item{1, nvec - L + (int)(r / nzt), (int)(r % nzt)};
+}
+
+__device__ __forceinline__ int job_of(const F16Jobs& J, int u) {
+  int j = 0;
+  while (j + 1 < J.n && u >= J.j[j + 1].vec0) ++j;
+  return j;
+}
+
+__device__ __forceinline__ void vec_ptrs(const F16Jobs& J, int u, long N, const double*& x, double*& y,
+                                         const double*& v) {
+  const int j = job_of(J, u);
+  const long off = (long)(u - J.j[j].vec0) * N;
+  x = J.j[j].x + off;
+  y = J.j[j].y + off;
+  v = J.j[j].v;
+}
+
+// One thread: the tensor copies of an item into the staging buffer,
+// completing on mbarrier bar.  An xy item: ceil(nx / 16) boxes of 16 x ny
+// values (plane idx of its vector), one region each; a z item: eight boxes
+// of 16 points x nz planes.  Values past the grid (the last box of a row,
+// the last tile) arrive as zeros; every box counts in full.  x coordinates
+// are multiples of 16 values.
+__device__ __forceinline__ void stage_item(const F16Geom& G, const F16Jobs& J, const Item& it, long nxny,
+                                           unsigned char* smem, uint32_t bar) {
+  if (it.kind < 0) return;
+  const int jb = job_of(J, it.u);
+  const int ul = it.u - J.j[jb].vec0;
+  const int nbox = it.kind == 0 ? (G.nx + 15) / 16 : kTile / 16;
+  const uint32_t box_bytes = 128u * (uint32_t)(it.kind == 0 ? G.ny : G.nz);
+  uint64_t state;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+               : "=l"(state)
+               : "r"(bar), "r"((uint32_t)nbox * box_bytes)
+               : "memory");
+  const uint32_t dst0 = smem_u32(smem + G.stg);
+  if (it.kind == 0) {
+    const void* map = &J.j[jb].txy;
+    const int zc = ul * G.nz + it.idx;
+    for (int b = 0; b < nbox; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+          "[%5];" ::"r"(dst0 + (uint32_t)b * G.reg_xy),
+          "l"(map), "r"(16 * b), "r"(0), "r"(zc), "r"(bar)
+          : "memory");
+  } else {
+    const void* map = &J.j[jb].tz;
+    const int p0 = it.idx * kTile;
+    const int yc = ul * G.nz;
+    for (int b = 0; b < nbox; ++b)
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+          "[%4];" ::"r"(dst0 + (uint32_t)b * G.reg_z),
+          "l"(map), "r"(p0 + 16 * b), "r"(yc), "r"(bar)
+          : "memory");
+  }
+}
+
+// Conversion tasks of an item: one 16-byte row of a core matrix each, from
+// eight staged doubles (zero for rows past the data).
+//   xy: task (j, q) (j < npy, q: i-octet < kx/8): core matrix (j/8, q) of
+//       the plane image, its row j%8 = X[j][8q .. 8q+7], staged in box q/2,
+//       row j, chunks 4 (q%2) .. +3 (swizzled).  Eight consecutive tasks are
+//       eight consecutive rows j of one core matrix: their reads fall in
+//       distinct banks and their stores fill 128 contiguous bytes.
+//   z:  task (k, m) (k < kz, m: point octet < 16): core matrix (k/8 along K,
+//       m along M) at (k/8 * 16 + m) * 128, its row k%8 = the tile's points
+//       8m .. 8m+7 of plane k, staged in box m/2, row k.
+struct Task {
+  int row;       // staged row (j or k), or -1 for a zero row
+  uint32_t src;  // byte offset of the staged row's first 16-byte chunk within the box region set
+  int chunk0;    // its first chunk, 0 or 4
+  uint32_t dst;  // byte offset of the image row
+};
+
+__device__ __forceinline__ Task task_xy(const F16Geom& G, int j, int q) {
+  Task k;
+  k.row = j < G.ny ? j : -1;
+  k.src = (uint32_t)(q >> 1) * G.reg_xy + (uint32_t)(j < G.ny ? j : 0) * 128u;
+  k.chunk0 = 4 * (q & 1);
+  k.dst = (uint32_t)((j >> 3) * (G.kx >> 3) + q) * 128u + (uint32_t)(j & 7) * 16u;
+  return k;
+}
+
+__device__ __forceinline__ Task task_z(const F16Geom& G, int k, int m) {
+  Task r;
+  r.row = k < G.nz ? k : -1;
+  r.src = (uint32_t)(m >> 1) * G.reg_z + (uint32_t)(k < G.nz ? k : 0) * 128u;
+  r.chunk0 = 4 * (m & 1);
+  r.dst = (uint32_t)((k >> 3) * 16 + m) * 128u + (uint32_t)(k & 7) * 16u;
+  return r;
+}
+
+// The eight staged doubles of a task (chunk c of staged row r sits at chunk
+// c ^ (r mod 8): the 128-byte swizzle).
+__device__ __forceinline__ void load8(const unsigned char* stg, const Task& k, double* v) {
+  if (k.row < 0) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = 0.0;
+    return;
+  }
+  const int sw = k.row & 7;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const double2 d = *reinterpret_cast<const double2*>(stg + k.src + (uint32_t)(((k.chunk0 + e) ^ sw) << 4));
+    v[2 * e] = d.x;
+    v[2 * e + 1] = d.y;
+  }
+}
+
+// The tasks of one producer thread, t = ptid, ptid + 224, ...: a task index
+// t = major * rows + row (rows = npy for xy, kz for z) kept as the pair
+// (row, major), advanced without a division.
+struct TaskIter {
+  int row, major, rows;
+  __device__ __forceinline__ TaskIter(int t, int rows_) : row(t % rows_), major(t / rows_), rows(rows_) {}
+  __device__ __forceinline__ void next() {
+    row += kProdWarps * 32;
+    while (row >= rows) row -= rows, ++major;
+  }
+};
+
+__device__ __forceinline__ Task task_of(const F16Geom& G, int kind, const TaskIter& ti) {
+  return kind == 0 ? task_xy(G, ti.row, ti.major) : task_z(G, ti.row, ti.major);
+}
+
+// Largest FP64 biased exponent among the staged values of an item's tasks.
+__device__ __forceinline__ int max_exponent(const unsigned char* stg, int ntask, int kind, const F16Geom& G,
+                                            int ptid) {
+  uint32_t emax = 0;
+  TaskIter ti(ptid, kind == 0 ? G.npy : G.kz);
+  for (int t = ptid; t < ntask; t += kProdWarps * 32, ti.next()) {
+    const Task k = task_of(G, kind, ti);
+    if (k.row < 0) continue;
+    double v[8];
+    load8(stg, k, v);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t e = (uint32_t)((unsigned long long)__double_as_longlong(v[q]) >> 52) & 0x7ffu;
+      emax = e > emax ? e : emax;
+    }
+  }
+  return (int)emax;
+}
+
+__global__ void __launch_bounds__(kThreadsAll, 1)
+    k_hx_f16(const __grid_constant__ F16Geom G, const unsigned short* __restrict__ t_hi,
+             const unsigned short* __restrict__ t_lo, const __grid_constant__ F16Jobs J, F16Counters* __restrict__ cnt,
+             int* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t mbar_t, mbar_full, mbar_empty, mbar_acc_full[kMaxAcc], mbar_acc_empty[kMaxAcc], mbar_stg;
+  __shared__ uint32_t tmem_base;
+  __shared__ unsigned ring[kRing];
+  __shared__ int sig[kRing];  // item scale exponents, by ticket slot
+  __shared__ int s_emax[kProdWarps];
+  __shared__ int s_abort, s_prod_ok, s_epi_ok, s_last, s_stg_issued;
+  volatile int* abort = &s_abort;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long nxny = (long)G.nx * G.ny;
+  const long N = nxny * G.nz;
+  const int nvec = J.nvec;
+
+  if (tid == 0) {
+    s_abort = 0;
+    s_stg_issued = 0;
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_t)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar_full)), "r"(kProdWarps * 32));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_empty)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_stg)));
+    for (int b = 0; b < kMaxAcc; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 2;" ::"r"(smem_u32(&mbar_acc_full[b])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar_acc_empty[b])));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    // the kinetic image (the grid's constant data) while the kernel ahead finishes
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(smem_u32(&mbar_t)), "r"(2u * G.t_bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(smem + G.t_hi)),
+                 "l"(t_hi), "r"(G.t_bytes), "r"(smem_u32(&mbar_t))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(smem + G.t_lo)),
+                 "l"(t_lo), "r"(G.t_bytes), "r"(smem_u32(&mbar_t))
+                 : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
+                 "r"(G.acc_cols << G.acc_shift));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  pg::pdl_wait();
+  pg::pdl_release();
+  const uint32_t tmem = tmem_base;
+  if (tid == 0) ring[0] = atomicAdd(&cnt->ticket, 1u);
+  __syncthreads();
+
+  if (warp < kProdWarps) {
+    // ------------------------------------------------------------ producers
+    const int ptid = tid;
+    const uint32_t bar_stg = smem_u32(&mbar_stg);
+    const unsigned char* stg = smem + G.stg;
+    if (ptid == 0) {
+      const Item it0 = decode(ring[0], nvec, G.nz, G.nzt, G.lag);
+      stage_item(G, J, it0, nxny, smem, bar_stg);
+      if (it0.kind >= 0) s_stg_issued = 1;
+    }
+    for (int i = 0;; ++i) {
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
+      if (ptid == 0) ring[(i + 1) % kRing] = atomicAdd(&cnt->ticket, 1u);
+      if (it.kind < 0) {
+        // no more work: hand the issuer its stop item once the images are free
+        if (ptid == 0) {
+          const int ok = i == 0 || mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
+          if (!ok) *abort = 1;
+        }
+        mbar_arrive(smem_u32(&mbar_full));
+        break;
+      }
+      // the item's rows have landed
+      if (ptid == 0) {
+        const int ok = mbar_wait_or_abort(bar_stg, (uint32_t)(i & 1), abort);
+        if (!ok) *abort = 1;
+        s_prod_ok = ok;
+      }
+      named_sync(1, kProdWarps * 32);
+      if (!s_prod_ok) break;
+      const int ntask = it.kind == 0 ? (G.kx >> 3) * G.npy : 16 * G.kz;
+      // the item's scale: its largest exponent over the producers
+      int em = max_exponent(stg, ntask, it.kind, G, ptid);
+      em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
+      if (lane == 0) s_emax[warp] = em;
+      // the images are free once the previous item's MMAs are done
+      if (ptid == 0) {
+        const int ok = i == 0 || mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
+        if (!ok) *abort = 1;
+        s_prod_ok = ok;
+      }
+      named_sync(1, kProdWarps * 32);
+      if (!s_prod_ok) break;
+      int emax = 0;
+#pragma unroll
+      for (int w = 0; w < kProdWarps; ++w) emax = s_emax[w] > emax ? s_emax[w] : emax;
+      // largest |x| < 2^(emax - 1022): scaled below 2^15.  The epilogue's
+      // factor 2^-(s + tau) must be a normal FP32 number; blocks whose values
+      // all lie below about 2^-100 (or above 2^100) are scaled less and lose
+      // what FP32 cannot hold, as the TF32 split of the other kernels does.
+      int s = (emax == 0 || emax == 0x7ff) ? 0 : 1037 - emax;
+      s = s > 126 - G.tau ? 126 - G.tau : (s < -127 - G.tau ? -127 - G.tau : s);
+      if (ptid == 0) sig[i % kRing] = s;
+      unsigned char* ohi = smem + G.op_hi;
+      unsigned char* olo = smem + G.op_lo;
+      TaskIter ti(ptid, it.kind == 0 ? G.npy : G.kz);
+      const int sb = s - 896;
+      for (int t = ptid; t < ntask; t += kProdWarps * 32, ti.next()) {
+        const Task k = task_of(G, it.kind, ti);
+        double v[8];
+        load8(stg, k, v);
+        uint4 h, l;
+        split8(v, sb, h, l);
+        *reinterpret_cast<uint4*>(ohi + k.dst) = h;
+        *reinterpret_cast<uint4*>(olo + k.dst) = l;
+      }
+      // the staging reads and image writes are done (and fenced against the
+      // async proxy): the next item's copies may start, the MMAs may read
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      named_sync(1, kProdWarps * 32);
+      // the MMAs may start now; one thread then issues the next item's copies
+      mbar_arrive(smem_u32(&mbar_full));
+      if (ptid == 0) {
+        const Item nx_it = decode(ring[(i + 1) % kRing], nvec, G.nz, G.nzt, G.lag);
+        stage_item(G, J, nx_it, nxny, smem, bar_stg);
+        if (nx_it.kind >= 0) s_stg_issued = i + 2;
+      }
+    }
+  } else if (warp < kIssueWarp) {
+    // ------------------------------------------------------------- epilogue
+    const int quarter = warp & 3, half = (warp - kProdWarps) >> 2;
+    const bool leader = warp == kProdWarps && lane == 0;
+    for (int i = 0;; ++i) {
+      const int b = i & ((1 << G.acc_shift) - 1);
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
+      const double *x = nullptr, *v = nullptr;
+      double* y = nullptr;
+      if (it.kind >= 0) vec_ptrs(J, it.u, N, x, y, v);
+      const int i0 = 32 * quarter + lane;
+      const long pl = nxny * (it.kind == 0 ? it.idx : 0);
+      const long p = (long)(it.kind == 1 ? it.idx : 0) * kTile + i0;
+      if (leader) {
+        int ok = 1;
+        if (it.kind == 1) {
+          // every plane of the vector has its W in Y (bounded wait, ~2 s)
+          const unsigned long long t0 = globaltimer_ns();
+          while (*(volatile unsigned*)&cnt->done[it.u] < (unsigned)G.nz) {
+            if (*abort || globaltimer_ns() - t0 > 2000000000ull) {
+              ok = 0;
+              break;
+            }
+            __nanosleep(128);
+          }
+          __threadfence();
+        }
+        if (ok) ok = mbar_wait_or_abort(smem_u32(&mbar_acc_full[b]), (uint32_t)((i >> G.acc_shift) & 1), abort);
+        if (!ok) *abort = 1;
+        s_epi_ok = ok;
+      }
+      named_sync(2, kEpiWarps * 32);
+      if (!s_epi_ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (it.kind < 0) break;
+      const float unscale = exp2i(-(sig[i % kRing] + G.tau));
+      const uint32_t acc = tmem + (uint32_t)b * G.acc_cols + ((uint32_t)(32 * quarter) << 16);
+      if (it.kind == 0) {
+        // the x + y sums of the plane, FP32, into the low word of each
+        // point's Y slot (the z item of the same points reads them)
+        float* yw = reinterpret_cast<float*>(y);
+        for (int c = half; c < (G.npy >> 4); c += 2) {
+          float d[16];
+          tmem_ld16(acc + (uint32_t)(16 * c), d);
+          if (i0 < G.nx) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int j = 16 * c + q;
+              if (j < G.ny) yw[2 * (pl + i0 + (long)G.nx * j)] = d[q] * unscale;
+            }
+          }
+        }
+      } else {
+        // Y = V X + (Kxy + Kz): the partial sums add in FP32 and V X joins in
+        // one FP64 multiply-add (the FP32 sum converted with integer operations)
+        const float* yw = reinterpret_cast<const float*>(y);
+        for (int c = half; c < (G.npz >> 4); c += 2) {
+          double vv[16], xx[16];
+          float w[16];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) {
+            const int k = 16 * c + q;
+            const bool in = p < nxny && k < G.nz;
+            const long a = p + nxny * k;
+            vv[q] = in ? v[a] : 0.0;
+            xx[q] = in ? x[a] : 0.0;
+            w[q] = in ? __ldcg(yw + 2 * a) : 0.f;
+          }
+          float d[16];
+          tmem_ld16(acc + (uint32_t)(16 * c), d);
+          if (p < nxny) {
+#pragma unroll
+            for (int q = 0; q < 16; ++q) {
+              const int k = 16 * c + q;
+              if (k < G.nz) y[p + nxny * k] = fma(vv[q], xx[q], f32_to_f64(fmaf(d[q], unscale, w[q])));
+            }
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      named_sync(2, kEpiWarps * 32);
+      if (leader) {
+        if (it.kind == 0) {
+          __threadfence();
+          atomicAdd(&cnt->done[it.u], 1u);
+        }
+        mbar_arrive(smem_u32(&mbar_acc_empty[b]));
+      }
+    }
+  } else if (lane == 0) {
+    // --------------------------------------------------------------- issuer
+    // kind::f16, FP16 A and B, FP32 D; bit 15: A MN-major
+    const uint32_t id_x = (1u << 4) | ((uint32_t)(G.npy >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+    const uint32_t id_y = id_x | (1u << 15);
+    const uint32_t id_z = (1u << 4) | (1u << 15) | ((uint32_t)(G.npz >> 3) << 17) | ((uint32_t)(kTile >> 4) << 24);
+    const uint32_t sb = smem_u32(smem);
+    const uint32_t kq_x = (uint32_t)(G.kx >> 3) * 128u;  // row-group stride of the plane / x-kinetic image
+    const uint32_t kq_y = (uint32_t)(G.ky >> 3) * 128u;
+    const uint32_t kq_z = (uint32_t)(G.kz >> 3) * 128u;
+    // K-major images: LBO = next 8 K values (128 B), SBO = next 8 rows.
+    // MN-major images: LBO = next 8 K values, SBO = next 8 M values.
+    const uint64_t d_th = smem_desc(sb + G.t_hi, 128, kq_x), d_tl = smem_desc(sb + G.t_lo, 128, kq_x);
+    const uint64_t d_tyh = smem_desc(sb + G.t_hi, 128, kq_y), d_tyl = smem_desc(sb + G.t_lo, 128, kq_y);
+    const uint64_t d_tzh = smem_desc(sb + G.t_hi, 128, kq_z), d_tzl = smem_desc(sb + G.t_lo, 128, kq_z);
+    const uint64_t d_pbh = smem_desc(sb + G.op_hi, 128, kq_x), d_pbl = smem_desc(sb + G.op_lo, 128, kq_x);
+    const uint64_t d_pah = smem_desc(sb + G.op_hi, kq_x, 128), d_pal = smem_desc(sb + G.op_lo, kq_x, 128);
+    const uint64_t d_zh = smem_desc(sb + G.op_hi, 16 * 128, 128), d_zl = smem_desc(sb + G.op_lo, 16 * 128, 128);
+    bool ok = mbar_wait_or_abort(smem_u32(&mbar_t), 0, abort);
+    int last_commit = -1;
+    for (int i = 0; ok; ++i) {
+      const int b = i & ((1 << G.acc_shift) - 1);
+      ok = mbar_wait_or_abort(smem_u32(&mbar_full), (uint32_t)(i & 1), abort);
+      const int nacc = 1 << G.acc_shift;
+      if (ok && i >= nacc)
+        ok = mbar_wait_or_abort(smem_u32(&mbar_acc_empty[b]), (uint32_t)(((i - nacc) >> G.acc_shift) & 1), abort);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
+      if (it.kind < 0) {
+        mbar_arrive(smem_u32(&mbar_acc_full[b]));
+        mbar_arrive(smem_u32(&mbar_acc_full[b]));
+        break;
+      }
+      const uint32_t acc = tmem + (uint32_t)b * G.acc_cols;
+      if (it.kind == 0) {
+        for (int kk = 0; kk < G.kx / 16; ++kk) {  // x: A = Tx (K = i), B = plane rows j
+          const uint64_t o = (uint64_t)kk * 16;    // 256 bytes: two core matrices along K
+          mma_f16(acc, d_tl + o, d_pbh + o, id_x, kk > 0 ? 1u : 0u);
+          mma_f16(acc, d_th + o, d_pbl + o, id_x, 1u);
+          mma_f16(acc, d_th + o, d_pbh + o, id_x, 1u);
+        }
+        for (int kk = 0; kk < G.ky / 16; ++kk) {  // y: A = plane, M = i, K = j (MN-major); B = Ty
+          const uint64_t oa = (uint64_t)kk * 2 * (kq_x >> 4), ob = (uint64_t)kk * 16;
+          mma_f16(acc, d_pal + oa, d_tyh + ob, id_y, 1u);
+          mma_f16(acc, d_pah + oa, d_tyl + ob, id_y, 1u);
+          mma_f16(acc, d_pah + oa, d_tyh + ob, id_y, 1u);
+        }
+      } else {
+        for (int kk = 0; kk < G.kz / 16; ++kk) {  // z: A = 128 lines, M = point, K = plane (MN-major); B = Tz
+          const uint64_t oa = (uint64_t)kk * 2 * 16 * (128 >> 4), ob = (uint64_t)kk * 16;
+          mma_f16(acc, d_zl + oa, d_tzh + ob, id_z, kk > 0 ? 1u : 0u);
+          mma_f16(acc, d_zh + oa, d_tzl + ob, id_z, 1u);
+          mma_f16(acc, d_zh + oa, d_tzh + ob, id_z, 1u);
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar_empty)));
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(&mbar_acc_full[b])));
+      mbar_arrive(smem_u32(&mbar_acc_full[b]));
+      last_commit = i;
+    }
+    if (!ok) {
+      *abort = 1;
+      if (last_commit >= 0) mbar_wait(smem_u32(&mbar_empty), (uint32_t)(last_commit & 1));
+      mbar_wait(smem_u32(&mbar_t), 0);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // a staging copy issued for an item that an aborted loop never consumed
+  // lands before the CTA leaves (bounded wait)
+  if (tid == 0 && s_abort && s_stg_issued > 0) mbar_wait(smem_u32(&mbar_stg), (uint32_t)((s_stg_issued - 1) & 1));
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(G.acc_cols << G.acc_shift));
+  if (tid == 0) {
+    if (s_abort) atomicExch(err, 1);
+    __threadfence();
+    s_last = atomicAdd(&cnt->finished, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (s_last) {
+    for (int u = tid; u < nvec; u += kThreadsAll) cnt->done[u] = 0;
+    if (tid == 0) {
+      cnt->ticket = 0;
+      cnt->finished = 0;
+    }
+    __threadfence();
+  }
+}
+
+}  // namespace
+
+namespace pg {
+
+namespace {
+
+struct F16Plan {
+  bool ok = false;
+  F16Geom G{};
+  size_t smem = 0;
+  char why[160] = "";
+};
+
+int g_f16_sms = 0;
+int g_f16_max_dyn = 0;
+
+cudaError_t f16_init() {
+  static const cudaError_t init = [] {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_f16_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_hx_f16);
+    if (e == cudaSuccess) {
+      g_f16_max_dyn = optin - (int)fa.sharedSizeBytes;
+      e = cudaFuncSetAttribute(k_hx_f16, cudaFuncAttributeMaxDynamicSharedMemorySize, g_f16_max_dyn);
+    }
+    if (g_f16_sms <= 0) g_f16_sms = 148;
+    return e;
+  }();
+  return init;
+}
+
+F16Plan plan_f16(const pg_grid* g) {
+  F16Plan P;
+  const int nx = g->n[0], ny = g->n[1], nz = g->n[2];
+  auto no = [&](const char* why) {
+    snprintf(P.why, sizeof(P.why), "%s", why);
+    return P;
+  };
+  if (!g->t16_hi[0].p) return no("no FP16 kinetic images (an axis has more than 128 points)");
+  if (nx > 96 || ny > 96 || nz > 96) return no("an axis has more than 96 points");
+  if (nx % 2 != 0) return no("odd nx (bulk copies need 16-byte rows)");
+  for (int a = 1; a < 3; ++a)
+    if (g->n[a] != nx || g->t[a] != g->t[0]) return no("the axes do not share one kinetic matrix");
+  F16Geom& G = P.G;
+  G.nx = nx;
+  G.ny = ny;
+  G.nz = nz;
+  G.kx = tc16_kpad(nx);
+  G.ky = tc16_kpad(ny);
+  G.kz = tc16_kpad(nz);
+  G.npy = tc_npad(ny);
+  G.npz = tc_npad(nz);
+  G.nzt = (int)(((long)nx * ny + kTile - 1) / kTile);
+  G.lag = 2;
+  G.tau = g->t16_scale;
+  const uint32_t npx = (uint32_t)tc_npad(nx);
+  // the kinetic image: npx rows as copied, read as 128 rows by the x
+  // contraction (the slot is 128 rows long)
+  G.t_bytes = npx * (uint32_t)G.kx * 2u;
+  const uint32_t t_slot = (uint32_t)kTile * (uint32_t)G.kx * 2u;
+  uint32_t cur = 0;
+  G.t_hi = cur;
+  cur += t_slot;
+  G.t_lo = cur;
+  cur += t_slot;
+  // operand images: the plane (npy x kx) plus the y contraction's overread,
+  // or the z tile (128 x kz)
+  const uint32_t plane = (uint32_t)G.npy * (uint32_t)G.kx * 2u + kOverread;
+  const uint32_t ztile = (uint32_t)kTile * (uint32_t)G.kz * 2u;
+  const uint32_t op = (std::max(plane, ztile) + 127u) / 128u * 128u;
+  G.op_hi = cur;
+  cur += op;
+  G.op_lo = cur;
+  cur += op;
+  // staging: box regions of 128-byte rows, 1024-byte aligned (the swizzle
+  // atom); ceil(nx / 16) regions of ny rows, or eight regions of nz rows
+  G.stg = (cur + 1023u) / 1024u * 1024u;
+  G.reg_xy = (uint32_t)(128 * ny + 1023) / 1024u * 1024u;
+  G.reg_z = (uint32_t)(128 * nz + 1023) / 1024u * 1024u;
+  cur = G.stg + std::max((uint32_t)((nx + 15) / 16) * G.reg_xy, (uint32_t)(kTile / 16) * G.reg_z);
+  P.smem = cur;
+  if ((long)P.smem > (long)g_f16_max_dyn) return no("operand images and staging exceed shared memory");
+  uint32_t cols = 32;
+  while (cols < (uint32_t)std::max(G.npy, G.npz)) cols <<= 1;
+  G.acc_cols = cols;
+  // as many accumulators as tensor memory holds (at most four), so that a
+  // long z epilogue does not hold up the next items' MMAs
+  G.acc_shift = cols * 4 <= 512 ? 2 : 1;
+  P.ok = true;
+  return P;
+}
+
+}  // namespace
+
+// Work counters of the FP16 kernel, one block per stream (as the fused kernel's).
+static pg_status f16_counters(const pg_grid* g, cudaStream_t st, F16Counters** out) {
+  unsigned long long id = 0;
+  PG_CUDA_TRY(cudaStreamGetId(st, &id));
+  std::lock_guard<std::mutex> l(g->fused_m);
+  const unsigned long long key = id ^ 0x8000000000000000ull;  // beside the fused kernel's blocks
+  auto it = g->fused_cnt.find(key);
+  if (it == g->fused_cnt.end()) {
+    if (g->fused_cnt.size() >= 512) {
+      set_error("FP16 H*X: more than 256 streams used on one grid");
+      return PG_UNSUPPORTED;
+    }
+    std::unique_ptr<DevBuf<unsigned>> b(new DevBuf<unsigned>());
+    PG_TRY(b->alloc(sizeof(F16Counters) / sizeof(unsigned)));
+    PG_CUDA_TRY(cudaMemset(b->p, 0, sizeof(F16Counters)));
+    it = g->fused_cnt.emplace(key, std::move(b)).first;
+  }
+  *out = reinterpret_cast<F16Counters*>(it->second->p);
+  return PG_OK;
+}
+
+bool f16_hx_ok(const pg_grid* g) {
+  if (f16_init() != cudaSuccess) return false;
+  return plan_f16(g).ok;
+}
+
+void f16_plan_text(const pg_grid* g, const HxParams& p, char* buf, int len) {
+  if (f16_init() != cudaSuccess) {
+    snprintf(buf, (size_t)len, "FP16 split (k_hx_f16): device query failed");
+    return;
+  }
+  const F16Plan P = plan_f16(g);
+  if (!P.ok) {
+    snprintf(buf, (size_t)len, "FP16 split (k_hx_f16): not available: %s", P.why);
+    return;
+  }
+  snprintf(buf, (size_t)len,
+           "FP16 split (k_hx_f16): xy planes %dx%d + z tiles of 128 lines (%d per vector, lag %d vectors), "
+           "K %d/%d/%d, rows bulk-copied to a staging buffer, %zu B shared memory, %u TMEM columns x %d, %d CTAs",
+           P.G.nx, P.G.ny, P.G.nzt, p.lag > 0 ? p.lag : P.G.lag, P.G.kx, P.G.ky, P.G.kz, P.smem, P.G.acc_cols,
+           1 << P.G.acc_shift,
+           p.ctas > 0 && p.ctas < g_f16_sms ? p.ctas : g_f16_sms);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependence on the driver library).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// The two tensor maps of a job: X (nvec vectors of the grid) as a 3-D
+// (x, y, plane) tensor with boxes of 16 x ny x 1, and as a 2-D (plane point,
+// plane) tensor with boxes of 16 x nz; FP64, 128-byte swizzle, zeros past
+// the edges.
+pg_status encode_job_maps(const pg_grid* g, const double* x, int nvec, CUtensorMap* txy, CUtensorMap* tz) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) {
+    set_error("FP16 H*X: cuTensorMapEncodeTiled is not available");
+    return PG_UNSUPPORTED;
+  }
+  const cuuint64_t nx = (cuuint64_t)g->n[0], ny = (cuuint64_t)g->n[1], nz = (cuuint64_t)g->n[2];
+  const cuuint32_t one[3] = {1, 1, 1};
+  {
+    const cuuint64_t dims[3] = {nx, ny, nz * (cuuint64_t)nvec};
+    const cuuint64_t strides[2] = {nx * 8, nx * ny * 8};
+    const cuuint32_t box[3] = {16, (cuuint32_t)ny, 1};
+    const CUresult r = enc(txy, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(x), dims, strides, box, one,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      set_error("FP16 H*X: tensor map (planes) rejected: driver error %d", (int)r);
+      return PG_CUDA;
+    }
+  }
+  {
+    const cuuint64_t dims[2] = {nx * ny, nz * (cuuint64_t)nvec};
+    const cuuint64_t strides[1] = {nx * ny * 8};
+    const cuuint32_t box[2] = {16, (cuuint32_t)nz};
+    const CUresult r = enc(tz, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(x), dims, strides, box, one,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+      set_error("FP16 H*X: tensor map (z tiles) rejected: driver error %d", (int)r);
+      return PG_CUDA;
+    }
+  }
+  return PG_OK;
+}
+
+// Mixed H*X of vector blocks on the same grid, up to kMaxJobs per launch of
+// the FP16 kernel (the caller has checked f16_hx_ok); X 16-byte aligned.
+pg_status hx_f16_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
+                      const int* nvec, int njobs, const HxParams& hp, cudaStream_t st) {
+  PG_ARG(njobs > 0, "FP16 H*X: no jobs");
+  if (njobs > kMaxJobs) {
+    PG_TRY(hx_f16_jobs(g, v, x, y, nvec, kMaxJobs, hp, st));
+    return hx_f16_jobs(g, v + kMaxJobs, x + kMaxJobs, y + kMaxJobs, nvec + kMaxJobs, njobs - kMaxJobs, hp, st);
+  }
+  PG_CUDA_TRY(f16_init());
+  F16Plan P = plan_f16(g);
+  if (!P.ok) {
+    set_error("FP16 H*X not available on this grid: %s", P.why);
+    return PG_UNSUPPORTED;
+  }
+  if (hp.lag > 0) P.G.lag = hp.lag;
+  for (int j = 0; j < njobs; ++j)
+    PG_ARG(nvec[j] == 0 || ((uintptr_t)x[j] & 15u) == 0, "FP16 H*X: X must be 16-byte aligned");
+  F16Counters* cnt = nullptr;
+  PG_TRY(f16_counters(g, st, &cnt));
+  F16Jobs J;
+  memset(&J, 0, sizeof(J));
+  int total = 0;
+  for (int j = 0; j < njobs; ++j) {
+    PG_ARG(nvec[j] >= 0, "FP16 H*X: negative vector count");
+    if (nvec[j] > 0) PG_TRY(encode_job_maps(g, x[j], nvec[j], &J.j[J.n].txy, &J.j[J.n].tz));
+    J.j[J.n].x = x[j];
+    J.j[J.n].y = y[j];
+    J.j[J.n].v = v[j];
+    J.j[J.n].nvec = nvec[j];
+    J.j[J.n].vec0 = total;
+    total += nvec[j];
+    if (nvec[j] > 0) ++J.n;
+  }
+  if (total == 0) return PG_OK;
+  PG_ARG(total <= kF16MaxVec, "FP16 H*X: %d vectors in one launch (at most %d)", total, kF16MaxVec);
+  J.nvec = total;
+  const long items = (long)total * (P.G.nz + P.G.nzt);
+  const int cap = hp.ctas > 0 && hp.ctas < g_f16_sms ? hp.ctas : g_f16_sms;
+  const int grid = (int)std::min<long>(items, cap);
+  PG_CUDA_TRY(launch_dependent(k_hx_f16, dim3(grid), dim3(kThreadsAll), P.smem, st, P.G,
+                               (const unsigned short*)g->t16_hi[0].p, (const unsigned short*)g->t16_lo[0].p, J, cnt,
+                               g->tc_err.p));
+  return check_launch("k_hx_f16");
+}
+
+pg_status hx_f16(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& hp,
+                 cudaStream_t st) {
+  for (int v0 = 0; v0 < nvec; v0 += kF16MaxVec) {
+    const int nb = std::min(kF16MaxVec, nvec - v0);
+    const double* xs = x + (long)v0 * g->N;
+    double* ys = y + (long)v0 * g->N;
+    PG_TRY(hx_f16_jobs(g, &v, &xs, &ys, &nb, 1, hp, st));
+  }
+  return PG_OK;
+}
+
+}  // namespace pg

@@ -550,13 +550,16 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (it.kind >= 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       if (G.staged && it.kind >= 0) {
         // every producer has read the staging buffer (and fenced those reads
-        // against the async proxy): the next item's copies may overwrite it
+        // against the async proxy): the MMAs may start, and the next item's
+        // copies may overwrite the buffer
         named_sync(1, kProdWarps * 32);
+        mbar_arrive(smem_u32(&mbar_full));
         if (warp == 0) {
           const Item nx_it = decode(ring[(i + 1) % kRing], nvec, G.nz, G.nzt, G.lag);
           stage_item(G, J, nx_it, N, nxny, smem, bar_stg, lane);
           if (lane == 0 && nx_it.kind >= 0) s_stg_issued = i + 2;
         }
+        continue;
       }
       mbar_arrive(smem_u32(&mbar_full));
       if (it.kind < 0) break;
@@ -991,8 +994,12 @@ static const TunedEntry kTuned[] = {
 #include "pg_hx_tuned.inc"
     {0, 0, 0, 0, 0, 0}};
 
+bool f16_hx_ok(const pg_grid* g);
+void f16_plan_text(const pg_grid* g, const HxParams& p, char* buf, int len);
+
 HxParams hx_params(const pg_grid* g, int nvec) {
   const bool fused_ok = fused_hx_ok(g);
+  const bool f16_ok = f16_hx_ok(g);
   HxParams p{fused_ok ? 2 : 1, 2, 0, 0};
   if (g->n[0] == g->n[1] && g->n[1] == g->n[2]) {
     // the entry of this grid size with the nearest block size
@@ -1001,10 +1008,14 @@ HxParams hx_params(const pg_grid* g, int nvec) {
       if (e->n == g->n[0] && (!best || std::abs(e->nvec - nvec) < std::abs(best->nvec - nvec))) best = e;
     if (best) p = HxParams{best->kind, best->lag, best->ctas, best->form};
   }
+  // the FP16-split kernel where the grid allows it (kind 3; the tuned table
+  // holds the other two kinds' parameters)
+  if (f16_ok && p.kind != 3) p = HxParams{3, 2, 0, 0};
   if (g->hx_kernel) p.kind = g->hx_kernel;
   if (g->hx_lag) p.lag = g->hx_lag;
   if (g->hx_ctas) p.ctas = g->hx_ctas;
   if (g->hx_form) p.form = g->hx_form;
+  if (p.kind == 3 && !f16_ok && g->hx_kernel != 3) p.kind = fused_ok ? 2 : 1;
   if (p.kind == 2 && !fused_ok && g->hx_kernel != 2) p.kind = 1;
   return p;
 }
@@ -1017,6 +1028,10 @@ void hx_plan_text(const pg_grid* g, int nvec, char* buf, int len) {
   }
   const FusedPlan P = plan_fused(g);
   const HxParams p = hx_params(g, nvec);
+  if (p.kind == 3) {
+    f16_plan_text(g, p, buf, len);
+    return;
+  }
   if (p.kind == 2 && P.ok)
     snprintf(buf, (size_t)len,
              "fused (k_hx_fused): xy planes %dx%d + z tiles of 128 lines (%d per vector, lag %d vectors), "
@@ -1036,7 +1051,14 @@ void hx_plan_text(const pg_grid* g, int nvec, char* buf, int len) {
 
 extern "C" pg_status pg_grid_set_hx_kernel(pg_grid* g, int kind) {
   PG_ARG(g, "pg_grid_set_hx_kernel: null grid");
-  PG_ARG(kind >= 0 && kind <= 2, "pg_grid_set_hx_kernel: kind must be 0, 1 or 2 (got %d)", kind);
+  PG_ARG(kind >= 0 && kind <= 3, "pg_grid_set_hx_kernel: kind must be 0, 1, 2 or 3 (got %d)", kind);
+  if (kind == 3 && !pg::f16_hx_ok(g)) {
+    char why[256];
+    pg::HxParams p{3, 2, 0, 0};
+    pg::f16_plan_text(g, p, why, sizeof(why));
+    pg::set_error("pg_grid_set_hx_kernel: %s", why);
+    return PG_UNSUPPORTED;
+  }
   if (kind == 2 && !pg::fused_hx_ok(g)) {
     char why[256];
     pg::hx_plan_text(g, 1, why, sizeof(why));

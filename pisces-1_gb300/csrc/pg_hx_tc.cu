@@ -743,6 +743,11 @@ pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, c
 }
 
 bool fused_hx_ok(const pg_grid* g);
+bool f16_hx_ok(const pg_grid* g);
+pg_status hx_f16(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& p,
+                 cudaStream_t st);
+pg_status hx_f16_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
+                      const int* nvec, int njobs, const HxParams& p, cudaStream_t st);
 pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& p,
                    cudaStream_t st);
 pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
@@ -754,7 +759,13 @@ pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double*
                          const int* nvec, int njobs, cudaStream_t st) {
   int total = 0;
   for (int j = 0; j < njobs; ++j) total += nvec[j];
-  const HxParams p = hx_params(g, total);
+  HxParams p = hx_params(g, total);
+  if (p.kind == 3) {
+    bool aligned = true;
+    for (int j = 0; j < njobs; ++j) aligned = aligned && (nvec[j] == 0 || ((uintptr_t)x[j] & 15u) == 0);
+    if (aligned) return hx_f16_jobs(g, v, x, y, nvec, njobs, p, st);
+    p.kind = fused_hx_ok(g) ? 2 : 1;
+  }
   if (p.kind == 2) return hx_fused_jobs(g, v, x, y, nvec, njobs, p, st);
   for (int a = 0; a < 3; ++a)
     PG_TRY(tc_axis_jobs(g, a, g->t_hi[a].p, g->t_lo[a].p, v, x, y, nvec, njobs, a == 0 ? 2 : 1, st, p.ctas, p.form));
@@ -768,12 +779,17 @@ pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double*
 // occurred (the eigensolver checks the word at its own synchronisation points).
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
                    bool check) {
-  const HxParams p = hx_params(g, nvec);
+  HxParams p = hx_params(g, nvec);
+  if (p.kind == 3 && ((uintptr_t)x & 15u) != 0) p.kind = fused_hx_ok(g) ? 2 : 1;  // bulk copies need alignment
+  if (p.kind == 3) {
+    PG_TRY(hx_f16(g, v, x, y, nvec, p, st));
+    return check ? check_tc_error(g, st) : PG_OK;
+  }
   if (p.kind == 2) {
     PG_TRY(hx_fused(g, v, x, y, nvec, p, st));
     return check ? check_tc_error(g, st) : PG_OK;
   }
-  if (g->hx_kernel == 2) {
+  if (g->hx_kernel == 2 || g->hx_kernel == 3) {
     set_error("pg_hx: the fused mixed H*X kernel does not take this grid");
     return PG_UNSUPPORTED;
   }

@@ -37,6 +37,7 @@ def rel_err(a, b):
                                     ((2, 17, 9), 3), ((32, 32, 32), 40)])
 def test_fused_matches_fp64_and_three_pass(pg, torch, n, nvec):
     grid = pg.Grid(n, tuple(0.6 * (k + 1) for k in n))
+    grid.set_hx_kernel(2)
     assert grid.hx_plan().startswith("fused"), grid.hx_plan()
     X, v = rand_block(torch, grid, nvec, sum(n) + nvec)
     y64 = grid.hx(v, X, nvec=nvec, precision=pg.PG_FP64)
@@ -54,6 +55,7 @@ def test_fused_repeats_bit_for_bit(pg, torch):
     # several launches in a row on one stream reuse its counter block, which
     # the last CTA of each launch resets; the output is the same bits
     grid = pg.Grid((64, 64, 64), (40.0, 40.0, 40.0))
+    grid.set_hx_kernel(2)
     X, v = rand_block(torch, grid, 6, 3)
     first = grid.hx(v, X, nvec=6, precision=pg.PG_MIXED)
     for _ in range(5):
@@ -65,6 +67,7 @@ def test_fused_repeats_bit_for_bit(pg, torch):
 def test_fused_two_streams_at_once(pg, torch):
     # the same grid on two streams concurrently: separate counter blocks
     grid = pg.Grid((48, 48, 48), (30.0, 30.0, 30.0))
+    grid.set_hx_kernel(2)
     X1, v = rand_block(torch, grid, 5, 8)
     X2, _ = rand_block(torch, grid, 5, 9)
     ref1 = grid.hx(v, X1, nvec=5, precision=pg.PG_MIXED)
@@ -88,6 +91,7 @@ def test_fused_smooth_vector(pg, torch):
     # three-pass kernels, and is no larger than theirs
     n, L = (64, 64, 64), (40.0, 40.0, 40.0)
     grid = pg.Grid(n, L)
+    grid.set_hx_kernel(2)
     w = grid.piab()
     v = torch.zeros_like(w)
     y64 = grid.hx(v, w, nvec=1, precision=pg.PG_FP64)
@@ -109,5 +113,5 @@ def test_fused_declines_large_axes(pg, torch):
             grid.set_hx_kernel(2)
         assert e.value.status == pg.PG_UNSUPPORTED
     with pytest.raises(pg.PiscesError) as e:
-        pg.Grid((8, 8, 8), (5.0, 5.0, 5.0)).set_hx_kernel(3)
+        pg.Grid((8, 8, 8), (5.0, 5.0, 5.0)).set_hx_kernel(4)
     assert e.value.status == pg.PG_BAD_ARG
