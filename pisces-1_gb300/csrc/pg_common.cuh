@@ -245,7 +245,10 @@ pg_status axis_apply(const pg_grid* g, int axis, const double* A64, const float*
                      const double* x, double* y, int nvec, int mode, int precision, cudaStream_t st);
 // H*X without the public call's synchronous status check (pg_hx.cu); the
 // caller checks check_tc_error() at its own synchronisation points.
+// unit: every value of X is known to lie in [-1, 1] (the Davidson's
+// orthonormal basis vectors), which lets the FP16-split kernel use a fixed
+// operand scale.
 pg_status hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
-             cudaStream_t st);
+             cudaStream_t st, bool unit = false);
 pg_status check_tc_error(const pg_grid* g, cudaStream_t st);
 }  // namespace pg

@@ -1061,7 +1061,7 @@ pg_status solve_with(const pg_grid* g, const double* v, const pg_solve_params* p
     pg_solve_stats s2;
     const pg_status s = solve_with(
         g, v, &q, evals, evecs, &s2, st,
-        [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, PG_FP64, st); }, &ws);
+        [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, PG_FP64, st, true); }, &ws);
     if (stats) {
       stats->nconv = s2.nconv;
       stats->n_matvec += s2.n_matvec;
@@ -1115,7 +1115,7 @@ extern "C" pg_status pg_solve(const pg_grid* g, const double* v, const pg_solve_
   const int prec = p ? p->precision : PG_FP64;
   return solve_with(
       g, v, p, evals, evecs, stats, st,
-      [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, prec, st); }, nullptr);
+      [&](const double* x, double* y, int nvec) { return hx(g, v, x, y, nvec, prec, st, true); }, nullptr);
 }
 
 namespace pg {
@@ -1186,7 +1186,7 @@ extern "C" pg_status pg_cluster_solve(const int n[3], const double L[3], int nw,
   const double* vp = v.p;
   pg_status s = solve_with(
       g, vp, p, evals, vec.p, stats, st,
-      [&](const double* x, double* y, int nvec) { return hx(g, vp, x, y, nvec, prec, st); }, &ws);
+      [&](const double* x, double* y, int nvec) { return hx(g, vp, x, y, nvec, prec, st, true); }, &ws);
   if (s != PG_OK && s != PG_NOT_CONVERGED) return s;
   if (evecs_host)
     PG_CUDA_TRY(cudaMemcpyAsync(evecs_host, vec.p, sizeof(double) * N * p->nroots, cudaMemcpyDeviceToHost, st));

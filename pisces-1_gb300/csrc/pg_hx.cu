@@ -125,15 +125,15 @@ pg_status axis_apply(const pg_grid* g, int axis, const double* A64, const float*
 }
 
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
-                   bool check);
+                   bool check, bool unit);
 
 pg_status hx(const pg_grid* g, const double* v, const double* x, double* y, int nvec, int precision,
-             cudaStream_t st) {
+             cudaStream_t st, bool unit) {
   PG_ARG(g && v && nvec >= 0, "pg_hx: bad arguments");
   if (nvec == 0) return PG_OK;  // an empty block may come with null X and Y
   PG_ARG(x && y, "pg_hx: null X or Y");
   PG_ARG(x != y, "pg_hx: X and Y must not alias");
-  if (precision == PG_MIXED) return hx_mixed(g, v, x, y, nvec, st, false);
+  if (precision == PG_MIXED) return hx_mixed(g, v, x, y, nvec, st, false, unit);
   PG_ARG(precision == PG_FP64, "pg_hx: unknown precision %d", precision);
   constexpr int NV = 4;
   dim3 grid((unsigned)((g->N + 255) / 256), (unsigned)((nvec + NV - 1) / NV));

@@ -14,10 +14,12 @@
 // copies per item; the producers read eight consecutive rows at a time, so
 // the swizzle puts their reads in distinct banks.  The
 // producer warps convert them to an FP16 high part and remainder scaled by a
-// power of two 2^s per item (the largest |x| of the item lands in
-// [2^14, 2^15): s from the largest FP64 exponent), so that hi + lo holds
-// about 22 significant bits, the precision of the TF32 split of the other
-// kernels.  The kinetic matrices are kept as FP16 images of T 2^tau
+// power of two 2^s per item, so that hi + lo holds about 22 significant
+// bits, the precision of the TF32 split of the other kernels: the item's
+// largest |x| lands in [2^14, 2^15) (s from the largest FP64 exponent of its
+// staged values, found by a pass over them); where the caller knows every
+// value lies in [-1, 1] (the Davidson's orthonormal basis vectors) s = 14
+// without the pass.  The kinetic matrices are kept as FP16 images of T 2^tau
 // (pg_grid.t16_*).  D = Ah Bh + Ah Bl + Al Bh accumulates in FP32 in TMEM and
 // the epilogue multiplies by 2^-(s + tau), exactly.
 //
@@ -215,6 +217,7 @@ struct F16Geom {
   int nzt;            // z items per vector
   int lag;            // vectors between a vector's xy items and its z items
   int tau;            // the kinetic images hold T 2^tau
+  int unit_bound;     // 1: every value of X lies in [-1, 1]; a fixed scale 2^14, no maximum pass
   uint32_t t_hi, t_lo;            // the kinetic image (shared by the three axes)
   uint32_t t_bytes;               // bytes of one kinetic image as copied
   uint32_t op_hi, op_lo;          // operand images of the current item
@@ -497,9 +500,11 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (!s_prod_ok) break;
       const int ntask = it.kind == 0 ? (G.kx >> 3) * G.npy : 16 * G.kz;
       // the item's scale: its largest exponent over the producers
-      int em = max_exponent(stg, ntask, it.kind, G, ptid);
-      em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
-      if (lane == 0) s_emax[warp] = em;
+      if (!G.unit_bound) {
+        int em = max_exponent(stg, ntask, it.kind, G, ptid);
+        em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
+        if (lane == 0) s_emax[warp] = em;
+      }
       // the images are free once the previous item's MMAs are done
       if (ptid == 0) {
         const int ok = i == 0 || mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
@@ -508,9 +513,12 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       }
       named_sync(1, kProdWarps * 32);
       if (!s_prod_ok) break;
-      int emax = 0;
+      int emax = 1023;  // |x| <= 1
+      if (!G.unit_bound) {
+        emax = 0;
 #pragma unroll
-      for (int w = 0; w < kProdWarps; ++w) emax = s_emax[w] > emax ? s_emax[w] : emax;
+        for (int w = 0; w < kProdWarps; ++w) emax = s_emax[w] > emax ? s_emax[w] : emax;
+      }
       // largest |x| < 2^(emax - 1022): scaled below 2^15.  The epilogue's
       // factor 2^-(s + tau) must be a normal FP32 number; blocks whose values
       // all lie below about 2^-100 (or above 2^100) are scaled less and lose
@@ -922,11 +930,11 @@ pg_status encode_job_maps(const pg_grid* g, const double* x, int nvec, CUtensorM
 // Mixed H*X of vector blocks on the same grid, up to kMaxJobs per launch of
 // the FP16 kernel (the caller has checked f16_hx_ok); X 16-byte aligned.
 pg_status hx_f16_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
-                      const int* nvec, int njobs, const HxParams& hp, cudaStream_t st) {
+                      const int* nvec, int njobs, const HxParams& hp, cudaStream_t st, bool unit) {
   PG_ARG(njobs > 0, "FP16 H*X: no jobs");
   if (njobs > kMaxJobs) {
-    PG_TRY(hx_f16_jobs(g, v, x, y, nvec, kMaxJobs, hp, st));
-    return hx_f16_jobs(g, v + kMaxJobs, x + kMaxJobs, y + kMaxJobs, nvec + kMaxJobs, njobs - kMaxJobs, hp, st);
+    PG_TRY(hx_f16_jobs(g, v, x, y, nvec, kMaxJobs, hp, st, unit));
+    return hx_f16_jobs(g, v + kMaxJobs, x + kMaxJobs, y + kMaxJobs, nvec + kMaxJobs, njobs - kMaxJobs, hp, st, unit);
   }
   PG_CUDA_TRY(f16_init());
   F16Plan P = plan_f16(g);
@@ -935,6 +943,7 @@ pg_status hx_f16_jobs(const pg_grid* g, const double* const* v, const double* co
     return PG_UNSUPPORTED;
   }
   if (hp.lag > 0) P.G.lag = hp.lag;
+  P.G.unit_bound = unit ? 1 : 0;
   for (int j = 0; j < njobs; ++j)
     PG_ARG(nvec[j] == 0 || ((uintptr_t)x[j] & 15u) == 0, "FP16 H*X: X must be 16-byte aligned");
   F16Counters* cnt = nullptr;
@@ -966,12 +975,12 @@ pg_status hx_f16_jobs(const pg_grid* g, const double* const* v, const double* co
 }
 
 pg_status hx_f16(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& hp,
-                 cudaStream_t st) {
+                 cudaStream_t st, bool unit) {
   for (int v0 = 0; v0 < nvec; v0 += kF16MaxVec) {
     const int nb = std::min(kF16MaxVec, nvec - v0);
     const double* xs = x + (long)v0 * g->N;
     double* ys = y + (long)v0 * g->N;
-    PG_TRY(hx_f16_jobs(g, &v, &xs, &ys, &nb, 1, hp, st));
+    PG_TRY(hx_f16_jobs(g, &v, &xs, &ys, &nb, 1, hp, st, unit));
   }
   return PG_OK;
 }

@@ -745,9 +745,9 @@ pg_status tc_axis(const pg_grid* g, int a, const float* Ahi, const float* Alo, c
 bool fused_hx_ok(const pg_grid* g);
 bool f16_hx_ok(const pg_grid* g);
 pg_status hx_f16(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& p,
-                 cudaStream_t st);
+                 cudaStream_t st, bool unit);
 pg_status hx_f16_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
-                      const int* nvec, int njobs, const HxParams& p, cudaStream_t st);
+                      const int* nvec, int njobs, const HxParams& p, cudaStream_t st, bool unit);
 pg_status hx_fused(const pg_grid* g, const double* v, const double* x, double* y, int nvec, const HxParams& p,
                    cudaStream_t st);
 pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
@@ -756,14 +756,14 @@ pg_status hx_fused_jobs(const pg_grid* g, const double* const* v, const double* 
 // Mixed H*X of several solves on the same grid in one launch (fused) or one
 // launch per axis, with the launch parameters tuned for the whole block.
 pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
-                         const int* nvec, int njobs, cudaStream_t st) {
+                         const int* nvec, int njobs, cudaStream_t st, bool unit) {
   int total = 0;
   for (int j = 0; j < njobs; ++j) total += nvec[j];
   HxParams p = hx_params(g, total);
   if (p.kind == 3) {
     bool aligned = true;
     for (int j = 0; j < njobs; ++j) aligned = aligned && (nvec[j] == 0 || ((uintptr_t)x[j] & 15u) == 0);
-    if (aligned) return hx_f16_jobs(g, v, x, y, nvec, njobs, p, st);
+    if (aligned) return hx_f16_jobs(g, v, x, y, nvec, njobs, p, st, unit);
     p.kind = fused_hx_ok(g) ? 2 : 1;
   }
   if (p.kind == 2) return hx_fused_jobs(g, v, x, y, nvec, njobs, p, st);
@@ -778,11 +778,11 @@ pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double*
 // check, the call waits for the stream and returns PG_DEVICE_TIMEOUT if one
 // occurred (the eigensolver checks the word at its own synchronisation points).
 pg_status hx_mixed(const pg_grid* g, const double* v, const double* x, double* y, int nvec, cudaStream_t st,
-                   bool check) {
+                   bool check, bool unit) {
   HxParams p = hx_params(g, nvec);
   if (p.kind == 3 && ((uintptr_t)x & 15u) != 0) p.kind = fused_hx_ok(g) ? 2 : 1;  // bulk copies need alignment
   if (p.kind == 3) {
-    PG_TRY(hx_f16(g, v, x, y, nvec, p, st));
+    PG_TRY(hx_f16(g, v, x, y, nvec, p, st, unit));
     return check ? check_tc_error(g, st) : PG_OK;
   }
   if (p.kind == 2) {

@@ -242,7 +242,7 @@ void pg_engine::batcher_main() {
       }
     }
     if (s == PG_OK) {
-      s = pg::hx_mixed_batch(g, vs.data(), xs.data(), ys.data(), nv.data(), nj, bs);
+      s = pg::hx_mixed_batch(g, vs.data(), xs.data(), ys.data(), nv.data(), nj, bs, true);
       if (s != PG_OK) err = pg::last_error();
     }
     // record every done event, also after a failure, so no stream waits on a stale one
@@ -322,7 +322,7 @@ void pg_engine::run_job(Job& job, cudaStream_t st, pg::SolveWorkspace* ws, pg::D
       g, v.p, &p, res.evals, evecs.p, &res.stats, st,
       [&](const double* x, double* y, int nvec) {
         if (batch) return batched_hx(g, v.p, x, y, nvec, st, ready, done_ev);
-        return pg::hx(g, v.p, x, y, nvec, p.precision, st);
+        return pg::hx(g, v.p, x, y, nvec, p.precision, st, true);
       },
       ws);
   {

@@ -38,7 +38,8 @@ pg_status scpol_add_points(const pg_grid* g, const pg_sites* t, const pg_scpol_m
 constexpr int kMaxBatchJobs = 16;  // job-table entries of one tensor-core launch
 
 // Mixed-form H*X of up to kMaxBatchJobs solves on the same grid: one launch per axis.
+// unit: as for hx (every value of the X blocks in [-1, 1]).
 pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
-                         const int* nvec, int njobs, cudaStream_t st);
+                         const int* nvec, int njobs, cudaStream_t st, bool unit = false);
 
 }  // namespace pg
