@@ -265,13 +265,33 @@ GRAM_SHAPE = (40, 4)  # P rows x Q rows of the timed Gram launch: mid-solve basi
 
 
 def _time_launches(torch, stream, fn, reps=20, warm=3):
-    """Mean CUDA-event time of fn(i), i = 0 .. reps-1, queued back to back on
-    stream after warm untimed calls."""
+    """Mean device time of fn(i), i = 0 .. reps-1, on stream: after warm
+    untimed calls the reps are captured in a CUDA graph and one replay is
+    timed with CUDA events, so the host's per-call work (Python, ctypes,
+    argument checks) is not part of the time.  Where capture is refused the
+    calls are timed back to back."""
     with torch.cuda.stream(stream):
         for i in range(warm):
             fn(i)
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    try:
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=stream):
+            for i in range(reps):
+                fn(i)
+        graph.replay()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            a.record(stream)
+            graph.replay()
+            b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+    except RuntimeError:
+        torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
         a.record(stream)
         for i in range(reps):
             fn(i)

@@ -1000,7 +1000,7 @@ void f16_plan_text(const pg_grid* g, const HxParams& p, char* buf, int len);
 HxParams hx_params(const pg_grid* g, int nvec) {
   const bool fused_ok = fused_hx_ok(g);
   const bool f16_ok = f16_hx_ok(g);
-  HxParams p{fused_ok ? 2 : 1, 2, 0, 0};
+  HxParams p{f16_ok ? 3 : (fused_ok ? 2 : 1), 2, 0, 0};
   if (g->n[0] == g->n[1] && g->n[1] == g->n[2]) {
     // the entry of this grid size with the nearest block size
     const TunedEntry* best = nullptr;
@@ -1008,9 +1008,6 @@ HxParams hx_params(const pg_grid* g, int nvec) {
       if (e->n == g->n[0] && (!best || std::abs(e->nvec - nvec) < std::abs(best->nvec - nvec))) best = e;
     if (best) p = HxParams{best->kind, best->lag, best->ctas, best->form};
   }
-  // the FP16-split kernel where the grid allows it (kind 3; the tuned table
-  // holds the other two kinds' parameters)
-  if (f16_ok && p.kind != 3) p = HxParams{3, 2, 0, 0};
   if (g->hx_kernel) p.kind = g->hx_kernel;
   if (g->hx_lag) p.lag = g->hx_lag;
   if (g->hx_ctas) p.ctas = g->hx_ctas;

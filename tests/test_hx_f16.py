@@ -38,6 +38,7 @@ def rel_err(a, b):
 @pytest.mark.parametrize("n,nvec", [(8, 3), (16, 2), (32, 40), (48, 4), (64, 4), (80, 2), (96, 8)])
 def test_f16_matches_fp64_and_tf32(pg, torch, n, nvec):
     grid = pg.Grid(n, 0.615 * (n + 1))
+    grid.set_hx_kernel(3)
     assert grid.hx_plan(nvec).startswith("FP16 split"), grid.hx_plan(nvec)
     X, v = rand_block(torch, grid, nvec, n + nvec)
     y64 = grid.hx(v, X, nvec=nvec, precision=pg.PG_FP64)
@@ -50,9 +51,16 @@ def test_f16_matches_fp64_and_tf32(pg, torch, n, nvec):
     grid.set_hx_kernel(0)
 
 
+def test_f16_is_the_automatic_choice_off_the_table(pg, torch):
+    # grid sizes the tuned table does not list take the FP16-split kernel
+    for n in (8, 16, 40):
+        assert pg.Grid(n, 0.615 * (n + 1)).hx_plan(4).startswith("FP16 split"), n
+
+
 @pytest.mark.parametrize("scale", [1e-20, 1e20])
 def test_f16_scaled_blocks(pg, torch, scale):
     grid = pg.Grid(48, 30.0)
+    grid.set_hx_kernel(3)
     X, v = rand_block(torch, grid, 3, 7)
     X = X * scale
     y64 = grid.hx(v, X, nvec=3, precision=pg.PG_FP64)
@@ -64,6 +72,7 @@ def test_f16_smooth_vector(pg, torch):
     # the half-box ground state on the c2 grid: the error is bounded by the
     # size of the kinetic terms, as for the TF32 kernels
     grid = pg.Grid(64, 40.0)
+    grid.set_hx_kernel(3)
     w = grid.piab()
     v = torch.zeros_like(w)
     y64 = grid.hx(v, w, nvec=1, precision=pg.PG_FP64)
@@ -74,6 +83,7 @@ def test_f16_smooth_vector(pg, torch):
 
 def test_f16_repeats_and_two_streams(pg, torch):
     grid = pg.Grid(64, 40.0)
+    grid.set_hx_kernel(3)
     X1, v = rand_block(torch, grid, 5, 3)
     X2, _ = rand_block(torch, grid, 5, 4)
     ref1 = grid.hx(v, X1, nvec=5, precision=pg.PG_MIXED)
@@ -92,6 +102,7 @@ def test_f16_repeats_and_two_streams(pg, torch):
 
 def test_f16_nan_reaches_output(pg, torch):
     grid = pg.Grid(32, 20.0)
+    grid.set_hx_kernel(3)
     X, v = rand_block(torch, grid, 2, 5)
     X[grid.N + 777] = float("nan")
     y = grid.hx(v, X, nvec=2, precision=pg.PG_MIXED)
