@@ -591,7 +591,6 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (it.kind == 0) {
         // the x + y sums of the plane, FP32, into the low word of each
         // point's Y slot (the z item of the same points reads them)
-        float* yw = reinterpret_cast<float*>(y);
         for (int c = half; c < (G.npy >> 4); c += 2) {
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
@@ -599,7 +598,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int j = 16 * c + q;
-              if (j < G.ny) yw[2 * (pl + i0 + (long)G.nx * j)] = d[q] * unscale;
+              if (j < G.ny)  // the whole 8-byte slot: full sectors, no fetch of Y before the write
+                reinterpret_cast<uint2*>(y)[pl + i0 + (long)G.nx * j] = make_uint2(__float_as_uint(d[q] * unscale), 0u);
             }
           }
         }
@@ -616,8 +616,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
             const bool in = p < nxny && k < G.nz;
             const long a = p + nxny * k;
             vv[q] = in ? v[a] : 0.0;
-            xx[q] = in ? x[a] : 0.0;
-            w[q] = in ? __ldcg(yw + 2 * a) : 0.f;
+            xx[q] = in ? __ldcs(x + a) : 0.0;  // last uses of X and W: evict first, V stays
+            w[q] = in ? __ldcs(yw + 2 * a) : 0.f;
           }
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int k = 16 * c + q;
-              if (k < G.nz) y[p + nxny * k] = fma(vv[q], xx[q], f32_to_f64(fmaf(d[q], unscale, w[q])));
+              if (k < G.nz) __stcs(y + p + nxny * k, fma(vv[q], xx[q], f32_to_f64(fmaf(d[q], unscale, w[q]))));
             }
           }
         }

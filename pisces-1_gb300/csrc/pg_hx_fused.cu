@@ -606,7 +606,6 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
         // the x + y sums of the plane, FP32, into the low word of each point's
         // Y slot (the z item of the same points reads them, then overwrites
         // the slot with the result)
-        float* yw = reinterpret_cast<float*>(y);
         for (int c = half; c < (G.npy >> 4); c += 2) {
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
@@ -614,7 +613,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 16; ++q) {
               const int j = 16 * c + q;
-              if (j < G.ny) yw[2 * (pl + i0 + (long)G.nx * j)] = d[q];
+              if (j < G.ny)  // the whole 8-byte slot: full sectors, no fetch of Y before the write
+                reinterpret_cast<uint2*>(y)[pl + i0 + (long)G.nx * j] = make_uint2(__float_as_uint(d[q]), 0u);
             }
           }
         }
@@ -631,8 +631,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
             const bool in = p < nxny && k < G.nz;
             const long a = p + nxny * k;
             vv[q] = in ? v[a] : 0.0;
-            xx[q] = in ? x[a] : 0.0;
-            w[q] = in ? __ldcg(yw + 2 * a) : 0.f;
+            xx[q] = in ? __ldcs(x + a) : 0.0;  // last uses of X and W: evict first, V stays
+            w[q] = in ? __ldcs(yw + 2 * a) : 0.f;
           }
           float d[8];
           tmem_ld8(acc + (uint32_t)(8 * c), d);
@@ -640,7 +640,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
               const int k = 8 * c + q;
-              if (k < G.nz) y[p + nxny * k] = fma(vv[q], xx[q], (double)(w[q] + d[q]));
+              if (k < G.nz) __stcs(y + p + nxny * k, fma(vv[q], xx[q], (double)(w[q] + d[q])));
             }
           }
         }
