@@ -281,29 +281,33 @@ __device__ __forceinline__ void vec_ptrs(const F16Jobs& J, int u, long N, const 
   v = J.j[j].v;
 }
 
-// One thread: the tensor copies of an item into the staging buffer,
+// The lanes of one warp: the tensor copies of an item into the staging buffer,
 // completing on mbarrier bar.  An xy item: ceil(nx / 16) boxes of 16 x ny
 // values (plane idx of its vector), one region each; a z item: eight boxes
 // of 16 points x nz planes.  Values past the grid (the last box of a row,
 // the last tile) arrive as zeros; every box counts in full.  x coordinates
 // are multiples of 16 values.
 __device__ __forceinline__ void stage_item(const F16Geom& G, const F16Jobs& J, const Item& it, long nxny,
-                                           unsigned char* smem, uint32_t bar) {
+                                           unsigned char* smem, uint32_t bar, int lane) {
   if (it.kind < 0) return;
   const int jb = job_of(J, it.u);
   const int ul = it.u - J.j[jb].vec0;
   const int nbox = it.kind == 0 ? (G.nx + 15) / 16 : kTile / 16;
   const uint32_t box_bytes = 128u * (uint32_t)(it.kind == 0 ? G.ny : G.nz);
-  uint64_t state;
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
-               : "=l"(state)
-               : "r"(bar), "r"((uint32_t)nbox * box_bytes)
-               : "memory");
+  if (lane == 0) {
+    uint64_t state;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 %0, [%1], %2;"
+                 : "=l"(state)
+                 : "r"(bar), "r"((uint32_t)nbox * box_bytes)
+                 : "memory");
+  }
+  __syncwarp();
   const uint32_t dst0 = smem_u32(smem + G.stg);
+  // one box per lane
   if (it.kind == 0) {
     const void* map = &J.j[jb].txy;
     const int zc = ul * G.nz + it.idx;
-    for (int b = 0; b < nbox; ++b)
+    for (int b = lane; b < nbox; b += 32)
       asm volatile(
           "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
           "[%5];" ::"r"(dst0 + (uint32_t)b * G.reg_xy),
@@ -313,7 +317,7 @@ __device__ __forceinline__ void stage_item(const F16Geom& G, const F16Jobs& J, c
     const void* map = &J.j[jb].tz;
     const int p0 = it.idx * kTile;
     const int yc = ul * G.nz;
-    for (int b = 0; b < nbox; ++b)
+    for (int b = lane; b < nbox; b += 32)
       asm volatile(
           "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
           "[%4];" ::"r"(dst0 + (uint32_t)b * G.reg_z),
@@ -395,14 +399,29 @@ __device__ __forceinline__ int max_exponent(const unsigned char* stg, int ntask,
                                             int ptid) {
   uint32_t emax = 0;
   TaskIter ti(ptid, kind == 0 ? G.npy : G.kz);
-  for (int t = ptid; t < ntask; t += kProdWarps * 32, ti.next()) {
+  // two tasks per turn: their loads are in flight together
+  int t = ptid;
+  for (; t + kProdWarps * 32 < ntask; t += 2 * kProdWarps * 32) {
+    const Task k0 = task_of(G, kind, ti);
+    ti.next();
+    const Task k1 = task_of(G, kind, ti);
+    ti.next();
+    double v[16];
+    load8(stg, k0, v);
+    load8(stg, k1, v + 8);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const uint32_t e = (uint32_t)__double2hiint(v[q]) >> 20 & 0x7ffu;
+      emax = e > emax ? e : emax;
+    }
+  }
+  if (t < ntask) {
     const Task k = task_of(G, kind, ti);
-    if (k.row < 0) continue;
     double v[8];
     load8(stg, k, v);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      const uint32_t e = (uint32_t)((unsigned long long)__double_as_longlong(v[q]) >> 52) & 0x7ffu;
+      const uint32_t e = (uint32_t)__double2hiint(v[q]) >> 20 & 0x7ffu;
       emax = e > emax ? e : emax;
     }
   }
@@ -473,10 +492,10 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     const int ptid = tid;
     const uint32_t bar_stg = smem_u32(&mbar_stg);
     const unsigned char* stg = smem + G.stg;
-    if (ptid == 0) {
+    if (warp == 0) {
       const Item it0 = decode(ring[0], nvec, G.nz, G.nzt, G.lag);
-      stage_item(G, J, it0, nxny, smem, bar_stg);
-      if (it0.kind >= 0) s_stg_issued = 1;
+      stage_item(G, J, it0, nxny, smem, bar_stg, lane);
+      if (lane == 0 && it0.kind >= 0) s_stg_issued = 1;
     }
     for (int i = 0;; ++i) {
       const Item it = decode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
@@ -530,7 +549,25 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       unsigned char* olo = smem + G.op_lo;
       TaskIter ti(ptid, it.kind == 0 ? G.npy : G.kz);
       const int sb = s - 896;
-      for (int t = ptid; t < ntask; t += kProdWarps * 32, ti.next()) {
+      // two tasks per turn: their loads and conversions overlap
+      int t = ptid;
+      for (; t + kProdWarps * 32 < ntask; t += 2 * kProdWarps * 32) {
+        const Task k0 = task_of(G, it.kind, ti);
+        ti.next();
+        const Task k1 = task_of(G, it.kind, ti);
+        ti.next();
+        double v0[8], v1[8];
+        load8(stg, k0, v0);
+        load8(stg, k1, v1);
+        uint4 h0, l0, h1, l1;
+        split8(v0, sb, h0, l0);
+        split8(v1, sb, h1, l1);
+        *reinterpret_cast<uint4*>(ohi + k0.dst) = h0;
+        *reinterpret_cast<uint4*>(olo + k0.dst) = l0;
+        *reinterpret_cast<uint4*>(ohi + k1.dst) = h1;
+        *reinterpret_cast<uint4*>(olo + k1.dst) = l1;
+      }
+      if (t < ntask) {
         const Task k = task_of(G, it.kind, ti);
         double v[8];
         load8(stg, k, v);
@@ -543,12 +580,12 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       // async proxy): the next item's copies may start, the MMAs may read
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       named_sync(1, kProdWarps * 32);
-      // the MMAs may start now; one thread then issues the next item's copies
+      // the MMAs may start now; warp 0 then issues the next item's copies
       mbar_arrive(smem_u32(&mbar_full));
-      if (ptid == 0) {
+      if (warp == 0) {
         const Item nx_it = decode(ring[(i + 1) % kRing], nvec, G.nz, G.nzt, G.lag);
-        stage_item(G, J, nx_it, nxny, smem, bar_stg);
-        if (nx_it.kind >= 0) s_stg_issued = i + 2;
+        stage_item(G, J, nx_it, nxny, smem, bar_stg, lane);
+        if (lane == 0 && nx_it.kind >= 0) s_stg_issued = i + 2;
       }
     }
   } else if (warp < kIssueWarp) {
