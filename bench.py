@@ -380,7 +380,8 @@ def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
           "vectors_per_launch": nb, "l2": f"operands rotated over {kh} copies (more than twice the L2 between reuses)"}
     if mixed:
         hx.update(achieved=hbytes / (ms * 1e-3) / 1e9, peak=peaks["hbm_gbs"], unit="GB/s",
-                  frac=hbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], peak_source=which)
+                  frac=hbytes / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"], peak_source=which,
+                  traffic=KERNEL_TRAFFIC.get(("hx", tuple(grid.n), nb, precision)))
     else:
         hx.update(achieved=flops / (ms * 1e-3) / 1e12, peak=1.0, unit="TFLOP/s", frac=flops / (ms * 1e-3) / 1e12,
                   peak_source="FP64 FMA pipe of this GB300, measured with a DFMA loop (not in MEASURED_PEAKS.json)")
@@ -388,10 +389,14 @@ def kernel_rooflines(pg, torch, grid, tables, nb, precision, stream):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of these shapes
-# (kernel, grid, vectors in, vectors out, precision), from an ncu capture of
-# `python bench.py --roofline-only`; shapes not captured report null
+# (kernel, grid, vectors in, vectors out, precision) for the subspace kernels
+# and (kernel, grid, vectors, precision) for H*X, from an ncu capture of
+# `python bench.py --roofline-only [--workload c3]`; shapes not captured
+# report null
 KERNEL_TRAFFIC = {("gram", (64, 64, 64), 40, 4, 1): 92536832 + 2773248,
-                  ("combine", (64, 64, 64), 40, 4, 1): 83933696 + 2898176}
+                  ("combine", (64, 64, 64), 40, 4, 1): 83933696 + 2898176,
+                  ("hx", (64, 64, 64), 4, 1): 10576384 + 0,
+                  ("hx", (96, 96, 96), 8, 1): 80203520 + 27850240}
 
 
 def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
