@@ -256,7 +256,7 @@ def run_ours(args, ws, rank, local):
 
     roof = kernel_rooflines(pg, torch, grid, tables, nroots, precision, stream)
     hx_plan = grid.hx_plan(nroots)
-    return dict(hx_plan=hx_plan, total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
+    return dict(hx_plan=hx_plan, precond_plan=grid.precond_plan(), total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
                 de=de, stats=st, fp64=fp64, refalg=refalg, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d,
                 d2h=d2h, roofline=roof, N=N, precision=args.precision, ptol=ptol)
 
@@ -397,6 +397,13 @@ KERNEL_TRAFFIC = {("gram", (64, 64, 64), 40, 4, 1): 92536832 + 2773248,
                   ("combine", (64, 64, 64), 40, 4, 1): 83933696 + 2898176,
                   ("hx", (64, 64, 64), 4, 1): 10576384 + 0,
                   ("hx", (96, 96, 96), 8, 1): 80203520 + 27850240}
+
+
+def mixed_dtype(plan):
+    """The arithmetic of the mixed form: FP64 everywhere but the H*X
+    contractions, which run as three split products on the tensor cores
+    (FP16 halves with a per-item scale, or TF32 halves)."""
+    return "f64+fp16x3" if plan.startswith("FP16") else "f64+tf32x3"
 
 
 def cpu_baseline(args, wl, n_matvec_full, budget_s=20.0):
@@ -603,7 +610,7 @@ def run_c4(args):
            "l2": "per-solve working sets of 48^3-96^3 grids; no flush (requests differ)"}
     line = {"metric": "solves/s", "value": mixed["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": nreq,
             "warmup": len(m["warm"]), "ms_per_step": 1000.0 * mixed["wall"] / nreq, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64+tf32x3", "data": "synthetic", "config": cfg,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+fp16x3|tf32x3", "data": "synthetic", "config": cfg,
             "solver": {"precision": "mixed", "corrflag": C4["corrflag"], "residual_tol": 10.0 ** -MIXED_PTOL,
                        "fp64_residual_tol": 10.0 ** -C4["ptol_fp64"]},
             "latency_ms": {"p50": mixed["p50"], "p99": mixed["p99"], "at": "saturation (all submitted at once)"},
@@ -691,11 +698,12 @@ def main():
     p99 = float(np.percentile(lat, 99))
     line = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["total_ms"] / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f64+tf32x3",
-            "data": "synthetic", "config": cfg,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else mixed_dtype(r["hx_plan"]), "data": "synthetic", "config": cfg,
             "solver": {"precision": args.precision, "corrflag": args.corrflag, "residual_tol": 10.0 ** -r["ptol"],
                        "refine": "FP64 Rayleigh-Ritz step" if args.precision == "mixed" else None,
-                       "hx_kernel": r["hx_plan"]},
+                       "hx_kernel": r["hx_plan"],
+                       "preconditioner": r["precond_plan"] if args.corrflag == 3 else None},
             "latency_ms": {"p50": p50, "p99": p99},
             "eigenvalues": r["evals"], "max_abs_dE_vs_fp64": r["de"],
             "solve": {k: r["stats"][k] for k in ("n_matvec", "n_iter", "n_restart", "nconv", "seconds",

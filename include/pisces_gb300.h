@@ -351,6 +351,24 @@ pg_status pg_davidson_set_arithmetic(pg_davidson* d, int precision);
  * g must outlive the solve. */
 pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int precision);
 
+/* The kinetic preconditioner on its own: R <- (T - sigma_j)^-1 R for the k
+ * contiguous vectors R (device, N each, 16-byte aligned for the FP16 kernel),
+ * sigma[k] on the host; |T - sigma_j| is kept at least a tenth of the lowest
+ * kinetic level.  PG_FP64: six FP64 axis passes and a diagonal scale; PG_MIXED:
+ * where every axis has the same n <= 96 (n even), one FP16-split tensor-core
+ * kernel (k_kin_f16: per vector, xy forward transforms of the planes, z
+ * forward transform + diagonal + z backward transform of 128-line tiles, xy
+ * backward transforms), else six split-TF32 axis passes.  Allocates 2 k N
+ * doubles of scratch and synchronises the stream.  No reference counterpart
+ * (the builder's corrflag 3). */
+pg_status pg_kinetic_precondition(const pg_grid* g, double* R, int k, const double* sigma, int precision,
+                                  void* stream);
+/* Mixed-form preconditioner kernel of this grid: 0 automatic (the FP16 kernel
+ * where it applies), 1 the axis passes. */
+pg_status pg_grid_set_precond_kernel(pg_grid* g, int kind);
+/* One line describing the mixed-form preconditioner this grid uses. */
+pg_status pg_grid_precond_plan(const pg_grid* g, char* text, int len);
+
 /* The subspace eigensolver of the Davidson iteration (host): the k lowest
  * eigenpairs of the symmetric m x m matrix whose upper triangle is stored in
  * S (column-major, leading dimension ld); eigenvalues ascending in w[k],

@@ -126,6 +126,9 @@ SYMBOLS = {
     "pg_grid_hx_plan": (C.c_int, [_vp, C.c_char_p, C.c_int]),
     "pg_grid_hx_plan_for": (C.c_int, [_vp, C.c_int, C.c_char_p, C.c_int]),
     "pg_grid_set_hx_params": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "pg_kinetic_precondition": (C.c_int, [_vp, _vp, C.c_int, _dp, C.c_int, _vp]),
+    "pg_grid_set_precond_kernel": (C.c_int, [_vp, C.c_int]),
+    "pg_grid_precond_plan": (C.c_int, [_vp, C.c_char_p, C.c_int]),
     "pg_davidson_create": (C.c_int, [C.POINTER(_vp)]),
     "pg_davidson_destroy": (C.c_int, [_vp]),
     "pg_davidson_work_size": (C.c_long, [C.c_int, C.c_int, C.c_int, C.c_int]),
@@ -481,6 +484,23 @@ class Grid:
         """One-line description of the mixed H*X kernel this grid uses for nvec vectors."""
         buf = C.create_string_buffer(512)
         _check(lib().pg_grid_hx_plan_for(self._h, int(nvec), buf, 512))
+        return buf.value.decode()
+
+    def precondition(self, R, sigma, precision=PG_MIXED, stream=None):
+        """R <- (T - sigma_j)^-1 R in place for the len(sigma) vectors of R (pg_kinetic_precondition)."""
+        sg = np.ascontiguousarray(np.atleast_1d(np.asarray(sigma, dtype=np.float64)))
+        _check(lib().pg_kinetic_precondition(self._h, _dev(R), len(sg), sg.ctypes.data_as(_dp), precision,
+                                             _stream(stream)))
+        return R
+
+    def set_precond_kernel(self, kind):
+        """Mixed-form preconditioner kernel of this grid: 0 automatic (FP16 kernel), 1 axis passes."""
+        _check(lib().pg_grid_set_precond_kernel(self._h, int(kind)))
+
+    def precond_plan(self):
+        """One-line description of the mixed-form preconditioner this grid uses."""
+        buf = C.create_string_buffer(512)
+        _check(lib().pg_grid_precond_plan(self._h, buf, 512))
         return buf.value.decode()
 
     def check(self, stream=None):

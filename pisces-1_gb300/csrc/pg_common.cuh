@@ -214,6 +214,14 @@ struct pg_grid {
   pg::DevBuf<double> qb_dev[3];
   pg::DevBuf<float> qb_hi[3], qb_lo[3];
   pg::DevBuf<double> d_dev[3];
+  // FP16 high part and remainder of Q^T 2^q16_scale (forward, q16f_*) and of
+  // Q 2^q16_scale (backward, q16b_*) as tc16_kmajor_off images, for the FP16
+  // kinetic preconditioner; built when every axis has the same n <= 128
+  // (one eigenbasis for the three axes).  q16_sym: Q^T = Q (the DST-I), the
+  // backward images are not stored.
+  pg::DevBuf<unsigned short> q16f_hi, q16f_lo, q16b_hi, q16b_lo;
+  int q16_scale = 0;
+  bool q16_sym = false;
   std::vector<double> ekin[3];     // FFT grids: plane-wave energies per axis (Tdiag)
   // random start columns (Randm11 from seed 1; the same values for every
   // solve on this grid), generated once and grown on demand
@@ -222,6 +230,7 @@ struct pg_grid {
   // mixed H*X kernel choice (0 automatic, 1 three axis passes, 2 fused) and
   // the fused kernel's work counters, one block per stream id
   int hx_kernel = 0;
+  int pc_kernel = 0;  // mixed kinetic preconditioner: 0 automatic (FP16 kernel where it applies), 1 axis passes
   int hx_lag = 0, hx_ctas = 0, hx_form = 0;  // overrides of the tuned launch parameters (0: tuned)
   mutable std::mutex fused_m;
   mutable std::map<unsigned long long, std::unique_ptr<pg::DevBuf<unsigned>>> fused_cnt;

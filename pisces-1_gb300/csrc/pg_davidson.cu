@@ -251,6 +251,40 @@ extern "C" pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_gri
   return PG_OK;
 }
 
+extern "C" pg_status pg_kinetic_precondition(const pg_grid* g, double* R, int k, const double* sigma, int precision,
+                                             void* stream) {
+  PG_ARG(g && k >= 0 && (precision == PG_FP64 || precision == PG_MIXED), "pg_kinetic_precondition: bad arguments");
+  if (k == 0) return PG_OK;
+  PG_ARG(R && sigma, "pg_kinetic_precondition: null R or sigma");
+  cudaStream_t st = pg::as_stream(stream);
+  pg::DevBuf<double> w, sg;
+  PG_TRY(w.alloc((size_t)2 * k * g->N));
+  PG_TRY(sg.alloc((size_t)k));
+  PG_CUDA_TRY(cudaMemcpyAsync(sg.p, sigma, sizeof(double) * k, cudaMemcpyHostToDevice, st));
+  PG_TRY(pg::kinetic_precondition(g, R, k, sg.p, w.p, w.p + (long)k * g->N, precision, st));
+  // the scratch is freed on return: finish with it first
+  PG_CUDA_TRY(cudaStreamSynchronize(st));
+  return precision == PG_MIXED ? pg::check_tc_error(g, st) : PG_OK;
+}
+
+extern "C" pg_status pg_grid_set_precond_kernel(pg_grid* g, int kind) {
+  PG_ARG(g && (kind == 0 || kind == 1), "pg_grid_set_precond_kernel: kind must be 0 or 1");
+  g->pc_kernel = kind;
+  return PG_OK;
+}
+
+extern "C" pg_status pg_grid_precond_plan(const pg_grid* g, char* text, int len) {
+  PG_ARG(g && text && len > 0, "pg_grid_precond_plan: bad arguments");
+  if (g->pc_kernel != 1 && pg::kin_f16_ok(g)) {
+    pg::kin_f16_plan_text(g, text, len);
+  } else {
+    char why[200] = "forced";
+    if (g->pc_kernel != 1) pg::kin_f16_plan_text(g, why, sizeof(why));
+    snprintf(text, (size_t)len, "axis passes (k_hx_tc x 6, k_kin_scale); %s", why);
+  }
+  return PG_OK;
+}
+
 extern "C" long pg_davidson_work_size(int ndim, int maxsub, int nroots, int corrflag) {
   // DavidsonWorkSize (src/Davidson.cpp:46-52); same layout of the work array.
   if (corrflag == 2) return 2L * maxsub * maxsub + 11L * maxsub + (2L * nroots + 1) * ndim;
@@ -460,23 +494,32 @@ __global__ void k_olsen_coef(const double* __restrict__ G, int k, double* __rest
   }
 }
 
+pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* sigma_dev, cudaStream_t st) {
+  const long N = d->pc_grid->N;
+  PG_TRY(d->pc_w1.ensure((size_t)k * N));
+  PG_TRY(d->pc_w2.ensure((size_t)k * N));
+  return pg::kinetic_precondition(d->pc_grid, R, k, sigma_dev, d->pc_w1.p, d->pc_w2.p, d->pc_precision, st);
+}
+
+}  // namespace
+
 // Kinetic preconditioner on the k contiguous vectors R: R <- (T - sigma_j)^-1 R
 // with T = Q diag(d) Q^T per axis (DST-I for the sine DVR, the real Fourier
 // basis for the periodic FFT kinetic term): three forward contractions
-// (Q^T), a diagonal scale and three backward contractions (Q).
-pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* sigma_dev, cudaStream_t st) {
-  const pg_grid* g = d->pc_grid;
+// (Q^T), a diagonal scale and three backward contractions (Q).  The mixed
+// form runs them as one FP16-split tensor-core kernel where the grid allows
+// (k_kin_f16), else as six axis passes and a scale kernel.
+pg_status kinetic_precondition(const pg_grid* g, double* R, int k, const double* sigma_dev, double* w1, double* w2,
+                               int pr, cudaStream_t st) {
   const long N = g->N;
-  PG_TRY(d->pc_w1.ensure((size_t)k * N));
-  PG_TRY(d->pc_w2.ensure((size_t)k * N));
-  double *w1 = d->pc_w1.p, *w2 = d->pc_w2.p;
-  const int pr = d->pc_precision;
-  PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, R, w1, k, 0, pr, st));
-  PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w1, w2, k, 0, pr, st));
-  PG_TRY(axis_apply(g, 0, g->q_dev[0].p, g->q_hi[0].p, g->q_lo[0].p, w2, w1, k, 0, pr, st));
   // the smallest kinetic level, a scale for the denominator floor
   double dmin = 0;
   for (int a = 0; a < 3; ++a) dmin += 0.5 * (M_PI / g->L[a]) * (M_PI / g->L[a]);
+  if (pr == PG_MIXED && g->pc_kernel != 1 && kin_f16_ok(g) && (((uintptr_t)R | (uintptr_t)w1 | (uintptr_t)w2) & 15u) == 0)
+    return kin_f16(g, R, w1, w2, k, sigma_dev, 0.1 * dmin, st);
+  PG_TRY(axis_apply(g, 2, g->q_dev[2].p, g->q_hi[2].p, g->q_lo[2].p, R, w1, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 1, g->q_dev[1].p, g->q_hi[1].p, g->q_lo[1].p, w1, w2, k, 0, pr, st));
+  PG_TRY(axis_apply(g, 0, g->q_dev[0].p, g->q_hi[0].p, g->q_lo[0].p, w2, w1, k, 0, pr, st));
   for (int v0 = 0; v0 < k; v0 += 16) {  // at most 16 vectors per launch
     const int kk = std::min(16, k - v0);
 #define PG_KIN_SCALE(NRV)                                                                                     \
@@ -496,6 +539,8 @@ pg_status kinetic_precondition(pg_davidson* d, double* R, int k, const double* s
   PG_TRY(axis_apply(g, 0, g->qb_dev[0].p, g->qb_hi[0].p, g->qb_lo[0].p, w1, R, k, 0, pr, st));
   return PG_OK;
 }
+
+namespace {
 
 // Orthonormalise the k vectors R (contiguous, R[j*N]) against the first nbas
 // columns of B and among themselves, into B[nbas .. nbas+k) (out must be

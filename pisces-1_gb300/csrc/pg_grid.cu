@@ -151,6 +151,40 @@ pg_status build_t16(pg_grid* g) {
   return PG_OK;
 }
 
+// FP16 images of the eigenbasis (forward Q^T and backward Q, n x n row-major,
+// [output][input]) scaled by 2^tau, the largest entry in [2^14, 2^15).
+pg_status build_q16(pg_grid* g, const std::vector<double>& q, const std::vector<double>& qt, int m) {
+  double qmax = 0.0;
+  for (double v : q) qmax = std::max(qmax, std::fabs(v));
+  int e = 0;
+  if (qmax > 0.0) std::frexp(qmax, &e);
+  const int tau = qmax > 0.0 ? 15 - e : 0;
+  g->q16_scale = tau;
+  g->q16_sym = q == qt;
+  const int npad = pg::tc_npad(m), kpad = pg::tc16_kpad(m);
+  auto image = [&](const std::vector<double>& M, pg::DevBuf<unsigned short>& dhi,
+                   pg::DevBuf<unsigned short>& dlo) -> pg_status {
+    std::vector<unsigned short> hi((size_t)npad * kpad, 0), lo((size_t)npad * kpad, 0);
+    for (int r = 0; r < m; ++r)
+      for (int k = 0; k < m; ++k) {
+        const double v = std::ldexp(M[(size_t)r * m + k], tau);
+        const __half h = __float2half_rn((float)v);
+        const __half l = __float2half_rn((float)(v - (double)__half2float(h)));
+        const size_t o = pg::tc16_kmajor_off(r, k, kpad) / 2;
+        hi[o] = __half_as_ushort(h);
+        lo[o] = __half_as_ushort(l);
+      }
+    PG_TRY(dhi.alloc(hi.size()));
+    PG_TRY(dlo.alloc(lo.size()));
+    PG_CUDA_TRY(cudaMemcpy(dhi.p, hi.data(), sizeof(unsigned short) * hi.size(), cudaMemcpyHostToDevice));
+    PG_CUDA_TRY(cudaMemcpy(dlo.p, lo.data(), sizeof(unsigned short) * lo.size(), cudaMemcpyHostToDevice));
+    return PG_OK;
+  };
+  PG_TRY(image(qt, g->q16f_hi, g->q16f_lo));
+  if (!g->q16_sym) PG_TRY(image(q, g->q16b_hi, g->q16b_lo));
+  return PG_OK;
+}
+
 float to_tf32(float f) {
   unsigned u;
   memcpy(&u, &f, 4);
@@ -326,6 +360,13 @@ extern "C" pg_status pg_grid_create_dvr(const int n[3], const double L[3], int d
       pg::set_error("pg_grid_create: kinetic eigenbasis upload failed");
       delete g;
       return PG_OOM;
+    }
+    if (a == 0 && n[1] == m && n[2] == m && m <= 128) {
+      const pg_status s16 = build_q16(g, q, qt, m);
+      if (s16 != PG_OK) {
+        delete g;
+        return s16;
+      }
     }
   }
   if (g->tc_err.alloc(1) != PG_OK || cudaMemset(g->tc_err.p, 0, sizeof(int)) != cudaSuccess) {

@@ -42,4 +42,17 @@ constexpr int kMaxBatchJobs = 16;  // job-table entries of one tensor-core launc
 pg_status hx_mixed_batch(const pg_grid* g, const double* const* v, const double* const* x, double* const* y,
                          const int* nvec, int njobs, cudaStream_t st, bool unit = false);
 
+// The FP16-split kinetic preconditioner (pg_kin_f16.cu): R <- (T - sigma_v)^-1 R
+// for the k contiguous vectors of R, with W1 and W2 k vectors of scratch each;
+// sigma on the device; PG_UNSUPPORTED where the grid does not fit it.
+bool kin_f16_ok(const pg_grid* g);
+void kin_f16_plan_text(const pg_grid* g, char* buf, int len);
+pg_status kin_f16(const pg_grid* g, double* R, double* w1, double* w2, int k, const double* sigma, double floor,
+                  cudaStream_t st);
+
+// The kinetic preconditioner R <- (T - sigma_v)^-1 R in the given arithmetic
+// (pg_davidson.cu), scratch w1 and w2 of k vectors each.
+pg_status kinetic_precondition(const pg_grid* g, double* R, int k, const double* sigma_dev, double* w1, double* w2,
+                               int precision, cudaStream_t st);
+
 }  // namespace pg
