@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     }
   } else if (warp < kIssueWarp) {
     // ------------------------------------------------------------- epilogue
-    const int quarter = warp & 3, half = (warp - kProdWarps) >> 2;
+    const int quarter = warp & 3, part = (warp - kProdWarps) >> 2;  // warps of one lane quarter share its columns
     const bool leader = warp == kProdWarps && lane == 0;
     for (int i = 0;; ++i) {
       const int b = i & ((1 << G.acc_shift) - 1);
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (it.kind == 0) {
         // the x + y sums of the plane, FP32, into the low word of each
         // point's Y slot (the z item of the same points reads them)
-        for (int c = half; c < (G.npy >> 4); c += 2) {
+        for (int c = part; c < (G.npy >> 4); c += kEpiParts) {
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
           if (i0 < G.nx) {
@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
         // Y = V X + (Kxy + Kz): the partial sums add in FP32 and V X joins in
         // one FP64 multiply-add (the FP32 sum converted with integer operations)
         const float* yw = reinterpret_cast<const float*>(y);
-        for (int c = half; c < (G.npz >> 4); c += 2) {
+        for (int c = part; c < (G.npz >> 4); c += kEpiParts) {
           double vv[16], xx[16];
           float w[16];
 #pragma unroll

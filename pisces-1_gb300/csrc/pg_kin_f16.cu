@@ -19,14 +19,17 @@
 // Per item, as the FP16 H*X kernel (pg_hx_f16.cu): the item's rows are copied
 // by the tensor memory accelerator into a staging buffer while the previous
 // item is in flight, the producers scale them by 2^s (the largest |x| into
-// [2^14, 2^15)) and split them into FP16 high parts and remainders, and the
-// first MMA (hi.hi + hi.lo + lo.hi, FP32 in TMEM) contracts one axis.  The
-// epilogue warps read that result from TMEM (one row per lane), multiply by
-// 2^-(tau + 4) (and, in a ZS item, by 1 / D), split it again and write it as
-// the K-major A operand of the second MMA, over the item's operand image
-// (its first MMA has finished).  The second MMA contracts the next axis; the
-// epilogue multiplies by the inverse of the product of the scales (a power of
-// two) and writes FP64.  The factor 2^-4 keeps the intermediate below 2^15:
+// [2^14, 2^15): an XF item's from a pass over its staged values, ZS and XB
+// items' from the largest exponent the previous phase wrote into the
+// vector's W1 or W2) and split them into FP16 high parts and remainders, and
+// the first MMA (hi.hi + hi.lo + lo.hi, FP32 in TMEM) contracts one axis.
+// The epilogue warps read that result from TMEM (one row per lane), multiply
+// by 2^-(tau + 4) (and, in a ZS item, by 1 / D), split it again and write it
+// as the K-major A operand of the second MMA: into a region of its own where
+// shared memory allows (the producers then convert the next item meanwhile),
+// else over the item's operand image.  The second MMA contracts the next
+// axis; the epilogue multiplies by the inverse of the product of the scales
+// (a power of two) and writes FP64.  The factor 2^-4 keeps the intermediate below 2^15:
 // an orthonormal transform grows no entry by more than sqrt(n) < 16, and in a
 // ZS item 2^-ef bounds 1 / |D| <= 1 / floor.
 //
@@ -61,7 +64,9 @@ struct KinGeom {
   uint32_t qf_hi, qf_lo, qb_hi, qb_lo;  // forward (Q^T) and backward (Q) images; the same offsets when Q^T = Q
   uint32_t q_bytes;                     // bytes of one image as copied
   int q_sym;
-  uint32_t op_hi, op_lo;  // the item's operand image, then its second MMA's A image
+  uint32_t op_hi, op_lo;  // the item's operand image
+  uint32_t mid_hi, mid_lo;  // the second MMA's A image: its own region where shared memory allows, else op_*
+  int mid_sep;
   uint32_t stg;           // staging buffer (1024-byte aligned)
   uint32_t reg_xy, reg_z; // bytes of one 16-value-wide box region (rounded to 1024)
   uint32_t acc_cols;      // TMEM columns per accumulator
@@ -85,6 +90,8 @@ struct KinCounters {
   unsigned finished;
   unsigned done_xf[kKinMaxVec];  // XF planes in W1, per vector
   unsigned done_zs[kKinMaxVec];  // ZS tiles in W2, per vector
+  unsigned exp_w1[kKinMaxVec];   // largest FP64 exponent (biased) in W1, per vector
+  unsigned exp_w2[kKinMaxVec];   // the same in W2
 };
 
 }  // namespace pg
@@ -131,7 +138,8 @@ __device__ __forceinline__ void fence_proxy_async_global() {
 // complete, then issue its tensor copies into the staging buffer, completing
 // on bar.  Returns false if the wait gave up.
 __device__ __forceinline__ bool kstage(const KinGeom& G, const KinArgs& A, const KItem& it, KinCounters* cnt,
-                                       unsigned char* smem, uint32_t bar, int lane, volatile int* abort) {
+                                       unsigned char* smem, uint32_t bar, int lane, volatile int* abort,
+                                       int* exp_out) {
   if (it.kind < 0) return true;
   int ok = 1;
   if (lane == 0 && it.kind != kXF) {
@@ -145,6 +153,9 @@ __device__ __forceinline__ bool kstage(const KinGeom& G, const KinArgs& A, const
       }
       __nanosleep(64);
     }
+    // the item's scale comes from the largest exponent of the whole input vector
+    __threadfence();
+    *exp_out = (int)*(it.kind == kZS ? (volatile unsigned*)&cnt->exp_w1[it.u] : (volatile unsigned*)&cnt->exp_w2[it.u]);
   }
   ok = __shfl_sync(0xffffffffu, ok, 0);
   if (!ok) return false;
@@ -220,6 +231,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
   __shared__ unsigned ring[kRing];
   __shared__ int sig[kRing];  // item scale exponents, by ticket slot
   __shared__ int s_emax[kProdWarps];
+  __shared__ int s_vexp[kRing];  // ZS and XB items: largest exponent of the input vector, by ticket slot
   __shared__ float s_d[3][kTile];  // eigenvalues per axis, zero past n
   __shared__ int s_abort, s_prod_ok, s_epi_ok, s_last, s_stg_issued;
   volatile int* abort = &s_abort;
@@ -282,7 +294,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     const unsigned char* stg = smem + G.stg;
     if (warp == 0) {
       const KItem it0 = kdecode(ring[0], nvec, G.nz, G.nzt, G.lag);
-      const bool ok = kstage(G, A, it0, cnt, smem, bar_stg, lane, abort);
+      const bool ok = kstage(G, A, it0, cnt, smem, bar_stg, lane, abort, &s_vexp[0]);
       if (lane == 0) {
         if (!ok) *abort = 1;
         else if (it0.kind >= 0) s_stg_issued = 1;
@@ -310,9 +322,11 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       if (!s_prod_ok) break;
       const int ck = it.kind == kZS ? 1 : 0;  // conversion tasks: z tile or plane
       const int ntask = ck == 0 ? (G.kx >> 3) * G.npy : 16 * G.kz;
-      int em = max_exponent(stg, ntask, ck, G, ptid);
-      em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
-      if (lane == 0) s_emax[warp] = em;
+      if (it.kind == kXF) {  // the item's scale: its largest exponent over the producers
+        int em = max_exponent(stg, ntask, ck, G, ptid);
+        em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
+        if (lane == 0) s_emax[warp] = em;
+      }
       // the image is free once the previous item's second MMA is done
       if (ptid == 0) {
         const int ok = i == 0 || mbar_wait_or_abort(smem_u32(&mbar_empty), (uint32_t)((i - 1) & 1), abort);
@@ -322,8 +336,12 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       named_sync(1, kProdWarps * 32);
       if (!s_prod_ok) break;
       int emax = 0;
+      if (it.kind == kXF) {
 #pragma unroll
-      for (int w = 0; w < kProdWarps; ++w) emax = s_emax[w] > emax ? s_emax[w] : emax;
+        for (int w = 0; w < kProdWarps; ++w) emax = s_emax[w] > emax ? s_emax[w] : emax;
+      } else {
+        emax = s_vexp[i % kRing];
+      }
       // largest |x| < 2^(emax - 1022): scaled below 2^15; the factors of both
       // epilogues, 2^-(s + tau - 4 [- ef]), stay normal FP32 numbers
       int s = (emax == 0 || emax == 0x7ff) ? 0 : 1037 - emax;
@@ -365,7 +383,7 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       mbar_arrive(smem_u32(&mbar_full));
       if (warp == 0) {
         const KItem nx_it = kdecode(ring[(i + 1) % kRing], nvec, G.nz, G.nzt, G.lag);
-        const bool ok = kstage(G, A, nx_it, cnt, smem, bar_stg, lane, abort);
+        const bool ok = kstage(G, A, nx_it, cnt, smem, bar_stg, lane, abort, &s_vexp[(i + 1) % kRing]);
         if (lane == 0) {
           if (!ok) *abort = 1;
           else if (nx_it.kind >= 0) s_stg_issued = i + 2;
@@ -374,11 +392,11 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     }
   } else if (warp < kIssueWarp) {
     // ------------------------------------------------------------- epilogue
-    const int quarter = warp & 3, half = (warp - kProdWarps) >> 2;
+    const int quarter = warp & 3, part = (warp - kProdWarps) >> 2;  // warps of one lane quarter share its columns
     const bool leader = warp == kProdWarps && lane == 0;
     const int r = 32 * quarter + lane;  // TMEM lane: x index (planes) or line of the tile
-    unsigned char* mhi = smem + G.op_hi;
-    unsigned char* mlo = smem + G.op_lo;
+    unsigned char* mhi = smem + G.mid_hi;
+    unsigned char* mlo = smem + G.mid_lo;
     for (int i = 0;; ++i) {
       const int b = i & ((1 << G.acc_shift) - 1);
       const KItem it = kdecode(ring[i % kRing], nvec, G.nz, G.nzt, G.lag);
@@ -408,16 +426,16 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
         }
         const float f = exp2i(-(G.tau + 4 + (zs ? G.ef : 0)));
         const uint32_t row = (uint32_t)(r >> 3) * (uint32_t)kq * 128u + (uint32_t)(r & 7) * 16u;
-        for (int c = half; c < (ncol >> 4); c += 2) {
+        for (int c = part; c < (ncol >> 4); c += kEpiParts) {
           float d[16];
           tmem_ld16(acc + (uint32_t)(16 * c), d);
 #pragma unroll
           for (int q = 0; q < 16; ++q) {
             float a = valid ? d[q] * f : 0.f;
-            if (zs) {
+            if (zs) {  // the diagonal in FP32 (it sets the convergence rate only)
               float den = (dxy + s_d[2][16 * c + q]) - sg;
               if (fabsf(den) < G.floor) den = den < 0.f ? -G.floor : G.floor;
-              a = a * (1.0f / den);
+              a = __fdividef(a, den);
             }
             d[q] = a;
           }
@@ -437,40 +455,60 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
       named_sync(2, kEpiWarps * 32);
       if (!s_epi_ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // ---- second result -> FP64
+      // ---- second result -> FP64, and the largest FP64 exponent written
+      // (W1 and W2: the scale of the next phase's items)
       {
         const float unscale = exp2i(-(s + G.tau - 4 - (zs ? G.ef : 0)));
+        uint32_t em = 0;
+        auto track = [&em](float v) {
+          const uint32_t e = (__float_as_uint(v) >> 23) & 0xffu;
+          const uint32_t e64 = e == 0 ? 0u : (e == 255 ? 0x7ffu : e + 896u);
+          em = e64 > em ? e64 : em;
+        };
         if (zs) {
           const long p = (long)it.idx * kTile + r;
           double* out = A.w2 + (long)it.u * nxny * G.nz;
-          for (int c = half; c < (G.npz >> 4); c += 2) {
+          for (int c = part; c < (G.npz >> 4); c += kEpiParts) {
             float d[16];
             tmem_ld16(acc + (uint32_t)(16 * c), d);
             if (p < nxny) {
 #pragma unroll
               for (int q = 0; q < 16; ++q) {
                 const int k = 16 * c + q;
-                if (k < G.nz) out[p + nxny * k] = f32_to_f64(d[q] * unscale);
+                if (k < G.nz) {
+                  const float v = d[q] * unscale;
+                  track(v);
+                  out[p + nxny * k] = f32_to_f64(v);
+                }
               }
             }
           }
         } else {
           double* out = (it.kind == kXF ? A.w1 : A.r) + (long)it.u * nxny * G.nz + nxny * it.idx;
-          for (int c = half; c < (G.npy >> 4); c += 2) {
+          for (int c = part; c < (G.npy >> 4); c += kEpiParts) {
             float d[16];
             tmem_ld16(acc + (uint32_t)(16 * c), d);
             if (r < G.nx) {
 #pragma unroll
               for (int q = 0; q < 16; ++q) {
                 const int j = 16 * c + q;
-                if (j < G.ny) out[r + (long)G.nx * j] = f32_to_f64(d[q] * unscale);
+                if (j < G.ny) {
+                  const float v = d[q] * unscale;
+                  track(v);
+                  out[r + (long)G.nx * j] = f32_to_f64(v);
+                }
               }
             }
           }
         }
+        if (it.kind != kXB) {
+          em = __reduce_max_sync(0xffffffffu, em);
+          if (lane == 0 && em > 0) atomicMax(zs ? &cnt->exp_w2[it.u] : &cnt->exp_w1[it.u], em);
+        }
       }
-      // W1 and W2 are read next by other CTAs' tensor copies
-      fence_proxy_async_global();
+      // W1 and W2 are read next by other CTAs' tensor copies: released by the
+      // leader's fence and counter below, acquired (with a proxy fence before
+      // the copies) in kstage
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       named_sync(2, kEpiWarps * 32);
       if (leader) {
@@ -498,8 +536,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     // z tile (MN-major A): LBO = next 8 planes, SBO = next 8 points
     const uint64_t d_zh = smem_desc(sb + G.op_hi, 16 * 128, 128), d_zl = smem_desc(sb + G.op_lo, 16 * 128, 128);
     // the second A image: K-major, 128 rows
-    const uint64_t d_mxh = smem_desc(sb + G.op_hi, 128, kq_y), d_mxl = smem_desc(sb + G.op_lo, 128, kq_y);
-    const uint64_t d_mzh = smem_desc(sb + G.op_hi, 128, kq_z), d_mzl = smem_desc(sb + G.op_lo, 128, kq_z);
+    const uint64_t d_mxh = smem_desc(sb + G.mid_hi, 128, kq_y), d_mxl = smem_desc(sb + G.mid_lo, 128, kq_y);
+    const uint64_t d_mzh = smem_desc(sb + G.mid_hi, 128, kq_z), d_mzl = smem_desc(sb + G.mid_lo, 128, kq_z);
     // the eigenbasis as a B operand (rows = output index, K = input index)
     const uint64_t d_qfyh = smem_desc(sb + G.qf_hi, 128, kq_y), d_qfyl = smem_desc(sb + G.qf_lo, 128, kq_y);
     const uint64_t d_qbyh = smem_desc(sb + G.qb_hi, 128, kq_y), d_qbyl = smem_desc(sb + G.qb_lo, 128, kq_y);
@@ -540,6 +578,11 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
           mma_f16(acc, d_zh + oa, d_qfzh + ob, id_z1, 1u);
         }
       }
+      // with its own region for the second A image, the operand image is free
+      // for the next item once the first MMA has read it
+      if (G.mid_sep)
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(&mbar_empty)));
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(&mbar_acc_full[b])));
       mbar_arrive(smem_u32(&mbar_acc_full[b]));
@@ -565,13 +608,14 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
           mma_f16(acc, d_mzh + o, d_qbzh + o, id_z2, 1u);
         }
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-          smem_u32(&mbar_empty)));
+      if (!G.mid_sep)
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+            smem_u32(&mbar_empty)));
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(&mbar_acc_full[b])));
       mbar_arrive(smem_u32(&mbar_acc_full[b]));
-      last_bar = smem_u32(&mbar_empty);
-      last_parity = (uint32_t)(i & 1);
+      last_bar = smem_u32(&mbar_acc_full[b]);
+      last_parity = 1;
     }
     if (!ok) {
       *abort = 1;
@@ -597,6 +641,8 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
     for (int u = tid; u < nvec; u += kThreadsAll) {
       cnt->done_xf[u] = 0;
       cnt->done_zs[u] = 0;
+      cnt->exp_w1[u] = 0;
+      cnt->exp_w2[u] = 0;
     }
     if (tid == 0) {
       cnt->ticket = 0;
@@ -691,10 +737,25 @@ KinPlan plan_kin(const pg_grid* g) {
   cur += op;
   G.op_lo = cur;
   cur += op;
-  G.stg = (cur + 1023u) / 1024u * 1024u;
   G.reg_xy = (uint32_t)(128 * ny + 1023) / 1024u * 1024u;
   G.reg_z = (uint32_t)(128 * nz + 1023) / 1024u * 1024u;
-  cur = G.stg + std::max((uint32_t)((nx + 15) / 16) * G.reg_xy, (uint32_t)(kTile / 16) * G.reg_z);
+  const uint32_t stg_bytes = std::max((uint32_t)((nx + 15) / 16) * G.reg_xy, (uint32_t)(kTile / 16) * G.reg_z);
+  // the second A image (128 rows): in a region of its own if that fits, so
+  // that the producers convert the next item while the second MMA runs
+  const uint32_t mid = (uint32_t)kTile * (uint32_t)std::max(G.ky, G.kz) * 2u;
+  const uint32_t sep_end = (cur + 2 * mid + 1023u) / 1024u * 1024u + stg_bytes;
+  G.mid_sep = (long)sep_end <= (long)g_kin_max_dyn ? 1 : 0;
+  if (G.mid_sep) {
+    G.mid_hi = cur;
+    cur += mid;
+    G.mid_lo = cur;
+    cur += mid;
+  } else {
+    G.mid_hi = G.op_hi;
+    G.mid_lo = G.op_lo;
+  }
+  G.stg = (cur + 1023u) / 1024u * 1024u;
+  cur = G.stg + stg_bytes;
   P.smem = cur;
   if ((long)P.smem > (long)g_kin_max_dyn) return no("images and staging exceed shared memory");
   uint32_t cols = 32;
@@ -744,9 +805,10 @@ void kin_f16_plan_text(const pg_grid* g, char* buf, int len) {
     return;
   }
   snprintf(buf, (size_t)len,
-           "FP16 split (k_kin_f16): XF planes, ZS tiles of 128 lines (%d per vector), XB planes, lag %d, "
-           "%zu B shared memory, %u TMEM columns x %d, %d CTAs",
-           P.G.nzt, P.G.lag, P.smem, P.G.acc_cols, 1 << P.G.acc_shift, g_kin_sms);
+           "FP16 split (k_kin_f16): XF planes, ZS tiles of 128 lines (%d per vector), XB planes, lag 3 steps "
+           "(1 for one or two vectors), intermediate image %s, %zu B shared memory, %u TMEM columns x %d, %d CTAs",
+           P.G.nzt, P.G.mid_sep ? "separate" : "over the operand image", P.smem, P.G.acc_cols,
+           1 << P.G.acc_shift, g_kin_sms);
 }
 
 // R <- (T - sigma_v)^-1 R for the k vectors of R (contiguous, 16-byte
@@ -784,6 +846,10 @@ pg_status kin_f16(const pg_grid* g, double* R, double* w1, double* w2, int k, co
     A.sigma = sigma + v0;
     for (int a = 0; a < 3; ++a) A.d[a] = g->d_dev[a].p;
     P.G.nvec = nb;
+    // steps between a vector's phases: three keep enough independent planes
+    // in flight that ZS and XB items seldom wait (measured at 48-96 points,
+    // 2-8 vectors); with one or two vectors the order matters little
+    P.G.lag = nb >= 3 ? 3 : 1;
     const long items = (long)nb * (2 * P.G.nz + P.G.nzt);
     const int grid = (int)std::min<long>(items, g_kin_sms);
     const unsigned short* qbh = g->q16_sym ? g->q16f_hi.p : g->q16b_hi.p;

@@ -4,8 +4,9 @@
 // the conversion tasks that turn staged rows into core-matrix images.
 //
 // Warp roles of a CTA: kProdWarps producer warps (operand conversion; warp 0
-// also issues the tensor copies), kEpiWarps epilogue warps (two per TMEM lane
-// quarter), one issuer warp whose lane 0 launches the MMAs.
+// also issues the tensor copies), kEpiWarps epilogue warps (kEpiParts per
+// TMEM lane quarter, each taking every kEpiParts-th block of 16 columns), one
+// issuer warp whose lane 0 launches the MMAs.
 //
 // Staged rows: an xy item's plane arrives as ceil(nx / 16) box regions of ny
 // rows of 16 doubles, a z item's 128 grid lines as eight box regions of nz
@@ -34,6 +35,8 @@ namespace {
 constexpr int kTile = 128;  // MMA M: TMEM lanes, z-tile points
 constexpr int kProdWarps = 7;
 constexpr int kEpiWarps = 8;
+constexpr int kEpiParts = kEpiWarps / 4;  // epilogue warps per TMEM lane quarter
+static_assert(kEpiWarps % 4 == 0, "the epilogue covers the four TMEM lane quarters evenly");
 constexpr int kIssueWarp = kProdWarps + kEpiWarps;
 constexpr int kThreadsAll = (kIssueWarp + 1) * 32;
 constexpr int kRing = 8;  // tickets in flight in one CTA
