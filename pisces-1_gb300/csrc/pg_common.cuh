@@ -234,6 +234,14 @@ struct pg_grid {
   int hx_lag = 0, hx_ctas = 0, hx_form = 0;  // overrides of the tuned launch parameters (0: tuned)
   mutable std::mutex fused_m;
   mutable std::map<unsigned long long, std::unique_ptr<pg::DevBuf<unsigned>>> fused_cnt;
+  // tensor maps of the FP16 kernels' vector blocks by (address, vectors): a
+  // map depends only on those and the grid's shape, so a solve's blocks are
+  // encoded once (under fused_m)
+  struct TensorMapPair {
+    alignas(64) unsigned char xy[128];
+    alignas(64) unsigned char z[128];
+  };
+  mutable std::map<std::pair<const void*, int>, TensorMapPair> tmaps;
 };
 
 namespace pg {

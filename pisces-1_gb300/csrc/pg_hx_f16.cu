@@ -688,7 +688,30 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 // (x, y, plane) tensor with boxes of 16 x ny x 1, and as a 2-D (plane point,
 // plane) tensor with boxes of 16 x nz; FP64, 128-byte swizzle, zeros past
 // the edges.
+static pg_status encode_maps(const pg_grid* g, const double* x, int nvec, CUtensorMap* txy, CUtensorMap* tz);
+
 pg_status encode_job_maps(const pg_grid* g, const double* x, int nvec, CUtensorMap* txy, CUtensorMap* tz) {
+  static_assert(sizeof(CUtensorMap) == sizeof(pg_grid::TensorMapPair::xy), "tensor map size");
+  const std::pair<const void*, int> key(x, nvec);
+  {
+    std::lock_guard<std::mutex> l(g->fused_m);
+    auto it = g->tmaps.find(key);
+    if (it != g->tmaps.end()) {
+      memcpy(txy, it->second.xy, sizeof(CUtensorMap));
+      memcpy(tz, it->second.z, sizeof(CUtensorMap));
+      return PG_OK;
+    }
+  }
+  PG_TRY(encode_maps(g, x, nvec, txy, tz));
+  std::lock_guard<std::mutex> l(g->fused_m);
+  if (g->tmaps.size() >= 4096) g->tmaps.clear();
+  pg_grid::TensorMapPair& e = g->tmaps[key];
+  memcpy(e.xy, txy, sizeof(CUtensorMap));
+  memcpy(e.z, tz, sizeof(CUtensorMap));
+  return PG_OK;
+}
+
+static pg_status encode_maps(const pg_grid* g, const double* x, int nvec, CUtensorMap* txy, CUtensorMap* tz) {
   const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
   if (!enc) {
     set_error("FP16 H*X: cuTensorMapEncodeTiled is not available");
