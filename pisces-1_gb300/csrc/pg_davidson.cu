@@ -702,11 +702,13 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
     memcpy(d->hpin.p + kPinLam, d->sse.data(), sizeof(double) * nroots);
     PG_CUDA_TRY(cudaMemcpyAsync(dV, d->hpin.p + kPinV, sizeof(double) * ms * nroots, cudaMemcpyHostToDevice, st));
     PG_CUDA_TRY(cudaMemcpyAsync(dlam, d->hpin.p + kPinLam, sizeof(double) * nroots, cudaMemcpyHostToDevice, st));
-    PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st, d->dfloat,
-                   d->dfloat ? d->bt.p : nullptr));
-    PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st, d->dfloat,
-                   d->dfloat ? d->zt.p : nullptr));
-    {
+    if (d->dfloat) {
+      // mixed form: both products, the residual and the norms in one pass
+      // over the twins of B and Z (U is not renormalised: |U| = 1 to ~1e-14)
+      PG_TRY(ritz_df(N, d->bt.p, d->zt.p, m, dV, ms, dlam, ritz, res, nroots, usq, d->rs, st));
+    } else {
+      PG_TRY(combine(N, B, m, dV, 1, ms, 1.0, nullptr, nullptr, false, ritz, nroots, usq, d->rs, st));
+      PG_TRY(combine(N, Z, m, dV, 1, ms, 1.0, nullptr, nullptr, false, res, nroots, nullptr, d->rs, st));
       const long chunk = (N + kRedBlocks - 1) / kRedBlocks;
       const int nblk = (int)((N + chunk - 1) / chunk);
 #define PG_RITZ(NRV) \
@@ -720,17 +722,18 @@ extern "C" pg_status pg_davidson_rci(pg_davidson* d, int ndim, int maxsub, int n
 #undef PG_RITZ
       PG_TRY(check_launch("k_ritz_residual"));
     }
-    // |r_r|^2 and |U_r|^2 in one read (rsq and usq both live in dsq)
+    // |r_r|^2 and |U_r|^2 in one read (rsq and usq both live in dsq; the
+    // mixed form's pass leaves |W_r|^2 right after |U_r|^2)
     static_assert(kUsq == 0 && kRsq > kUsq, "dsq layout");
     const auto w1 = std::chrono::steady_clock::now();
     PG_CUDA_TRY(cudaMemcpyAsync(d->hpin.p + kPinHsq, d->dsq.p, sizeof(double) * (kRsq + nroots),
                                 cudaMemcpyDeviceToHost, st));
-    const double* hr = d->hpin.p + kPinHsq + kRsq;
+    const double* hr = d->hpin.p + kPinHsq + (d->dfloat ? kUsq + nroots : kRsq);
     const double* hu = d->hpin.p + kPinHsq + kUsq;
     PG_CUDA_TRY(cudaStreamSynchronize(st));
     d->t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - w1).count();
     for (int r = 0; r < nroots; ++r) {
-      d->residuals[r] = sqrt(hr[r]);
+      d->residuals[r] = d->dfloat ? sqrt(hr[r] / hu[r]) : sqrt(hr[r]);  // |Z v - lambda B v| / |B v|
       if (!std::isfinite(d->residuals[r])) {
         set_error("pg_davidson_rci: non-finite residual norm for root %d", r);
         d->status = 0;

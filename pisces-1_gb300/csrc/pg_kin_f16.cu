@@ -506,9 +506,11 @@ __global__ void __launch_bounds__(kThreadsAll, 1)
           if (lane == 0 && em > 0) atomicMax(zs ? &cnt->exp_w2[it.u] : &cnt->exp_w1[it.u], em);
         }
       }
-      // W1 and W2 are read next by other CTAs' tensor copies: released by the
-      // leader's fence and counter below, acquired (with a proxy fence before
-      // the copies) in kstage
+      // W1 and W2 are read next by other CTAs' tensor copies: every writer
+      // orders its stores before the async proxy, the leader's fence and
+      // counter below release them, kstage acquires them (with a proxy fence
+      // before the copies)
+      if (it.kind != kXB) fence_proxy_async_global();
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       named_sync(2, kEpiWarps * 32);
       if (leader) {

@@ -652,6 +652,144 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
   return PG_OK;  // with sq, the kernel's last block has reduced the norms
 }
 
+// FP32 -> FP64 with integer operations (exact for normal numbers and zero;
+// FP32 subnormals flush to a signed zero; Inf and NaN are kept): keeps the
+// conversion off the FP64 pipe, which retires about two operations per SM
+// per clock on this part.
+__device__ __forceinline__ double f32_to_f64_int(float v) {
+  const uint32_t u = __float_as_uint(v);
+  const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xffu, mt = u & 0x7fffffu;
+  uint32_t hi = sign | ((e + 896u) << 20) | (mt >> 3);
+  uint32_t lo = mt << 29;
+  hi = e == 0 ? sign : hi;
+  lo = e == 0 ? 0u : lo;
+  hi = e == 255 ? (sign | 0x7ff00000u | (mt >> 3) | (mt ? 0x80000u : 0u)) : hi;
+  lo = e == 255 ? 0u : lo;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// The Ritz step of the mixed form in one pass: U_r = B v_r and
+// W_r = Z v_r - lambda_r U_r in double-float from the twins of the m rows of
+// B and Z (v_r = column r of V, leading dimension ldv), written as FP64, and
+// |U_r|^2, |W_r|^2 (squares summed in FP32 per thread, in FP64 across threads)
+// reduced by the last block into out[r] and out[nr + r].  Two FP64 additions
+// per output and point (the pairs to FP64); the rest runs on the FP32 pipe.
+template <int NR>
+__global__ void __launch_bounds__(kT, NR <= 4 ? 3 : 2) k_ritz_df(long N, long chunk, const double* Bt, const double* Zt,
+                                                               int m, const double* __restrict__ V, int ldv,
+                                                               const double* __restrict__ lam, double* U, double* W,
+                                                               int nr, double* __restrict__ partial, double* out,
+                                                               unsigned* counter) {
+  pdl_wait();
+  pdl_release();
+  extern __shared__ float smf[];
+  float* Ch = smf;  // m x nr
+  float* Cl = smf + m * nr;
+  __shared__ float nlh[NR], nll[NR];
+  __shared__ double red[kT / 32][2 * NR];
+  for (int e = threadIdx.x; e < m * nr; e += kT) {
+    float h, l;
+    df_split(V[(long)(e / nr) + (long)(e % nr) * ldv], h, l);
+    Ch[e] = h;
+    Cl[e] = l;
+  }
+  if (threadIdx.x < nr) {
+    float h, l;
+    df_split(-lam[threadIdx.x], h, l);
+    nlh[threadIdx.x] = h;
+    nll[threadIdx.x] = l;
+  }
+  __syncthreads();
+  float su[NR], sw[NR];  // about one point per thread: FP32 sums of the squares
+#pragma unroll
+  for (int r = 0; r < NR; ++r) su[r] = sw[r] = 0.f;
+  const long g_begin = blockIdx.x * chunk;
+  const long g_end = g_begin + chunk < N ? g_begin + chunk : N;
+  for (long g = g_begin + threadIdx.x; g < g_end; g += kT) {
+    float uh[NR], ul[NR], zh[NR], zl[NR];
+#pragma unroll
+    for (int r = 0; r < NR; ++r) uh[r] = ul[r] = zh[r] = zl[r] = 0.f;
+    for (int a0 = 0; a0 < m; a0 += kBatch / 2) {
+      double pb[kBatch / 2], pz[kBatch / 2];
+#pragma unroll
+      for (int u = 0; u < kBatch / 2; ++u) {
+        pb[u] = a0 + u < m ? Bt[(long)(a0 + u) * N + g] : 0.0;
+        pz[u] = a0 + u < m ? Zt[(long)(a0 + u) * N + g] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < kBatch / 2; ++u) {
+        if (a0 + u >= m) break;
+        // the 8 bytes are a float2 (hi, lo): hi in the low word
+        const float bh = __int_as_float(__double2loint(pb[u])), bl = __int_as_float(__double2hiint(pb[u]));
+        const float qh = __int_as_float(__double2loint(pz[u])), ql = __int_as_float(__double2hiint(pz[u]));
+        const float* ch = Ch + (a0 + u) * nr;
+        const float* cl = Cl + (a0 + u) * nr;
+#pragma unroll
+        for (int r = 0; r < NR; ++r)
+          if (r < nr) {
+            df_fma(uh[r], ul[r], bh, bl, ch[r], cl[r]);
+            df_fma(zh[r], zl[r], qh, ql, ch[r], cl[r]);
+          }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < NR; ++r)
+      if (r < nr) {
+        df_fma(zh[r], zl[r], nlh[r], nll[r], uh[r], ul[r]);  // W = Z v - lambda U
+        const double u = f32_to_f64_int(uh[r]) + f32_to_f64_int(ul[r]);
+        const double w = f32_to_f64_int(zh[r]) + f32_to_f64_int(zl[r]);
+        U[(long)r * N + g] = u;
+        W[(long)r * N + g] = w;
+        // the pair's sum in FP32 (after the cancellation in W its low part
+        // need not be small against its high part), then its square
+        const float uf = uh[r] + ul[r], wf = zh[r] + zl[r];
+        su[r] = fmaf(uf, uf, su[r]);
+        sw[r] = fmaf(wf, wf, sw[r]);
+      }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int r = 0; r < NR; ++r) {
+    double a = (double)su[r], b = (double)sw[r];
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      red[warp][r] = a;
+      red[warp][NR + r] = b;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * nr) {
+    const int o = threadIdx.x < nr ? threadIdx.x : NR + threadIdx.x - nr;
+    double t = 0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w][o];
+    partial[(long)blockIdx.x * 2 * nr + threadIdx.x] = t;
+  }
+  reduce_in_last_block(partial, 2 * nr, out, 0, counter);
+}
+
+pg_status ritz_df(long N, const double* Bt, const double* Zt, int m, const double* V, int ldv, const double* lam,
+                  double* U, double* W, int nr, double* sq, RedScratch& rs, cudaStream_t st) {
+  PG_ARG(m > 0 && nr > 0 && nr <= kMaxCombine && m * nr <= 128 * kMaxCombine && Bt && Zt,
+         "ritz_df: bad sizes m=%d nr=%d", m, nr);
+  PG_TRY(rs.ensure());
+  const long chunk = chunk_for(N, kStreamBlocks, kT);
+  const int blocks = (int)((N + chunk - 1) / chunk);
+  const size_t smem = sizeof(float) * 2 * (size_t)m * nr;
+#define PG_RITZ_DF(NRV)                                                                                           \
+  PG_CUDA_TRY(launch_dependent(k_ritz_df<NRV>, dim3(blocks), dim3(kT), smem, st, N, chunk, Bt, Zt, m, V, ldv, lam, U, \
+                               W, nr, rs.partial.p, sq, rs.counter.p))
+  if (nr <= 1) PG_RITZ_DF(1);
+  else if (nr <= 2) PG_RITZ_DF(2);
+  else if (nr <= 4) PG_RITZ_DF(4);
+  else if (nr <= 8) PG_RITZ_DF(8);
+  else PG_RITZ_DF(16);
+#undef PG_RITZ_DF
+  return check_launch("k_ritz_df");
+}
+
 pg_status split_twin(long count, const double* x, double* t, cudaStream_t st, double* copy) {
   if (count <= 0) return PG_OK;
   const long b = (count + kT - 1) / kT;

@@ -90,4 +90,12 @@ pg_status combine(long N, const double* P, int na, const double* C, int ca, int 
 // with copy (not overlapping x), also copy[i] = x[i] in the same pass.
 pg_status split_twin(long count, const double* x, double* t, cudaStream_t st, double* copy = nullptr);
 
+// The Ritz step of the mixed form in one pass: U_r = B v_r and
+// W_r = Z v_r - lambda_r U_r (r < nr) from the double-float twins Bt, Zt of
+// the first m rows of B and Z, v_r = V[r*ldv ...] (device), lambda on the
+// device; sq[r] = |U_r|^2 and sq[nr + r] = |W_r|^2.  U is not renormalised:
+// with B orthonormal to double-float precision |U_r| = 1 to ~1e-14.
+pg_status ritz_df(long N, const double* Bt, const double* Zt, int m, const double* V, int ldv, const double* lam,
+                  double* U, double* W, int nr, double* sq, RedScratch& rs, cudaStream_t st);
+
 }  // namespace pg
