@@ -750,11 +750,16 @@ __global__ void __launch_bounds__(kT, NR <= 4 ? 3 : 2) k_ritz_df(long N, long ch
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int r = 0; r < NR; ++r) {
-    double a = (double)su[r], b = (double)sw[r];
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_down_sync(0xffffffffu, a, o);
-      b += __shfl_down_sync(0xffffffffu, b, o);
+    // sums of 16 lanes in FP32 (2^-22 relative at most), the last step and
+    // everything after it in FP64: few operations on the FP64 pipe
+    float af = su[r], bf = sw[r];
+    for (int o = 16; o > 1; o >>= 1) {
+      af += __shfl_down_sync(0xffffffffu, af, o);
+      bf += __shfl_down_sync(0xffffffffu, bf, o);
     }
+    double a = f32_to_f64_int(af), b = f32_to_f64_int(bf);
+    a += __shfl_down_sync(0xffffffffu, a, 1);
+    b += __shfl_down_sync(0xffffffffu, b, 1);
     if (lane == 0) {
       red[warp][r] = a;
       red[warp][NR + r] = b;
