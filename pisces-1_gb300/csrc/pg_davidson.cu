@@ -295,7 +295,7 @@ namespace pg {
 namespace {
 
 // Device scalars of one Davidson handle (offsets into pg_davidson::dsq).
-constexpr int kUsq = 0;     // |U_r|^2 and 1/|U_r| (2 x 16)
+constexpr int kUsq = 0;     // |U_r|^2 and 1/|U_r| (2 x 16); mixed form: |U_r|^2 and |W_r|^2 (k_ritz_df)
 constexpr int kLam = 32;    // Ritz values (16)
 constexpr int kRsq = 64;    // |r_r|^2 and 1/|r_r| (2 x 16)
 constexpr int kOnes = 96;   // 1.0 (16), the "keep X" coefficients of combine
