@@ -234,12 +234,13 @@ class Grid:
 
 
 # ------------------------------------------------------------ FFT kinetic path
-# numpy restatement of the reference's DVRType 3 (periodic FFT kinetic term).
-# FFTW is not part of the reference tree, so the reference's own FFT path is
-# not built here; numpy's FFT stands in for FFTW (same unnormalised forward /
-# backward pair up to numpy's 1/N on the inverse).  Parity for this path is
-# therefore against this restatement and analytic spectra, not against a run
-# of the reference.
+# numpy restatement of the reference's DVRType 3 (periodic FFT kinetic term),
+# numpy's FFT standing in for FFTW (the same unnormalised forward / backward
+# pair up to numpy's 1/N on the inverse).  FFTW is not part of the reference
+# tree; the oracle build of the reference links a DFT computed from its
+# definition in its place (oracle/ref/shim/shim.c), so the reference's own
+# DVR::SetupDVR (type 3) and VectorFFT::apply run, and this restatement is
+# pinned against them (tests/golden/fft.npz, test_fft_path_matches_reference_run).
 
 REF_PI = 3.14159265358979  # src/KE_diag.cpp:28-30
 
@@ -375,8 +376,10 @@ def have_reference() -> bool:
 
 def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, maxiter=100, ptol=5, startvec=1,
                   spherical_k=None, matvec_seed=None, fulldiag=False, diagonalize=True, dump_wavefn=True,
-                  threads=None, observables=None, poltype=None, gradient=False, dual=False, rtol=None):
-    """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration."""
+                  threads=None, observables=None, poltype=None, gradient=False, dual=False, rtol=None, fft=False):
+    """Run the reference CPU code (built by oracle/ref/Makefile) on one configuration.
+    fft: the FFT kinetic path instead (DVRType 3 grid, KE_diag, two
+    VectorFFT::apply products on seeded vectors; nothing else runs)."""
     if not have_reference():
         raise FileNotFoundError(REF_BIN)
     os.makedirs(os.path.join(HERE, "_ref", "tmp"), exist_ok=True)
@@ -407,6 +410,8 @@ def run_reference(n, L, waters=None, ions=None, nstates=1, method=2, maxsub=20, 
             lines.append("dual 1")
         if rtol is not None:
             lines.append(f"rtol {float(rtol)!r}")
+        if fft:
+            lines.append("fft 1")
         lines += [f"fulldiag {int(fulldiag)}", f"diagonalize {int(diagonalize)}",
                   f"dump_wavefn {int(dump_wavefn)}", f"out {out}"]
         with open(inp, "w") as f:

@@ -48,6 +48,7 @@
 #include "WriteCubeFile.h"
 #include "ReadCubeFile.h"
 #include "Small2Large.h"
+#include "VectorFFT.hpp"
 
 namespace {
 
@@ -111,6 +112,7 @@ struct Input {
   int gradient = 0;        // 1: the Hellmann-Feynman gradient records (needs poltype 3)
   int dual = 0;            // 1: the dual-grid single point of PotFlag[3] = 6 (coarse solve, then this grid)
   double rtol = 20.0;      // PotPara[10]: distance from every site beyond which V is interpolated
+  int fft = 0;             // 1: the FFT kinetic path (DVRType 3): its grid, KE_diag and VectorFFT::apply products
   std::string out = "out.rec";
 };
 
@@ -134,6 +136,7 @@ Input read_input(const char* path) {
     else if (key == "gradient") { f >> in.gradient; }
     else if (key == "dual") { f >> in.dual; }
     else if (key == "rtol") { f >> in.rtol; }
+    else if (key == "fft") { f >> in.fft; }
     else if (key == "out") { f >> in.out; }
     else { fprintf(stderr, "unknown key %s\n", key.c_str()); exit(2); }
   }
@@ -175,10 +178,49 @@ std::string read_file(const std::string& path) {
 
 }  // namespace
 
+// The FFT kinetic path (DVRType 3): DVR::SetupDVR with type 3 (Tdiag per axis
+// and the KE_diag composition, src/DVR.cpp:64-651, src/KE_diag.cpp:33-80), then
+// VectorFFT::apply (src/VectorFFTW.cpp:14-112, the product davdriver calls for
+// this type, src/davdriver.cpp:48, 72-74) on two seeded vectors with a seeded
+// V.  DVR::ComputeDiagonal is not called: with DVRType 3 the per-axis kinetic
+// arrays hold n values, and it reads them as packed triangles
+// (src/DVR.cpp:1808-1881), past their ends, so the reference's Davidson on this
+// path starts from an undefined diagonal.
+int fft_records(const Input& in) {
+  DVR Hel;
+  int n[3] = {in.n[0], in.n[1], in.n[2]};
+  Hel.SetupDVR(n, 3, 1, in.L, 0);
+  Hel.SetVerbose(0);
+  const int ngp = Hel.ngp;
+  put("n", in.n, 3);
+  put("L", in.L, 3);
+  for (int a = 0; a < 3; ++a) {
+    int off = a == 0 ? 0 : (a == 1 ? Hel.max1db[0] : Hel.max1db[0] + Hel.max1db[1]);
+    put(std::string("x") + char('0' + a), Hel.x_dvr + off, n[a]);
+    put(std::string("ekin") + char('0' + a), Hel.e_kin[a], n[a]);
+  }
+  put("ke_diag", Hel.KE_diag, ngp);
+  unsigned long long s = (unsigned long long)(in.matvec_seed >= 0 ? in.matvec_seed : 1);
+  dVec v(ngp);
+  for (double& t : v) t = next_uniform(s);
+  put("fft_v", v.data(), ngp);
+  VectorFFT engine(n);
+  for (int rep = 0; rep < 2; ++rep) {
+    dVec x(ngp), y(ngp);
+    for (double& t : x) t = next_uniform(s);
+    engine.apply(x.data(), y.data(), v.data(), Hel.KE_diag);
+    put(std::string("fft_x") + char('0' + rep), x.data(), ngp);
+    put(std::string("fft_y") + char('0' + rep), y.data(), ngp);
+  }
+  write_records(in.out);
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 2) { fprintf(stderr, "usage: %s input.txt\n", argv[0]); return 2; }
   Input in = read_input(argv[1]);
   int provided; MPI_Init_thread(&argc, &argv, MPI_THREAD_FUNNELED, &provided);
+  if (in.fft) return fft_records(in);
 
   // Default electron-water model parameters (src/GetInput.cpp:43-63).
   iVec potflag(6);

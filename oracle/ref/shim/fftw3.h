@@ -1,6 +1,6 @@
-/* FFTW3 stand-in for the oracle build.  The sine-DVR path only constructs and
- * destroys plans (the Davidson driver builds an FFT engine it never uses); any
- * attempt to execute a plan aborts, so a silent wrong answer is impossible. */
+/* FFTW3 stand-in for the oracle build: the declarations the reference uses.
+ * shim.c computes the transforms from the definition of the DFT (FFTW itself
+ * is not in the reference tree). */
 #ifndef ORACLE_SHIM_FFTW3_H
 #define ORACLE_SHIM_FFTW3_H
 #include <stdlib.h>

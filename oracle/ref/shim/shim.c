@@ -2,28 +2,140 @@
  * only to build that code as the test oracle:
  *  - BLAS/LAPACK entry points forwarded to the OpenBLAS that ships inside the
  *    installed scipy wheel (its symbols carry a "scipy_" prefix);
- *  - FFTW plan constructors that hand back a dummy plan (the sine-DVR Davidson
- *    driver builds an FFT engine it never executes) and an fftw_execute that
- *    aborts, so the FFT kinetic path can never return a silent wrong answer;
+ *  - FFTW 3 (a third-party library the reference links, absent from its
+ *    tree; its CMake file takes any installed FFTW 3): the plan constructors
+ *    and fftw_execute the reference calls, computing the transforms FFTW
+ *    defines -- the multi-dimensional DFT y[k] = sum_j x[j] e^{s 2 pi i j.k / n}
+ *    (s = -1 forward, +1 backward, unnormalised), row-major arrays, the real
+ *    input (r2c) giving the n_last/2 + 1 non-redundant outputs of the last
+ *    dimension and c2r the real inverse of such a half spectrum -- directly
+ *    from that definition, one axis at a time, in FP64 (O(N sum n) work);
  *  - ARPACK and L-BFGS symbols that abort (neither is on the Davidson path). */
+#include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <stddef.h>
+#include <string.h>
 
 typedef double fftw_complex[2];
-typedef struct oracle_fftw_plan_s* fftw_plan;
-static int dummy_plan;
+typedef struct oracle_fftw_plan_s {
+  int kind;  /* 0 c2c, 1 r2c, 2 c2r */
+  int n[3];  /* leading dimensions padded with 1 */
+  int sign;
+  void* in;
+  void* out;
+}* fftw_plan;
 static void die(const char* what) { fprintf(stderr, "oracle shim: %s is not available in the oracle build\n", what); abort(); }
 void* fftw_malloc(size_t n) { return malloc(n); }
 void fftw_free(void* p) { free(p); }
-fftw_plan fftw_plan_dft_r2c(int r, const int* n, double* i, fftw_complex* o, unsigned f) { (void)r; (void)n; (void)i; (void)o; (void)f; return (fftw_plan)&dummy_plan; }
-fftw_plan fftw_plan_dft_c2r(int r, const int* n, fftw_complex* i, double* o, unsigned f) { (void)r; (void)n; (void)i; (void)o; (void)f; return (fftw_plan)&dummy_plan; }
-fftw_plan fftw_plan_dft(int r, const int* n, fftw_complex* i, fftw_complex* o, int s, unsigned f) { (void)r; (void)n; (void)i; (void)o; (void)s; (void)f; return (fftw_plan)&dummy_plan; }
-fftw_plan fftw_plan_dft_r2c_3d(int a, int b, int c, double* i, fftw_complex* o, unsigned f) { (void)a; (void)b; (void)c; (void)i; (void)o; (void)f; return (fftw_plan)&dummy_plan; }
-fftw_plan fftw_plan_dft_c2r_3d(int a, int b, int c, fftw_complex* i, double* o, unsigned f) { (void)a; (void)b; (void)c; (void)i; (void)o; (void)f; return (fftw_plan)&dummy_plan; }
-fftw_plan fftw_plan_dft_3d(int a, int b, int c, fftw_complex* i, fftw_complex* o, int s, unsigned f) { (void)a; (void)b; (void)c; (void)i; (void)o; (void)s; (void)f; return (fftw_plan)&dummy_plan; }
-void fftw_execute(const fftw_plan p) { (void)p; die("fftw_execute"); }
-void fftw_destroy_plan(fftw_plan p) { (void)p; }
+
+static fftw_plan make_plan(int kind, int rank, const int* n, void* in, void* out, int sign) {
+  if (rank < 1 || rank > 3) die("a transform of rank other than 1-3");
+  fftw_plan p = (fftw_plan)malloc(sizeof(*p));
+  if (!p) die("plan allocation");
+  p->kind = kind;
+  p->n[0] = p->n[1] = p->n[2] = 1;
+  for (int a = 0; a < rank; ++a) p->n[3 - rank + a] = n[a];
+  p->sign = sign;
+  p->in = in;
+  p->out = out;
+  return p;
+}
+fftw_plan fftw_plan_dft_r2c(int r, const int* n, double* i, fftw_complex* o, unsigned f) { (void)f; return make_plan(1, r, n, i, o, -1); }
+fftw_plan fftw_plan_dft_c2r(int r, const int* n, fftw_complex* i, double* o, unsigned f) { (void)f; return make_plan(2, r, n, i, o, +1); }
+fftw_plan fftw_plan_dft(int r, const int* n, fftw_complex* i, fftw_complex* o, int s, unsigned f) { (void)f; return make_plan(0, r, n, i, o, s); }
+fftw_plan fftw_plan_dft_r2c_3d(int a, int b, int c, double* i, fftw_complex* o, unsigned f) { const int n[3] = {a, b, c}; return fftw_plan_dft_r2c(3, n, i, o, f); }
+fftw_plan fftw_plan_dft_c2r_3d(int a, int b, int c, fftw_complex* i, double* o, unsigned f) { const int n[3] = {a, b, c}; return fftw_plan_dft_c2r(3, n, i, o, f); }
+fftw_plan fftw_plan_dft_3d(int a, int b, int c, fftw_complex* i, fftw_complex* o, int s, unsigned f) { const int n[3] = {a, b, c}; return fftw_plan_dft(3, n, i, o, s, f); }
+
+/* In-place DFT of the complex array z[n0][n1][n2] along axis ax, sign s:
+ * the twiddles e^{s 2 pi i m / n} for m = j k mod n (exact arguments). */
+static void dft_axis(double* z, const int* n, int ax, int s) {
+  const int len = n[ax];
+  const long stride = ax == 2 ? 1 : (ax == 1 ? n[2] : (long)n[1] * n[2]);
+  const long count = (long)n[0] * n[1] * n[2] / len;
+  double* cw = (double*)malloc(sizeof(double) * 2 * len);
+  double* buf = (double*)malloc(sizeof(double) * 2 * len);
+  if (!cw || !buf) die("DFT scratch");
+  const double pi = 3.14159265358979323846;
+  for (int m = 0; m < len; ++m) {
+    cw[2 * m] = cos(2.0 * pi * m / len);
+    cw[2 * m + 1] = s * sin(2.0 * pi * m / len);
+  }
+  for (long line = 0; line < count; ++line) {
+    /* the line's first element: all index combinations of the other axes */
+    long base;
+    if (ax == 2) base = line * len;
+    else if (ax == 1) base = (line / n[2]) * (long)n[1] * n[2] + line % n[2];
+    else base = line;
+    for (int k = 0; k < len; ++k) {
+      double re = 0, im = 0;
+      for (int j = 0; j < len; ++j) {
+        const int m = (int)(((long)j * k) % len);
+        const double xr = z[2 * (base + j * stride)], xi = z[2 * (base + j * stride) + 1];
+        re += xr * cw[2 * m] - xi * cw[2 * m + 1];
+        im += xr * cw[2 * m + 1] + xi * cw[2 * m];
+      }
+      buf[2 * k] = re;
+      buf[2 * k + 1] = im;
+    }
+    for (int k = 0; k < len; ++k) {
+      z[2 * (base + k * stride)] = buf[2 * k];
+      z[2 * (base + k * stride) + 1] = buf[2 * k + 1];
+    }
+  }
+  free(cw);
+  free(buf);
+}
+
+void fftw_execute(const fftw_plan p) {
+  const int n0 = p->n[0], n1 = p->n[1], n2 = p->n[2], nh = n2 / 2 + 1;
+  const long N = (long)n0 * n1 * n2;
+  double* z = (double*)calloc((size_t)(2 * N), sizeof(double));
+  if (!z) die("DFT array");
+  if (p->kind == 0) {
+    memcpy(z, p->in, sizeof(double) * 2 * N);
+  } else if (p->kind == 1) {
+    const double* x = (const double*)p->in;
+    for (long g = 0; g < N; ++g) z[2 * g] = x[g];
+  } else {
+    /* the full spectrum from its half: X[k] = conj(X[-k]) for k2 > n2/2 */
+    const double* h = (const double*)p->in;
+    for (int a = 0; a < n0; ++a)
+      for (int b = 0; b < n1; ++b)
+        for (int c = 0; c < n2; ++c) {
+          const long g = ((long)a * n1 + b) * n2 + c;
+          if (c < nh) {
+            const long q = ((long)a * n1 + b) * nh + c;
+            z[2 * g] = h[2 * q];
+            z[2 * g + 1] = h[2 * q + 1];
+          } else {
+            const long q = ((long)((n0 - a) % n0) * n1 + (n1 - b) % n1) * nh + (n2 - c);
+            z[2 * g] = h[2 * q];
+            z[2 * g + 1] = -h[2 * q + 1];
+          }
+        }
+  }
+  for (int ax = 0; ax < 3; ++ax)
+    if (p->n[ax] > 1) dft_axis(z, p->n, ax, p->sign);
+  if (p->kind == 0) {
+    memcpy(p->out, z, sizeof(double) * 2 * N);
+  } else if (p->kind == 1) {
+    double* h = (double*)p->out;
+    for (int a = 0; a < n0; ++a)
+      for (int b = 0; b < n1; ++b)
+        for (int c = 0; c < nh; ++c) {
+          const long g = ((long)a * n1 + b) * n2 + c, q = ((long)a * n1 + b) * nh + c;
+          h[2 * q] = z[2 * g];
+          h[2 * q + 1] = z[2 * g + 1];
+        }
+  } else {
+    double* y = (double*)p->out;
+    for (long g = 0; g < N; ++g) y[g] = z[2 * g];
+  }
+  free(z);
+}
+void fftw_destroy_plan(fftw_plan p) { free(p); }
 int fftw_init_threads(void) { return 1; }
 void fftw_plan_with_nthreads(int n) { (void)n; }
 void fftw_cleanup_threads(void) {}

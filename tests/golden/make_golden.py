@@ -169,6 +169,25 @@ def dual():
     save("dual.npz", **out)
 
 
+def fft():
+    """The FFT kinetic path (DVRType 3): the reference's grid points, Tdiag
+    energies and KE_diag, and two VectorFFT::apply products on seeded vectors
+    with a seeded V, on cubic grids of even and odd size (the reference's
+    KE_diag indexing assumes n0 = n2).  FFTW, which the reference links but
+    does not ship, is replaced in the oracle build by the DFT from its
+    definition (oracle/ref/shim/shim.c)."""
+    out = {}
+    for n, L in [(12, 10.0), (13, 11.0)]:
+        r = oracle.run_reference((n, n, n), (L, L, L), fft=True, matvec_seed=7, diagonalize=False)
+        out[f"L_{n}"] = np.array([L])
+        for a in range(3):
+            out[f"x{a}_{n}"] = r[f"x{a}"]
+            out[f"ekin{a}_{n}"] = r[f"ekin{a}"]
+        for k in ("ke_diag", "fft_v", "fft_x0", "fft_y0", "fft_x1", "fft_y1"):
+            out[f"{k}_{n}"] = r[k]
+    save("fft.npz", **out)
+
+
 def c2():
     # (H2O)24, 9 A sphere, 64^3 over 40 bohr, 4 states, residual 1e-8.  With
     # the default 20-vector subspace the reference stalls on four roots (its
@@ -194,7 +213,7 @@ if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("build the reference first: make -C oracle/ref")
     jobs = {"kinetic": kinetic, "dpp": dpp_and_small, "c1": c1, "ions": ions_small, "analytic": analytic,
-            "observables": observables, "scpol": scpol, "dual": dual}
+            "observables": observables, "scpol": scpol, "dual": dual, "fft": fft}
     if a.c2:
         jobs["c2"] = c2
     for name, fn in jobs.items():

@@ -161,6 +161,32 @@ def test_fft_kinetic_builder_matches_tdiag_restatement(orc, pg):
         assert np.max(np.abs(t - cols)) <= 1e-13 * np.max(np.abs(t))
 
 
+@pytest.mark.parametrize("n", [12, 13])
+def test_fft_path_matches_reference_run(orc, pg, n):
+    """The FFT kinetic path against the reference run (fft.npz: DVR::SetupDVR
+    with DVRType 3 and VectorFFT::apply on seeded vectors, cubic grids of even
+    and odd size, FFTW replaced by the DFT from its definition in the oracle
+    build): the restated grid points, Tdiag energies and KE_diag bit for bit,
+    the library's host builder's points and energies likewise, and the
+    restated VectorFFT::apply within 1e-14 of the largest |y| (the transforms
+    sum in another order)."""
+    g = golden("fft.npz")
+    L = float(g[f"L_{n}"][0])
+    for a in range(3):
+        xo, eo = orc.fft_tdiag(n, 1.0, -0.5 * L, 0.5 * L)
+        assert np.array_equal(xo, g[f"x{a}_{n}"])
+        assert np.array_equal(eo, g[f"ekin{a}_{n}"])
+        x, e, _ = pg.fft_kinetic(n, L)
+        assert np.array_equal(x, g[f"x{a}_{n}"])
+        assert np.array_equal(e, g[f"ekin{a}_{n}"])
+    ke = orc.fft_ke_diag((n, n, n), (L, L, L))
+    assert np.array_equal(ke, g[f"ke_diag_{n}"])
+    for rep in range(2):
+        y = orc.fft_apply(g[f"fft_x{rep}_{n}"], g[f"fft_v_{n}"], (n, n, n), ke)
+        ref = g[f"fft_y{rep}_{n}"]
+        assert np.max(np.abs(y - ref)) <= 1e-14 * np.max(np.abs(ref))
+
+
 def test_fft_apply_is_three_axis_circulants(orc, pg):
     """The reference's 3-D FFT matvec equals V x plus the per-axis circulant
     contractions (cubic grid, where the reference's KE_diag indexing is
