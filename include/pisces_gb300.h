@@ -360,7 +360,7 @@ pg_status pg_davidson_set_preconditioner(pg_davidson* d, const pg_grid* g, int p
  * forward transform + diagonal + z backward transform of 128-line tiles, xy
  * backward transforms), else six split-TF32 axis passes.  Allocates 2 k N
  * doubles of scratch and synchronises the stream.  No reference counterpart
- * (the builder's corrflag 3). */
+ * (corrflag 3 is this library's own). */
 pg_status pg_kinetic_precondition(const pg_grid* g, double* R, int k, const double* sigma, int precision,
                                   void* stream);
 /* Mixed-form preconditioner kernel of this grid: 0 automatic (the FP16 kernel
