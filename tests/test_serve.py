@@ -5,7 +5,8 @@ Each request is one ClusterAnion::EnergyFromConfiguration-style single point
 check that
   - a solve's result is the same alone and in a mix of concurrent solves on
     the same and on different grids (bit for bit: merged tensor-core launches
-    compute every column as a launch of its own would);
+    compute every column as a launch of its own would), also with the
+    kinetic preconditioner, whose launches from several solves overlap;
   - the engine's solve equals the single-call path pg_cluster_solve;
   - admission keeps the admitted footprint within the memory budget and
     rejects a request that can never fit;
@@ -75,6 +76,26 @@ def test_alone_equals_in_the_mix(pg, torch, mix, precision):
         assert a["evals"] == b["evals"]
         assert np.array_equal(a["vectors"], b["vectors"])
         assert a["stats"]["n_matvec"] == b["stats"]["n_matvec"]
+
+
+def test_alone_equals_in_the_mix_kinetic_preconditioner(pg, torch, mix):
+    # the mixed form with corrflag 3: every solve runs the FP16-split H*X
+    # (merged across solves) and the FP16 kinetic preconditioner, whose
+    # launches from the eight slots overlap on the device; each solve must
+    # still give the bits it gives alone
+    def reqs():
+        return [pg.Engine.request(grid, L, w, nroots=nr, maxsub=40, maxiter=400, ptol=6, corrflag=3, precision=1,
+                                  want_vectors=True) for (w, grid, L, nr) in mix]
+    alone = [_run(pg, [r], slots=1, warm_start=False)[0][0] for r in reqs()]
+    together, stats = _run(pg, reqs(), slots=8, warm_start=False, batch_window_us=2000)
+    assert stats["peak_in_flight"] > 1
+    assert sum(a["status"] == 0 for a in alone) >= 3, [a["error"] for a in alone]
+    for a, b in zip(alone, together):
+        assert a["status"] == b["status"], (a["error"], b["error"])
+        if a["status"] == 0:
+            assert a["evals"] == b["evals"]
+            assert np.array_equal(a["vectors"], b["vectors"])
+            assert a["stats"]["n_matvec"] == b["stats"]["n_matvec"]
 
 
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
