@@ -255,10 +255,44 @@ def run_ours(args, ws, rank, local):
         e2e_ms = (time.perf_counter() - t0) * 1000 / reps
 
     roof = kernel_rooflines(pg, torch, grid, tables, nroots, precision, stream)
+    try:
+        pot = potential_rate(torch, grid, tables, wl["nw"], stream)
+    except Exception as exc:  # reported, not fatal: the line's own numbers are measured above
+        pot = {"error": str(exc)}
     hx_plan = grid.hx_plan(nroots)
-    return dict(hx_plan=hx_plan, precond_plan=grid.precond_plan(), total_ms=max_ms, lat_ms=lat_ms, evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)),
-                de=de, stats=st, fp64=fp64, refalg=refalg, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d,
-                d2h=d2h, roofline=roof, N=N, precision=args.precision, ptol=ptol)
+    return dict(hx_plan=hx_plan, precond_plan=grid.precond_plan(), total_ms=max_ms, lat_ms=lat_ms,
+                evals=list(map(float, ev)), evals_fp64=list(map(float, ev64)), de=de, stats=st, fp64=fp64,
+                refalg=refalg, clocks=clk, launches=launches, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, roofline=roof,
+                potential=pot, N=N, precision=args.precision, ptol=ptol)
+
+
+# FP64 operations per (grid point, water) pair of k_potential_dpp besides its
+# 4 reciprocal square roots and up to 4 exponentials (charges, induced
+# dipoles, Slater cores, damped polarisation, the per-water distances)
+POTENTIAL_FLOPS_PER_PAIR = 80
+
+
+def potential_rate(torch, grid, tables, nwaters, stream, reps=5):
+    """V(r) alone (k_potential_dpp) on the bench grid: (grid point, water)
+    pairs per second and the FP64 rate they imply, CUDA events on the
+    launching stream after one warm-up call."""
+    sptr = stream.cuda_stream
+    grid.potential(tables, stream=sptr)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        grid.potential(tables, stream=sptr)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / reps
+    pairs = grid.N * nwaters
+    rate = pairs / (ms * 1e-3)
+    return {"kernel": "k_potential_dpp", "bound": "fp64", "ms_per_launch": ms, "pairs": pairs,
+            "pairs_per_s": rate, "fp64_tflops": rate * POTENTIAL_FLOPS_PER_PAIR / 1e12,
+            "flops_per_pair": f"{POTENTIAL_FLOPS_PER_PAIR} FP64 operations besides 4 rsqrt and up to 4 exp",
+            "peak_source": "FP64 pipe of this part, about 1.0-1.1 TFLOP/s (a DFMA loop; not in MEASURED_PEAKS.json)"}
 
 
 GRAM_SHAPE = (40, 4)  # P rows x Q rows of the timed Gram launch: mid-solve basis against a new block
@@ -709,7 +743,7 @@ def main():
             "solve": {k: r["stats"][k] for k in ("n_matvec", "n_iter", "n_restart", "nconv", "seconds",
                                                  "host_eig_seconds", "device_wait_seconds")},
             "roofline": r["roofline"][0], "roofline_combine": r["roofline"][2],
-            "roofline_hx": r["roofline"][1], "clocks": r["clocks"],
+            "roofline_hx": r["roofline"][1], "potential": r["potential"], "clocks": r["clocks"],
             "gpu_launches": r["launches"]}
     if r["fp64"]:
         line["fp64_gpu"] = dict(r["fp64"], solves_per_s=ws * r["fp64"]["solves_per_s"])
